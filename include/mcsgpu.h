@@ -1,0 +1,171 @@
+/*
+ * mcsgpu.h -- C ABI of the GB300 Monte Carlo spin-lattice engine (libmcsgpu.so).
+ *
+ * Plain C: pointers, sizes and int status codes; no exceptions and no
+ * framework types cross this boundary.  The CPython modules isinglib, xylib and
+ * heisenberglib (drop-in for mcsolver's compiled libraries) are thin wrappers
+ * over mcs_solve(); ctypes, a serving loop or a C program can call it directly.
+ *
+ * Reference interfaces replaced (golddoushi/mcsolver):
+ *   mcs_solve() with model MCS_ISING      <- MCMainFunction, mcsolver/isingLib.c:259-451
+ *                                            (arguments isingLib.c:277-284, result :436-447)
+ *   mcs_solve() with model MCS_XY         <- MCMainFunction, mcsolver/xyLib.c:413-809
+ *                                            (arguments xyLib.c:439-447, result :782-809)
+ *   mcs_solve() with model MCS_HEISENBERG <- MCMainFunction, mcsolver/heisenbergLib.c:478-885
+ *                                            (arguments heisenbergLib.c:504-512, result :853-884)
+ *   mcs_batch_*()                         <- the process-pool fan-out over the (T,H) grid,
+ *                                            mcsolver/win.py:399-428 and :440-469
+ *   mcs_pt_*()                            <- (no counterpart: the reference runs each
+ *                                            temperature independently, win.py:440-444)
+ *   mcs_server_*()                        <- (no counterpart: continuous-batching request loop)
+ */
+#ifndef MCSGPU_H
+#define MCSGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define MCS_OK 0
+#define MCS_EINVAL 1       /* malformed input (sizes, indices, ranges)        */
+#define MCS_ECUDA 2        /* CUDA runtime error                              */
+#define MCS_ETIMEOUT 3     /* a bounded device wait ran out                   */
+#define MCS_ENOMEM 4       /* device memory / HBM budget exhausted            */
+#define MCS_EUNSUPPORTED 5 /* model outside what the engine implements        */
+#define MCS_EBUSY 6        /* server: no free slot (try again)                */
+#define MCS_ENOTFOUND 7    /* server: unknown ticket                          */
+
+#define MCS_ISING 1
+#define MCS_XY 2
+#define MCS_HEISENBERG 3
+
+#define MCS_METROPOLIS 0
+#define MCS_WOLFF 1
+
+/* One solve, in the reference's flattened layout (units: energies already
+ * multiplied by beta = 1/T, exactly as mcMain.py passes them: mcMain.py:26,
+ * :30-31, :121, :244).  Arrays are borrowed for the duration of the call. */
+typedef struct mcs_problem {
+    int32_t model;              /* MCS_ISING / MCS_XY / MCS_HEISENBERG        */
+    int32_t algorithm;          /* MCS_METROPOLIS / MCS_WOLFF                 */
+    int32_t n_sites;            /* totOrbs = len(initSpin)                    */
+    int32_t max_links;          /* maxNLinking                                */
+    int64_t nthermal, nsweep, ninterval;
+    const double *init_spin;    /* [n_sites] signed spin length S            */
+    const double *init_d;       /* [3*n_sites] D/T, O(n) only (may be NULL)  */
+    const int32_t *nlink;       /* [n_sites]                                  */
+    const double *link_strength;/* Ising [n_sites*max_links]; O(n) [9*n_sites*max_links],
+                                   components xx,yy,zz,xy,xz,yz,yx,zx,zy     */
+    const int32_t *linked_orb;  /* [n_sites*max_links], -1 padded            */
+    const int32_t *circuits;    /* [3*n_circuits] (Heisenberg)               */
+    const int32_t *corr_pair;   /* [2*n_lat]                                  */
+    const int32_t *group_list;  /* [n_group*max_group], -1 padded            */
+    const int32_t *r_orb;       /* [n_rorb]                                   */
+    const int32_t *r_cluster;   /* [n_rorb*n_in_cluster]                      */
+    const int32_t *r_link;      /* [n_rorb*max_links], -1 padded             */
+    double flunc, h;            /* initial tilt; field h/T                    */
+    int32_t n_circuits, n_lat, n_group, max_group;
+    int32_t n_rorb, n_in_cluster, ignore_offdiag, spin_frames;
+} mcs_problem;
+
+/* Engine knobs that the reference signature does not carry. */
+typedef struct mcs_options {
+    uint64_t seed;              /* Philox key of this solve                   */
+    int32_t schedule;           /* 0 auto, 1 plain (host-driven, one launch per
+                                   colour and per measurement), 2 resident
+                                   (whole lattice in one CTA's shared memory),
+                                   3 tiled (lattice in global memory)        */
+    int32_t absolute_energy;    /* Ising Metropolis: report absolute <e>
+                                   instead of the reference's offset one      */
+    int32_t recheck_every;      /* O(n): full FP64 energy re-check every k
+                                   measurements (0 = default 32)             */
+    int32_t record_series;      /* keep per-measurement e, M, e_r, <si.sj>    */
+    int32_t random_init;        /* 1: ignore init_spin directions, draw them
+                                   from the seed (Ising sign, XY angle,
+                                   Heisenberg sphere); lengths stay |S|       */
+    int32_t fp64_update;        /* 1: FP64 spin updates (drift study)         */
+    int32_t device;             /* CUDA device ordinal                        */
+    int32_t reserved_;
+} mcs_options;
+
+#define MCS_RESULT_VALUES 29
+typedef struct mcs_result {
+    /* the reference's result tuple; Ising uses values[0..9] (isingLib.c:437-446),
+       O(n) uses values[0..26] (heisenbergLib.c:855-881) */
+    double values[MCS_RESULT_VALUES];
+    double *group_values;       /* caller buffer, (G+1)^2+(G+1) doubles (or NULL) */
+    int32_t group_capacity;
+    int32_t frames_written;
+    float *frames;              /* caller buffer, spin_frames*n_sites*3 floats (or NULL) */
+    double *series;             /* caller buffer, nsweep*4 doubles (or NULL)   */
+    int64_t site_updates;       /* Metropolis site visits + Wolff flipped sites */
+    int64_t clusters;           /* Wolff clusters built                       */
+    int64_t flipped;            /* Wolff sites flipped                        */
+    int64_t accepted;           /* accepted moves / clusters                  */
+    int64_t exact_mismatches;   /* Ising: measurements where incremental E != full recompute */
+    double energy_drift;        /* O(n): max |E_incr - E_full| seen at re-checks (beta units) */
+    double device_ms;           /* device time of the solve                   */
+    int32_t schedule_used;
+    int32_t n_colours;
+} mcs_result;
+
+/* Solve one (T,H) point.  Returns MCS_OK or an error code; the message is in
+ * mcs_last_error().  Never aborts the process. */
+int mcs_solve(const mcs_problem *problem, const mcs_options *options, mcs_result *result);
+
+/* Last error message of this thread. */
+const char *mcs_last_error(void);
+
+/* Version and build information. */
+int mcs_abi_version(void);
+const char *mcs_build_info(void);
+
+/* ---- batched engine: many replicas of uneven sizes in one launch sequence -- */
+typedef struct mcs_batch mcs_batch;
+int mcs_batch_create(int32_t device, mcs_batch **out);
+/* Compile and upload one replica; returns its index in *replica. */
+int mcs_batch_add(mcs_batch *b, const mcs_problem *problem, const mcs_options *options, int32_t *replica);
+/* Run every replica to completion (persistent launches, CUDA graphs). */
+int mcs_batch_run(mcs_batch *b);
+int mcs_batch_result(mcs_batch *b, int32_t replica, mcs_result *result);
+/* Device time of the last mcs_batch_run and its total site updates. */
+int mcs_batch_stats(mcs_batch *b, double *device_ms, int64_t *site_updates, int32_t *launches);
+void mcs_batch_destroy(mcs_batch *b);
+
+/* ---- parallel tempering over a temperature ladder (one model) ------------- */
+/* The problem's couplings, anisotropy and field are PHYSICAL (not divided by T);
+ * betas[k] = 1/T_k.  One replica per temperature; after every sweep neighbouring
+ * temperatures try to swap with probability min(1, exp((b_i-b_j)(E_i-E_j))).
+ * Results are per temperature (index k). */
+typedef struct mcs_pt mcs_pt;
+int mcs_pt_create(const mcs_problem *problem, const mcs_options *options, const double *betas,
+                  int32_t n_temps, mcs_pt **out);
+int mcs_pt_run(mcs_pt *pt);
+int mcs_pt_result(mcs_pt *pt, int32_t temp_index, mcs_result *result);
+/* swap acceptance per neighbouring pair [n_temps-1] and round trips */
+int mcs_pt_stats(mcs_pt *pt, double *swap_acceptance, double *device_ms, int64_t *site_updates);
+void mcs_pt_destroy(mcs_pt *pt);
+
+/* ---- continuous-batching server --------------------------------------- */
+typedef struct mcs_server mcs_server;
+/* hbm_budget_bytes: device memory the server may hold for request state. */
+int mcs_server_create(int32_t device, uint64_t hbm_budget_bytes, int32_t max_slots, mcs_server **out);
+/* Queue one solve; *ticket identifies it.  Admission happens in mcs_server_step
+ * when slots and memory allow. */
+int mcs_server_submit(mcs_server *s, const mcs_problem *problem, const mcs_options *options, uint64_t *ticket);
+/* Advance the device by one tick (admit, run a chunk of sweeps on every active
+ * slot, retire finished ones).  Returns the number of requests completed. */
+int mcs_server_step(mcs_server *s, int32_t *completed);
+/* 0 = done (result filled, ticket released), 1 = pending. */
+int mcs_server_poll(mcs_server *s, uint64_t ticket, mcs_result *result);
+int mcs_server_stats(mcs_server *s, int32_t *active, int32_t *queued, uint64_t *bytes_in_use, int64_t *site_updates);
+void mcs_server_destroy(mcs_server *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MCSGPU_H */

@@ -1,0 +1,631 @@
+// mcs_device.cuh -- device-side building blocks of the Monte Carlo engine.
+//
+// Restated algorithms (reference file:line):
+//   Ising Metropolis trial        isingLib.c:238-254  (corr = 2(sum_l K s_i s_j - h s_i); accept corr>=0 or exp(corr)>U)
+//   O(n) reflection Metropolis    heisenbergLib.c:441-473, xyLib.c:382-409 (ds = -2(s.r)r)
+//   onsite delta                  heisenbergLib.c:299-308, xyLib.c:247-254
+//   majority block spin           isingLib.c:133-150, heisenbergLib.c:250-262
+//   renormalised energy           isingLib.c:152-163 / 388-391, heisenbergLib.c:264-275 / 789-799
+//   signed solid angle            heisenbergLib.c:114-127
+//   measurement loop              isingLib.c:375-432, heisenbergLib.c:661-831, xyLib.c:589-758
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mcs_internal.h"
+
+namespace mcs {
+
+#define MCS_PI_REF 3.1415926535  // heisenbergLib.c:6
+
+// ------------------------------------------------------------------ Philox
+// Philox4x32-10 (Salmon et al., SC'11); key = 64-bit seed.
+__device__ __forceinline__ uint4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, unsigned long long seed)
+{
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    return make_uint4(c0, c1, c2, c3);
+}
+__device__ __forceinline__ uint4 philox_t(uint32_t c0, long long t, uint32_t c3, unsigned long long seed)
+{
+    return philox(c0, (uint32_t)t, (uint32_t)((unsigned long long)t >> 32), c3, seed);
+}
+__device__ __forceinline__ float u24(uint32_t w) { return (float)(w >> 8) * (1.0f / 16777216.0f); }
+
+// ------------------------------------------------------------------ geometry
+// SQUARE: N = Lx*Ly, Lx, Ly even; sweep index v = c*N/2 + x*(Ly/2) + (y>>1), c = (x+y)&1.
+struct SqPos { int x, y, c, Lx, Ly, hy, half; };
+__device__ __forceinline__ SqPos sq_pos(const Rep &R, int v)
+{
+    SqPos p;
+    p.Ly = R.Ly; p.hy = R.Ly >> 1; p.half = R.N >> 1; p.Lx = R.N / R.Ly;
+    p.c = v >= p.half;
+    int k = v - p.c * p.half;
+    p.x = k / p.hy;
+    int yh = k - p.x * p.hy;
+    p.y = 2 * yh + ((p.x + p.c) & 1);
+    return p;
+}
+
+// Iterate the links of site v: f(slot, neighbour sweep index, code).  For the
+// square lattice the slots are +x, -x, +y, -y.
+template <int GEOM, class F>
+__device__ __forceinline__ void for_links(const Rep &R, int v, F &&f)
+{
+    if (GEOM == MCS_GEOM_SQUARE) {
+        SqPos p = sq_pos(R, v);
+        int base = (1 - p.c) * p.half;
+        int xp = (p.x + 1 == p.Lx) ? 0 : p.x + 1;
+        int xm = (p.x == 0) ? p.Lx - 1 : p.x - 1;
+        int yp = (p.y + 1 == p.Ly) ? 0 : p.y + 1;
+        int ym = (p.y == 0) ? p.Ly - 1 : p.y - 1;
+        f(0, base + xp * p.hy + (p.y >> 1), R.sq_code[0]);
+        f(1, base + xm * p.hy + (p.y >> 1), R.sq_code[1]);
+        f(2, base + p.x * p.hy + (yp >> 1), R.sq_code[2]);
+        f(3, base + p.x * p.hy + (ym >> 1), R.sq_code[3]);
+    } else {
+        int d = R.deg[v];
+        for (int l = 0; l < d; ++l)
+            f(l, __ldg(&R.nbr[(size_t)l * R.N + v]), (int)__ldg(&R.lcode[(size_t)l * R.N + v]));
+    }
+}
+template <int GEOM>
+__device__ __forceinline__ int link_class(const Rep &R, int v, int l)
+{
+    if (GEOM == MCS_GEOM_SQUARE) return R.sq_cls[l];
+    return R.lcls[(size_t)l * R.N + v];
+}
+
+// ------------------------------------------------------------------ spins
+struct Spins {
+    signed char *s;     // Ising
+    float *x, *y, *z;   // O(n) components (z unused for XY)
+};
+__device__ __forceinline__ Spins spins_global(const Rep &R)
+{
+    Spins S;
+    S.s = (signed char *)R.spins;
+    float *b = (float *)R.spins;
+    S.x = b; S.y = b + R.spad; S.z = b + 2 * (size_t)R.spad;
+    return S;
+}
+
+// ------------------------------------------------------------------ Ising trial
+// Threshold-table Metropolis: the neighbour-sign pattern selects an entry whose
+// threshold is ceil(exp(corr) * 2^32) (2^32 when corr >= 0); the trial is
+// accepted iff the Philox word is below it -- the same decision as
+// exp(corr) > w * 2^-32 of the reference rule with U = w * 2^-32.
+template <int GEOM>
+__device__ __forceinline__ void ising_trial(const Rep &R, const IsEntry *__restrict__ itab, signed char *s, int v,
+                                            uint32_t w, int (&dn)[MCS_MAXC], int (&dm)[MCS_MAXT])
+{
+    int si = s[v];
+    int t = R.stype ? R.stype[v] : 0;
+    int idx = R.ibase[t];
+    for_links<GEOM>(R, v, [&](int, int j, int code) { if (s[j] > 0) idx += code; });
+    const IsEntry e = itab[idx];
+    unsigned long long thr = e.thr[si > 0];
+    if ((unsigned long long)w < thr) {
+        s[v] = (signed char)(-si);
+        int nc = e.nc;
+        dn[0] += si * (int)(signed char)(nc & 0xff);
+        dn[1] += si * (int)(signed char)((nc >> 8) & 0xff);
+        dn[2] += si * (int)(signed char)((nc >> 16) & 0xff);
+        dn[3] += si * (int)(signed char)((nc >> 24) & 0xff);
+#pragma unroll
+        for (int q = 0; q < MCS_MAXT; ++q) dm[q] += (q == t) ? si : 0;
+    }
+}
+
+// ------------------------------------------------------------------ O(n) trial
+// Reflection proposal s' = s - 2(s.r)r with r uniform on the circle / sphere.
+// dE = ds . (sum_l J_l s_j) + D.((s+ds)^2 - s^2) - h ds_axis (field along x for
+// XY, z for Heisenberg).  Accept dE <= 0 or exp(-beta dE) > U.
+template <int DIM>
+__device__ __forceinline__ void on_direction(const uint4 &w, float &r0, float &r1, float &r2)
+{
+    if (DIM == 2) {
+        float sp, cp;
+        sincospif(2.0f * u24(w.x), &sp, &cp);
+        r0 = cp; r1 = sp; r2 = 0.f;
+    } else {
+        float zz = 2.0f * u24(w.x) - 1.0f;
+        float sp, cp;
+        sincospif(2.0f * u24(w.y), &sp, &cp);
+        float rho = sqrtf(fmaxf(0.f, 1.f - zz * zz));
+        r0 = rho * cp; r1 = rho * sp; r2 = zz;
+    }
+}
+
+template <int DIM, int GEOM>
+__device__ __forceinline__ void on_field(const Rep &R, const float *__restrict__ jt, const Spins &S, int v,
+                                         float &h0, float &h1, float &h2)
+{
+    h0 = h1 = h2 = 0.f;
+    const bool full = R.fullJ;
+    for_links<GEOM>(R, v, [&](int, int j, int code) {
+        const float *M = jt + 9 * code;
+        float a = S.x[j], b = S.y[j];
+        float c = (DIM == 3) ? S.z[j] : 0.f;
+        h0 = fmaf(M[0], a, h0);
+        h1 = fmaf(M[1], b, h1);
+        if (DIM == 3) h2 = fmaf(M[2], c, h2);
+        if (full) {
+            h0 = fmaf(M[3], b, h0);
+            h1 = fmaf(M[6], a, h1);
+            if (DIM == 3) {
+                h0 = fmaf(M[4], c, h0);
+                h1 = fmaf(M[5], c, h1);
+                h2 = fmaf(M[7], a, h2);
+                h2 = fmaf(M[8], b, h2);
+            }
+        }
+    });
+}
+
+// returns true when accepted; dE (table units, before beta) in *dEout
+template <int DIM, int GEOM>
+__device__ __forceinline__ bool on_trial(const Rep &R, const float *__restrict__ jt, const float *__restrict__ dt,
+                                         const Spins &S, int v, const uint4 &w, float beta, float h, float *dEout)
+{
+    float h0, h1, h2;
+    on_field<DIM, GEOM>(R, jt, S, v, h0, h1, h2);
+    float r0, r1, r2;
+    on_direction<DIM>(w, r0, r1, r2);
+    float s0 = S.x[v], s1 = S.y[v];
+    float s2 = (DIM == 3) ? S.z[v] : 0.f;
+    float sr = s0 * r0 + s1 * r1 + s2 * r2;
+    float f = -2.f * sr;
+    float d0 = f * r0, d1 = f * r1, d2 = f * r2;
+    float dE = d0 * h0 + d1 * h1 + d2 * h2;
+    if (R.has_d) {
+        int dc = R.stype ? R.stype[v] : 0;
+        const float *D = dt + 3 * dc;
+        dE += D[0] * (d0 * (2.f * s0 + d0)) + D[1] * (d1 * (2.f * s1 + d1));
+        if (DIM == 3) dE += D[2] * (d2 * (2.f * s2 + d2));
+    }
+    dE -= h * ((DIM == 3) ? d2 : d0);
+    float x = beta * dE;
+    uint32_t wa = (DIM == 3) ? w.z : w.y;
+    bool acc = (x <= 0.f) || (__expf(-x) > u24(wa));
+    if (acc) {
+        S.x[v] = s0 + d0;
+        S.y[v] = s1 + d1;
+        if (DIM == 3) S.z[v] = s2 + d2;
+        *dEout = dE;
+    }
+    return acc;
+}
+
+// ------------------------------------------------------------------ reductions
+// Sum K doubles over the block in a fixed order.  red: shared [32*K] doubles.
+// Result valid in out[0..K-1] (shared) after the call for all threads.
+template <int K>
+__device__ __forceinline__ void block_sum(double (&v)[K], double *red, double *out)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double x = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) red[wid * K + k] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double a = 0.0;
+        for (int w = 0; w < nw; ++w) a += red[w * K + threadIdx.x];
+        out[threadIdx.x] = a;
+    }
+    __syncthreads();
+}
+template <int K>
+__device__ __forceinline__ void block_sum_ll(long long (&v)[K], long long *red, long long *out)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        long long x = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) red[wid * K + k] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        long long a = 0;
+        for (int w = 0; w < nw; ++w) a += red[w * K + threadIdx.x];
+        out[threadIdx.x] = a;
+    }
+    __syncthreads();
+}
+
+// ------------------------------------------------------------------ measurement helpers
+__device__ __forceinline__ void v_norm_ref(float &x, float &y, float &z)
+{
+    float len = sqrtf(x * x + y * y + z * z);
+    if (len < 1e-5f) return;  // normalize() leaves short vectors unchanged
+    x /= len; y /= len; z /= len;
+}
+
+// getMajoritySpin (O(n)): normalize(sum of cluster spins) * S (signed)
+template <int DIM>
+__device__ __forceinline__ void on_majority(const Rep &R, const Spins &S, int v, float &mx, float &my, float &mz)
+{
+    mx = my = mz = 0.f;
+    int r = R.rindex[v];
+    if (r >= 0) {
+        for (int k = 0; k < R.ncl; ++k) {
+            int c = __ldg(&R.rcl[(size_t)r * R.ncl + k]);
+            mx += S.x[c]; my += S.y[c];
+            if (DIM == 3) mz += S.z[c];
+        }
+    }
+    v_norm_ref(mx, my, mz);
+    float sv = R.sval[v];
+    mx *= sv; my *= sv; mz *= sv;
+}
+
+template <int DIM>
+__device__ __forceinline__ float on_jdot(const float *M, bool full, float ax, float ay, float az, float bx, float by, float bz)
+{
+    float e = ax * bx * M[0] + ay * by * M[1];
+    if (DIM == 3) e += az * bz * M[2];
+    if (full) {
+        e += ax * by * M[3] + ay * bx * M[6];
+        if (DIM == 3) e += ax * bz * M[4] + ay * bz * M[5] + az * bx * M[7] + az * by * M[8];
+    }
+    return e;
+}
+
+template <int DIM>
+__device__ __forceinline__ float on_onsite(const Rep &R, const float *dt, const Spins &S, int v)
+{
+    float s0 = S.x[v], s1 = S.y[v], s2 = (DIM == 3) ? S.z[v] : 0.f;
+    float e = 0.f;
+    if (R.has_d) {
+        int dc = R.stype ? R.stype[v] : 0;
+        const float *D = dt + 3 * dc;
+        e = D[0] * s0 * s0 + D[1] * s1 * s1;
+        if (DIM == 3) e += D[2] * s2 * s2;
+    }
+    return e - R.h * ((DIM == 3) ? s2 : s0);
+}
+
+// Berg-Luescher solid angle with atan (not atan2), +-pi when |re| < 1e-6.
+__device__ __forceinline__ double on_signed_area(const Rep &R, const Spins &S, int a, int b, int c)
+{
+    float l1 = R.slen[a], l2 = R.slen[b], l3 = R.slen[c];
+    float ax = S.x[a], ay = S.y[a], az = S.z[a];
+    float bx = S.x[b], by = S.y[b], bz = S.z[b];
+    float cx = S.x[c], cy = S.y[c], cz = S.z[c];
+    float s1s2 = (ax * bx + ay * by + az * bz) / l1 / l2;
+    float s2s3 = (bx * cx + by * cy + bz * cz) / l2 / l3;
+    float s3s1 = (cx * ax + cy * ay + cz * az) / l3 / l1;
+    float kx = by * cz - bz * cy, ky = bz * cx - bx * cz, kz = bx * cy - by * cx;
+    float re = 1.f + s1s2 + s2s3 + s3s1;
+    float im = (ax * kx + ay * ky + az * kz) / l1 / l2 / l3;
+    if (fabsf(re) < 1e-6f) return im > 0.f ? MCS_PI_REF : -MCS_PI_REF;
+    return 2.0 * (double)atanf(im / re);
+}
+
+// ------------------------------------------------------------------ O(n) frame over a virtual index range
+// Every thread of the block calls this; vb..ve is the index range of this block
+// (resident: 0..max list length).  Results in Fout (shared, F_NON doubles),
+// valid after return.  red: shared scratch [32*12] doubles.  efull: also sum
+// the full energy (bond and onsite parts).
+template <int DIM, int GEOM>
+__device__ void on_frame(const Rep &R, const float *jt, const float *dt, const Spins &S, int vb, int ve,
+                         bool efull, double *red, double *Fout)
+{
+    const int tid = threadIdx.x, bd = blockDim.x;
+    // pass 1: correlated pairs
+    {
+        float a[7] = {0, 0, 0, 0, 0, 0, 0};
+        int e = min(ve, R.nlat);
+        for (int v = vb + tid; v < e; v += bd) {
+            int p = __ldg(&R.cpair[2 * v]), q = __ldg(&R.cpair[2 * v + 1]);
+            float px = S.x[p], py = S.y[p], pz = DIM == 3 ? S.z[p] : 0.f;
+            float qx = S.x[q], qy = S.y[q], qz = DIM == 3 ? S.z[q] : 0.f;
+            a[0] += px; a[1] += py; a[2] += pz; a[3] += qx; a[4] += qy; a[5] += qz;
+            a[6] += px * qx + py * qy + pz * qz;
+        }
+        double d[7];
+#pragma unroll
+        for (int k = 0; k < 7; ++k) d[k] = a[k];
+        block_sum<7>(d, red, Fout + F_SI);
+    }
+    // pass 2: all sites (total spin, full energy on re-checks)
+    {
+        float a[5] = {0, 0, 0, 0, 0};
+        int e = min(ve, R.N);
+        for (int v = vb + tid; v < e; v += bd) {
+            a[0] += S.x[v]; a[1] += S.y[v];
+            if (DIM == 3) a[2] += S.z[v];
+            if (efull) {
+                float h0, h1, h2;
+                on_field<DIM, GEOM>(R, jt, S, v, h0, h1, h2);
+                float sz = DIM == 3 ? S.z[v] : 0.f;
+                a[3] += S.x[v] * h0 + S.y[v] * h1 + sz * h2;
+                a[4] += on_onsite<DIM>(R, dt, S, v);
+            }
+        }
+        double d[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) d[k] = a[k];
+        double o[5];
+        block_sum<5>(d, red, red + 32 * 5);
+        if (tid < 5) o[0] = 0;  // silence
+        if (tid == 0) {
+            Fout[F_TOT] = red[32 * 5 + 0]; Fout[F_TOT + 1] = red[32 * 5 + 1]; Fout[F_TOT + 2] = red[32 * 5 + 2];
+            Fout[F_EFB] = red[32 * 5 + 3]; Fout[F_EFO] = red[32 * 5 + 4];
+        }
+        __syncthreads();
+    }
+    // pass 2b: orbital groups
+    if (R.ngroup > 0) {
+        for (int g0 = 0; g0 < R.ngroup; g0 += 4) {
+            float a[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+            int e = min(ve, R.N);
+            for (int v = vb + tid; v < e; v += bd) {
+                int m = R.gmask[v] >> g0;
+                if (!(m & 15)) continue;
+                float x = S.x[v], y = S.y[v], z = DIM == 3 ? S.z[v] : 0.f;
+#pragma unroll
+                for (int g = 0; g < 4; ++g)
+                    if (m & (1 << g)) { a[3 * g] += x; a[3 * g + 1] += y; a[3 * g + 2] += z; }
+            }
+            double d[12];
+#pragma unroll
+            for (int k = 0; k < 12; ++k) d[k] = a[k];
+            block_sum<12>(d, red, red + 32 * 12);
+            if (tid < 12 && g0 + tid / 3 < MCS_MAXG) Fout[F_G + 3 * g0 + tid] = red[32 * 12 + tid];
+            __syncthreads();
+        }
+    }
+    // pass 3: renormalised lattice
+    {
+        float a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        const bool full = R.fullJ;
+        int e = min(ve, R.nlat);
+        for (int v = vb + tid; v < e; v += bd) {
+            int p = __ldg(&R.cpair[2 * v]), q = __ldg(&R.cpair[2 * v + 1]);
+            bool cp = R.rindex[p] >= 0, cq = R.rindex[q] >= 0;
+            float px = 0, py = 0, pz = 0, qx = 0, qy = 0, qz = 0;
+            if (cp) { on_majority<DIM>(R, S, p, px, py, pz); a[0] += px; a[1] += py; a[2] += pz; }
+            if (cq) { on_majority<DIM>(R, S, q, qx, qy, qz); a[3] += qx; a[4] += qy; a[5] += qz; }
+            if (cp && cq) a[6] += px * qx + py * qy + pz * qz;
+        }
+        e = min(ve, R.n_rorb);
+        for (int v = vb + tid; v < e; v += bd) {
+            int j = __ldg(&R.rorb[v]);
+            float mx, my, mz;
+            on_majority<DIM>(R, S, j, mx, my, mz);
+            float corr = 0.f;
+            int d = R.rdeg[v];
+            for (int l = 0; l < d; ++l) {
+                int t = __ldg(&R.rlink[(size_t)v * R.zmax + l]);
+                if (t < 0) continue;
+                float tx, ty, tz;
+                on_majority<DIM>(R, S, t, tx, ty, tz);
+                corr += on_jdot<DIM>(jt + 9 * R.rjc[(size_t)v * R.zmax + l], full, mx, my, mz, tx, ty, tz);
+            }
+            a[7] += corr;
+            a[8] += on_onsite<DIM>(R, dt, S, j);
+        }
+        double dd[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) dd[k] = a[k];
+        block_sum<9>(dd, red, Fout + F_SIR);
+    }
+    // pass 4: topological charge over circuits (Heisenberg)
+    if (DIM == 3 && R.ncirc > 0) {
+        double q[1] = {0.0};
+        int e = min(ve, R.ncirc);
+        for (int v = vb + tid; v < e; v += bd)
+            q[0] += on_signed_area(R, S, __ldg(&R.circ[3 * v]), __ldg(&R.circ[3 * v + 1]), __ldg(&R.circ[3 * v + 2]));
+        block_sum<1>(q, red, Fout + F_Q);
+    } else if (tid == 0) {
+        Fout[F_Q] = 0.0;
+    }
+    __syncthreads();
+}
+
+// Fold one measurement frame into the FP64 accumulators (one thread).
+// Follows heisenbergLib.c:678-830 / xyLib.c:606-757 in FP64.
+template <int DIM>
+__device__ void on_accumulate(Rep &R, const double *F, double E, long long m)
+{
+    double *acc = R.acc;
+    const double nl = (double)R.nlat;
+    double tx = F[F_TOT], ty = F[F_TOT + 1], tz = DIM == 3 ? F[F_TOT + 2] : 0.0;
+    double dx = tx, dy = ty, dz = tz;
+    double len = sqrt(dx * dx + dy * dy + dz * dz);
+    if (len >= 1e-5) { dx /= len; dy /= len; dz /= len; }
+    double six = F[F_SI], siy = F[F_SI + 1], siz = DIM == 3 ? F[F_SI + 2] : 0.0;
+    double sjx = F[F_SJ], sjy = F[F_SJ + 1], sjz = DIM == 3 ? F[F_SJ + 2] : 0.0;
+    acc[A_SIZ] += (dx * six + dy * siy + dz * siz) / nl;
+    acc[A_SJZ] += (dx * sjx + dy * sjy + dz * sjz) / nl;
+    acc[A_STZ] += (dx * tx + dy * ty + dz * tz) / nl;
+    acc[A_SIH] += (DIM == 3 ? siz : six) / nl;
+    acc[A_SJH] += (DIM == 3 ? sjz : sjx) / nl;
+    acc[A_STH] += (DIM == 3 ? tz : tx) / nl;
+    double M = (DIM == 3) ? sqrt(tx * tx + ty * ty + tz * tz) / nl : sqrt(six * six + siy * siy) / nl;
+    acc[A_M2] += M * M;
+    acc[A_M4] += M * M * M * M;
+    acc[A_MTOT] += M;
+    acc[A_MDM] += acc[A_MPREV] * M;
+    acc[A_MPREV] = M;
+    acc[A_SI] += fabs(six / nl); acc[A_SI + 1] += fabs(siy / nl); acc[A_SI + 2] += fabs(siz / nl);
+    acc[A_SJ] += fabs(sjx / nl); acc[A_SJ + 1] += fabs(sjy / nl); acc[A_SJ + 2] += fabs(sjz / nl);
+    acc[A_SIJ] += F[F_SIJ] / nl;
+    double e = E / R.N;
+    acc[A_E] += e;
+    acc[A_E2] += e * e;
+    for (int k = 0; k < 3; ++k) {
+        acc[A_SIR + k] += fabs(F[F_SIR + k] / R.ci);
+        acc[A_SJR + k] += fabs(F[F_SJR + k] / R.cj);
+    }
+    acc[A_SIJR] += F[F_SIJR] / R.cij;
+    double er = (F[F_ERB] / 2 + F[F_ERO]) / R.n_rorb;
+    acc[A_ER] += er;
+    acc[A_ER2] += er * er;
+    if (DIM == 3) acc[A_Q] += F[F_Q] / MCS_PI_REF / 4;
+    const int G = R.ngroup;
+    if (G > 0) {
+        double gx[MCS_MAXG + 1], gy[MCS_MAXG + 1], gz[MCS_MAXG + 1];
+        for (int g = 0; g < G; ++g) { gx[g] = F[F_G + 3 * g]; gy[g] = F[F_G + 3 * g + 1]; gz[g] = DIM == 3 ? F[F_G + 3 * g + 2] : 0.0; }
+        gx[G] = tx / nl; gy[G] = ty / nl; gz[G] = tz / nl;
+        for (int a = 0; a <= G; ++a)
+            for (int b = 0; b <= G; ++b) {
+                double d = gx[a] * gx[b] + gy[a] * gy[b] + gz[a] * gz[b];
+                acc[A_GRP + a * (G + 1) + b] += d;
+                if (a == b) acc[A_GRP + (G + 1) * (G + 1) + a] += d * d;
+            }
+    }
+    if (R.series) {
+        double *s = R.series + (size_t)m * MCS_NSER;
+        s[0] = e; s[1] = M; s[2] = er; s[3] = F[F_SIJ] / nl;
+    }
+}
+
+// ------------------------------------------------------------------ Ising frame
+// Majority sign of the block around v; tie -> Philox word of (a, m, slot).
+__device__ __forceinline__ double is_majority(const Rep &R, const signed char *s, int v, const uint4 &w, int slot)
+{
+    double avg = 0.0;
+    int r = R.rindex[v];
+    if (r >= 0)
+        for (int k = 0; k < R.ncl; ++k) {
+            int c = __ldg(&R.rcl[(size_t)r * R.ncl + k]);
+            int t = R.stype ? R.stype[c] : 0;
+            avg += R.Stype[t] * (double)s[c];
+        }
+    int tv = R.stype ? R.stype[v] : 0;
+    double a = R.Stype[tv];
+    if (avg > 0) return a;
+    if (avg < 0) return -a;
+    uint32_t word = (slot & 3) == 0 ? w.x : (slot & 3) == 1 ? w.y : (slot & 3) == 2 ? w.z : w.w;
+    return ((double)word * (1.0 / 4294967296.0) > 0.5) ? a : -a;
+}
+
+// Ising frame over [vb, ve): pairs, renormalised energy, per-type sign sums,
+// full per-class directed bond sums.  Fd (4 doubles) and Fi (MAXT+MAXC ints).
+template <int GEOM>
+__device__ void is_frame(const Rep &R, const IsEntry *itab, const signed char *s, int vb, int ve, long long m,
+                         double *red, double *Fd, long long *redl, long long *Fi)
+{
+    const int tid = threadIdx.x, bd = blockDim.x;
+    double a[4] = {0, 0, 0, 0};
+    int e = min(ve, R.nlat);
+    for (int v = vb + tid; v < e; v += bd) {
+        int p = __ldg(&R.cpair[2 * v]), q = __ldg(&R.cpair[2 * v + 1]);
+        double sp = R.Stype[R.stype ? R.stype[p] : 0] * (double)s[p];
+        double sq = R.Stype[R.stype ? R.stype[q] : 0] * (double)s[q];
+        a[0] += sp; a[1] += sq; a[2] += sp * sq;
+    }
+    e = min(ve, R.n_rorb);
+    for (int v = vb + tid; v < e; v += bd) {
+        int j = __ldg(&R.rorb[v]);
+        uint4 w = philox_t((uint32_t)j, m, 0x3000u, R.seed);
+        double mj = is_majority(R, s, j, w, 0);
+        double corr = 0;
+        int d = R.rdeg[v];
+        for (int l = 0; l < d; ++l) {
+            int slot = 1 + l;
+            if ((slot & 3) == 0) w = philox_t((uint32_t)j, m, 0x3000u + (uint32_t)(slot >> 2), R.seed);
+            int t = __ldg(&R.rlink[(size_t)v * R.zmax + l]);
+            if (t < 0) continue;
+            double mt = is_majority(R, s, t, w, slot);
+            corr += R.rK[(size_t)v * R.zmax + l] * mj * mt;
+        }
+        double sj = R.Stype[R.stype ? R.stype[j] : 0] * (double)s[j];
+        a[3] += corr / 2 - R.hd * sj;
+    }
+    block_sum<4>(a, red, Fd);
+    long long c[MCS_MAXT + MCS_MAXC];
+#pragma unroll
+    for (int k = 0; k < MCS_MAXT + MCS_MAXC; ++k) c[k] = 0;
+    e = min(ve, R.N);
+    for (int v = vb + tid; v < e; v += bd) {
+        int si = s[v];
+        int t = R.stype ? R.stype[v] : 0;
+        int idx = R.ibase[t];
+        for_links<GEOM>(R, v, [&](int, int j, int code) { if (s[j] > 0) idx += code; });
+        int nc = itab[idx].nc;
+#pragma unroll
+        for (int q = 0; q < MCS_MAXT; ++q) c[q] += (q == t) ? si : 0;
+        c[MCS_MAXT + 0] += si * (int)(signed char)(nc & 0xff);
+        c[MCS_MAXT + 1] += si * (int)(signed char)((nc >> 8) & 0xff);
+        c[MCS_MAXT + 2] += si * (int)(signed char)((nc >> 16) & 0xff);
+        c[MCS_MAXT + 3] += si * (int)(signed char)((nc >> 24) & 0xff);
+    }
+    block_sum_ll<MCS_MAXT + MCS_MAXC>(c, redl, Fi);
+}
+
+// Fold one Ising measurement (one thread).  isingLib.c:388-431.
+__device__ void is_accumulate(Rep &R, const double *Fd, const long long *Fi, int last_sign, long long m)
+{
+    double *acc = R.acc;
+    long long *ic = R.icnt;
+    const double nl = (double)R.nlat;
+    double Mtrue = 0;
+    for (int t = 0; t < R.ntype; ++t) Mtrue += R.Stype[t] * (double)Fi[t];
+    // exact check: incremental bookkeeping vs full recompute
+    bool ok = true;
+    for (int c = 0; c < MCS_MAXC; ++c) ok &= (Fi[MCS_MAXT + c] - ic[C_N0 + c]) == ic[C_DN + c];
+    for (int t = 0; t < MCS_MAXT; ++t) ok &= (Fi[t] - ic[C_M0 + t]) == ic[C_DM + t];
+    if (!ok && R.exact_ok) ic[C_MISM] += 1;
+    double e_rep;
+    if (R.alg == 0) {
+        double Einc = 0;
+        for (int c = 0; c < R.nclass; ++c) Einc += 0.5 * R.Q[c] * (double)ic[C_DN + c];
+        for (int t = 0; t < R.ntype; ++t) Einc -= R.hd * R.Stype[t] * (double)ic[C_DM + t];
+        if (R.offset_energy) e_rep = Einc - acc[B_EMEAS0];
+        else {
+            double E0 = 0;
+            for (int c = 0; c < R.nclass; ++c) E0 += 0.5 * R.Q[c] * (double)ic[C_N0 + c];
+            for (int t = 0; t < R.ntype; ++t) E0 -= R.hd * R.Stype[t] * (double)ic[C_M0 + t];
+            e_rep = E0 + Einc;
+        }
+    } else {
+        double Eabs = 0;
+        for (int c = 0; c < R.nclass; ++c) Eabs += 0.5 * R.Q[c] * (double)Fi[MCS_MAXT + c];
+        for (int t = 0; t < R.ntype; ++t) Eabs -= R.hd * R.Stype[t] * (double)Fi[t];
+        e_rep = (ic[C_ACC_MEAS] || !R.offset_energy) ? Eabs : 0.0;
+    }
+    double ts = Mtrue - R.ts_const;
+    if (R.ts_wolff_last) ts -= R.Stype[R.stype ? R.stype[R.last_site] : 0] * (double)last_sign;
+    acc[B_STOT] += ts;
+    double M = Fd[0] / nl;
+    acc[B_M2] += M * M;
+    acc[B_M4] += M * M * M * M;
+    acc[B_MTOT] += M;
+    acc[B_MDM] += acc[B_MPREV] * M;
+    acc[B_MPREV] = M;
+    acc[B_SI] += fabs(Fd[0]) / nl;
+    acc[B_SJ] += fabs(Fd[1]) / nl;
+    acc[B_SIJ] += Fd[2] / nl;
+    double e = e_rep / R.N, er = Fd[3] / R.n_rorb;
+    acc[B_E] += e;
+    acc[B_ER] += er;
+    acc[B_E2] += e * e;
+    acc[B_ER2] += er * er;
+    if (R.series) {
+        double *s = R.series + (size_t)m * MCS_NSER;
+        s[0] = e; s[1] = M; s[2] = er; s[3] = Fd[2] / nl;
+    }
+}
+
+__device__ __forceinline__ bool measures_after(const Rep &R, long long u)
+{
+    return u >= R.units_thermal && ((u - R.units_thermal + 1) % R.upm) == 0;
+}
+
+}  // namespace mcs

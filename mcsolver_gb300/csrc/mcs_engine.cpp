@@ -1,0 +1,650 @@
+// mcs_engine.cpp -- host engine and C ABI of libmcsgpu.so.
+//
+// A Batch holds replicas (independent solves).  Each replica owns one device
+// arena (descriptor arrays, tables, spins, FP64 accumulators).  At run time
+// the replicas are grouped by (model dimension, geometry, algorithm, schedule):
+//   resident groups: one persistent launch per chunk of units (one CTA per
+//                    replica, lattice in shared memory);
+//   tiled groups   : lockstep units, one launch per colour + measure + finalize,
+//                    captured in a CUDA graph and replayed;
+//   plain          : the tiled sequence for one replica at a time without
+//                    graphs (the one-solve-per-launch-sequence baseline).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/mcsgpu.h"
+#include "mcs_engine.h"
+#include "mcs_internal.h"
+#include "mcs_model.h"
+
+namespace mcs {
+
+static thread_local std::string g_err;
+void set_error(const std::string &s) { g_err = s; }
+const std::string &get_error() { return g_err; }
+
+#define CUDA_TRY(x)                                                                              \
+    do {                                                                                         \
+        cudaError_t e_ = (x);                                                                    \
+        if (e_ != cudaSuccess) {                                                                 \
+            set_error(std::string("CUDA error: ") + cudaGetErrorString(e_) + " at " #x);         \
+            return MCS_ECUDA;                                                                    \
+        }                                                                                        \
+    } while (0)
+
+// ------------------------------------------------------------------ arena builder
+struct ArenaBuilder {
+    std::vector<unsigned char> host;
+    size_t add(const void *data, size_t bytes)
+    {
+        size_t off = (host.size() + 255) & ~(size_t)255;
+        host.resize(off + bytes);
+        if (data && bytes) memcpy(host.data() + off, data, bytes);
+        else if (bytes) memset(host.data() + off, 0, bytes);
+        return off;
+    }
+    template <class T> size_t addv(const std::vector<T> &v) { return add(v.empty() ? nullptr : v.data(), v.size() * sizeof(T)); }
+};
+
+Replica::~Replica()
+{
+    if (arena) cudaFree(arena);
+}
+
+size_t replica_acc_count(const HostModel &m)
+{
+    if (m.dim == 1) return B_NACC;
+    int G = m.ngroup;
+    return A_GRP + (size_t)(G + 1) * (G + 1) + (G + 1);
+}
+
+int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r)
+{
+    std::string err;
+    int rc = compile_model(p, o, &r->hm, &err);
+    if (rc != MCS_OK) { set_error(err); return rc; }
+    CUDA_TRY(cudaSetDevice(r->device));
+    const HostModel &m = r->hm;
+    r->record_series = o && o->record_series;
+    r->requested_schedule = o ? o->schedule : 0;
+    r->recheck = (o && o->recheck_every > 0) ? o->recheck_every : 32;
+    ArenaBuilder A;
+    size_t o_nbr = 0, o_lcode = 0, o_lcls = 0, o_deg = 0, o_stype = 0, o_jt = 0, o_jt64 = 0, o_dt = 0, o_it = 0;
+    if (m.geom == MCS_GEOM_ELL) {
+        o_nbr = A.addv(m.nbr);
+        o_lcode = A.addv(m.lcode);
+        o_deg = A.addv(m.deg);
+    }
+    if (m.dim == 1) o_lcls = A.addv(m.lcls);
+    o_stype = A.addv(m.stype);
+    if (m.dim > 1) { o_jt = A.addv(m.jtab); o_jt64 = A.addv(m.jtab64); o_dt = A.addv(m.dtab); }
+    else o_it = A.addv(m.itab);
+    size_t o_cp = A.addv(m.cpair), o_rorb = A.addv(m.rorb), o_rcl = A.addv(m.rcl), o_rlink = A.addv(m.rlink);
+    size_t o_rjc = 0, o_rK = 0;
+    if (m.dim > 1) o_rjc = A.addv(m.rjc);
+    else o_rK = A.addv(m.rK);
+    size_t o_rdeg = A.addv(m.rdeg), o_rindex = A.addv(m.rindex), o_circ = A.addv(m.circ);
+    size_t o_slen = A.addv(m.slen), o_sval = A.addv(m.sval), o_gmask = A.addv(m.gmask);
+    int spad = (m.N + 31) & ~31;
+    size_t o_spins;
+    if (m.dim == 1) o_spins = A.addv(m.init_sigma);
+    else {
+        std::vector<float> sp((size_t)m.dim * spad, 0.f);
+        for (int c = 0; c < m.dim; ++c)
+            memcpy(sp.data() + (size_t)c * spad, m.init_vec.data() + (size_t)c * m.N, sizeof(float) * m.N);
+        o_spins = A.addv(sp);
+    }
+    size_t nacc = replica_acc_count(m);
+    size_t o_acc = A.add(nullptr, nacc * sizeof(double));
+    size_t o_icnt = A.add(nullptr, C_NINT * sizeof(long long));
+    size_t o_stats = A.add(nullptr, S_NSTAT * sizeof(long long));
+    size_t o_series = 0;
+    if (r->record_series) o_series = A.add(nullptr, (size_t)m.nsweep * MCS_NSER * sizeof(double));
+    size_t o_frames = 0;
+    if (m.frames > 0) o_frames = A.add(nullptr, (size_t)m.frames * m.N * 3 * sizeof(float));
+    size_t o_wbits = 0, o_wq = 0;
+    if (m.alg == 1) {
+        o_wbits = A.add(nullptr, ((size_t)(m.N + 31) / 32) * sizeof(unsigned));
+        o_wq = A.add(nullptr, (size_t)m.N * sizeof(int));
+    }
+    r->bytes = A.host.size();
+    CUDA_TRY(cudaMalloc(&r->arena, r->bytes));
+    CUDA_TRY(cudaMemcpy(r->arena, A.host.data(), r->bytes, cudaMemcpyHostToDevice));
+    unsigned char *b = (unsigned char *)r->arena;
+    Rep &R = r->rep;
+    memset(&R, 0, sizeof R);
+    R.model = m.model; R.dim = m.dim; R.geom = m.geom; R.alg = m.alg;
+    R.N = m.N; R.zmax = m.zmax; R.ncol = m.ncol; R.Ly = m.Ly;
+    for (int d = 0; d < 4; ++d) { R.sq_code[d] = m.sq_code[d]; R.sq_cls[d] = m.sq_cls[d]; }
+    for (int c = 0; c <= m.ncol; ++c) R.col_start[c] = m.col_start[c];
+    if (m.geom == MCS_GEOM_ELL) {
+        R.nbr = (const int *)(b + o_nbr);
+        R.lcode = (const unsigned short *)(b + o_lcode);
+        R.deg = (const unsigned char *)(b + o_deg);
+    }
+    if (m.dim == 1) R.lcls = (const unsigned char *)(b + o_lcls);
+    R.stype = (const unsigned char *)(b + o_stype);
+    if (m.dim > 1) {
+        R.jtab = (const float *)(b + o_jt); R.jtab64 = (const double *)(b + o_jt64);
+        R.njc = m.njc; R.fullJ = m.fullJ;
+        R.dtab = (const float *)(b + o_dt); R.ndc = m.ndc; R.has_d = m.has_d;
+    } else {
+        R.itab = (const IsEntry *)(b + o_it); R.nite = (int)m.itab.size(); R.ntype = m.ntype;
+        for (int t = 0; t < MCS_MAXT; ++t) { R.ibase[t] = m.ibase[t]; R.Stype[t] = m.Stype[t]; }
+        for (int c = 0; c < MCS_MAXC; ++c) {
+            R.Q[c] = m.Q[c];
+            R.wthr[c][0] = m.wthr[c][0]; R.wthr[c][1] = m.wthr[c][1];
+        }
+        R.nclass = m.nclass; R.exact_ok = m.exact_ok;
+    }
+    R.beta = 1.0f; R.h = (float)m.h; R.hd = m.h;
+    R.fp64 = 0;
+    R.seed = m.seed;
+    R.nlat = m.nlat; R.cpair = (const int *)(b + o_cp);
+    R.n_rorb = m.n_rorb; R.ncl = m.ncl;
+    R.rorb = (const int *)(b + o_rorb); R.rcl = (const int *)(b + o_rcl); R.rlink = (const int *)(b + o_rlink);
+    if (m.dim > 1) R.rjc = (const unsigned short *)(b + o_rjc);
+    else R.rK = (const double *)(b + o_rK);
+    R.rdeg = (const unsigned char *)(b + o_rdeg);
+    R.rindex = (const int *)(b + o_rindex);
+    R.ncirc = m.ncirc; R.circ = (const int *)(b + o_circ);
+    R.slen = (const float *)(b + o_slen); R.sval = (const float *)(b + o_sval);
+    R.ngroup = m.ngroup; R.gmask = (const unsigned char *)(b + o_gmask);
+    R.ci = m.ci; R.cj = m.cj; R.cij = m.cij;
+    R.units_thermal = m.units_thermal; R.units_total = m.units_total; R.nsweep = m.nsweep; R.upm = m.upm;
+    R.frames = m.frames; R.frame_every = m.frame_every;
+    R.recheck = r->recheck;
+    R.ts_const = m.ts_const; R.ts_wolff_last = m.ts_wolff_last; R.last_site = m.last_site;
+    R.offset_energy = m.offset_energy;
+    R.spins = b + o_spins; R.spad = spad;
+    R.acc = (double *)(b + o_acc);
+    R.series = r->record_series ? (double *)(b + o_series) : nullptr;
+    R.frame_buf = m.frames > 0 ? (float *)(b + o_frames) : nullptr;
+    R.icnt = (long long *)(b + o_icnt);
+    R.stats = (long long *)(b + o_stats);
+    if (m.alg == 1) { R.wbits = (unsigned *)(b + o_wbits); R.wqueue = (int *)(b + o_wq); }
+    R.u0 = 0; R.u = 0; R.m = 0;
+    r->acc_off = o_acc; r->icnt_off = o_icnt; r->stats_off = o_stats; r->series_off = o_series;
+    r->frames_off = o_frames; r->spins_off = o_spins;
+    r->nacc = nacc;
+    return MCS_OK;
+}
+
+// ------------------------------------------------------------------ results
+int replica_results(Replica *r, const Rep &Rfinal, mcs_result *res)
+{
+    const HostModel &m = r->hm;
+    std::vector<double> acc(r->nacc);
+    std::vector<long long> icnt(C_NINT), stats(S_NSTAT);
+    unsigned char *b = (unsigned char *)r->arena;
+    CUDA_TRY(cudaMemcpy(acc.data(), b + r->acc_off, acc.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(icnt.data(), b + r->icnt_off, icnt.size() * sizeof(long long), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(stats.data(), b + r->stats_off, stats.size() * sizeof(long long), cudaMemcpyDeviceToHost));
+    if (!res) return MCS_OK;
+    double *g = res->group_values;
+    int gcap = res->group_capacity;
+    float *fr = res->frames;
+    double *ser = res->series;
+    memset(res->values, 0, sizeof res->values);
+    const double ns = (double)m.nsweep, nl = (double)m.nlat;
+    double *v = res->values;
+    if (m.dim == 1) {
+        double M2 = acc[B_M2], M4 = acc[B_M4], Mt = acc[B_MTOT];
+        v[0] = acc[B_SI] / ns; v[1] = acc[B_SJ] / ns; v[2] = acc[B_SIJ] / ns;
+        v[3] = (acc[B_MDM] / ns - (Mt / ns) * (Mt / ns));
+        v[4] = acc[B_E] / ns; v[5] = acc[B_E2] / ns; v[6] = acc[B_ER] / ns; v[7] = acc[B_ER2] / ns;
+        v[8] = (M2 / ns) * (M2 / ns) / (M4 / ns);
+        v[9] = acc[B_STOT] / ns / nl;
+    } else {
+        bool xy = m.dim == 2;
+        double M2 = acc[A_M2], M4 = acc[A_M4], Mt = acc[A_MTOT];
+        v[0] = acc[A_SI] / ns; v[1] = acc[A_SI + 1] / ns; v[2] = xy ? 0 : acc[A_SI + 2] / ns;
+        v[3] = acc[A_SJ] / ns; v[4] = acc[A_SJ + 1] / ns; v[5] = xy ? 0 : acc[A_SJ + 2] / ns;
+        v[6] = acc[A_SIJ] / ns;
+        v[7] = xy ? (acc[A_MDM] / ns - (Mt / ns) * (Mt / ns)) : (acc[A_MDM] / ns - Mt / ns * Mt / ns);
+        v[8] = acc[A_E] / ns; v[9] = acc[A_E2] / ns;
+        v[10] = (M2 / ns) * (M2 / ns) / (M4 / ns);
+        v[11] = acc[A_SIR] / ns; v[12] = acc[A_SIR + 1] / ns; v[13] = xy ? 0 : acc[A_SIR + 2] / ns;
+        v[14] = acc[A_SJR] / ns; v[15] = acc[A_SJR + 1] / ns; v[16] = xy ? 0 : acc[A_SJR + 2] / ns;
+        v[17] = acc[A_SIJR] / ns; v[18] = acc[A_ER] / ns; v[19] = acc[A_ER2] / ns;
+        v[20] = acc[A_SIZ] / ns; v[21] = acc[A_SJZ] / ns; v[22] = acc[A_STZ] / ns;
+        v[23] = acc[A_SIH] / ns; v[24] = acc[A_SJH] / ns; v[25] = acc[A_STH] / ns;
+        v[26] = xy ? 0 : acc[A_Q] / ns;
+        int G = m.ngroup, ng = (G + 1) * (G + 1) + (G + 1);
+        if (g && G > 0)
+            for (int k = 0; k < ng && k < gcap; ++k) g[k] = acc[A_GRP + k] / ns;
+        res->energy_drift = acc[A_DRIFT];
+    }
+    res->frames_written = 0;
+    if (fr && m.frames > 0) {
+        int nf = Rfinal.frames_written;
+        std::vector<float> buf((size_t)nf * m.N * 3);
+        if (nf > 0)
+            CUDA_TRY(cudaMemcpy(buf.data(), b + r->frames_off, buf.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        for (int f = 0; f < nf; ++f)
+            for (int i = 0; i < m.N; ++i)
+                for (int c = 0; c < 3; ++c) fr[((size_t)f * m.N + i) * 3 + c] = buf[((size_t)f * m.N + m.pos[i]) * 3 + c];
+        res->frames_written = nf;
+    }
+    if (ser && r->record_series)
+        CUDA_TRY(cudaMemcpy(ser, b + r->series_off, (size_t)m.nsweep * MCS_NSER * sizeof(double), cudaMemcpyDeviceToHost));
+    res->accepted = stats[S_ACCEPT];
+    res->clusters = stats[S_CLUSTERS];
+    res->flipped = stats[S_FLIPPED];
+    res->site_updates = m.alg == 0 ? stats[S_VISITS] : stats[S_FLIPPED];
+    res->exact_mismatches = m.dim == 1 ? icnt[C_MISM] : 0;
+    res->n_colours = m.ncol;
+    res->schedule_used = r->schedule;
+    return MCS_OK;
+}
+
+int replica_spins(Replica *r, std::vector<double> &out)
+{
+    const HostModel &m = r->hm;
+    out.assign((size_t)3 * m.N, 0.0);
+    unsigned char *b = (unsigned char *)r->arena;
+    if (m.dim == 1) {
+        std::vector<int8_t> s(m.N);
+        CUDA_TRY(cudaMemcpy(s.data(), b + r->spins_off, m.N, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < m.N; ++i) out[3 * i] = fabs(m.sval[m.pos[i]]) * s[m.pos[i]];
+    } else {
+        std::vector<float> s((size_t)m.dim * r->rep.spad);
+        CUDA_TRY(cudaMemcpy(s.data(), b + r->spins_off, s.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < m.N; ++i)
+            for (int c = 0; c < m.dim; ++c) out[3 * i + c] = s[(size_t)c * r->rep.spad + m.pos[i]];
+    }
+    return MCS_OK;
+}
+
+int replica_set_spins(Replica *r, const double *in)
+{
+    const HostModel &m = r->hm;
+    unsigned char *b = (unsigned char *)r->arena;
+    if (m.dim == 1) {
+        std::vector<int8_t> s(m.N);
+        for (int i = 0; i < m.N; ++i) s[m.pos[i]] = in[3 * i] < 0 ? -1 : 1;
+        CUDA_TRY(cudaMemcpy(b + r->spins_off, s.data(), m.N, cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> s((size_t)m.dim * r->rep.spad, 0.f);
+        for (int i = 0; i < m.N; ++i)
+            for (int c = 0; c < m.dim; ++c) s[(size_t)c * r->rep.spad + m.pos[i]] = (float)in[3 * i + c];
+        CUDA_TRY(cudaMemcpy(b + r->spins_off, s.data(), s.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    return MCS_OK;
+}
+
+// ------------------------------------------------------------------ batch execution
+Batch::~Batch()
+{
+    if (d_reps) cudaFree(d_reps);
+    if (d_scratch) cudaFree(d_scratch);
+    if (stream) cudaStreamDestroy(stream);
+    if (stream2) cudaStreamDestroy(stream2);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+}
+
+int Batch::init(int dev)
+{
+    device = dev;
+    return MCS_OK;
+}
+
+int Batch::ensure_streams()
+{
+    if (stream) return MCS_OK;
+    CUDA_TRY(cudaSetDevice(device));
+    CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreate(&ev0));
+    CUDA_TRY(cudaEventCreate(&ev1));
+    return MCS_OK;
+}
+
+int Batch::add(const mcs_problem *p, const mcs_options *o, int *idx)
+{
+    std::unique_ptr<Replica> r(new Replica());
+    r->device = device;
+    int rc = build_replica(p, o, r.get());
+    if (rc != MCS_OK) return rc;
+    replicas.push_back(std::move(r));
+    if (idx) *idx = (int)replicas.size() - 1;
+    return MCS_OK;
+}
+
+static int choose_schedule(const Replica &r, int requested, int max_smem)
+{
+    if (requested == 1) return 1;            // plain
+    if (requested == 3) return 3;            // tiled
+    long long need = resident_smem_bytes(r.rep);
+    if (r.hm.alg == 0) {
+        if (need <= max_smem) return 2;
+        return 3;
+    }
+    return 3;
+}
+
+struct TiledPlan {
+    std::vector<int> ids;                       // replica ordinals
+    int dim = 0, geom = 0, maxcol = 0;
+    std::vector<std::vector<Item>> sweep_items; // per colour
+    std::vector<Item> meas_items;
+    std::vector<int> item_off, mitem_off;       // per replica (in plan order)
+    int nslots = 0;
+};
+
+int Batch::run_tiled(std::vector<int> &ids, int dim, int geom, bool use_graph, cudaStream_t st,
+                     std::vector<void *> &allocs)
+{
+    TiledPlan P;
+    P.ids = ids; P.dim = dim; P.geom = geom;
+    for (int id : ids) P.maxcol = std::max(P.maxcol, replicas[id]->hm.ncol);
+    P.sweep_items.assign(P.maxcol, {});
+    // slot ranges per replica: all its sweep items over every colour
+    int slot = 0;
+    const int per = dim == 1 ? 4 * 256 : 256;
+    P.item_off.push_back(0);
+    for (int id : ids) {
+        const HostModel &m = replicas[id]->hm;
+        for (int c = 0; c < m.ncol; ++c) {
+            int n = m.col_start[c + 1] - m.col_start[c];
+            for (int b0 = 0; b0 < n; b0 += per) {
+                Item it; it.rep = id; it.begin = b0; it.end = std::min(n, b0 + per); it.slot = slot++;
+                P.sweep_items[c].push_back(it);
+            }
+        }
+        P.item_off.push_back(slot);
+    }
+    P.nslots = slot;
+    const int mper = 512;
+    P.mitem_off.push_back(0);
+    for (int id : ids) {
+        const HostModel &m = replicas[id]->hm;
+        int V = std::max(std::max(m.N, m.nlat), std::max(m.n_rorb, m.ncirc));
+        for (int b0 = 0; b0 < V; b0 += mper) {
+            Item it; it.rep = id; it.begin = b0; it.end = std::min(V, b0 + mper); it.slot = 0;
+            P.meas_items.push_back(it);
+        }
+        P.mitem_off.push_back((int)P.meas_items.size());
+    }
+    // device buffers
+    size_t nsw = 0;
+    for (auto &v : P.sweep_items) nsw += v.size();
+    std::vector<Item> all_sw;
+    std::vector<size_t> cofs;
+    for (auto &v : P.sweep_items) { cofs.push_back(all_sw.size()); all_sw.insert(all_sw.end(), v.begin(), v.end()); }
+    Item *d_sw = nullptr, *d_mi = nullptr;
+    int *d_ids = nullptr, *d_ioff = nullptr, *d_moff = nullptr;
+    double *d_dE = nullptr, *d_fp = nullptr;
+    long long *d_ip = nullptr;
+    CUDA_TRY(cudaMalloc(&d_sw, std::max<size_t>(1, all_sw.size()) * sizeof(Item)));
+    CUDA_TRY(cudaMalloc(&d_mi, std::max<size_t>(1, P.meas_items.size()) * sizeof(Item)));
+    CUDA_TRY(cudaMalloc(&d_ids, ids.size() * sizeof(int)));
+    CUDA_TRY(cudaMalloc(&d_ioff, P.item_off.size() * sizeof(int)));
+    CUDA_TRY(cudaMalloc(&d_moff, P.mitem_off.size() * sizeof(int)));
+    CUDA_TRY(cudaMalloc(&d_dE, std::max(1, P.nslots) * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&d_ip, std::max(1, P.nslots) * 9 * sizeof(long long)));
+    CUDA_TRY(cudaMalloc(&d_fp, std::max<size_t>(1, P.meas_items.size()) * F_NON * sizeof(double)));
+    allocs.insert(allocs.end(), {d_sw, d_mi, d_ids, d_ioff, d_moff, d_dE, d_ip, d_fp});
+    CUDA_TRY(cudaMemcpyAsync(d_sw, all_sw.data(), all_sw.size() * sizeof(Item), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_mi, P.meas_items.data(), P.meas_items.size() * sizeof(Item), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_ids, ids.data(), ids.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_ioff, P.item_off.data(), P.item_off.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_moff, P.mitem_off.data(), P.mitem_off.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemsetAsync(d_dE, 0, std::max(1, P.nslots) * sizeof(double), st));
+    CUDA_TRY(cudaMemsetAsync(d_ip, 0, std::max(1, P.nslots) * 9 * sizeof(long long), st));
+    // the sweep kernel writes its partial at item.colour (slot); pass the colour separately
+    long long steps = 0;
+    for (int id : ids) steps = std::max(steps, replicas[id]->hm.units_total);
+    auto one_unit = [&](cudaStream_t s) -> cudaError_t {
+        for (int c = 0; c < P.maxcol; ++c) {
+            cudaError_t e = launch_tiled_sweep(dim, geom, d_reps, d_sw + cofs[c], (int)P.sweep_items[c].size(), c,
+                                               d_dE, d_ip, dim == 1 ? 256 : 256, s);
+            if (e != cudaSuccess) return e;
+            launches++;
+        }
+        cudaError_t e = launch_tiled_measure(dim, geom, d_reps, d_mi, (int)P.meas_items.size(), d_fp, 256, s);
+        if (e != cudaSuccess) return e;
+        e = launch_tiled_finalize_dim(dim, d_reps, d_ids, (int)ids.size(), d_ioff, d_dE, d_ip, d_moff, d_fp, s);
+        launches += 2;
+        return e;
+    };
+    if (!use_graph || steps < 8) {
+        for (long long u = 0; u < steps; ++u) CUDA_TRY(one_unit(st));
+        return MCS_OK;
+    }
+    const int K = (int)std::min<long long>(steps, 32);
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    long long saved = launches;
+    for (int k = 0; k < K; ++k) {
+        cudaError_t e = one_unit(st);
+        if (e != cudaSuccess) {
+            cudaStreamEndCapture(st, &graph);
+            set_error(std::string("CUDA error during capture: ") + cudaGetErrorString(e));
+            return MCS_ECUDA;
+        }
+    }
+    CUDA_TRY(cudaStreamEndCapture(st, &graph));
+    long long per_graph = launches - saved;
+    launches = saved;
+    CUDA_TRY(cudaGraphInstantiate(&exec, graph, 0));
+    long long done = 0;
+    while (done + K <= steps) {
+        CUDA_TRY(cudaGraphLaunch(exec, st));
+        launches += per_graph;
+        done += K;
+    }
+    for (; done < steps; ++done) CUDA_TRY(one_unit(st));
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    return MCS_OK;
+}
+
+int Batch::run()
+{
+    int src = ensure_streams();
+    if (src != MCS_OK) return src;
+    const int nrep = (int)replicas.size();
+    if (nrep == 0) return MCS_OK;
+    const int max_smem = resident_max_smem();
+    std::vector<Rep> host(nrep);
+    for (int i = 0; i < nrep; ++i) {
+        Replica &r = *replicas[i];
+        r.schedule = choose_schedule(r, r.requested_schedule, max_smem);
+        host[i] = r.rep;
+    }
+    if (d_reps) cudaFree(d_reps);
+    CUDA_TRY(cudaMalloc(&d_reps, nrep * sizeof(Rep)));
+    CUDA_TRY(cudaMemcpy(d_reps, host.data(), nrep * sizeof(Rep), cudaMemcpyHostToDevice));
+    launches = 0;
+    std::vector<void *> allocs;
+    auto cleanup = [&]() { for (void *p : allocs) cudaFree(p); };
+    CUDA_TRY(cudaEventRecord(ev0, stream));
+    // initial energies / exact sums
+    {
+        std::vector<int> all(nrep);
+        for (int i = 0; i < nrep; ++i) all[i] = i;
+        int *d_all = nullptr;
+        CUDA_TRY(cudaMalloc(&d_all, nrep * sizeof(int)));
+        allocs.push_back(d_all);
+        CUDA_TRY(cudaMemcpyAsync(d_all, all.data(), nrep * sizeof(int), cudaMemcpyHostToDevice, stream));
+        for (int d = 1; d <= 3; ++d)
+            for (int g = 0; g <= 1; ++g) {
+                bool any = false;
+                for (auto &r : replicas) any |= (r->hm.dim == d && r->hm.geom == g);
+                if (!any) continue;
+                cudaError_t e = launch_init_state_dg(d, g, d_reps, d_all, nrep, stream);
+                if (e != cudaSuccess) { cleanup(); set_error(cudaGetErrorString(e)); return MCS_ECUDA; }
+                launches++;
+            }
+    }
+    // resident groups
+    for (int d = 1; d <= 3; ++d)
+        for (int g = 0; g <= 1; ++g) {
+            std::vector<int> ids;
+            long long maxu = 0, maxn = 0;
+            size_t smem = 0;
+            int maxcs = 0;
+            for (int i = 0; i < nrep; ++i) {
+                Replica &r = *replicas[i];
+                if (r.schedule != 2 || r.hm.dim != d || r.hm.geom != g || r.hm.alg != 0) continue;
+                ids.push_back(i);
+                maxu = std::max(maxu, r.hm.units_total);
+                maxn = std::max<long long>(maxn, r.hm.N);
+                smem = std::max<size_t>(smem, (size_t)resident_smem_bytes(r.rep));
+                for (int c = 0; c < r.hm.ncol; ++c)
+                    maxcs = std::max(maxcs, r.hm.col_start[c + 1] - r.hm.col_start[c]);
+            }
+            if (ids.empty()) continue;
+            int *d_ids = nullptr;
+            CUDA_TRY(cudaMalloc(&d_ids, ids.size() * sizeof(int)));
+            allocs.push_back(d_ids);
+            CUDA_TRY(cudaMemcpyAsync(d_ids, ids.data(), ids.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
+            int work = d == 1 ? (maxcs + 3) / 4 : maxcs;
+            int threads = std::min(1024, std::max(64, ((work + 31) / 32) * 32));
+            if (threads_override > 0) threads = threads_override;
+            long long chunk = std::max<long long>(1, (1LL << 28) / std::max<long long>(1, maxn));
+            if (chunk_override > 0) chunk = chunk_override;
+            for (long long u = 0; u < maxu; u += chunk) {
+                cudaError_t e = launch_resident_metro(d, g, d_reps, d_ids, (int)ids.size(), threads, smem, chunk, stream);
+                if (e != cudaSuccess) { cleanup(); set_error(std::string("resident launch: ") + cudaGetErrorString(e)); return MCS_ECUDA; }
+                launches++;
+            }
+        }
+    // tiled / plain groups
+    for (int d = 1; d <= 3; ++d)
+        for (int g = 0; g <= 1; ++g) {
+            std::vector<int> ids;
+            for (int i = 0; i < nrep; ++i) {
+                Replica &r = *replicas[i];
+                if (r.schedule == 3 && r.hm.dim == d && r.hm.geom == g && r.hm.alg == 0) ids.push_back(i);
+            }
+            if (!ids.empty()) {
+                int rc = run_tiled(ids, d, g, true, stream, allocs);
+                if (rc != MCS_OK) { cleanup(); return rc; }
+            }
+            for (int i = 0; i < nrep; ++i) {
+                Replica &r = *replicas[i];
+                if (r.schedule == 1 && r.hm.dim == d && r.hm.geom == g && r.hm.alg == 0) {
+                    std::vector<int> one = {i};
+                    int rc = run_tiled(one, d, g, false, stream, allocs);
+                    if (rc != MCS_OK) { cleanup(); return rc; }
+                }
+            }
+        }
+    // Wolff replicas
+    for (int i = 0; i < nrep; ++i)
+        if (replicas[i]->hm.alg == 1) {
+            cleanup();
+            set_error("Wolff updates are not built in this engine version");
+            return MCS_EUNSUPPORTED;
+        }
+    CUDA_TRY(cudaEventRecord(ev1, stream));
+    cudaError_t e = cudaStreamSynchronize(stream);
+    cleanup();
+    if (e != cudaSuccess) { set_error(std::string("CUDA error in run: ") + cudaGetErrorString(e)); return MCS_ECUDA; }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    device_ms = ms;
+    CUDA_TRY(cudaMemcpy(host.data(), d_reps, nrep * sizeof(Rep), cudaMemcpyDeviceToHost));
+    final_reps = host;
+    site_updates = 0;
+    for (int i = 0; i < nrep; ++i) {
+        long long st[S_NSTAT];
+        CUDA_TRY(cudaMemcpy(st, (unsigned char *)replicas[i]->arena + replicas[i]->stats_off, sizeof st, cudaMemcpyDeviceToHost));
+        site_updates += replicas[i]->hm.alg == 0 ? st[S_VISITS] : st[S_FLIPPED];
+    }
+    return MCS_OK;
+}
+
+int Batch::result(int i, mcs_result *res)
+{
+    if (i < 0 || i >= (int)replicas.size()) { set_error("replica index out of range"); return MCS_EINVAL; }
+    if ((int)final_reps.size() != (int)replicas.size()) { set_error("batch has not been run"); return MCS_EINVAL; }
+    int rc = replica_results(replicas[i].get(), final_reps[i], res);
+    if (rc == MCS_OK && res) res->device_ms = device_ms;
+    return rc;
+}
+
+}  // namespace mcs
+
+// ====================================================================== C ABI
+using namespace mcs;
+
+extern "C" {
+
+const char *mcs_last_error(void) { return get_error().c_str(); }
+int mcs_abi_version(void) { return 1; }
+const char *mcs_build_info(void)
+{
+    return "mcsgpu: sm_103a Monte Carlo spin-lattice engine (Ising/XY/Heisenberg; Metropolis colour sweeps, "
+           "Philox4x32-10, FP32 updates with FP64 accumulation)";
+}
+
+int mcs_solve(const mcs_problem *problem, const mcs_options *options, mcs_result *result)
+{
+    try {
+        mcs_options def;
+        memset(&def, 0, sizeof def);
+        if (!options) options = &def;
+        Batch b;
+        int rc = b.init(options->device);
+        if (rc != MCS_OK) return rc;
+        int idx = 0;
+        rc = b.add(problem, options, &idx);
+        if (rc != MCS_OK) return rc;
+        rc = b.run();
+        if (rc != MCS_OK) return rc;
+        return b.result(idx, result);
+    } catch (const std::exception &e) {
+        set_error(std::string("exception: ") + e.what());
+        return MCS_ECUDA;
+    }
+}
+
+struct mcs_batch {
+    mcs::Batch b;
+};
+
+int mcs_batch_create(int32_t device, mcs_batch **out)
+{
+    if (!out) return MCS_EINVAL;
+    mcs_batch *x = new mcs_batch();
+    int rc = x->b.init(device);
+    if (rc != MCS_OK) { delete x; return rc; }
+    *out = x;
+    return MCS_OK;
+}
+int mcs_batch_add(mcs_batch *b, const mcs_problem *problem, const mcs_options *options, int32_t *replica)
+{
+    if (!b) return MCS_EINVAL;
+    mcs_options def;
+    memset(&def, 0, sizeof def);
+    int idx = 0;
+    int rc = b->b.add(problem, options ? options : &def, &idx);
+    if (replica) *replica = idx;
+    return rc;
+}
+int mcs_batch_run(mcs_batch *b) { return b ? b->b.run() : MCS_EINVAL; }
+int mcs_batch_result(mcs_batch *b, int32_t replica, mcs_result *result) { return b ? b->b.result(replica, result) : MCS_EINVAL; }
+int mcs_batch_stats(mcs_batch *b, double *device_ms, int64_t *site_updates, int32_t *launches)
+{
+    if (!b) return MCS_EINVAL;
+    if (device_ms) *device_ms = b->b.device_ms;
+    if (site_updates) *site_updates = b->b.site_updates;
+    if (launches) *launches = (int32_t)b->b.launches;
+    return MCS_OK;
+}
+void mcs_batch_destroy(mcs_batch *b) { delete b; }
+
+}  // extern "C"

@@ -1,0 +1,64 @@
+// mcs_engine.h -- host engine objects behind the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/mcsgpu.h"
+#include "mcs_internal.h"
+#include "mcs_model.h"
+
+namespace mcs {
+
+void set_error(const std::string &s);
+const std::string &get_error();
+
+// One solve on the device.
+struct Replica {
+    HostModel hm;
+    Rep rep;                 // descriptor (device pointers into the arena)
+    void *arena = nullptr;   // one device allocation per replica
+    size_t bytes = 0;
+    size_t acc_off = 0, icnt_off = 0, stats_off = 0, series_off = 0, frames_off = 0, spins_off = 0;
+    size_t nacc = 0;
+    int schedule = 0;        // 1 plain, 2 resident, 3 tiled
+    int requested_schedule = 0;
+    int record_series = 0;
+    int recheck = 32;
+    int device = 0;
+    ~Replica();
+};
+
+int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r);
+int replica_results(Replica *r, const Rep &Rfinal, mcs_result *res);
+int replica_spins(Replica *r, std::vector<double> &out);
+int replica_set_spins(Replica *r, const double *in);
+size_t replica_acc_count(const HostModel &m);
+
+// Many replicas of uneven sizes run together.
+struct Batch {
+    int device = 0;
+    std::vector<std::unique_ptr<Replica>> replicas;
+    Rep *d_reps = nullptr;
+    void *d_scratch = nullptr;
+    cudaStream_t stream = nullptr, stream2 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double device_ms = 0;
+    long long site_updates = 0;
+    long long launches = 0;
+    int threads_override = 0;
+    long long chunk_override = 0;
+    std::vector<Rep> final_reps;
+    ~Batch();
+    int init(int dev);
+    int ensure_streams();
+    int add(const mcs_problem *p, const mcs_options *o, int *idx);
+    int run();
+    int result(int i, mcs_result *res);
+    int run_tiled(std::vector<int> &ids, int dim, int geom, bool use_graph, cudaStream_t st,
+                  std::vector<void *> &allocs);
+};
+
+}  // namespace mcs

@@ -1,0 +1,509 @@
+// mcs_kernels.cu -- sm_103a kernels of the Monte Carlo engine.
+//
+// Schedules
+//   resident : one CTA owns one replica; its whole lattice, coupling tables and
+//              reduction scratch live in shared memory; the CTA runs many sweeps
+//              (and the measurements between them) per launch.  Lattices up to
+//              ~220 KB of spin state (Heisenberg L=128, XY L~165, Ising L~470).
+//   tiled    : the lattice lives in global memory (L2-resident for the sizes of
+//              interest); one launch per colour updates that colour of every
+//              replica of the group, tile by tile; a measurement launch writes
+//              per-tile partial sums and a finalize launch (one CTA per replica)
+//              folds them in a fixed order.
+// Both schedules call the same per-site update, so a replica's spin trajectory
+// does not depend on the schedule or on the other replicas of the batch.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mcs_device.cuh"
+#include "mcs_internal.h"
+
+namespace mcs {
+
+static __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+#define MCS_RED_DOUBLES (32 * 12 + 16)
+
+struct SmemLayout {
+    size_t spins, tables, red, F, redl, Fi, total;
+};
+__host__ __device__ inline SmemLayout smem_layout(const Rep &R)
+{
+    SmemLayout L;
+    size_t off = 0;
+    L.spins = off;
+    if (R.dim == 1) off += align16((size_t)R.N);
+    else off += align16((size_t)R.dim * R.N * sizeof(float));
+    L.tables = off;
+    if (R.dim == 1) off += align16((size_t)R.nite * sizeof(IsEntry));
+    else off += align16((size_t)R.njc * 9 * sizeof(float) + (size_t)R.ndc * 3 * sizeof(float));
+    L.red = off; off += MCS_RED_DOUBLES * sizeof(double);
+    L.F = off; off += F_NON * sizeof(double);
+    L.redl = off; off += 32 * (MCS_MAXT + MCS_MAXC + 1) * sizeof(long long);
+    L.Fi = off; off += 16 * sizeof(long long);
+    L.total = off;
+    return L;
+}
+
+long long resident_smem_bytes(const Rep &r) { return (long long)smem_layout(r).total; }
+
+int resident_max_smem()
+{
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return v;
+}
+
+// copy the replica descriptor into shared memory with all threads
+__device__ __forceinline__ void load_rep(Rep &dst, const Rep *src)
+{
+    const int *s = (const int *)src;
+    int *d = (int *)&dst;
+    for (int i = threadIdx.x; i < (int)(sizeof(Rep) / 4); i += blockDim.x) d[i] = s[i];
+    __syncthreads();
+}
+
+// ======================================================================= resident Metropolis
+template <int DIM, int GEOM>
+__global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *ids, long long max_units)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ Rep R;
+    Rep *Rg = reps + ids[blockIdx.x];
+    load_rep(R, Rg);
+    if (R.u >= R.units_total) return;
+    const SmemLayout L = smem_layout(R);
+    const int tid = threadIdx.x, bd = blockDim.x, N = R.N;
+    double *red = (double *)(smem + L.red);
+    double *F = (double *)(smem + L.F);
+    long long *redl = (long long *)(smem + L.redl);
+    long long *Fi = (long long *)(smem + L.Fi);
+    Spins S;
+    Spins G = spins_global(R);
+    IsEntry *itab = (IsEntry *)(smem + L.tables);
+    float *jt = (float *)(smem + L.tables);
+    float *dt = jt + R.njc * 9;
+    if (DIM == 1) {
+        S.s = (signed char *)(smem + L.spins);
+        for (int v = tid; v < N; v += bd) S.s[v] = G.s[v];
+        for (int k = tid; k < R.nite; k += bd) itab[k] = R.itab[k];
+    } else {
+        S.x = (float *)(smem + L.spins);
+        S.y = S.x + N;
+        S.z = S.y + N;
+        for (int v = tid; v < N; v += bd) {
+            S.x[v] = G.x[v]; S.y[v] = G.y[v];
+            if (DIM == 3) S.z[v] = G.z[v];
+        }
+        for (int k = tid; k < R.njc * 9; k += bd) jt[k] = R.jtab[k];
+        for (int k = tid; k < R.ndc * 3; k += bd) dt[k] = R.dtab[k];
+    }
+    __syncthreads();
+
+    int dn[MCS_MAXC] = {0, 0, 0, 0}, dm[MCS_MAXT] = {0, 0, 0, 0};
+    long long nacc = 0;
+    double dEd = 0.0;
+    const float beta = R.beta, h = R.h;
+
+    auto fold = [&]() {
+        if (DIM == 1) {
+            long long c[MCS_MAXC + MCS_MAXT + 1];
+#pragma unroll
+            for (int k = 0; k < MCS_MAXC; ++k) c[k] = dn[k];
+#pragma unroll
+            for (int k = 0; k < MCS_MAXT; ++k) c[MCS_MAXC + k] = dm[k];
+            c[MCS_MAXC + MCS_MAXT] = nacc;
+            block_sum_ll<MCS_MAXC + MCS_MAXT + 1>(c, redl, Fi);
+            if (tid == 0) {
+                for (int k = 0; k < MCS_MAXC; ++k) R.icnt[C_DN + k] += -4 * Fi[k];
+                for (int k = 0; k < MCS_MAXT; ++k) R.icnt[C_DM + k] += -2 * Fi[MCS_MAXC + k];
+                R.stats[S_ACCEPT] += Fi[MCS_MAXC + MCS_MAXT];
+            }
+#pragma unroll
+            for (int k = 0; k < MCS_MAXC; ++k) dn[k] = 0;
+#pragma unroll
+            for (int k = 0; k < MCS_MAXT; ++k) dm[k] = 0;
+        } else {
+            double c[2] = {dEd, (double)nacc};
+            block_sum<2>(c, red, F);
+            if (tid == 0) {
+                R.acc[A_ECUR] += F[0];
+                R.stats[S_ACCEPT] += (long long)F[1];
+            }
+            dEd = 0.0;
+        }
+        nacc = 0;
+        __syncthreads();
+    };
+
+    long long u = R.u;
+    const long long uend = min(R.units_total, u + max_units);
+    for (; u < uend; ++u) {
+        if (DIM == 1 && u == R.units_thermal) {
+            fold();
+            if (tid == 0) {
+                double Einc = 0;
+                for (int c = 0; c < R.nclass; ++c) Einc += 0.5 * R.Q[c] * (double)R.icnt[C_DN + c];
+                for (int t = 0; t < R.ntype; ++t) Einc -= R.hd * R.Stype[t] * (double)R.icnt[C_DM + t];
+                R.acc[B_EMEAS0] = Einc;
+            }
+        }
+        const long long t = R.u0 + u;
+        for (int c = 0; c < R.ncol; ++c) {
+            const int c0 = R.col_start[c], nc = R.col_start[c + 1] - c0;
+            if (DIM == 1) {
+                const int nq = (nc + 3) >> 2;
+                for (int q = tid; q < nq; q += bd) {
+                    uint4 w = philox_t((uint32_t)q, t, (uint32_t)c, R.seed);
+                    uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        int k = 4 * q + e;
+                        if (k < nc) {
+                            int before = dm[0] + dm[1] + dm[2] + dm[3];
+                            ising_trial<GEOM>(R, itab, S.s, c0 + k, ws[e], dn, dm);
+                            nacc += (dm[0] + dm[1] + dm[2] + dm[3]) != before;
+                        }
+                    }
+                }
+            } else {
+                float dEf = 0.f;
+                for (int k = tid; k < nc; k += bd) {
+                    uint4 w = philox_t((uint32_t)k, t, (uint32_t)c, R.seed);
+                    float dE;
+                    if (on_trial<DIM, GEOM>(R, jt, dt, S, c0 + k, w, beta, h, &dE)) { dEf += dE; ++nacc; }
+                }
+                dEd += (double)dEf;
+            }
+            __syncthreads();
+        }
+        if (measures_after(R, u)) {
+            fold();
+            const long long m = R.m;
+            if (DIM == 1) {
+                is_frame<GEOM>(R, itab, S.s, 0, max(N, max(R.nlat, R.n_rorb)), m, red, F, redl, Fi);
+                if (tid == 0) {
+                    if (R.alg == 1 && u >= R.units_thermal) R.icnt[C_ACC_MEAS] = 1;
+                    is_accumulate(R, F, Fi, S.s[R.last_site], m);
+                }
+            } else {
+                const bool efull = (m % R.recheck) == 0;
+                on_frame<DIM, GEOM>(R, jt, dt, S, 0, max(max(N, R.nlat), max(R.n_rorb, R.ncirc)), efull, red, F);
+                if (tid == 0) {
+                    if (efull) {
+                        double Ef = F[F_EFB] / 2 + F[F_EFO];
+                        double d = fabs(R.acc[A_ECUR] - Ef);
+                        if (d > R.acc[A_DRIFT]) R.acc[A_DRIFT] = d;
+                        R.acc[A_ECUR] = Ef;
+                    }
+                    on_accumulate<DIM>(R, F, R.acc[A_ECUR], m);
+                }
+            }
+            if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) {
+                float *fb = R.frame_buf + (size_t)R.frames_written * N * 3;
+                for (int v = tid; v < N; v += bd) {
+                    if (DIM == 1) { fb[3 * v] = (float)(R.Stype[R.stype ? R.stype[v] : 0] * S.s[v]); fb[3 * v + 1] = 0; fb[3 * v + 2] = 0; }
+                    else { fb[3 * v] = S.x[v]; fb[3 * v + 1] = S.y[v]; fb[3 * v + 2] = DIM == 3 ? S.z[v] : 0.f; }
+                }
+            }
+            __syncthreads();
+            if (tid == 0) {
+                if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) R.frames_written++;
+                R.m = m + 1;
+            }
+            __syncthreads();
+        }
+    }
+    fold();
+    for (int v = tid; v < N; v += bd) {
+        if (DIM == 1) G.s[v] = S.s[v];
+        else {
+            G.x[v] = S.x[v]; G.y[v] = S.y[v];
+            if (DIM == 3) G.z[v] = S.z[v];
+        }
+    }
+    if (tid == 0) {
+        R.stats[S_VISITS] += (uend - R.u) * (long long)N;
+        Rg->u = uend;
+        Rg->m = R.m;
+        Rg->frames_written = R.frames_written;
+    }
+}
+
+// ======================================================================= tiled Metropolis
+template <int DIM, int GEOM>
+__global__ void __launch_bounds__(256) k_tiled_sweep(Rep *reps, const Item *items, int colour, double *dEpart,
+                                                     long long *ipart)
+{
+    __shared__ double red[32 * 2 + 4];
+    __shared__ long long redl[32 * 9 + 9];
+    const Item it = items[blockIdx.x];
+    const Rep &R = reps[it.rep];
+    if (R.u >= R.units_total) return;
+    const long long t = R.u0 + R.u;
+    const int c = colour, c0 = R.col_start[c];
+    Spins S = spins_global(R);
+    const int tid = threadIdx.x;
+    if (DIM == 1) {
+        int dn[MCS_MAXC] = {0, 0, 0, 0}, dm[MCS_MAXT] = {0, 0, 0, 0};
+        long long nacc = 0;
+        const int k0 = it.begin + 4 * tid;
+        if (k0 < it.end) {
+            uint4 w = philox_t((uint32_t)(k0 >> 2), t, (uint32_t)c, R.seed);
+            uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                int k = k0 + e;
+                if (k < it.end) {
+                    int before = dm[0] + dm[1] + dm[2] + dm[3];
+                    ising_trial<GEOM>(R, R.itab, S.s, c0 + k, ws[e], dn, dm);
+                    nacc += (dm[0] + dm[1] + dm[2] + dm[3]) != before;
+                }
+            }
+        }
+        long long v[9] = {dn[0], dn[1], dn[2], dn[3], dm[0], dm[1], dm[2], dm[3], nacc};
+        block_sum_ll<9>(v, redl, redl + 32 * 9);
+        if (tid < 9) ipart[(size_t)it.slot * 9 + tid] = redl[32 * 9 + tid];
+    } else {
+        float dEf = 0.f;
+        double nacc = 0;
+        const int k = it.begin + tid;
+        if (k < it.end) {
+            uint4 w = philox_t((uint32_t)k, t, (uint32_t)c, R.seed);
+            float dE;
+            if (on_trial<DIM, GEOM>(R, R.jtab, R.dtab, S, c0 + k, w, R.beta, R.h, &dE)) { dEf = dE; nacc = 1; }
+        }
+        double v[2] = {(double)dEf, nacc};
+        block_sum<2>(v, red, red + 64);
+        if (tid == 0) {
+            dEpart[it.slot] = red[64];
+            ipart[(size_t)it.slot * 9 + 8] = (long long)red[65];
+        }
+    }
+}
+
+#define MCS_FPART 24  // doubles per measurement tile (Ising: 4 + 8 ints; O(n): compact F)
+
+// O(n) tile partial: the F frame restricted to the tile's virtual index range.
+template <int DIM, int GEOM>
+__global__ void __launch_bounds__(256) k_tiled_measure(Rep *reps, const Item *items, double *fpart)
+{
+    __shared__ double red[MCS_RED_DOUBLES];
+    __shared__ double F[F_NON];
+    __shared__ long long redl[32 * 9];
+    __shared__ long long Fi[16];
+    const Item it = items[blockIdx.x];
+    const Rep &R = reps[it.rep];
+    if (R.u >= R.units_total || !measures_after(R, R.u)) return;
+    Spins S = spins_global(R);
+    double *out = fpart + (size_t)blockIdx.x * F_NON;
+    if (DIM == 1) {
+        is_frame<GEOM>(R, R.itab, S.s, it.begin, it.end, R.m, red, F, redl, Fi);
+        if (threadIdx.x < 4) out[threadIdx.x] = F[threadIdx.x];
+        if (threadIdx.x < MCS_MAXT + MCS_MAXC) out[4 + threadIdx.x] = (double)Fi[threadIdx.x];
+    } else {
+        const bool efull = (R.m % R.recheck) == 0;
+        for (int k = threadIdx.x; k < F_NON; k += blockDim.x) F[k] = 0.0;
+        __syncthreads();
+        on_frame<DIM, GEOM>(R, R.jtab, R.dtab, S, it.begin, it.end, efull, red, F);
+        for (int k = threadIdx.x; k < F_NON; k += blockDim.x) out[k] = F[k];
+    }
+}
+
+// One CTA per replica: fold sweep partials, measurement partials, advance.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_tiled_finalize(Rep *reps, const int *ids, const int *item_off, double *dEpart,
+                                                        long long *ipart, const int *mitem_off, double *fpart)
+{
+    __shared__ double red[MCS_RED_DOUBLES];
+    __shared__ double F[F_NON];
+    __shared__ long long redl[32 * 9 + 9];
+    __shared__ long long Fi[16];
+    __shared__ int meas;
+    const int r = ids[blockIdx.x];
+    Rep &R = reps[r];
+    if (R.u >= R.units_total) return;
+    const int tid = threadIdx.x;
+    const int i0 = item_off[blockIdx.x], i1 = item_off[blockIdx.x + 1];
+    const long long u = R.u;
+    if (DIM == 1) {
+        long long v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int i = i0 + tid; i < i1; i += blockDim.x)
+            for (int k = 0; k < 9; ++k) v[k] += ipart[(size_t)i * 9 + k];
+        block_sum_ll<9>(v, redl, redl + 32 * 9);
+        if (tid == 0) {
+            for (int k = 0; k < MCS_MAXC; ++k) R.icnt[C_DN + k] += -4 * redl[32 * 9 + k];
+            for (int k = 0; k < MCS_MAXT; ++k) R.icnt[C_DM + k] += -2 * redl[32 * 9 + MCS_MAXC + k];
+            R.stats[S_ACCEPT] += redl[32 * 9 + 8];
+            if (R.alg == 0 && u + 1 == R.units_thermal) {
+                double Einc = 0;
+                for (int c = 0; c < R.nclass; ++c) Einc += 0.5 * R.Q[c] * (double)R.icnt[C_DN + c];
+                for (int t = 0; t < R.ntype; ++t) Einc -= R.hd * R.Stype[t] * (double)R.icnt[C_DM + t];
+                R.acc[B_EMEAS0] = Einc;
+            }
+        }
+    } else {
+        double v[2] = {0.0, 0.0};
+        for (int i = i0 + tid; i < i1; i += blockDim.x) { v[0] += dEpart[i]; v[1] += (double)ipart[(size_t)i * 9 + 8]; }
+        block_sum<2>(v, red, F);
+        if (tid == 0) { R.acc[A_ECUR] += F[0]; R.stats[S_ACCEPT] += (long long)F[1]; }
+    }
+    if (tid == 0) meas = measures_after(R, u);
+    __syncthreads();
+    if (meas) {
+        const int m0 = mitem_off[blockIdx.x], m1 = mitem_off[blockIdx.x + 1];
+        const int nf = DIM == 1 ? 4 + MCS_MAXT + MCS_MAXC : F_NON;
+        for (int k = tid; k < nf; k += blockDim.x) {
+            double a = 0.0;
+            for (int i = m0; i < m1; ++i) a += fpart[(size_t)i * F_NON + k];
+            F[k] = a;
+        }
+        __syncthreads();
+        const long long m = R.m;
+        if (tid == 0) {
+            if (DIM == 1) {
+                for (int k = 0; k < MCS_MAXT + MCS_MAXC; ++k) Fi[k] = (long long)F[4 + k];
+                signed char *s = (signed char *)R.spins;
+                is_accumulate(R, F, Fi, s[R.last_site], m);
+            } else {
+                if ((m % R.recheck) == 0) {
+                    double Ef = F[F_EFB] / 2 + F[F_EFO];
+                    double d = fabs(R.acc[A_ECUR] - Ef);
+                    if (d > R.acc[A_DRIFT]) R.acc[A_DRIFT] = d;
+                    R.acc[A_ECUR] = Ef;
+                }
+                if (DIM == 2) on_accumulate<2>(R, F, R.acc[A_ECUR], m);
+                else on_accumulate<3>(R, F, R.acc[A_ECUR], m);
+            }
+        }
+        if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) {
+            float *fb = R.frame_buf + (size_t)R.frames_written * R.N * 3;
+            Spins S = spins_global(R);
+            for (int v = tid; v < R.N; v += blockDim.x) {
+                if (DIM == 1) { fb[3 * v] = (float)(R.Stype[R.stype ? R.stype[v] : 0] * S.s[v]); fb[3 * v + 1] = 0; fb[3 * v + 2] = 0; }
+                else { fb[3 * v] = S.x[v]; fb[3 * v + 1] = S.y[v]; fb[3 * v + 2] = DIM == 3 ? S.z[v] : 0.f; }
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) R.frames_written++;
+            R.m = m + 1;
+        }
+    }
+    if (tid == 0) {
+        R.u = u + 1;
+        R.stats[S_VISITS] += R.N;
+    }
+}
+
+// ======================================================================= initial state
+// One CTA per replica: full energy (O(n)) or the exact integer sums (Ising)
+// of the initial lattice.
+template <int DIM, int GEOM>
+__global__ void __launch_bounds__(1024) k_init(Rep *reps, const int *ids)
+{
+    __shared__ double red[MCS_RED_DOUBLES];
+    __shared__ double F[F_NON];
+    __shared__ long long redl[32 * 9];
+    __shared__ long long Fi[16];
+    Rep &R = reps[ids[blockIdx.x]];
+    if (R.dim != (DIM == 1 ? 1 : DIM) || R.geom != GEOM) return;
+    Spins S = spins_global(R);
+    const int vmax = max(max(R.N, R.nlat), max(R.n_rorb, R.ncirc));
+    if (DIM == 1) {
+        is_frame<GEOM>(R, R.itab, S.s, 0, vmax, 0, red, F, redl, Fi);
+        if (threadIdx.x == 0) {
+            for (int k = 0; k < MCS_MAXT; ++k) { R.icnt[C_M0 + k] = Fi[k]; R.icnt[C_DM + k] = 0; }
+            for (int k = 0; k < MCS_MAXC; ++k) { R.icnt[C_N0 + k] = Fi[MCS_MAXT + k]; R.icnt[C_DN + k] = 0; }
+        }
+    } else {
+        for (int k = threadIdx.x; k < F_NON; k += blockDim.x) F[k] = 0.0;
+        __syncthreads();
+        on_frame<DIM, GEOM>(R, R.jtab, R.dtab, S, 0, vmax, true, red, F);
+        if (threadIdx.x == 0) R.acc[A_ECUR] = F[F_EFB] / 2 + F[F_EFO];
+    }
+}
+
+// ======================================================================= launchers
+template <int DIM, int GEOM>
+static cudaError_t set_smem_attr(size_t smem)
+{
+    static size_t done = 0;
+    if (smem > 48 * 1024 && smem > done) {
+        cudaError_t e = cudaFuncSetAttribute(k_resident_metro<DIM, GEOM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        done = smem;
+    }
+    return cudaSuccess;
+}
+
+#define MCS_DISPATCH(dim, geom, CALL)                                                   \
+    do {                                                                                 \
+        if (geom == MCS_GEOM_SQUARE) {                                                   \
+            if (dim == 1) { CALL(1, MCS_GEOM_SQUARE); }                                  \
+            else if (dim == 2) { CALL(2, MCS_GEOM_SQUARE); }                             \
+            else { CALL(3, MCS_GEOM_SQUARE); }                                           \
+        } else {                                                                         \
+            if (dim == 1) { CALL(1, MCS_GEOM_ELL); }                                     \
+            else if (dim == 2) { CALL(2, MCS_GEOM_ELL); }                                \
+            else { CALL(3, MCS_GEOM_ELL); }                                              \
+        }                                                                                \
+    } while (0)
+
+cudaError_t launch_resident_metro(int dim, int geom, Rep *reps, const int *ids, int nrep, int threads, size_t smem,
+                                  long long max_units, cudaStream_t st)
+{
+    if (nrep <= 0) return cudaSuccess;
+#define CALL_RES(D, G)                                                                   \
+    {                                                                                    \
+        cudaError_t e = set_smem_attr<D, G>(smem);                                       \
+        if (e != cudaSuccess) return e;                                                  \
+        k_resident_metro<D, G><<<nrep, threads, smem, st>>>(reps, ids, max_units);       \
+    }
+    MCS_DISPATCH(dim, geom, CALL_RES);
+#undef CALL_RES
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tiled_sweep(int dim, int geom, Rep *reps, const Item *items, int nitems, int colour,
+                               double *dEpart, long long *ipart, int threads, cudaStream_t st)
+{
+    if (nitems <= 0) return cudaSuccess;
+#define CALL_TS(D, G) k_tiled_sweep<D, G><<<nitems, threads, 0, st>>>(reps, items, colour, dEpart, ipart);
+    MCS_DISPATCH(dim, geom, CALL_TS);
+#undef CALL_TS
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tiled_measure(int dim, int geom, Rep *reps, const Item *items, int nitems, double *fpart,
+                                 int threads, cudaStream_t st)
+{
+    if (nitems <= 0) return cudaSuccess;
+#define CALL_TM(D, G) k_tiled_measure<D, G><<<nitems, threads, 0, st>>>(reps, items, fpart);
+    MCS_DISPATCH(dim, geom, CALL_TM);
+#undef CALL_TM
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tiled_finalize_dim(int dim, Rep *reps, const int *ids, int nrep, const int *item_off,
+                                      double *dEpart, long long *ipart, const int *mitem_off, double *fpart,
+                                      cudaStream_t st)
+{
+    if (nrep <= 0) return cudaSuccess;
+    if (dim == 1) k_tiled_finalize<1><<<nrep, 256, 0, st>>>(reps, ids, item_off, dEpart, ipart, mitem_off, fpart);
+    else if (dim == 2) k_tiled_finalize<2><<<nrep, 256, 0, st>>>(reps, ids, item_off, dEpart, ipart, mitem_off, fpart);
+    else k_tiled_finalize<3><<<nrep, 256, 0, st>>>(reps, ids, item_off, dEpart, ipart, mitem_off, fpart);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_init_state_dg(int dim, int geom, Rep *reps, const int *ids, int nrep, cudaStream_t st)
+{
+    if (nrep <= 0) return cudaSuccess;
+#define CALL_IN(D, G) k_init<D, G><<<nrep, 1024, 0, st>>>(reps, ids);
+    MCS_DISPATCH(dim, geom, CALL_IN);
+#undef CALL_IN
+    return cudaGetLastError();
+}
+
+}  // namespace mcs

@@ -1,0 +1,531 @@
+// mcs_model.cpp -- model compiler.
+//
+// Input: the flattened arrays of one MCMainFunction call (isingLib.c:277-335,
+// heisenbergLib.c:504-583).  Output: the engine's device layout
+//   * greedy colouring of the bond graph in site order; sites renumbered into
+//     colour-major "sweep index" order (contiguous colour ranges);
+//   * 2D square lattices detected and given an arithmetic neighbour rule;
+//     everything else keeps an ELL neighbour table [link][site];
+//   * O(n): exchange matrices de-duplicated into a small class table, the
+//     anisotropy vectors into a D table;
+//   * Ising: directed couplings K*|s_i|*|s_j| grouped into <= 4 classes and
+//     sites into <= 4 types; per type an exact acceptance table indexed by the
+//     neighbour-sign pattern (thresholds ceil(exp(corr)*2^32)).
+#include "mcs_model.h"
+
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <set>
+#include <utility>
+
+namespace mcs {
+
+void philox_host(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, unsigned long long seed, uint32_t out[4])
+{
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        c0 = n0; c1 = (uint32_t)p1; c2 = n2; c3 = (uint32_t)p0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+static double u24d(uint32_t w) { return (double)(w >> 8) * (1.0 / 16777216.0); }
+static const double kTwoPi = 6.28318530717958647692528676655900577;
+
+static void eng_dir(int dim, uint32_t w0, uint32_t w1, double d[3])
+{
+    if (dim == 2) {
+        double phi = kTwoPi * u24d(w0);
+        d[0] = cos(phi); d[1] = sin(phi); d[2] = 0;
+    } else {
+        double zz = 2.0 * u24d(w0) - 1.0;
+        double phi = kTwoPi * u24d(w1);
+        double rho = sqrt(fmax(0.0, 1.0 - zz * zz));
+        d[0] = rho * cos(phi); d[1] = rho * sin(phi); d[2] = zz;
+    }
+}
+
+#define FAIL(code, msg)           \
+    do {                          \
+        if (err) *err = (msg);    \
+        return (code);            \
+    } while (0)
+
+int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std::string *err)
+{
+    if (!p) FAIL(MCS_EINVAL, "null problem");
+    if (p->model < 1 || p->model > 3) FAIL(MCS_EINVAL, "model must be 1 (Ising), 2 (XY) or 3 (Heisenberg)");
+    if (p->algorithm != 0 && p->algorithm != 1) FAIL(MCS_EINVAL, "algorithm must be 0 (Metropolis) or 1 (Wolff)");
+    const int N = p->n_sites, z = p->max_links;
+    if (N <= 0) FAIL(MCS_EINVAL, "empty lattice (no sites)");
+    if (N > (1 << 28)) FAIL(MCS_EINVAL, "lattice too large");
+    if (z < 0 || z > MCS_MAXZ) FAIL(MCS_EINVAL, "maxNLinking out of range (0..32)");
+    if (!p->init_spin || !p->nlink || (z > 0 && (!p->link_strength || !p->linked_orb)))
+        FAIL(MCS_EINVAL, "missing site or link arrays");
+    if (p->nthermal < 0 || p->nsweep < 1) FAIL(MCS_EINVAL, "nsweep must be >= 1 and nthermal >= 0");
+    if (p->ninterval < 1) FAIL(MCS_EINVAL, "ninterval must be >= 1");
+    if (p->n_lat < 1 || !p->corr_pair) FAIL(MCS_EINVAL, "corrOrbPair must hold at least one pair");
+    if (p->n_rorb < 1 || !p->r_orb || p->n_in_cluster < 1 || !p->r_cluster)
+        FAIL(MCS_EINVAL, "renormalisation lists (rOrb, rOrbCluster) must be non-empty");
+    if (p->model != 1 && p->n_group > MCS_MAXG) FAIL(MCS_EUNSUPPORTED, "more than 8 orbital groups");
+    if (p->n_group < 0 || (p->n_group > 0 && (p->max_group < 1 || !p->group_list)))
+        FAIL(MCS_EINVAL, "bad orbital-group list");
+    if (p->n_circuits < 0 || (p->n_circuits > 0 && !p->circuits)) FAIL(MCS_EINVAL, "bad circuit list");
+    if (p->spin_frames < 0 || p->spin_frames > p->nsweep)
+        FAIL(MCS_EINVAL, "spinFrame must be in [0, nsweep]");
+    const int dim = p->model == 1 ? 1 : (p->model == 2 ? 2 : 3);
+    if (dim > 1 && !p->init_d) FAIL(MCS_EINVAL, "initD missing");
+    m->model = p->model; m->dim = dim; m->alg = p->algorithm; m->N = N; m->zmax = z;
+    m->h = p->h; m->flunc = p->flunc;
+    m->seed = o ? o->seed : 0;
+
+    for (int i = 0; i < N; ++i) {
+        if (p->nlink[i] < 0 || p->nlink[i] > z) FAIL(MCS_EINVAL, "nlink out of range");
+        for (int l = 0; l < p->nlink[i]; ++l) {
+            int j = p->linked_orb[(size_t)i * z + l];
+            if (j < 0 || j >= N) FAIL(MCS_EINVAL, "linkedOrb index out of range");
+        }
+    }
+    for (int k = 0; k < 2 * p->n_lat; ++k)
+        if (p->corr_pair[k] < 0 || p->corr_pair[k] >= N) FAIL(MCS_EINVAL, "corrOrbPair index out of range");
+    for (int k = 0; k < p->n_rorb; ++k)
+        if (p->r_orb[k] < 0 || p->r_orb[k] >= N) FAIL(MCS_EINVAL, "rOrb index out of range");
+    for (long long k = 0; k < (long long)p->n_rorb * p->n_in_cluster; ++k)
+        if (p->r_cluster[k] < 0 || p->r_cluster[k] >= N) FAIL(MCS_EINVAL, "rOrbCluster index out of range");
+    if (z > 0 && p->r_link)
+        for (long long k = 0; k < (long long)p->n_rorb * z; ++k)
+            if (p->r_link[k] < -1 || p->r_link[k] >= N) FAIL(MCS_EINVAL, "linkedOrb_rnorm index out of range");
+    for (int k = 0; k < 3 * p->n_circuits; ++k)
+        if (p->circuits[k] < 0 || p->circuits[k] >= N) FAIL(MCS_EINVAL, "circuit index out of range");
+    for (long long k = 0; k < (long long)p->n_group * p->max_group; ++k)
+        if (p->group_list[k] >= N) FAIL(MCS_EINVAL, "orbital-group index out of range");
+
+    // ---------------------------------------------------------------- colouring
+    std::vector<int> off(N + 1, 0), adj;
+    {
+        std::vector<int> degc(N, 0);
+        for (int i = 0; i < N; ++i)
+            for (int l = 0; l < p->nlink[i]; ++l) {
+                int j = p->linked_orb[(size_t)i * z + l];
+                if (j == i) continue;
+                degc[i]++; degc[j]++;
+            }
+        for (int i = 0; i < N; ++i) off[i + 1] = off[i] + degc[i];
+        adj.resize(off[N]);
+        std::vector<int> fill(N, 0);
+        for (int i = 0; i < N; ++i)
+            for (int l = 0; l < p->nlink[i]; ++l) {
+                int j = p->linked_orb[(size_t)i * z + l];
+                if (j == i) continue;
+                adj[off[i] + fill[i]++] = j;
+                adj[off[j] + fill[j]++] = i;
+            }
+    }
+    std::vector<int> colour(N, 0);
+    int ncol = 0;
+    {
+        std::vector<int> mark(2 * MCS_MAXZ + 8, -1);
+        std::vector<char> used;
+        for (int i = 0; i < N; ++i) {
+            used.assign(off[i + 1] - off[i] + 2, 0);
+            for (int k = off[i]; k < off[i + 1]; ++k) {
+                int j = adj[k];
+                if (j < i && colour[j] < (int)used.size()) used[colour[j]] = 1;
+            }
+            int c = 0;
+            while (used[c]) ++c;
+            colour[i] = c;
+            ncol = std::max(ncol, c + 1);
+        }
+    }
+    if (ncol > 64) FAIL(MCS_EUNSUPPORTED, "bond graph needs more than 64 colours");
+    m->ncol = ncol;
+    m->col_start.assign(ncol + 1, 0);
+    for (int i = 0; i < N; ++i) m->col_start[colour[i] + 1]++;
+    for (int c = 0; c < ncol; ++c) m->col_start[c + 1] += m->col_start[c];
+    m->sites.resize(N);
+    m->pos.resize(N);
+    {
+        std::vector<int> fillc(m->col_start.begin(), m->col_start.end() - 1);
+        for (int i = 0; i < N; ++i) m->sites[fillc[colour[i]]++] = i;
+        for (int k = 0; k < N; ++k) m->pos[m->sites[k]] = k;
+    }
+    const std::vector<int> &pos = m->pos, &sites = m->sites;
+
+    // ---------------------------------------------------------------- coupling classes
+    // O(n): exchange-matrix classes over all links (exact equality).
+    std::vector<int> linkcls((size_t)N * std::max(z, 1), 0);
+    if (dim > 1) {
+        const bool ign = p->ignore_offdiag > 0;
+        std::map<std::vector<double>, int> cls;
+        std::vector<std::vector<double>> tab;
+        bool anyoff = false;
+        for (int i = 0; i < N; ++i)
+            for (int l = 0; l < p->nlink[i]; ++l) {
+                const double *J = p->link_strength + ((size_t)i * z + l) * 9;
+                std::vector<double> v(J, J + 9);
+                if (ign) v[3] = v[4] = v[5] = v[6] = v[7] = v[8] = 0.0;
+                if (dim == 2) v[2] = v[4] = v[5] = v[7] = v[8] = 0.0;  // XY reads xx,yy,xy,yx (xyLib.c:150-153)
+                for (int k = 3; k < 9; ++k) anyoff |= v[k] != 0.0;
+                auto it = cls.find(v);
+                int c;
+                if (it == cls.end()) { c = (int)tab.size(); cls[v] = c; tab.push_back(v); }
+                else c = it->second;
+                linkcls[(size_t)i * z + l] = c;
+            }
+        if (tab.size() > 65535) FAIL(MCS_EUNSUPPORTED, "too many distinct exchange matrices");
+        if (tab.empty()) tab.push_back(std::vector<double>(9, 0.0));
+        m->njc = (int)tab.size();
+        m->fullJ = anyoff ? 1 : 0;
+        m->jtab.resize(9 * tab.size());
+        m->jtab64.resize(9 * tab.size());
+        for (size_t c = 0; c < tab.size(); ++c)
+            for (int k = 0; k < 9; ++k) { m->jtab[9 * c + k] = (float)tab[c][k]; m->jtab64[9 * c + k] = tab[c][k]; }
+        // anisotropy classes
+        std::map<std::vector<double>, int> dcls;
+        std::vector<std::vector<double>> dt;
+        m->stype.assign(N, 0);
+        bool anyd = false;
+        for (int k = 0; k < N; ++k) {
+            int i = sites[k];
+            std::vector<double> v(p->init_d + 3 * (size_t)i, p->init_d + 3 * (size_t)i + 3);
+            if (dim == 2) v[2] = 0.0;
+            for (double x : v) anyd |= x != 0.0;
+            auto it = dcls.find(v);
+            int c;
+            if (it == dcls.end()) { c = (int)dt.size(); dcls[v] = c; dt.push_back(v); }
+            else c = it->second;
+            if (c > 255) FAIL(MCS_EUNSUPPORTED, "more than 256 distinct anisotropy vectors");
+            m->stype[k] = (uint8_t)c;
+        }
+        m->ndc = (int)dt.size();
+        m->has_d = anyd ? 1 : 0;
+        m->dtab.resize(3 * dt.size());
+        for (size_t c = 0; c < dt.size(); ++c)
+            for (int k = 0; k < 3; ++k) m->dtab[3 * c + k] = (float)dt[c][k];
+    } else {
+        // Ising: classes of Q = K |s_i| |s_j|, site types (|s_i|, class counts)
+        std::map<double, int> qcls;
+        std::vector<double> qv;
+        for (int i = 0; i < N; ++i)
+            for (int l = 0; l < p->nlink[i]; ++l) {
+                int j = p->linked_orb[(size_t)i * z + l];
+                double q = p->link_strength[(size_t)i * z + l] * fabs(p->init_spin[i]) * fabs(p->init_spin[j]);
+                auto it = qcls.find(q);
+                int c;
+                if (it == qcls.end()) { c = (int)qv.size(); qcls[q] = c; qv.push_back(q); }
+                else c = it->second;
+                linkcls[(size_t)i * z + l] = c;
+            }
+        if (qv.size() > MCS_MAXC) FAIL(MCS_EUNSUPPORTED, "Ising model with more than 4 distinct coupling values");
+        if (qv.empty()) qv.push_back(0.0);
+        m->nclass = (int)qv.size();
+        for (int c = 0; c < m->nclass; ++c) m->Q[c] = qv[c];
+        std::map<std::vector<double>, int> tmap;
+        std::vector<std::vector<int>> tcount;
+        std::vector<double> tS;
+        m->stype.assign(N, 0);
+        for (int k = 0; k < N; ++k) {
+            int i = sites[k];
+            std::vector<double> key(1 + MCS_MAXC, 0.0);
+            key[0] = fabs(p->init_spin[i]);
+            for (int l = 0; l < p->nlink[i]; ++l) key[1 + linkcls[(size_t)i * z + l]] += 1.0;
+            auto it = tmap.find(key);
+            int t;
+            if (it == tmap.end()) {
+                t = (int)tS.size();
+                tmap[key] = t;
+                tS.push_back(key[0]);
+                std::vector<int> cnt(MCS_MAXC, 0);
+                for (int c = 0; c < MCS_MAXC; ++c) cnt[c] = (int)key[1 + c];
+                tcount.push_back(cnt);
+            } else t = it->second;
+            if (t >= MCS_MAXT) FAIL(MCS_EUNSUPPORTED, "Ising model with more than 4 site types");
+            m->stype[k] = (uint8_t)t;
+        }
+        m->ntype = (int)tS.size();
+        int base = 0;
+        for (int t = 0; t < m->ntype; ++t) {
+            m->Stype[t] = tS[t];
+            m->ibase[t] = base;
+            int stride[MCS_MAXC], ne = 1;
+            for (int c = 0; c < MCS_MAXC; ++c) { stride[c] = ne; ne *= (tcount[t][c] + 1); }
+            if (ne > 4096) FAIL(MCS_EUNSUPPORTED, "Ising acceptance table too large");
+            for (int e = 0; e < ne; ++e) {
+                int rem = e, ncv[MCS_MAXC];
+                double sumq = 0.0;
+                for (int c = 0; c < MCS_MAXC; ++c) {
+                    int np = rem % (tcount[t][c] + 1);
+                    rem /= (tcount[t][c] + 1);
+                    ncv[c] = 2 * np - tcount[t][c];
+                    sumq += m->Q[c] * ncv[c];
+                }
+                IsEntry en;
+                memset(&en, 0, sizeof en);
+                for (int sg = 0; sg < 2; ++sg) {
+                    double sigma = sg ? 1.0 : -1.0;
+                    double corr = 2 * (sigma * sumq - p->h * tS[t] * sigma);
+                    unsigned long long thr;
+                    if (corr >= 0) thr = 1ULL << 32;
+                    else {
+                        double x = ceil(exp(corr) * 4294967296.0);
+                        thr = x >= 4294967296.0 ? (1ULL << 32) : (unsigned long long)x;
+                    }
+                    en.thr[sg] = thr;
+                }
+                en.nc = (ncv[0] & 0xff) | ((ncv[1] & 0xff) << 8) | ((ncv[2] & 0xff) << 16) | ((ncv[3] & 0xff) << 24);
+                m->itab.push_back(en);
+            }
+            // per-link code = stride of its class
+            (void)stride;
+            base += ne;
+        }
+        // link codes per (site, link)
+        // Wolff add thresholds: corr = Q sigma_i sigma_j; add iff corr<0 and 1-exp(2corr) > U
+        for (int c = 0; c < m->nclass; ++c)
+            for (int sg = 0; sg < 2; ++sg) {
+                double corr = sg ? m->Q[c] : -m->Q[c];
+                unsigned long long thr = 0;
+                if (corr < 0) {
+                    double x = ceil((1 - exp(2 * corr)) * 4294967296.0);
+                    thr = x >= 4294967296.0 ? (1ULL << 32) : (unsigned long long)x;
+                }
+                m->wthr[c][sg] = thr;
+            }
+        // exactness of the incremental bookkeeping: no self links, symmetric couplings
+        bool ok = true;
+        std::multiset<std::pair<std::pair<int, int>, int>> fw;
+        for (int i = 0; i < N && ok; ++i)
+            for (int l = 0; l < p->nlink[i]; ++l) {
+                int j = p->linked_orb[(size_t)i * z + l];
+                if (j == i) { ok = false; break; }
+                fw.insert({{i, j}, linkcls[(size_t)i * z + l]});
+            }
+        if (ok)
+            for (auto &e : fw)
+                if (fw.find({{e.first.second, e.first.first}, e.second}) == fw.end()) { ok = false; break; }
+        m->exact_ok = ok ? 1 : 0;
+    }
+
+    // ---------------------------------------------------------------- geometry
+    // square lattice: site id = x*Ly + y, four links to (x+-1,y), (x,y+-1)
+    m->geom = MCS_GEOM_ELL;
+    if (z >= 4) {
+        for (int Ly = 4; Ly <= N / 4 && m->geom == MCS_GEOM_ELL; Ly += 2) {
+            if (N % Ly) continue;
+            int Lx = N / Ly;
+            if (Lx < 4 || (Lx & 1)) continue;
+            bool okg = true;
+            int code0[4] = {-1, -1, -1, -1};
+            for (int i = 0; i < N && okg; ++i) {
+                if (p->nlink[i] != 4) { okg = false; break; }
+                int x = i / Ly, y = i % Ly;
+                int want[4] = {((x + 1) % Lx) * Ly + y, ((x - 1 + Lx) % Lx) * Ly + y, x * Ly + (y + 1) % Ly,
+                               x * Ly + (y - 1 + Ly) % Ly};
+                int seen = 0;
+                for (int l = 0; l < 4; ++l) {
+                    int j = p->linked_orb[(size_t)i * z + l];
+                    int d = -1;
+                    for (int q = 0; q < 4; ++q)
+                        if (j == want[q] && !(seen & (1 << q))) { d = q; break; }
+                    if (d < 0) { okg = false; break; }
+                    seen |= 1 << d;
+                    int cc = linkcls[(size_t)i * z + l];
+                    if (code0[d] < 0) code0[d] = cc;
+                    else if (code0[d] != cc) { okg = false; break; }
+                }
+                if (okg && colour[i] != ((x + y) & 1)) okg = false;
+            }
+            if (okg && (dim > 1 || m->ntype == 1)) {
+                m->geom = MCS_GEOM_SQUARE;
+                m->Lx = Lx; m->Ly = Ly;
+                for (int d = 0; d < 4; ++d) {
+                    m->sq_cls[d] = code0[d];
+                    if (dim > 1) m->sq_code[d] = code0[d];
+                }
+            }
+        }
+    }
+    // per-link codes in sweep-index space
+    if (dim == 1) {
+        // stride of a class for each type
+        std::vector<std::vector<int>> tstride(m->ntype, std::vector<int>(MCS_MAXC, 0));
+        {
+            // recompute counts per type from the table sizes
+            std::vector<std::vector<int>> cnt(m->ntype, std::vector<int>(MCS_MAXC, 0));
+            std::vector<char> seen(m->ntype, 0);
+            for (int k = 0; k < N; ++k) {
+                int t = m->stype[k];
+                if (seen[t]) continue;
+                seen[t] = 1;
+                int i = sites[k];
+                for (int l = 0; l < p->nlink[i]; ++l) cnt[t][linkcls[(size_t)i * z + l]]++;
+            }
+            for (int t = 0; t < m->ntype; ++t) {
+                int s = 1;
+                for (int c = 0; c < MCS_MAXC; ++c) { tstride[t][c] = s; s *= cnt[t][c] + 1; }
+            }
+        }
+        if (m->geom == MCS_GEOM_SQUARE)
+            for (int d = 0; d < 4; ++d) m->sq_code[d] = tstride[0][m->sq_cls[d]];
+        if (m->geom == MCS_GEOM_ELL || true) {
+            m->lcode.assign((size_t)std::max(z, 1) * N, 0);
+            m->lcls.assign((size_t)std::max(z, 1) * N, 0);
+        }
+        for (int k = 0; k < N; ++k) {
+            int i = sites[k], t = m->stype[k];
+            for (int l = 0; l < p->nlink[i]; ++l) {
+                int c = linkcls[(size_t)i * z + l];
+                m->lcode[(size_t)l * N + k] = (uint16_t)tstride[t][c];
+                m->lcls[(size_t)l * N + k] = (uint8_t)c;
+            }
+        }
+    } else {
+        m->lcode.assign((size_t)std::max(z, 1) * N, 0);
+        for (int k = 0; k < N; ++k) {
+            int i = sites[k];
+            for (int l = 0; l < p->nlink[i]; ++l) m->lcode[(size_t)l * N + k] = (uint16_t)linkcls[(size_t)i * z + l];
+        }
+    }
+    m->nbr.assign((size_t)std::max(z, 1) * N, 0);
+    m->deg.assign(N, 0);
+    for (int k = 0; k < N; ++k) {
+        int i = sites[k];
+        m->deg[k] = (uint8_t)p->nlink[i];
+        for (int l = 0; l < p->nlink[i]; ++l) m->nbr[(size_t)l * N + k] = pos[p->linked_orb[(size_t)i * z + l]];
+    }
+
+    // ---------------------------------------------------------------- measurement lists
+    m->nlat = p->n_lat;
+    m->cpair.resize(2 * (size_t)p->n_lat);
+    for (int k = 0; k < 2 * p->n_lat; ++k) m->cpair[k] = pos[p->corr_pair[k]];
+    m->n_rorb = p->n_rorb;
+    m->ncl = p->n_in_cluster;
+    m->rorb.resize(p->n_rorb);
+    m->rindex.assign(N, -1);
+    m->rcl.resize((size_t)p->n_rorb * p->n_in_cluster);
+    m->rlink.assign((size_t)p->n_rorb * std::max(z, 1), -1);
+    m->rdeg.resize(p->n_rorb);
+    if (dim > 1) m->rjc.assign((size_t)p->n_rorb * std::max(z, 1), 0);
+    else m->rK.assign((size_t)p->n_rorb * std::max(z, 1), 0.0);
+    for (int v = 0; v < p->n_rorb; ++v) {
+        int j = p->r_orb[v];
+        m->rorb[v] = pos[j];
+        m->rindex[pos[j]] = v;
+        for (int k = 0; k < p->n_in_cluster; ++k)
+            m->rcl[(size_t)v * p->n_in_cluster + k] = pos[p->r_cluster[(size_t)v * p->n_in_cluster + k]];
+        m->rdeg[v] = (uint8_t)p->nlink[j];
+        for (int l = 0; l < p->nlink[j]; ++l) {
+            int t = p->r_link ? p->r_link[(size_t)v * z + l] : -1;
+            m->rlink[(size_t)v * z + l] = t < 0 ? -1 : pos[t];
+            if (dim > 1) m->rjc[(size_t)v * z + l] = (uint16_t)linkcls[(size_t)j * z + l];
+            else m->rK[(size_t)v * z + l] = p->link_strength[(size_t)j * z + l];
+        }
+    }
+    m->ci = m->cj = m->cij = 0;
+    for (int v = 0; v < p->n_lat; ++v) {
+        bool a = m->rindex[m->cpair[2 * v]] >= 0, b = m->rindex[m->cpair[2 * v + 1]] >= 0;
+        m->ci += a; m->cj += b; m->cij += a && b;
+    }
+    m->ncirc = dim == 3 ? p->n_circuits : 0;
+    m->circ.resize(3 * (size_t)m->ncirc);
+    for (int k = 0; k < 3 * m->ncirc; ++k) m->circ[k] = pos[p->circuits[k]];
+    m->ngroup = dim > 1 ? p->n_group : 0;
+    m->gmask.assign(N, 0);
+    for (int g = 0; g < m->ngroup; ++g)
+        for (int k = 0; k < p->max_group; ++k) {
+            int id = p->group_list[(size_t)g * p->max_group + k];
+            if (id < 0) break;
+            m->gmask[pos[id]] |= (uint8_t)(1u << g);
+        }
+    m->slen.resize(N);
+    m->sval.resize(N);
+    for (int k = 0; k < N; ++k) { m->slen[k] = (float)fabs(p->init_spin[sites[k]]); m->sval[k] = (float)p->init_spin[sites[k]]; }
+
+    // ---------------------------------------------------------------- program
+    if (p->algorithm == 0) {
+        m->upm = (int)std::min<long long>((p->ninterval + N - 1) / N, 1 << 30);
+    } else {
+        if (p->ninterval > (1 << 30)) FAIL(MCS_EINVAL, "ninterval too large for Wolff");
+        m->upm = (int)p->ninterval;
+    }
+    m->nsweep = p->nsweep;
+    m->units_thermal = p->nthermal * (long long)m->upm;
+    m->units_total = m->units_thermal + p->nsweep * (long long)m->upm;
+    m->frames = p->spin_frames;
+    m->frame_every = p->spin_frames > 0 ? p->nsweep / p->spin_frames : 1;
+    if (m->frame_every < 1) m->frame_every = 1;
+    const bool rnd = o && o->random_init;
+    m->offset_energy = (o && o->absolute_energy) ? 0 : 1;
+
+    // ---------------------------------------------------------------- initial state
+    if (dim == 1) {
+        m->init_sigma.resize(N);
+        double M0 = 0, first = 0;
+        for (int k = 0; k < N; ++k) {
+            int i = sites[k];
+            int8_t sg = p->init_spin[i] < 0 ? -1 : 1;
+            if (rnd) {
+                uint32_t w[4];
+                philox_host((uint32_t)k, 0, 0, 0x5000u, m->seed, w);
+                sg = (w[0] & 1) ? 1 : -1;
+            }
+            m->init_sigma[k] = sg;
+            M0 += fabs(p->init_spin[i]) * sg;
+        }
+        long long nfirst = std::min<long long>(p->ninterval, N);
+        for (long long i = 0; i < nfirst; ++i) first += p->init_spin[i];
+        int lastk = pos[N - 1];
+        double slast0 = fabs(p->init_spin[N - 1]) * m->init_sigma[lastk];
+        m->last_site = lastk;
+        if (rnd) {
+            m->ts_const = 0.0;
+            m->ts_wolff_last = 0;
+        } else if (p->algorithm == 0) {
+            m->ts_const = M0 - first;
+            m->ts_wolff_last = 0;
+        } else {
+            m->ts_const = M0 - slast0 - first;
+            m->ts_wolff_last = 1;
+        }
+    } else {
+        m->init_vec.assign((size_t)3 * N, 0.f);
+        m->init_vec64.assign((size_t)3 * N, 0.0);
+        for (int k = 0; k < N; ++k) {
+            int i = sites[k];
+            double S0 = p->init_spin[i];
+            double v[3] = {S0, 0, 0}, d[3];
+            uint32_t w[4];
+            if (rnd) {
+                philox_host((uint32_t)k, 0, 0, 0x5000u, m->seed, w);
+                eng_dir(dim, w[0], w[1], d);
+                v[0] = d[0]; v[1] = d[1]; v[2] = d[2];
+            } else {
+                philox_host((uint32_t)k, 0, 0, 0x4000u, m->seed, w);
+                eng_dir(dim, w[0], w[1], d);
+                v[0] += d[0] * p->flunc; v[1] += d[1] * p->flunc;
+                if (dim == 3) v[2] += d[2] * p->flunc;
+            }
+            double len = dim == 3 ? sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) : sqrt(v[0] * v[0] + v[1] * v[1]);
+            if (len >= 1e-5) { v[0] /= len; v[1] /= len; if (dim == 3) v[2] /= len; }
+            double a = fabs(S0);
+            for (int c = 0; c < 3; ++c) {
+                double x = (c < dim) ? v[c] * a : 0.0;
+                m->init_vec64[(size_t)c * N + k] = x;
+                m->init_vec[(size_t)c * N + k] = (float)x;
+            }
+        }
+        m->last_site = pos[N - 1];
+    }
+    return MCS_OK;
+}
+
+}  // namespace mcs

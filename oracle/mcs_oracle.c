@@ -26,18 +26,23 @@
  *          arithmetic is the reference's; only site order and random source
  *          change.
  *
+ * The "sweep index" of a site is its position in the concatenation of the
+ * colour lists (colour 0 first, ascending site id inside a colour).  Every
+ * counter below names sites by sweep index, so that a device that stores the
+ * lattice in that order draws the same words.
  * Philox counter layout of the engine stream (key = seed lo/hi 32 bits):
  *   Metropolis, sweep t, colour c, k-th site of the colour:
  *       Ising   ctr = (k>>2, t_lo, t_hi, c), word k&3
  *       O(n)    ctr = (k,    t_lo, t_hi, c), words 0.. (direction), last = accept
- *   Wolff cluster q: ctr = (0, q_lo, q_hi, 0x1000): w0 seed site, w1/w2
- *       direction, w3 cluster acceptance
- *   Wolff bond coin, cluster q, source site i, link slot l:
- *       ctr = (i, q_lo, q_hi, 0x2000 + (l>>2)), word l&3
- *   Ising majority tie-break, measurement m, chosen site j, slot s
+ *   Wolff cluster q: ctr = (0, q_lo, q_hi, 0x1000): seed = sites[(w0*N)>>32],
+ *       w1/w2 direction, w3 cluster acceptance
+ *   Wolff bond coin, cluster q, directed bond from sweep index a to b:
+ *       ctr = (a, b, q_lo, 0x2000 ^ (q_hi << 16)), word 0
+ *   Ising majority tie-break, measurement m, chosen site of sweep index a, slot s
  *       (0 = the site itself, 1+l = its l-th renormalised neighbour):
- *       ctr = (j, m_lo, m_hi, 0x3000 + (s>>2)), word s&3
- *   O(n) initial tilt (flunc) of site i: ctr = (i, 0, 0, 0x4000)
+ *       ctr = (a, m_lo, m_hi, 0x3000 + (s>>2)), word s&3
+ *   O(n) initial tilt (flunc) of the site of sweep index a: ctr = (a, 0, 0, 0x4000)
+ *   random initial state (engine API option) of sweep index a: ctr = (a, 0, 0, 0x5000)
  *   uniform in [0,1): Ising/coins of Ising  U = w * 2^-32,
  *                     O(n)                  U = (w>>8) * 2^-24
  *   directions: XY  phi = 2*pi*U(w);  Heisenberg z = 2U(w0)-1, phi = 2*pi*U(w1)
@@ -108,6 +113,12 @@ static void phil(const Rng *g, uint32_t c0, uint64_t t, uint32_t c3, uint32_t ou
     uint32_t c[4] = {c0, (uint32_t)t, (uint32_t)(t >> 32), c3};
     or_philox4x32_10(c, g->key, out);
 }
+static uint32_t coin(const Rng *g, uint32_t a, uint32_t b, uint64_t q)
+{
+    uint32_t c[4] = {a, b, (uint32_t)q, 0x2000u ^ ((uint32_t)(q >> 32) << 16)}, out[4];
+    or_philox4x32_10(c, g->key, out);
+    return out[0];
+}
 static double u32d(uint32_t w) { return (double)w * (1.0 / 4294967296.0); }
 static double u24d(uint32_t w) { return (double)(w >> 8) * (1.0 / 16777216.0); }
 
@@ -172,7 +183,8 @@ static int greedy_colour(const OrProblem *p, int *colour)
 typedef struct Sweep {
     int ncol;
     int *start;  /* ncol+1 */
-    int *sites;  /* N */
+    int *sites;  /* N: sweep index -> site */
+    int *pos;    /* N: site -> sweep index */
 } Sweep;
 
 static void sweep_build(const OrProblem *p, Sweep *s)
@@ -187,9 +199,11 @@ static void sweep_build(const OrProblem *p, Sweep *s)
     for (int c = 0; c < s->ncol; c++) pos[c] = s->start[c];
     s->sites = malloc((size_t)N * sizeof(int));
     for (int i = 0; i < N; i++) s->sites[pos[colour[i]]++] = i;
+    s->pos = malloc((size_t)N * sizeof(int));
+    for (int k = 0; k < N; k++) s->pos[s->sites[k]] = k;
     free(pos); free(colour);
 }
-static void sweep_free(Sweep *s) { free(s->start); free(s->sites); }
+static void sweep_free(Sweep *s) { free(s->start); free(s->sites); free(s->pos); }
 
 static int64_t sweeps_per(int64_t tau, int N) { return (tau + N - 1) / N; }
 
@@ -204,6 +218,7 @@ typedef struct IsingState {
     double energy, totspin;
     int64_t *stats;
     int64_t meas_index; /* engine: measurement counter for tie-breaks */
+    const Sweep *sw;    /* engine: colour lists and sweep indices */
 } IsingState;
 
 /* getCorrEnergy, isingLib.c:121-127 */
@@ -245,7 +260,7 @@ static void is_wolff(IsingState *S, uint64_t q)
     long seed;
     if (engine) {
         phil(&S->g, 0, q, 0x1000, w);
-        seed = (long)(((uint64_t)w[0] * (uint64_t)N) >> 32);
+        seed = S->sw->sites[(((uint64_t)w[0] * (uint64_t)N) >> 32)];
     } else {
         seed = ref_seed_site(&S->g, N);
     }
@@ -255,14 +270,13 @@ static void is_wolff(IsingState *S, uint64_t q)
     int begin = 0, end = 0, blen = 1;
     while (begin <= end) {
         int out = S->buffer[begin++];
-        uint32_t cw[4] = {0, 0, 0, 0};
         for (int l = 0; l < p->nlink[out]; l++) {
             int j = p->linked_orb[(size_t)out * z + l];
-            if (engine && (l & 3) == 0) phil(&S->g, (uint32_t)out, q, 0x2000u + (uint32_t)(l >> 2), cw);
             if (S->inblock[j] == 0) {
                 double corr = (p->link_strength[(size_t)out * z + l]) * (S->s[out]) * (S->s[j]);
                 if (corr < 0) {
-                    double u = engine ? u32d(cw[l & 3]) : ref_u(&S->g);
+                    double u = engine ? u32d(coin(&S->g, (uint32_t)S->sw->pos[out], (uint32_t)S->sw->pos[j], q))
+                                      : ref_u(&S->g);
                     if ((1 - exp(2 * corr)) > u) {
                         S->block[blen++] = j;
                         S->inblock[j] = 1;
@@ -312,12 +326,13 @@ static double is_corr_rnorm(IsingState *S, int j)
     int engine = S->g.mode == 1;
     int r = S->chosen[j] - 1;
     uint32_t tw[4] = {0, 0, 0, 0};
-    if (engine) phil(&S->g, (uint32_t)j, (uint64_t)S->meas_index, 0x3000, tw);
+    uint32_t sj = engine ? (uint32_t)S->sw->pos[j] : 0;
+    if (engine) phil(&S->g, sj, (uint64_t)S->meas_index, 0x3000, tw);
     double corr = 0;
     double a = is_majority(S, j, engine, tw, 0);
     for (int l = 0; l < p->nlink[j]; l++) {
         int slot = 1 + l;
-        if (engine && (slot & 3) == 0) phil(&S->g, (uint32_t)j, (uint64_t)S->meas_index, 0x3000u + (uint32_t)(slot >> 2), tw);
+        if (engine && (slot & 3) == 0) phil(&S->g, sj, (uint64_t)S->meas_index, 0x3000u + (uint32_t)(slot >> 2), tw);
         int t = p->r_link[(size_t)r * p->z + l];
         if (t < 0) continue; /* the reference reads lattice[-1] here (undefined); skipped */
         double b = is_majority(S, t, engine, tw, slot);
@@ -354,9 +369,10 @@ static int ising_run(const OrProblem *p, OrRun *run)
     int64_t nfirst = p->ninterval < N ? p->ninterval : N;
     for (int64_t i = 0; i < nfirst; i++) S.totspin += p->init_spin[i];
 
-    Sweep sw = {0, NULL, NULL};
+    Sweep sw = {0, NULL, NULL, NULL};
     int engine = run->mode == 1;
-    if (engine && p->algorithm == 0) sweep_build(p, &sw);
+    if (engine) sweep_build(p, &sw);
+    S.sw = &sw;
     int64_t t = run->sweep_offset; /* engine sweep / cluster counter */
 
     /* one reference "update" or one engine unit of ninterval updates */
@@ -450,7 +466,7 @@ static int ising_run(const OrProblem *p, OrRun *run)
     r[8] = U4; r[9] = spin_tot / ns / nlat; r[10] = 0.0;
     if (run->spins_io)
         for (int i = 0; i < N; i++) { run->spins_io[3 * i] = S.s[i]; run->spins_io[3 * i + 1] = 0; run->spins_io[3 * i + 2] = 0; }
-    if (engine && p->algorithm == 0) sweep_free(&sw);
+    if (engine) sweep_free(&sw);
     free(S.s); free(S.inblock); free(S.block); free(S.buffer); free(S.chosen);
 #undef IS_UNIT_REF
     return 0;
@@ -473,6 +489,7 @@ typedef struct OnState {
     double energy;
     V3 totspin;
     int64_t *stats;
+    const Sweep *sw;
 } OnState;
 
 static double v_dot(int dim, V3 a, V3 b)
@@ -625,7 +642,7 @@ static void on_wolff(OnState *S, uint64_t q)
     V3 r;
     if (engine) {
         phil(&S->g, 0, q, 0x1000, w);
-        seed = (long)(((uint64_t)w[0] * (uint64_t)N) >> 32);
+        seed = S->sw->sites[(((uint64_t)w[0] * (uint64_t)N) >> 32)];
         r = on_eng_dir(dim, w[1], w[2]);
     } else {
         seed = ref_seed_site(&S->g, N);
@@ -638,15 +655,14 @@ static void on_wolff(OnState *S, uint64_t q)
     while (begin <= end) {
         int out = S->buffer[begin++];
         on_project(S, out, r);
-        uint32_t cw[4] = {0, 0, 0, 0};
         for (int l = 0; l < p->nlink[out]; l++) {
             int j = p->linked_orb[(size_t)out * z + l];
-            if (engine && (l & 3) == 0) phil(&S->g, (uint32_t)out, q, 0x2000u + (uint32_t)(l >> 2), cw);
             if (S->inblock[j] == 0) {
                 on_project(S, j, r);
                 double corr = 2 * S->sdotn[out] * S->sdotn[j] * v_jdot(S, r, r, on_J(S, out, l));
                 if (corr < 0) {
-                    double u = engine ? u24d(cw[l & 3]) : ref_u(&S->g);
+                    double u = engine ? u24d(coin(&S->g, (uint32_t)S->sw->pos[out], (uint32_t)S->sw->pos[j], q))
+                                      : ref_u(&S->g);
                     if ((1 - exp(corr)) > u) {
                         S->block[blen++] = j;
                         S->inblock[j] = 1;
@@ -786,6 +802,9 @@ static int on_run(const OrProblem *p, OrRun *run)
     S.buffer = malloc((size_t)N * sizeof(int));
     S.chosen = calloc((size_t)N, sizeof(int));
     for (int i = 0; i < p->n_rorb; i++) S.chosen[p->r_orb[i]] = i + 1;
+    Sweep sw = {0, NULL, NULL, NULL};
+    if (run->mode == 1) sweep_build(p, &sw);
+    S.sw = &sw;
 
     /* establishLattice: heisenbergLib.c:153-220, xyLib.c:116-165 */
     for (int i = 0; i < N; i++) {
@@ -796,7 +815,7 @@ static int on_run(const OrProblem *p, OrRun *run)
         if (run->mode == 0) fl = on_ref_randvec(&S);
         else {
             uint32_t w[4];
-            phil(&S.g, (uint32_t)i, 0, 0x4000, w);
+            phil(&S.g, (uint32_t)sw.pos[i], 0, 0x4000, w);
             fl = on_eng_dir(dim, w[0], w[1]);
         }
         fl.x *= p->flunc; fl.y *= p->flunc; if (dim == 3) fl.z *= p->flunc;
@@ -817,8 +836,6 @@ static int on_run(const OrProblem *p, OrRun *run)
     S.totspin.x = S.totspin.y = S.totspin.z = 0;
     for (int i = 0; i < N; i++) v_add(dim, &S.totspin, S.s[i]);
 
-    Sweep sw = {0, NULL, NULL};
-    if (run->mode == 1 && p->algorithm == 0) sweep_build(p, &sw);
     int64_t t = run->sweep_offset;
 
     if (run->mode == 0) {
@@ -971,7 +988,7 @@ static int on_run(const OrProblem *p, OrRun *run)
             run->spins_io[3 * i + 1] = S.s[i].y;
             run->spins_io[3 * i + 2] = dim == 3 ? S.s[i].z : 0;
         }
-    if (run->mode == 1 && p->algorithm == 0) sweep_free(&sw);
+    if (run->mode == 1) sweep_free(&sw);
     free(sds); free(s4); free(gsum);
     free(S.s); free(S.trans); free(S.perp); free(S.sdotn); free(S.len);
     free(S.inblock); free(S.projected); free(S.block); free(S.buffer); free(S.chosen);

@@ -1,0 +1,55 @@
+"""CPU tests of the C ABI boundary: the library loads, exports every
+declared symbol, and rejects malformed input before touching a GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from tests import cases as C
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "mcsgpu.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|void|const char \*)\s*(mcs_\w+)\s*\(", src, re.M)))
+
+
+def test_header_lists_match_python_front_end():
+    import mcsolver_gb300 as eng
+    assert declared_functions() == sorted(eng.ABI_FUNCTIONS)
+
+
+def test_library_exports_every_declared_symbol(engine):
+    L = engine.lib()
+    for name in declared_functions():
+        assert hasattr(L, name), name
+    assert L.mcs_abi_version() == 1
+    assert b"sm_103a" in L.mcs_build_info()
+
+
+def test_dropin_modules_import_and_export_mcmainfunction(engine):
+    for name in ("isinglib", "xylib", "heisenberglib"):
+        mod = engine.load_dropin(name)
+        assert callable(mod.MCMainFunction)
+
+
+@pytest.mark.parametrize("mutate,msg", [
+    (lambda a: a[:1] + ((),) + a[2:], "empty"),
+    (lambda a: a[:8] + (tuple([10 ** 6] + list(a[8][1:])),) + a[9:], "out of range"),
+    (lambda a: a[:9] + ((),) + a[10:], "pair"),
+    (lambda a: a[:4] + (0,) + a[5:], "ninterval"),
+])
+def test_malformed_input_is_rejected_without_gpu(engine, mutate, msg):
+    args = C.square_args("ising", 8, 2.0)
+    bad = mutate(args)
+    with pytest.raises(Exception) as ei:
+        engine.solve("ising", bad)
+    assert msg.split()[0] in str(ei.value).lower() or "mcsgpu error" in str(ei.value)
+
+
+def test_dropin_rejects_wrong_arity(engine):
+    mod = engine.load_dropin("isinglib")
+    with pytest.raises(TypeError):
+        mod.MCMainFunction(1, 2, 3)

@@ -1,0 +1,182 @@
+"""GPU parity: the CUDA engine against the oracle and the reference.
+
+* Ising: bit-exact against the oracle's engine stream (same colour order,
+  same Philox words, integer acceptance thresholds); observables within
+  1e-9 relative (FP64 sums in a different order); the incremental energy and
+  magnetisation bookkeeping equals a full recompute at every measurement.
+* XY / Heisenberg: the kernel updates spins in FP32, the oracle in FP64.  From
+  the same state, after the same sweeps, spins agree to 1e-4 except sites
+  whose acceptance decision sat within FP32 rounding of the threshold
+  (at most 1% of the sites, tolerance written below).
+* Statistics: means over 24 seeds within 3.5 standard errors of the
+  reference library's 24-seed means (golden fixtures).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from tests import cases as C
+
+pytestmark = pytest.mark.gpu
+
+SPIN_TOL = 1e-4        # per-component spin agreement, FP32 kernel vs FP64 oracle
+FLIP_FRACTION = 0.01   # fraction of sites allowed to differ by a borderline decision
+OBS_RTOL = 1e-9        # Ising observables (same trajectory, FP64 sums in another order)
+
+
+def _frames_last(ex):
+    return ex["frames"][-1]
+
+
+ISING_CASES = [
+    ("sq8", lambda: C.square_args("ising", 8, 2.0, nthermal=5, nsweep=12, frames=12)),
+    ("sq8_h", lambda: C.square_args("ising", 8, 2.0, h=0.3, nthermal=5, nsweep=12, frames=12)),
+    ("sq16_tc", lambda: C.square_args("ising", 16, 2.269, nthermal=10, nsweep=20, frames=20)),
+    ("sq7_odd", lambda: C.square_args("ising", 7, 2.5, nthermal=5, nsweep=10, frames=10)),
+    ("hc6_ell", lambda: C.lattice_args("ising", (6, 6, 1), 2, [(0, 1, o, C.J9(-1)) for o in ((0, 0, 0), (-1, 0, 0), (0, 1, 0))],
+                                       3.0, S=[1.5, 1.5], nthermal=5, nsweep=10, ki=((0, 1), (0, 0, 0)), frames=10)),
+    ("sq32_afm_h", lambda: C.square_args("ising", 32, 1.5, J=1.0, h=0.5, nthermal=4, nsweep=8, frames=8)),
+]
+
+
+@pytest.mark.parametrize("schedule", ["resident", "tiled", "plain"])
+@pytest.mark.parametrize("name,mk", ISING_CASES, ids=[c[0] for c in ISING_CASES])
+def test_ising_metropolis_bit_exact(engine, oracle_lib, name, mk, schedule):
+    args = mk()
+    res, ex = engine.solve("ising", args, seed=123, schedule=schedule)
+    ref, rex = oracle_lib.solve("ising", args, seed=123, mode=1)
+    assert ex["exact_mismatches"] == 0
+    np.testing.assert_array_equal(_frames_last(ex)[:, 0], rex["spins"][:, 0].astype(np.float32))
+    np.testing.assert_allclose(np.array(res[:10]), np.array(ref[:10]), rtol=OBS_RTOL, atol=1e-12)
+    assert ex["site_updates"] == rex["stats"][3]
+    assert ex["accepted"] == rex["stats"][0]
+
+
+def _tilted(model, mk):
+    a = list(mk())
+    a[15] = 0.6  # flunc: random initial tilt drawn from the engine stream
+    return tuple(a)
+
+
+ON_CASES = [
+    ("xy_sq16", "xy", lambda: C.square_args("xy", 16, 0.9, nthermal=1, nsweep=1, frames=1)),
+    ("heis_sq16_dmi", "heisenberg", lambda: C.square_args("heisenberg", 16, 0.5, h=0.3, dmi=0.4, D=[0, 0, -0.2],
+                                                          nthermal=1, nsweep=1, frames=1)),
+    ("heis_hc8_ell", "heisenberg", lambda: C.honeycomb_args("heisenberg", 8, 8.0, nthermal=1, nsweep=1)),
+    ("heis_sq7_odd", "heisenberg", lambda: C.square_args("heisenberg", 7, 0.7, nthermal=1, nsweep=1, frames=1)),
+    ("xy_sq32", "xy", lambda: C.square_args("xy", 32, 1.1, D=[0.1, -0.2, 0], h=0.2, nthermal=1, nsweep=1, frames=1)),
+]
+
+
+@pytest.mark.parametrize("schedule", ["resident", "tiled"])
+@pytest.mark.parametrize("name,model,mk", ON_CASES, ids=[c[0] for c in ON_CASES])
+def test_on_metropolis_matches_oracle(engine, oracle_lib, name, model, mk, schedule):
+    args = list(_tilted(model, mk))
+    args[20] = 1  # one spin frame: the state after the measured sweep
+    args = tuple(args)
+    res, ex = engine.solve(model, args, seed=77, schedule=schedule)
+    ref, rex = oracle_lib.solve(model, args, seed=77, mode=1)
+    got = _frames_last(ex).astype(np.float64)
+    want = rex["spins"]
+    dim = 2 if model == "xy" else 3
+    d = np.abs(got[:, :dim] - want[:, :dim]).max(axis=1)
+    bad = d > 1e-3
+    assert bad.mean() <= FLIP_FRACTION, (bad.sum(), len(d))
+    assert d[~bad].max() <= SPIN_TOL
+    if not bad.any():
+        # energy per site and spin-spin correlation of the one measurement
+        assert res[8] == pytest.approx(ref[8], rel=1e-4, abs=1e-5)
+        assert res[6] == pytest.approx(ref[6], rel=1e-4, abs=1e-5)
+        assert res[26] == pytest.approx(ref[26], rel=1e-3, abs=1e-4)
+
+
+@pytest.mark.parametrize("model", ["xy", "heisenberg"])
+def test_on_resident_and_tiled_trajectories_agree(engine, model):
+    args = C.square_args(model, 16, 0.8, dmi=0.3 if model == "heisenberg" else 0.0, nthermal=20, nsweep=30, frames=30)
+    a, ea = engine.solve(model, args, seed=9, schedule="resident")
+    b, eb = engine.solve(model, args, seed=9, schedule="tiled")
+    np.testing.assert_allclose(ea["frames"], eb["frames"], atol=1e-5)
+    np.testing.assert_allclose(np.array(a[:27]), np.array(b[:27]), rtol=1e-6, atol=1e-7)
+
+
+STAT = [n for n in C.golden()["cases"] if n.startswith("stat_") and "wolff" not in n]
+
+
+@pytest.mark.parametrize("name", STAT)
+def test_statistics_agree_with_reference(engine, name):
+    model, args, c = C.golden_case(name)
+    nv = 10 if model == "ising" else 27
+    ref = np.array([c["ref"][str(s)][:nv] for s in c["seeds"]], float)
+    b = engine.Batch()
+    for s in c["seeds"]:
+        b.add(model, args, seed=5000 + int(s))
+    b.run()
+    mine = np.array([b.result(i)[0][:nv] for i in range(len(c["seeds"]))], float)
+    b.close()
+    idx = [0, 4, 5, 6, 8] if model == "ising" else [0, 6, 8, 9, 10, 18, 22, 26]
+    for k in idx:
+        x, y = ref[:, k], mine[:, k]
+        se = math.sqrt(x.var(ddof=1) / len(x) + y.var(ddof=1) / len(y))
+        if se == 0:
+            assert x.mean() == pytest.approx(y.mean(), abs=1e-12)
+            continue
+        assert abs(x.mean() - y.mean()) / se < 3.5, (k, x.mean(), y.mean(), se)
+
+
+def onsager_energy(T, J=1.0):
+    """Exact internal energy per site of the infinite 2D square Ising model
+    (Onsager 1944): u = -J coth(2K) [1 + (2/pi)(2 tanh^2(2K) - 1) K(k)],
+    k = 2 sinh(2K)/cosh^2(2K), K = J/T."""
+    from scipy.special import ellipk
+    K = J / T
+    k = 2 * math.sinh(2 * K) / math.cosh(2 * K) ** 2
+    return -J / math.tanh(2 * K) * (1 + 2 / math.pi * (2 * math.tanh(2 * K) ** 2 - 1) * ellipk(k * k))
+
+
+@pytest.mark.parametrize("T", [1.6, 3.2])
+def test_ising_energy_matches_onsager(engine, T):
+    """L=64 away from Tc: finite-size effects are below 1e-4 per site."""
+    b = engine.Batch()
+    R = 8
+    for s in range(R):
+        b.add("ising", C.square_args("ising", 64, T, nthermal=500, nsweep=2000), seed=100 + s, absolute_energy=True)
+    b.run()
+    e = np.array([b.result(i)[0][4] * T for i in range(R)])
+    b.close()
+    exact = onsager_energy(T)
+    se = e.std(ddof=1) / math.sqrt(R)
+    assert abs(e.mean() - exact) < 3.5 * se + 2e-4, (e.mean(), exact, se)
+
+
+def test_batch_results_equal_individual_solves(engine):
+    """Replicas of different models and sizes in one batch give the same
+    results as alone (Ising bit-exact; O(n) to FP32 level)."""
+    probs = [("ising", C.square_args("ising", 16, 2.2, nthermal=10, nsweep=20)),
+             ("ising", C.square_args("ising", 40, 2.6, h=0.1, nthermal=10, nsweep=20)),
+             ("xy", C.square_args("xy", 24, 0.9, nthermal=10, nsweep=20)),
+             ("heisenberg", C.square_args("heisenberg", 12, 0.6, dmi=0.4, nthermal=10, nsweep=20)),
+             ("heisenberg", C.honeycomb_args("heisenberg", 6, 8.0, nthermal=10, nsweep=20))]
+    b = engine.Batch()
+    for i, (m, a) in enumerate(probs):
+        b.add(m, a, seed=40 + i)
+    b.run()
+    for i, (m, a) in enumerate(probs):
+        got, _ = b.result(i)
+        alone, _ = engine.solve(m, a, seed=40 + i)
+        n = 10 if m == "ising" else 27
+        np.testing.assert_allclose(np.array(got[:n]), np.array(alone[:n]), rtol=1e-9 if m == "ising" else 1e-6, atol=1e-9)
+    b.close()
+
+
+def test_dropin_module_matches_c_abi(engine):
+    mod = engine.load_dropin("isinglib")
+    args = C.square_args("ising", 16, 2.3, nthermal=10, nsweep=20)
+    out = mod.MCMainFunction(*args, lambda k: None)
+    direct, _ = engine.solve("ising", args, seed=1)
+    assert len(out) == 11
+    np.testing.assert_allclose(np.array(out[:10]), np.array(direct[:10]), rtol=1e-12)
+    mod = engine.load_dropin("heisenberglib")
+    args = C.square_args("heisenberg", 8, 0.5, nthermal=5, nsweep=5)
+    out = mod.MCMainFunction(*args, lambda k: None)
+    assert len(out) == 29 and isinstance(out[28], tuple)
