@@ -1,0 +1,323 @@
+#!/usr/bin/env python
+"""Benchmark of the batched Monte Carlo engine on one GB300.
+
+Workload (the headline configuration): 2D square-lattice isotropic XY model,
+J = 1 K ferromagnetic (mcsolver sign convention Jxx = Jyy = -1), no
+anisotropy, L = 128 periodic (16384 sites), FP32 unit vectors with angles
+uniform in [0, 2pi) from the seed, Metropolis with one sweep per measurement
+(tau = N), 32 temperatures linear in 0.5..1.5 K, FP64 moment accumulators.
+All 32 replicas run in one batch.  A "step" is STEP_SWEEPS sweeps of every
+replica, each sweep followed by the full measurement of the reference.
+
+Metric: site updates per second (one Metropolis trial on one site = 1).
+* value: device time of the steps with the lattices already on the device
+  (L2 flushed between steps by writing a 256 MB buffer);
+* e2e:   the same work through the C ABI from host buffers: batch creation,
+  model compile and upload, the sweeps, and the read-back of every result;
+* cpu_baseline / --impl reference: the oracle's restatement of the reference
+  CPU library (bit-identical to it on the same random stream), one process
+  per host core, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import platform
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L = 128
+NTEMP = 32
+TEMPS = [0.5 + k * (1.5 - 0.5) / (NTEMP - 1) for k in range(NTEMP)]
+STEP_SWEEPS = 50
+WORKLOAD = "xy_square_L128_32T_metropolis"
+
+
+def workload_args(nsweep, nthermal=0):
+    from mcsolver_gb300.lattice import rescale_args, square_args
+    base = square_args("xy", L, 1.0, nthermal=nthermal, nsweep=nsweep, tau=0, groups=((0,),))
+    return [rescale_args("xy", base, T) for T in TEMPS]
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.p = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [l.strip().split(",") for l in open(self.path) if l.strip()]
+        except Exception:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in rows if len(r) > 8 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) > 8 and r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            if len(r) > 8:
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip().lower() == "active":
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def l2_flush():
+    import torch
+    global _flushbuf
+    try:
+        _flushbuf
+    except NameError:
+        _flushbuf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    _flushbuf.zero_()
+    torch.cuda.synchronize()
+
+
+# ---------------------------------------------------------------- CPU baseline
+def _cpu_one(job):
+    model, args, seed = job
+    from oracle import oracle as orc
+    t = time.time()
+    orc.solve(model, args, seed=seed, mode=0)
+    return time.time() - t
+
+
+def cpu_baseline(target_s=15.0):
+    """The oracle's reference-stream restatement (bit-identical to the
+    reference library) on every host core through a process pool, the way
+    the reference's win.startSimulation fans temperatures out."""
+    from oracle import oracle as orc
+    orc.build()
+    cores = os.cpu_count() or 1
+    cal = workload_args(nsweep=4)[0]
+    t0 = time.time()
+    orc.solve("xy", cal, seed=1, mode=0)
+    per_sweep = max(1e-4, (time.time() - t0) / 4)
+    sweeps = max(4, int(target_s * cores / (NTEMP * per_sweep)))
+    jobs = [("xy", a, 1 + k) for k, a in enumerate(workload_args(nsweep=sweeps))]
+    ctx = mp.get_context("spawn")
+    t = time.time()
+    with ctx.Pool(processes=cores) as pool:
+        pool.map(_cpu_one, jobs)
+    wall = time.time() - t
+    updates = NTEMP * sweeps * L * L
+    return {"value": updates / wall, "unit": "site_updates/s", "cores": cores, "kind": "port",
+            "sample": "%d temperatures x %d sweeps (tau=N, measurement every sweep) of XY L=%d, %s %s" % (
+                NTEMP, sweeps, L, platform.machine(), platform.processor() or ""),
+            "wall_s": wall}
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(args):
+    import numpy as np
+
+    import mcsolver_gb300 as eng
+    from mcsolver_gb300 import build as b
+    b.build()
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        peaks = {"hbm_gbs": 6800.0}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    K, W, S = args.steps, args.warmup, args.sweeps
+    total_sweeps = (W + K) * S + 1
+    prob_args = workload_args(nsweep=total_sweeps)
+    batch = eng.Batch(device=0)
+    for k, a in enumerate(prob_args):
+        batch.add("xy", a, seed=1000 + k, random_init=True)
+    batch.prepare()
+    for _ in range(W):
+        batch.advance(S)
+    l0 = batch.stats()["launches"]
+    times = []
+    with ClockSampler() as clk:
+        wall0 = time.time()
+        for _ in range(K):
+            l2_flush()
+            times.append(batch.advance(S))
+        wall = time.time() - wall0
+    launches = batch.stats()["launches"] - l0
+    batch.close()
+    per_step_updates = NTEMP * L * L * S
+    dev_s = sum(times) / 1000.0
+    value = per_step_updates * K / dev_s
+    ms_per_step = sum(times) / K
+    # roofline of the resident Metropolis kernel (one launch per step):
+    # algorithmic bytes = lattice read + written once per sweep, FP32 (x,y) = 16 B / site update
+    alg_bytes = 16.0 * per_step_updates
+    achieved = alg_bytes / (ms_per_step / 1000.0) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.isfile(tpath):
+        try:
+            tj = json.load(open(tpath))
+            traffic = tj.get("dram_bytes_per_step")
+        except Exception:
+            traffic = None
+    # e2e through the C ABI from host buffers
+    e2e_args = workload_args(nsweep=S)
+    problems = [eng.Problem("xy", a) for a in e2e_args]
+    e2e_t = []
+    h2d = d2h = 0
+    for it in range(max(2, min(K, 5))):
+        t = time.time()
+        bb = eng.Batch(device=0)
+        for k, a in enumerate(e2e_args):
+            bb.add("xy", a, seed=2000 + k, random_init=True)
+        bb.run()
+        outs = [bb.result(i) for i in range(NTEMP)]
+        e2e_t.append(time.time() - t)
+        mem = bb.memory()
+        h2d, d2h = mem["device_bytes"], mem["readback_bytes"]
+        bb.close()
+    del outs, problems
+    e2e_s = statistics.median(e2e_t[1:]) if len(e2e_t) > 1 else e2e_t[0]
+    e2e_value = per_step_updates / e2e_s
+    # plain engine (one solve per launch sequence, host-driven sweeps) on a sample
+    plain = None
+    if not args.no_plain:
+        t_plain = []
+        for k, a in enumerate(e2e_args[:4]):
+            r, ex = eng.solve("xy", a, seed=3000 + k, schedule="plain", random_init=True)
+            t_plain.append(ex["device_ms"])
+        plain_v = (L * L * S) / (statistics.mean(t_plain) / 1000.0)
+        plain = {"value": plain_v, "unit": "site_updates/s", "sample": "4 of the 32 replicas, one solve per launch "
+                 "sequence (one launch per colour, per measurement and per finalize, no graph)",
+                 "batched_over_plain": value / plain_v}
+    cpu = cpu_baseline(args.cpu_seconds) if not args.no_cpu else None
+    clocks = clk.summary()
+    line = {
+        "metric": "site_updates_per_s", "value": value, "unit": "site_updates/s", "n_gpus": 1, "steps": K,
+        "warmup": W, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 update / f64 accumulate", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "model": "XY", "L": L, "n_temperatures": NTEMP, "T_range_K": [0.5, 1.5],
+                   "algorithm": "Metropolis", "sweeps_per_step": S, "measurement": "every sweep (tau=N)",
+                   "replicas": NTEMP, "l2": "flushed between steps (256 MB write)", "schedule": "resident"},
+        "e2e": {"value": e2e_value, "unit": "site_updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "path": "C ABI mcs_batch_* from host arrays: create, compile+upload 32 replicas, run, read results"},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "kernel": "k_resident_metro<2,SQUARE>",
+                     "note": "lattice is shared-memory resident inside a launch; HBM is touched once per launch"},
+        "cpu_baseline": cpu,
+        "plain_engine": plain,
+        "clocks": clocks,
+        "wall_s_timed": wall,
+    }
+    print(json.dumps(line))
+
+
+def run_reference(args):
+    K, W = args.steps, args.warmup
+    vals = []
+    info = None
+    for i in range(W + K):
+        info = cpu_baseline(args.cpu_seconds / max(1, (W + K) / 3))
+        if i >= W:
+            vals.append(info["value"])
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": "site_updates_per_s", "value": v, "unit": "site_updates/s", "n_gpus": 1,
+            "steps": K, "warmup": W, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "config": {"workload": WORKLOAD, "model": "XY", "L": L,
+                                                             "n_temperatures": NTEMP, "algorithm": "Metropolis"},
+            "cpu_baseline": {"value": v, "unit": "site_updates/s", "cores": info["cores"], "kind": info["kind"],
+                             "sample": info["sample"]},
+            "e2e": {"value": v, "unit": "site_updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--sweeps", type=int, default=STEP_SWEEPS)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+    if args.gpus > 1 or int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        run_multi(args)
+        return
+    run_ours(args)
+
+
+def run_multi(args):
+    """Replicas only: every rank runs the full workload on its own GPU; value
+    sums the ranks' work over the slowest rank's time."""
+    import torch
+    import torch.distributed as dist
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    import mcsolver_gb300 as eng
+    from mcsolver_gb300 import build as b
+    if local == 0:
+        b.build()
+    dist.barrier()
+    K, W, S = args.steps, args.warmup, args.sweeps
+    batch = eng.Batch(device=local)
+    for k, a in enumerate(workload_args(nsweep=(W + K) * S + 1)):
+        batch.add("xy", a, seed=1000 + 100000 * dist.get_rank() + k, random_init=True)
+    batch.prepare()
+    for _ in range(W):
+        batch.advance(S)
+    dist.barrier()
+    torch.cuda.synchronize()
+    t = sum(batch.advance(S) for _ in range(K)) / 1000.0
+    tt = torch.tensor([t], device="cuda")
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    n = dist.get_world_size()
+    if dist.get_rank() == 0:
+        per = NTEMP * L * L * S * K
+        print(json.dumps({"metric": "site_updates_per_s", "value": per * n / tt.item(), "unit": "site_updates/s",
+                          "n_gpus": n, "steps": K, "warmup": W, "ms_per_step": tt.item() * 1000 / K,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "f32 update / f64 accumulate", "data": "synthetic",
+                          "config": {"workload": WORKLOAD, "parallelism": "replicas only"}}))
+    dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

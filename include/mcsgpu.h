@@ -131,9 +131,18 @@ int mcs_batch_create(int32_t device, mcs_batch **out);
 int mcs_batch_add(mcs_batch *b, const mcs_problem *problem, const mcs_options *options, int32_t *replica);
 /* Run every replica to completion (persistent launches, CUDA graphs). */
 int mcs_batch_run(mcs_batch *b);
+/* Upload and initialise without running (optional; mcs_batch_advance does it). */
+int mcs_batch_prepare(mcs_batch *b);
+/* Advance every unfinished replica by up to `units` units (Metropolis sweeps
+ * or Wolff clusters, each followed by its measurements); *device_ms receives
+ * the device time of this call. */
+int mcs_batch_advance(mcs_batch *b, int64_t units, double *device_ms);
 int mcs_batch_result(mcs_batch *b, int32_t replica, mcs_result *result);
 /* Device time of the last mcs_batch_run and its total site updates. */
 int mcs_batch_stats(mcs_batch *b, double *device_ms, int64_t *site_updates, int32_t *launches);
+/* Device bytes the batch holds (uploaded from the host) and bytes read back
+ * per result collection. */
+int mcs_batch_memory(mcs_batch *b, uint64_t *device_bytes, uint64_t *readback_bytes);
 void mcs_batch_destroy(mcs_batch *b);
 
 /* ---- parallel tempering over a temperature ladder (one model) ------------- */

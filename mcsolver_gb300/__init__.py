@@ -83,7 +83,8 @@ _lib = None
 # every function declared in include/mcsgpu.h
 ABI_FUNCTIONS = [
     "mcs_solve", "mcs_last_error", "mcs_abi_version", "mcs_build_info",
-    "mcs_batch_create", "mcs_batch_add", "mcs_batch_run", "mcs_batch_result", "mcs_batch_stats", "mcs_batch_destroy",
+    "mcs_batch_create", "mcs_batch_add", "mcs_batch_run", "mcs_batch_prepare", "mcs_batch_advance",
+    "mcs_batch_result", "mcs_batch_stats", "mcs_batch_memory", "mcs_batch_destroy",
     "mcs_pt_create", "mcs_pt_run", "mcs_pt_result", "mcs_pt_stats", "mcs_pt_destroy",
     "mcs_server_create", "mcs_server_submit", "mcs_server_step", "mcs_server_poll", "mcs_server_stats",
     "mcs_server_destroy",
@@ -104,8 +105,11 @@ def lib():
         L.mcs_batch_create.argtypes = [ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]
         L.mcs_batch_add.argtypes = [ctypes.c_void_p, ctypes.POINTER(McsProblem), ctypes.POINTER(McsOptions), _i32p]
         L.mcs_batch_run.argtypes = [ctypes.c_void_p]
+        L.mcs_batch_prepare.argtypes = [ctypes.c_void_p]
+        L.mcs_batch_advance.argtypes = [ctypes.c_void_p, ctypes.c_int64, _f64p]
         L.mcs_batch_result.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(McsResult)]
         L.mcs_batch_stats.argtypes = [ctypes.c_void_p, _f64p, ctypes.POINTER(ctypes.c_int64), _i32p]
+        L.mcs_batch_memory.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
         L.mcs_batch_destroy.argtypes = [ctypes.c_void_p]
         L.mcs_batch_destroy.restype = None
         _lib = L
@@ -268,6 +272,15 @@ class Batch:
     def run(self):
         _check(lib().mcs_batch_run(self._h))
 
+    def prepare(self):
+        _check(lib().mcs_batch_prepare(self._h))
+
+    def advance(self, units: int) -> float:
+        """Run every replica `units` more units; returns the device milliseconds."""
+        ms = ctypes.c_double()
+        _check(lib().mcs_batch_advance(self._h, int(units), ctypes.byref(ms)))
+        return ms.value
+
     def result(self, i: int):
         P = self._problems[i]
         rb = _ResultBuf(P, self._bufs[i])
@@ -280,6 +293,12 @@ class Batch:
         nl = ctypes.c_int32()
         _check(lib().mcs_batch_stats(self._h, ctypes.byref(ms), ctypes.byref(su), ctypes.byref(nl)))
         return {"device_ms": ms.value, "site_updates": su.value, "launches": nl.value}
+
+    def memory(self):
+        dev = ctypes.c_uint64()
+        rb = ctypes.c_uint64()
+        _check(lib().mcs_batch_memory(self._h, ctypes.byref(dev), ctypes.byref(rb)))
+        return {"device_bytes": dev.value, "readback_bytes": rb.value}
 
     def close(self):
         if self._h:

@@ -187,7 +187,7 @@ __device__ __forceinline__ bool on_trial(const Rep &R, const float *__restrict__
     float dE = d0 * h0 + d1 * h1 + d2 * h2;
     if (R.has_d) {
         int dc = R.stype ? R.stype[v] : 0;
-        const float *D = dt + 3 * dc;
+        const float *D = dt + 4 * dc;
         dE += D[0] * (d0 * (2.f * s0 + d0)) + D[1] * (d1 * (2.f * s1 + d1));
         if (DIM == 3) dE += D[2] * (d2 * (2.f * s2 + d2));
     }
@@ -196,9 +196,15 @@ __device__ __forceinline__ bool on_trial(const Rep &R, const float *__restrict__
     uint32_t wa = (DIM == 3) ? w.z : w.y;
     bool acc = (x <= 0.f) || (__expf(-x) > u24(wa));
     if (acc) {
-        S.x[v] = s0 + d0;
-        S.y[v] = s1 + d1;
-        if (DIM == 3) S.z[v] = s2 + d2;
+        // the reflection preserves |s| exactly; in FP32 the result is pulled
+        // back onto |s| = S so that the length cannot random-walk
+        float n0 = s0 + d0, n1 = s1 + d1, n2 = s2 + d2;
+        float len2 = n0 * n0 + n1 * n1 + n2 * n2;
+        float Sabs = dt[4 * (R.stype ? R.stype[v] : 0) + 3];
+        float k = len2 > 0.f ? Sabs * rsqrtf(len2) : 1.f;
+        S.x[v] = n0 * k;
+        S.y[v] = n1 * k;
+        if (DIM == 3) S.z[v] = n2 * k;
         *dEout = dE;
     }
     return acc;
@@ -291,7 +297,7 @@ __device__ __forceinline__ float on_onsite(const Rep &R, const float *dt, const 
     float e = 0.f;
     if (R.has_d) {
         int dc = R.stype ? R.stype[v] : 0;
-        const float *D = dt + 3 * dc;
+        const float *D = dt + 4 * dc;
         e = D[0] * s0 * s0 + D[1] * s1 * s1;
         if (DIM == 3) e += D[2] * s2 * s2;
     }

@@ -284,7 +284,9 @@ int replica_set_spins(Replica *r, const double *in)
 // ------------------------------------------------------------------ batch execution
 Batch::~Batch()
 {
+    groups.clear();
     if (d_reps) cudaFree(d_reps);
+    if (d_all) cudaFree(d_all);
     if (d_scratch) cudaFree(d_scratch);
     if (stream) cudaStreamDestroy(stream);
     if (stream2) cudaStreamDestroy(stream2);
@@ -332,231 +334,226 @@ static int choose_schedule(const Replica &r, int requested, int max_smem)
     return 3;
 }
 
-struct TiledPlan {
-    std::vector<int> ids;                       // replica ordinals
-    int dim = 0, geom = 0, maxcol = 0;
-    std::vector<std::vector<Item>> sweep_items; // per colour
-    std::vector<Item> meas_items;
-    std::vector<int> item_off, mitem_off;       // per replica (in plan order)
-    int nslots = 0;
-};
-
-int Batch::run_tiled(std::vector<int> &ids, int dim, int geom, bool use_graph, cudaStream_t st,
-                     std::vector<void *> &allocs)
+// ------------------------------------------------------------------ groups
+// Replicas run in groups of one kernel family; each group is set up once
+// (descriptor ids, tile lists, partial-sum buffers, captured graph) and then
+// advanced by any number of units.
+Group::~Group()
 {
-    TiledPlan P;
-    P.ids = ids; P.dim = dim; P.geom = geom;
-    for (int id : ids) P.maxcol = std::max(P.maxcol, replicas[id]->hm.ncol);
-    P.sweep_items.assign(P.maxcol, {});
-    // slot ranges per replica: all its sweep items over every colour
-    int slot = 0;
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (void *p : bufs) cudaFree(p);
+}
+
+int Batch::setup_tiled(Group &G)
+{
+    const int dim = G.dim, geom = G.geom;
+    for (int id : G.ids) G.maxcol = std::max(G.maxcol, replicas[id]->hm.ncol);
+    std::vector<std::vector<Item>> sweep(G.maxcol);
     const int per = dim == 1 ? 4 * 256 : 256;
-    P.item_off.push_back(0);
-    for (int id : ids) {
+    int slot = 0;
+    std::vector<int> ioff(1, 0), moff(1, 0);
+    std::vector<Item> meas;
+    for (int id : G.ids) {
         const HostModel &m = replicas[id]->hm;
         for (int c = 0; c < m.ncol; ++c) {
             int n = m.col_start[c + 1] - m.col_start[c];
             for (int b0 = 0; b0 < n; b0 += per) {
                 Item it; it.rep = id; it.begin = b0; it.end = std::min(n, b0 + per); it.slot = slot++;
-                P.sweep_items[c].push_back(it);
+                sweep[c].push_back(it);
             }
         }
-        P.item_off.push_back(slot);
-    }
-    P.nslots = slot;
-    const int mper = 512;
-    P.mitem_off.push_back(0);
-    for (int id : ids) {
-        const HostModel &m = replicas[id]->hm;
+        ioff.push_back(slot);
         int V = std::max(std::max(m.N, m.nlat), std::max(m.n_rorb, m.ncirc));
-        for (int b0 = 0; b0 < V; b0 += mper) {
-            Item it; it.rep = id; it.begin = b0; it.end = std::min(V, b0 + mper); it.slot = 0;
-            P.meas_items.push_back(it);
+        for (int b0 = 0; b0 < V; b0 += 512) {
+            Item it; it.rep = id; it.begin = b0; it.end = std::min(V, b0 + 512); it.slot = 0;
+            meas.push_back(it);
         }
-        P.mitem_off.push_back((int)P.meas_items.size());
+        moff.push_back((int)meas.size());
     }
-    // device buffers
-    size_t nsw = 0;
-    for (auto &v : P.sweep_items) nsw += v.size();
-    std::vector<Item> all_sw;
-    std::vector<size_t> cofs;
-    for (auto &v : P.sweep_items) { cofs.push_back(all_sw.size()); all_sw.insert(all_sw.end(), v.begin(), v.end()); }
-    Item *d_sw = nullptr, *d_mi = nullptr;
-    int *d_ids = nullptr, *d_ioff = nullptr, *d_moff = nullptr;
-    double *d_dE = nullptr, *d_fp = nullptr;
-    long long *d_ip = nullptr;
-    CUDA_TRY(cudaMalloc(&d_sw, std::max<size_t>(1, all_sw.size()) * sizeof(Item)));
-    CUDA_TRY(cudaMalloc(&d_mi, std::max<size_t>(1, P.meas_items.size()) * sizeof(Item)));
-    CUDA_TRY(cudaMalloc(&d_ids, ids.size() * sizeof(int)));
-    CUDA_TRY(cudaMalloc(&d_ioff, P.item_off.size() * sizeof(int)));
-    CUDA_TRY(cudaMalloc(&d_moff, P.mitem_off.size() * sizeof(int)));
-    CUDA_TRY(cudaMalloc(&d_dE, std::max(1, P.nslots) * sizeof(double)));
-    CUDA_TRY(cudaMalloc(&d_ip, std::max(1, P.nslots) * 9 * sizeof(long long)));
-    CUDA_TRY(cudaMalloc(&d_fp, std::max<size_t>(1, P.meas_items.size()) * F_NON * sizeof(double)));
-    allocs.insert(allocs.end(), {d_sw, d_mi, d_ids, d_ioff, d_moff, d_dE, d_ip, d_fp});
-    CUDA_TRY(cudaMemcpyAsync(d_sw, all_sw.data(), all_sw.size() * sizeof(Item), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(d_mi, P.meas_items.data(), P.meas_items.size() * sizeof(Item), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(d_ids, ids.data(), ids.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(d_ioff, P.item_off.data(), P.item_off.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(d_moff, P.mitem_off.data(), P.mitem_off.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemsetAsync(d_dE, 0, std::max(1, P.nslots) * sizeof(double), st));
-    CUDA_TRY(cudaMemsetAsync(d_ip, 0, std::max(1, P.nslots) * 9 * sizeof(long long), st));
-    // the sweep kernel writes its partial at item.colour (slot); pass the colour separately
-    long long steps = 0;
-    for (int id : ids) steps = std::max(steps, replicas[id]->hm.units_total);
-    auto one_unit = [&](cudaStream_t s) -> cudaError_t {
-        for (int c = 0; c < P.maxcol; ++c) {
-            cudaError_t e = launch_tiled_sweep(dim, geom, d_reps, d_sw + cofs[c], (int)P.sweep_items[c].size(), c,
-                                               d_dE, d_ip, dim == 1 ? 256 : 256, s);
-            if (e != cudaSuccess) return e;
-            launches++;
-        }
-        cudaError_t e = launch_tiled_measure(dim, geom, d_reps, d_mi, (int)P.meas_items.size(), d_fp, 256, s);
-        if (e != cudaSuccess) return e;
-        e = launch_tiled_finalize_dim(dim, d_reps, d_ids, (int)ids.size(), d_ioff, d_dE, d_ip, d_moff, d_fp, s);
-        launches += 2;
-        return e;
-    };
-    if (!use_graph || steps < 8) {
-        for (long long u = 0; u < steps; ++u) CUDA_TRY(one_unit(st));
+    std::vector<Item> all;
+    for (auto &v : sweep) { G.cofs.push_back(all.size()); G.ccount.push_back((int)v.size()); all.insert(all.end(), v.begin(), v.end()); }
+    G.nmeas = (int)meas.size();
+    auto dalloc = [&](size_t bytes, void **p) -> int {
+        CUDA_TRY(cudaMalloc(p, std::max<size_t>(bytes, 16)));
+        G.bufs.push_back(*p);
         return MCS_OK;
-    }
-    const int K = (int)std::min<long long>(steps, 32);
-    cudaGraph_t graph;
-    cudaGraphExec_t exec;
-    CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    long long saved = launches;
-    for (int k = 0; k < K; ++k) {
-        cudaError_t e = one_unit(st);
-        if (e != cudaSuccess) {
-            cudaStreamEndCapture(st, &graph);
-            set_error(std::string("CUDA error during capture: ") + cudaGetErrorString(e));
-            return MCS_ECUDA;
-        }
-    }
-    CUDA_TRY(cudaStreamEndCapture(st, &graph));
-    long long per_graph = launches - saved;
-    launches = saved;
-    CUDA_TRY(cudaGraphInstantiate(&exec, graph, 0));
-    long long done = 0;
-    while (done + K <= steps) {
-        CUDA_TRY(cudaGraphLaunch(exec, st));
-        launches += per_graph;
-        done += K;
-    }
-    for (; done < steps; ++done) CUDA_TRY(one_unit(st));
-    cudaGraphExecDestroy(exec);
-    cudaGraphDestroy(graph);
+    };
+    int rc;
+    if ((rc = dalloc(all.size() * sizeof(Item), (void **)&G.d_sw))) return rc;
+    if ((rc = dalloc(meas.size() * sizeof(Item), (void **)&G.d_mi))) return rc;
+    if ((rc = dalloc(ioff.size() * sizeof(int), (void **)&G.d_ioff))) return rc;
+    if ((rc = dalloc(moff.size() * sizeof(int), (void **)&G.d_moff))) return rc;
+    if ((rc = dalloc(std::max(1, slot) * sizeof(double), (void **)&G.d_dE))) return rc;
+    if ((rc = dalloc(std::max(1, slot) * 9 * sizeof(long long), (void **)&G.d_ip))) return rc;
+    if ((rc = dalloc(meas.size() * F_NON * sizeof(double), (void **)&G.d_fp))) return rc;
+    CUDA_TRY(cudaMemcpy(G.d_sw, all.data(), all.size() * sizeof(Item), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(G.d_mi, meas.data(), meas.size() * sizeof(Item), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(G.d_ioff, ioff.data(), ioff.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(G.d_moff, moff.data(), moff.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemset(G.d_dE, 0, std::max(1, slot) * sizeof(double)));
+    CUDA_TRY(cudaMemset(G.d_ip, 0, std::max(1, slot) * 9 * sizeof(long long)));
+    (void)geom;
     return MCS_OK;
 }
 
-int Batch::run()
+cudaError_t Batch::tiled_unit(Group &G, cudaStream_t s, long long *nl)
 {
+    for (int c = 0; c < G.maxcol; ++c) {
+        cudaError_t e = launch_tiled_sweep(G.dim, G.geom, d_reps, G.d_sw + G.cofs[c], G.ccount[c], c, G.d_dE, G.d_ip, 256, s);
+        if (e != cudaSuccess) return e;
+        ++*nl;
+    }
+    cudaError_t e = launch_tiled_measure(G.dim, G.geom, d_reps, G.d_mi, G.nmeas, G.d_fp, 256, s);
+    if (e != cudaSuccess) return e;
+    e = launch_tiled_finalize_dim(G.dim, d_reps, G.d_ids, (int)G.ids.size(), G.d_ioff, G.d_dE, G.d_ip, G.d_moff, G.d_fp, s);
+    *nl += 2;
+    return e;
+}
+
+int Batch::prepare()
+{
+    if (prepared) return MCS_OK;
     int src = ensure_streams();
     if (src != MCS_OK) return src;
     const int nrep = (int)replicas.size();
-    if (nrep == 0) return MCS_OK;
+    if (nrep == 0) { prepared = true; return MCS_OK; }
     const int max_smem = resident_max_smem();
     std::vector<Rep> host(nrep);
     for (int i = 0; i < nrep; ++i) {
         Replica &r = *replicas[i];
         r.schedule = choose_schedule(r, r.requested_schedule, max_smem);
+        if (r.hm.alg == 1) {
+            set_error("Wolff updates are not built in this engine version");
+            return MCS_EUNSUPPORTED;
+        }
         host[i] = r.rep;
     }
-    if (d_reps) cudaFree(d_reps);
     CUDA_TRY(cudaMalloc(&d_reps, nrep * sizeof(Rep)));
     CUDA_TRY(cudaMemcpy(d_reps, host.data(), nrep * sizeof(Rep), cudaMemcpyHostToDevice));
-    launches = 0;
-    std::vector<void *> allocs;
-    auto cleanup = [&]() { for (void *p : allocs) cudaFree(p); };
-    CUDA_TRY(cudaEventRecord(ev0, stream));
     // initial energies / exact sums
     {
         std::vector<int> all(nrep);
         for (int i = 0; i < nrep; ++i) all[i] = i;
-        int *d_all = nullptr;
         CUDA_TRY(cudaMalloc(&d_all, nrep * sizeof(int)));
-        allocs.push_back(d_all);
-        CUDA_TRY(cudaMemcpyAsync(d_all, all.data(), nrep * sizeof(int), cudaMemcpyHostToDevice, stream));
+        CUDA_TRY(cudaMemcpy(d_all, all.data(), nrep * sizeof(int), cudaMemcpyHostToDevice));
         for (int d = 1; d <= 3; ++d)
             for (int g = 0; g <= 1; ++g) {
                 bool any = false;
                 for (auto &r : replicas) any |= (r->hm.dim == d && r->hm.geom == g);
                 if (!any) continue;
-                cudaError_t e = launch_init_state_dg(d, g, d_reps, d_all, nrep, stream);
-                if (e != cudaSuccess) { cleanup(); set_error(cudaGetErrorString(e)); return MCS_ECUDA; }
+                CUDA_TRY(launch_init_state_dg(d, g, d_reps, d_all, nrep, stream));
                 launches++;
             }
     }
-    // resident groups
-    for (int d = 1; d <= 3; ++d)
-        for (int g = 0; g <= 1; ++g) {
-            std::vector<int> ids;
-            long long maxu = 0, maxn = 0;
-            size_t smem = 0;
-            int maxcs = 0;
-            for (int i = 0; i < nrep; ++i) {
-                Replica &r = *replicas[i];
-                if (r.schedule != 2 || r.hm.dim != d || r.hm.geom != g || r.hm.alg != 0) continue;
-                ids.push_back(i);
-                maxu = std::max(maxu, r.hm.units_total);
-                maxn = std::max<long long>(maxn, r.hm.N);
-                smem = std::max<size_t>(smem, (size_t)resident_smem_bytes(r.rep));
-                for (int c = 0; c < r.hm.ncol; ++c)
-                    maxcs = std::max(maxcs, r.hm.col_start[c + 1] - r.hm.col_start[c]);
-            }
-            if (ids.empty()) continue;
-            int *d_ids = nullptr;
-            CUDA_TRY(cudaMalloc(&d_ids, ids.size() * sizeof(int)));
-            allocs.push_back(d_ids);
-            CUDA_TRY(cudaMemcpyAsync(d_ids, ids.data(), ids.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
-            int work = d == 1 ? (maxcs + 3) / 4 : maxcs;
-            int threads = std::min(1024, std::max(64, ((work + 31) / 32) * 32));
-            if (threads_override > 0) threads = threads_override;
-            long long chunk = std::max<long long>(1, (1LL << 28) / std::max<long long>(1, maxn));
-            if (chunk_override > 0) chunk = chunk_override;
-            for (long long u = 0; u < maxu; u += chunk) {
-                cudaError_t e = launch_resident_metro(d, g, d_reps, d_ids, (int)ids.size(), threads, smem, chunk, stream);
-                if (e != cudaSuccess) { cleanup(); set_error(std::string("resident launch: ") + cudaGetErrorString(e)); return MCS_ECUDA; }
-                launches++;
-            }
-        }
-    // tiled / plain groups
-    for (int d = 1; d <= 3; ++d)
-        for (int g = 0; g <= 1; ++g) {
-            std::vector<int> ids;
-            for (int i = 0; i < nrep; ++i) {
-                Replica &r = *replicas[i];
-                if (r.schedule == 3 && r.hm.dim == d && r.hm.geom == g && r.hm.alg == 0) ids.push_back(i);
-            }
-            if (!ids.empty()) {
-                int rc = run_tiled(ids, d, g, true, stream, allocs);
-                if (rc != MCS_OK) { cleanup(); return rc; }
-            }
-            for (int i = 0; i < nrep; ++i) {
-                Replica &r = *replicas[i];
-                if (r.schedule == 1 && r.hm.dim == d && r.hm.geom == g && r.hm.alg == 0) {
-                    std::vector<int> one = {i};
-                    int rc = run_tiled(one, d, g, false, stream, allocs);
-                    if (rc != MCS_OK) { cleanup(); return rc; }
+    // groups
+    for (int kind : {2, 3, 1})
+        for (int d = 1; d <= 3; ++d)
+            for (int g = 0; g <= 1; ++g) {
+                std::vector<int> ids;
+                for (int i = 0; i < nrep; ++i) {
+                    Replica &r = *replicas[i];
+                    if (r.schedule == kind && r.hm.dim == d && r.hm.geom == g) ids.push_back(i);
+                }
+                if (ids.empty()) continue;
+                std::vector<std::vector<int>> sets;
+                if (kind == 1) for (int id : ids) sets.push_back({id});
+                else sets.push_back(ids);
+                for (auto &set : sets) {
+                    std::unique_ptr<Group> G(new Group());
+                    G->kind = kind; G->dim = d; G->geom = g; G->ids = set;
+                    CUDA_TRY(cudaMalloc(&G->d_ids, set.size() * sizeof(int)));
+                    G->bufs.push_back(G->d_ids);
+                    CUDA_TRY(cudaMemcpy(G->d_ids, set.data(), set.size() * sizeof(int), cudaMemcpyHostToDevice));
+                    long long maxn = 0;
+                    int maxcs = 0;
+                    for (int id : set) {
+                        Replica &r = *replicas[id];
+                        G->max_units = std::max(G->max_units, r.hm.units_total);
+                        maxn = std::max<long long>(maxn, r.hm.N);
+                        G->smem = std::max<size_t>(G->smem, (size_t)resident_smem_bytes(r.rep));
+                        for (int c = 0; c < r.hm.ncol; ++c)
+                            maxcs = std::max(maxcs, r.hm.col_start[c + 1] - r.hm.col_start[c]);
+                    }
+                    if (kind == 2) {
+                        int work = d == 1 ? (maxcs + 3) / 4 : maxcs;
+                        G->threads = std::min(1024, std::max(64, ((work + 31) / 32) * 32));
+                        if (threads_override > 0) G->threads = threads_override;
+                        G->chunk = std::max<long long>(1, (1LL << 28) / std::max<long long>(1, maxn));
+                        if (chunk_override > 0) G->chunk = chunk_override;
+                    } else {
+                        int rc = setup_tiled(*G);
+                        if (rc != MCS_OK) return rc;
+                    }
+                    groups.push_back(std::move(G));
                 }
             }
+    prepared = true;
+    return MCS_OK;
+}
+
+int Batch::advance(long long units)
+{
+    int rc = prepare();
+    if (rc != MCS_OK) return rc;
+    if (replicas.empty()) return MCS_OK;
+    CUDA_TRY(cudaEventRecord(ev0, stream));
+    for (auto &Gp : groups) {
+        Group &G = *Gp;
+        long long todo = std::min(units, G.max_units - G.done_units);
+        if (todo <= 0) continue;
+        if (G.kind == 2) {
+            for (long long u = 0; u < todo; u += G.chunk) {
+                long long n = std::min(G.chunk, todo - u);
+                cudaError_t e = launch_resident_metro(G.dim, G.geom, d_reps, G.d_ids, (int)G.ids.size(), G.threads, G.smem, n, stream);
+                if (e != cudaSuccess) { set_error(std::string("resident launch: ") + cudaGetErrorString(e)); return MCS_ECUDA; }
+                launches++;
+            }
+        } else if (G.kind == 3 && todo >= 8) {
+            if (!G.exec) {
+                G.K = (int)std::min<long long>(32, std::max<long long>(1, todo));
+                long long nl = 0;
+                CUDA_TRY(cudaStreamBeginCapture(stream2, cudaStreamCaptureModeThreadLocal));
+                for (int k = 0; k < G.K; ++k) {
+                    cudaError_t e = tiled_unit(G, stream2, &nl);
+                    if (e != cudaSuccess) {
+                        cudaGraph_t g0;
+                        cudaStreamEndCapture(stream2, &g0);
+                        if (g0) cudaGraphDestroy(g0);
+                        set_error(std::string("capture: ") + cudaGetErrorString(e));
+                        return MCS_ECUDA;
+                    }
+                }
+                CUDA_TRY(cudaStreamEndCapture(stream2, &G.graph));
+                CUDA_TRY(cudaGraphInstantiate(&G.exec, G.graph, 0));
+                G.per_graph = nl;
+            }
+            long long u = 0;
+            for (; u + G.K <= todo; u += G.K) {
+                CUDA_TRY(cudaGraphLaunch(G.exec, stream));
+                launches += G.per_graph;
+            }
+            for (; u < todo; ++u) CUDA_TRY(tiled_unit(G, stream, &launches));
+        } else {
+            for (long long u = 0; u < todo; ++u) CUDA_TRY(tiled_unit(G, stream, &launches));
         }
-    // Wolff replicas
-    for (int i = 0; i < nrep; ++i)
-        if (replicas[i]->hm.alg == 1) {
-            cleanup();
-            set_error("Wolff updates are not built in this engine version");
-            return MCS_EUNSUPPORTED;
-        }
+        G.done_units += todo;
+    }
     CUDA_TRY(cudaEventRecord(ev1, stream));
     cudaError_t e = cudaStreamSynchronize(stream);
-    cleanup();
     if (e != cudaSuccess) { set_error(std::string("CUDA error in run: ") + cudaGetErrorString(e)); return MCS_ECUDA; }
     float ms = 0;
     cudaEventElapsedTime(&ms, ev0, ev1);
-    device_ms = ms;
-    CUDA_TRY(cudaMemcpy(host.data(), d_reps, nrep * sizeof(Rep), cudaMemcpyDeviceToHost));
+    device_ms += ms;
+    last_ms = ms;
+    return MCS_OK;
+}
+
+int Batch::collect()
+{
+    const int nrep = (int)replicas.size();
+    std::vector<Rep> host(nrep);
+    if (nrep) CUDA_TRY(cudaMemcpy(host.data(), d_reps, nrep * sizeof(Rep), cudaMemcpyDeviceToHost));
     final_reps = host;
     site_updates = 0;
     for (int i = 0; i < nrep; ++i) {
@@ -565,6 +562,16 @@ int Batch::run()
         site_updates += replicas[i]->hm.alg == 0 ? st[S_VISITS] : st[S_FLIPPED];
     }
     return MCS_OK;
+}
+
+int Batch::run()
+{
+    device_ms = 0;
+    long long maxu = 0;
+    for (auto &r : replicas) maxu = std::max(maxu, r->hm.units_total);
+    int rc = advance(maxu);
+    if (rc != MCS_OK) return rc;
+    return collect();
 }
 
 int Batch::result(int i, mcs_result *res)
@@ -636,6 +643,15 @@ int mcs_batch_add(mcs_batch *b, const mcs_problem *problem, const mcs_options *o
     return rc;
 }
 int mcs_batch_run(mcs_batch *b) { return b ? b->b.run() : MCS_EINVAL; }
+int mcs_batch_prepare(mcs_batch *b) { return b ? b->b.prepare() : MCS_EINVAL; }
+int mcs_batch_advance(mcs_batch *b, int64_t units, double *device_ms)
+{
+    if (!b) return MCS_EINVAL;
+    int rc = b->b.advance(units);
+    if (rc == MCS_OK) rc = b->b.collect();
+    if (device_ms) *device_ms = b->b.last_ms;
+    return rc;
+}
 int mcs_batch_result(mcs_batch *b, int32_t replica, mcs_result *result) { return b ? b->b.result(replica, result) : MCS_EINVAL; }
 int mcs_batch_stats(mcs_batch *b, double *device_ms, int64_t *site_updates, int32_t *launches)
 {
@@ -643,6 +659,18 @@ int mcs_batch_stats(mcs_batch *b, double *device_ms, int64_t *site_updates, int3
     if (device_ms) *device_ms = b->b.device_ms;
     if (site_updates) *site_updates = b->b.site_updates;
     if (launches) *launches = (int32_t)b->b.launches;
+    return MCS_OK;
+}
+int mcs_batch_memory(mcs_batch *b, uint64_t *device_bytes, uint64_t *readback_bytes)
+{
+    if (!b) return MCS_EINVAL;
+    uint64_t dev = 0, rb = 0;
+    for (auto &r : b->b.replicas) {
+        dev += r->bytes + sizeof(Rep);
+        rb += sizeof(Rep) + r->nacc * sizeof(double) + (C_NINT + S_NSTAT) * sizeof(long long);
+    }
+    if (device_bytes) *device_bytes = dev;
+    if (readback_bytes) *readback_bytes = rb;
     return MCS_OK;
 }
 void mcs_batch_destroy(mcs_batch *b) { delete b; }

@@ -37,12 +37,43 @@ int replica_spins(Replica *r, std::vector<double> &out);
 int replica_set_spins(Replica *r, const double *in);
 size_t replica_acc_count(const HostModel &m);
 
+// A set of replicas advanced by one kernel family.
+struct Group {
+    int kind = 0;              // 1 plain, 2 resident, 3 tiled
+    int dim = 0, geom = 0;
+    std::vector<int> ids;
+    int *d_ids = nullptr;
+    long long max_units = 0, done_units = 0;
+    // resident
+    int threads = 0;
+    size_t smem = 0;
+    long long chunk = 0;
+    // tiled
+    int maxcol = 0, nmeas = 0;
+    std::vector<size_t> cofs;
+    std::vector<int> ccount;
+    Item *d_sw = nullptr, *d_mi = nullptr;
+    int *d_ioff = nullptr, *d_moff = nullptr;
+    double *d_dE = nullptr, *d_fp = nullptr;
+    long long *d_ip = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int K = 0;
+    long long per_graph = 0;
+    std::vector<void *> bufs;
+    ~Group();
+};
+
 // Many replicas of uneven sizes run together.
 struct Batch {
     int device = 0;
     std::vector<std::unique_ptr<Replica>> replicas;
     Rep *d_reps = nullptr;
+    int *d_all = nullptr;
     void *d_scratch = nullptr;
+    bool prepared = false;
+    std::vector<std::unique_ptr<Group>> groups;
+    double last_ms = 0;
     cudaStream_t stream = nullptr, stream2 = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double device_ms = 0;
@@ -55,10 +86,13 @@ struct Batch {
     int init(int dev);
     int ensure_streams();
     int add(const mcs_problem *p, const mcs_options *o, int *idx);
-    int run();
+    int prepare();                 // upload descriptors, initial energies, build groups
+    int advance(long long units);  // every replica runs up to `units` more units
+    int collect();                 // read back descriptors and counters
+    int run();                     // prepare + advance to completion + collect
     int result(int i, mcs_result *res);
-    int run_tiled(std::vector<int> &ids, int dim, int geom, bool use_graph, cudaStream_t st,
-                  std::vector<void *> &allocs);
+    int setup_tiled(Group &G);
+    cudaError_t tiled_unit(Group &G, cudaStream_t s, long long *nl);
 };
 
 }  // namespace mcs

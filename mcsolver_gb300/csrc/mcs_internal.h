@@ -82,7 +82,7 @@ struct Rep {
     // ---- parameters
     const float *jtab; int njc; int fullJ;       // O(n) [njc][9] xx,yy,zz,xy,xz,yz,yx,zx,zy
     const double *jtab64;                        // same in FP64 (fp64 updates)
-    const float *dtab; int ndc; int has_d;       // O(n) [ndc][3]
+    const float *dtab; int ndc; int has_d;       // O(n) [ndc][4]: Dx, Dy, Dz, |S|
     const IsEntry *itab; int nite; int ntype;    // Ising
     int ibase[MCS_MAXT];
     double Q[MCS_MAXC]; int nclass; int exact_ok;

@@ -36,7 +36,7 @@ __host__ __device__ inline SmemLayout smem_layout(const Rep &R)
     else off += align16((size_t)R.dim * R.N * sizeof(float));
     L.tables = off;
     if (R.dim == 1) off += align16((size_t)R.nite * sizeof(IsEntry));
-    else off += align16((size_t)R.njc * 9 * sizeof(float) + (size_t)R.ndc * 3 * sizeof(float));
+    else off += align16((size_t)R.njc * 9 * sizeof(float) + (size_t)R.ndc * 4 * sizeof(float));
     L.red = off; off += MCS_RED_DOUBLES * sizeof(double);
     L.F = off; off += F_NON * sizeof(double);
     L.redl = off; off += 32 * (MCS_MAXT + MCS_MAXC + 1) * sizeof(long long);
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
             if (DIM == 3) S.z[v] = G.z[v];
         }
         for (int k = tid; k < R.njc * 9; k += bd) jt[k] = R.jtab[k];
-        for (int k = tid; k < R.ndc * 3; k += bd) dt[k] = R.dtab[k];
+        for (int k = tid; k < R.ndc * 4; k += bd) dt[k] = R.dtab[k];
     }
     __syncthreads();
 

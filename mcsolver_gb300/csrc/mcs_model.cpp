@@ -189,7 +189,7 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
         m->jtab64.resize(9 * tab.size());
         for (size_t c = 0; c < tab.size(); ++c)
             for (int k = 0; k < 9; ++k) { m->jtab[9 * c + k] = (float)tab[c][k]; m->jtab64[9 * c + k] = tab[c][k]; }
-        // anisotropy classes
+        // site classes: anisotropy vector and spin length |S|
         std::map<std::vector<double>, int> dcls;
         std::vector<std::vector<double>> dt;
         m->stype.assign(N, 0);
@@ -199,18 +199,19 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
             std::vector<double> v(p->init_d + 3 * (size_t)i, p->init_d + 3 * (size_t)i + 3);
             if (dim == 2) v[2] = 0.0;
             for (double x : v) anyd |= x != 0.0;
+            v.push_back(fabs(p->init_spin[i]));
             auto it = dcls.find(v);
             int c;
             if (it == dcls.end()) { c = (int)dt.size(); dcls[v] = c; dt.push_back(v); }
             else c = it->second;
-            if (c > 255) FAIL(MCS_EUNSUPPORTED, "more than 256 distinct anisotropy vectors");
+            if (c > 255) FAIL(MCS_EUNSUPPORTED, "more than 256 distinct (anisotropy, spin length) site classes");
             m->stype[k] = (uint8_t)c;
         }
         m->ndc = (int)dt.size();
         m->has_d = anyd ? 1 : 0;
-        m->dtab.resize(3 * dt.size());
+        m->dtab.resize(4 * dt.size());
         for (size_t c = 0; c < dt.size(); ++c)
-            for (int k = 0; k < 3; ++k) m->dtab[3 * c + k] = (float)dt[c][k];
+            for (int k = 0; k < 4; ++k) m->dtab[4 * c + k] = (float)dt[c][k];
     } else {
         // Ising: classes of Q = K |s_i| |s_j|, site types (|s_i|, class counts)
         std::map<double, int> qcls;

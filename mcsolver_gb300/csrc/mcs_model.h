@@ -32,7 +32,7 @@ struct HostModel {
     std::vector<float> jtab;             // [njc][9]
     std::vector<double> jtab64;
     int njc = 0, fullJ = 0;
-    std::vector<float> dtab;             // [ndc][3]
+    std::vector<float> dtab;             // [ndc][4]: Dx, Dy, Dz, |S|
     int ndc = 0, has_d = 0;
     // Ising tables
     std::vector<IsEntry> itab;

@@ -1,0 +1,204 @@
+"""Model builder: the MCMainFunction argument tuples of periodic lattices.
+
+``lattice_args`` produces, for a periodic supercell of a lattice with
+``norb`` orbitals per cell and a list of bonds, exactly the positional tuple
+that mcsolver's ``mcMain.MC`` builds and passes to the compiled library
+(site id order x, y, z, orbital as Lattice.py:172-184; links in the order of
+Lattice.addLinking, merging duplicate targets as Lattice.py:34-57; the
+renormalised cluster and link lists of Lattice.py:185-205 and :263-271;
+J, D and h divided by T as mcMain.py:21-31, :121, :244).  It lets callers
+drive the engine without mcsolver's Python object graph, and it is checked
+against tuples captured from the reference's own code in the test suite.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def _lattice_links(L, norb, bonds):
+    """Links per site in the reference's insertion order (Lattice.py:247-271)."""
+    Lx, Ly, Lz = L
+    N = Lx * Ly * Lz * norb
+
+    def sid(x, y, z, o):
+        return ((x % Lx) * Ly * Lz + (y % Ly) * Lz + (z % Lz)) * norb + o
+
+    links = [[] for _ in range(N)]   # (target, strength)
+    rlinks = [[] for _ in range(N)]
+    chosen = [False] * N
+    for x in range(Lx):
+        for y in range(Ly):
+            for z in range(Lz):
+                for o in range(norb):
+                    if x % 2 + y % 2 + z % 2 == 0:
+                        chosen[sid(x, y, z, o)] = True
+
+    def add(lst, i, j, s, merge):
+        for k, (t, s0) in enumerate(lst[i]):
+            if t == j:
+                if merge:
+                    if np.sum(np.abs(np.asarray(s0) - np.asarray(s))) < 1e-5:
+                        return
+                    lst[i][k] = (t, np.asarray(s0) + np.asarray(s))
+                return
+        lst[i].append((j, np.asarray(s)))
+
+    for x in range(Lx):
+        for y in range(Ly):
+            for z in range(Lz):
+                for o in range(norb):
+                    i = sid(x, y, z, o)
+                    for (src, tgt, ov, J, Jinv) in bonds:
+                        if o != src:
+                            continue
+                        j = sid(x + ov[0], y + ov[1], z + ov[2], tgt)
+                        add(links, i, j, J, True)
+                        if i != j:
+                            add(links, j, i, Jinv, True)
+                    if chosen[i]:
+                        for (src, tgt, ov, J, Jinv) in bonds:
+                            if o != src:
+                                continue
+                            j = sid(x + 2 * ov[0], y + 2 * ov[1], z + 2 * ov[2], tgt)
+                            add(rlinks, i, j, J, False)
+                            if i != j:
+                                add(rlinks, j, i, Jinv, False)
+    return N, links, rlinks, chosen, sid
+
+
+def lattice_args(model, L, norb, bonds, T, h=0.0, S=None, D=None, nthermal=10, nsweep=10, tau=0, algo=0,
+                 ki=((0, 0), (0, 0, 0)), groups=(), circuits=(), frames=0, flunc=0.0):
+    """MCMainFunction tuple for a periodic lattice; J, D and h are divided by T
+    as mcMain.py does (mcMain.py:21-31, :121, :244)."""
+    T = max(T, 0.1)
+    S = S or [1.0] * norb
+    D = D or [[0.0, 0.0, 0.0]] * norb
+    on = model != "ising"
+    bl = []
+    for (src, tgt, ov, J9) in bonds:
+        J9 = np.asarray(J9, dtype=float) / T
+        if on:
+            Jxx, Jyy, Jzz, Jxy, Jxz, Jyz, Jyx, Jzx, Jzy = J9
+            inv = np.array([Jxx, Jyy, Jzz, Jyx, Jzx, Jzy, Jxy, Jxz, Jyz])
+            bl.append((src, tgt, ov, J9, inv))
+        else:
+            bl.append((src, tgt, ov, J9[0], J9[0]))
+    N, links, rlinks, chosen, sid = _lattice_links(L, norb, bl)
+    Lx, Ly, Lz = L
+    z = max(len(l) for l in links)
+    init = [S[i % norb] for i in range(N)]
+    nlink = [len(l) for l in links]
+    lo, ls = [], []
+    for i in range(N):
+        for k in range(z):
+            if k < len(links[i]):
+                lo.append(links[i][k][0])
+                s = links[i][k][1]
+                ls += (list(map(float, s)) if on else [float(s)])
+            else:
+                lo.append(-1)
+                ls += ([0.0] * 9 if on else [0.0])
+    rorb, rcl, rlk = [], [], []
+    for x in range(Lx):
+        for y in range(Ly):
+            for zz in range(Lz):
+                for o in range(norb):
+                    i = sid(x, y, zz, o)
+                    if not chosen[i]:
+                        continue
+                    rorb.append(i)
+                    cl = []
+                    for (dx, dy, dz) in ((0, 0, 0), (0, 0, 1), (0, 1, 0), (1, 0, 0), (0, 1, 1), (1, 0, 1), (1, 1, 0), (1, 1, 1)):
+                        c = sid(x + dx, y + dy, zz + dz, o)
+                        if c not in cl:
+                            cl.append(c)
+                    rcl.append(cl)
+                    rlk += [rlinks[i][k][0] if k < len(rlinks[i]) else -1 for k in range(z)]
+    ncl = len(rcl[0])
+    rcl = [c for cl in rcl for c in cl[:ncl]]
+    cp = []
+    (ks, kt), kov = ki
+    for x in range(Lx):
+        for y in range(Ly):
+            for zz in range(Lz):
+                cp += [sid(x, y, zz, ks), sid(x + kov[0], y + kov[1], zz + kov[2], kt)]
+    tau = N if tau <= 0 else tau
+    if not on:
+        return (algo, tuple(init), nthermal, nsweep, tau, z, tuple(nlink), tuple(ls), tuple(lo), tuple(cp),
+                h / T, tuple(rorb), tuple(rcl), tuple(rlk), frames)
+    initD = []
+    for i in range(N):
+        initD += [float(d) / T for d in D[i % norb]]
+    circ = []
+    for x in range(Lx):
+        for y in range(Ly):
+            for zz in range(Lz):
+                for c in circuits:
+                    for (o, ov) in c:
+                        circ.append(sid(x + ov[0], y + ov[1], zz + ov[2], o))
+    grp = []
+    maxg = 1
+    gl = [[sid(x, y, zz, o) for o in g for x in range(Lx) for y in range(Ly) for zz in range(Lz)] for g in groups]
+    if gl:
+        maxg = max(len(g) for g in gl)
+        for g in gl:
+            grp += g + [-1] * (maxg - len(g))
+    ign = 1
+    for i in range(N):
+        for k in range(len(links[i])):
+            if any(abs(v) > 1e-6 for v in links[i][k][1][3:]):
+                ign = 0
+    return (algo, tuple(init), tuple(initD), nthermal, nsweep, tau, z, tuple(nlink), tuple(ls), tuple(lo),
+            tuple(circ), tuple(cp), len(groups), maxg, tuple(grp), flunc, h / T, tuple(rorb), tuple(rcl),
+            tuple(rlk), frames, ign)
+
+
+def J9(xx, yy=0, zz=0, xy=0, xz=0, yz=0, yx=0, zx=0, zy=0):
+    return [xx, yy, zz, xy, xz, yz, yx, zx, zy]
+
+
+SQ_CIRCUITS = [((0, (0, 0, 0)), (0, (1, 0, 0)), (0, (1, 1, 0))), ((0, (0, 0, 0)), (0, (1, 1, 0)), (0, (0, 1, 0)))]
+
+
+def square_args(model, L, T, J=-1.0, h=0.0, dmi=0.0, D=None, nthermal=10, nsweep=10, tau=0, algo=0, frames=0,
+                groups=((0,),), circuits=True):
+    if model == "ising":
+        bonds = [(0, 0, (1, 0, 0), J9(J)), (0, 0, (0, 1, 0), J9(J))]
+        return lattice_args("ising", (L, L, 1), 1, bonds, T, h=h, nthermal=nthermal, nsweep=nsweep, tau=tau,
+                            algo=algo, frames=frames)
+    bonds = [(0, 0, (1, 0, 0), J9(J, J, J, xz=dmi, zx=-dmi)), (0, 0, (0, 1, 0), J9(J, J, J, yz=dmi, zy=-dmi))]
+    return lattice_args(model, (L, L, 1), 1, bonds, T, h=h, D=[D or [0, 0, 0]], nthermal=nthermal, nsweep=nsweep,
+                        tau=tau, algo=algo, frames=frames, groups=groups,
+                        circuits=SQ_CIRCUITS if (circuits and model == "heisenberg") else ())
+
+
+HC_POS = [[0.333333333, 0.666666667, 0.0], [0.666666667, 0.333333333, 0.0]]
+
+
+def honeycomb_args(model, L, T, nthermal=10, nsweep=10, tau=0, algo=0, h=0.0):
+    """Honeycomb, 1NN Kitaev-type J=diag(-1.5,-1.5,-1.8) with Jxy=Jyx=0.3, 2NN -0.3, Az=-0.5."""
+    b1 = [(0, 1, o, J9(-1.5, -1.5, -1.8, xy=0.3, yx=0.3)) for o in ((0, 0, 0), (-1, 0, 0), (0, 1, 0))]
+    b2 = [(a, a, o, J9(-0.3, -0.3, -0.3)) for a in (0, 1) for o in ((1, 0, 0), (1, 1, 0), (0, 1, 0))]
+    if model == "ising":
+        return lattice_args("ising", (L, L, 1), 2, [(s, t, o, J9(-1)) for (s, t, o, _) in b1], T, h=h,
+                            nthermal=nthermal, nsweep=nsweep, tau=tau, algo=algo)
+    return lattice_args(model, (L, L, 1), 2, b1 + b2, T, D=[[0, 0, -0.5], [0, 0, -0.5]], h=h,
+                        nthermal=nthermal, nsweep=nsweep, tau=tau, algo=algo, groups=((0,), (1,)))
+
+
+
+
+def rescale_args(model, args, T, T0=1.0):
+    """The tuple of the same lattice at temperature T from one built at T0:
+    couplings, anisotropy and field scale as 1/T (mcMain.py:21-31)."""
+    T = max(T, 0.1)
+    f = T0 / T
+    a = list(args)
+    if model == "ising":
+        a[7] = tuple((np.asarray(a[7], dtype=float) * f).tolist())
+        a[10] = a[10] * f
+    else:
+        a[2] = tuple((np.asarray(a[2], dtype=float) * f).tolist())
+        a[8] = tuple((np.asarray(a[8], dtype=float) * f).tolist())
+        a[16] = a[16] * f
+    return tuple(a)

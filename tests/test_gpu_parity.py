@@ -23,6 +23,7 @@ pytestmark = pytest.mark.gpu
 SPIN_TOL = 1e-4        # per-component spin agreement, FP32 kernel vs FP64 oracle
 FLIP_FRACTION = 0.01   # fraction of sites allowed to differ by a borderline decision
 OBS_RTOL = 1e-9        # Ising observables (same trajectory, FP64 sums in another order)
+FP32_FLOOR = 2e-6      # resolution of FP32 spin state in statistical comparisons
 
 
 def _frames_last(ex):
@@ -121,7 +122,9 @@ def test_statistics_agree_with_reference(engine, name):
         if se == 0:
             assert x.mean() == pytest.approx(y.mean(), abs=1e-12)
             continue
-        assert abs(x.mean() - y.mean()) / se < 3.5, (k, x.mean(), y.mean(), se)
+        # FP32 state: a unit spin is represented to ~1e-7, so means that the
+        # FP64 reference holds to 1e-16 (e.g. <s_i.s_i> = S^2) agree to 2e-6
+        assert abs(x.mean() - y.mean()) < 3.5 * se + FP32_FLOOR * max(1.0, abs(x.mean())), (k, x.mean(), y.mean(), se)
 
 
 def onsager_energy(T, J=1.0):
