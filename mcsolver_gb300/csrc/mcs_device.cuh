@@ -40,36 +40,35 @@ __device__ __forceinline__ uint4 philox_t(uint32_t c0, long long t, uint32_t c3,
 __device__ __forceinline__ float u24(uint32_t w) { return (float)(w >> 8) * (1.0f / 16777216.0f); }
 
 // ------------------------------------------------------------------ geometry
-// SQUARE: N = Lx*Ly, Lx, Ly even; sweep index v = c*N/2 + x*(Ly/2) + (y>>1), c = (x+y)&1.
-struct SqPos { int x, y, c, Lx, Ly, hy, half; };
-__device__ __forceinline__ SqPos sq_pos(const Rep &R, int v)
+// SQUARE: N = Lx*Ly, Lx, Ly even; hy = Ly/2, half = N/2.  A site of colour c
+// with colour-local index k = x*hy + yh sits at (x, y = 2*yh + ((x+c)&1)) and
+// has sweep index c*half + k.  Its four neighbours have the other colour.
+template <class F>
+__device__ __forceinline__ void sq_links(const Rep &R, int c, int x, int yh, F &&f)
 {
-    SqPos p;
-    p.Ly = R.Ly; p.hy = R.Ly >> 1; p.half = R.N >> 1; p.Lx = R.N / R.Ly;
-    p.c = v >= p.half;
-    int k = v - p.c * p.half;
-    p.x = k / p.hy;
-    int yh = k - p.x * p.hy;
-    p.y = 2 * yh + ((p.x + p.c) & 1);
-    return p;
+    const int Lx = R.Lx, Ly = R.Ly, hy = R.hy;
+    const int y = 2 * yh + ((x + c) & 1);
+    const int base = (1 - c) * R.half;
+    const int xp = (x + 1 == Lx) ? 0 : x + 1;
+    const int xm = (x == 0) ? Lx - 1 : x - 1;
+    const int yp = (y + 1 == Ly) ? 0 : y + 1;
+    const int ym = (y == 0) ? Ly - 1 : y - 1;
+    f(0, base + xp * hy + yh, R.sq_code[0]);
+    f(1, base + xm * hy + yh, R.sq_code[1]);
+    f(2, base + x * hy + (yp >> 1), R.sq_code[2]);
+    f(3, base + x * hy + (ym >> 1), R.sq_code[3]);
 }
 
-// Iterate the links of site v: f(slot, neighbour sweep index, code).  For the
-// square lattice the slots are +x, -x, +y, -y.
+// Iterate the links of site v (sweep index): f(slot, neighbour, code).  The
+// square lattice slots are +x, -x, +y, -y.
 template <int GEOM, class F>
 __device__ __forceinline__ void for_links(const Rep &R, int v, F &&f)
 {
     if (GEOM == MCS_GEOM_SQUARE) {
-        SqPos p = sq_pos(R, v);
-        int base = (1 - p.c) * p.half;
-        int xp = (p.x + 1 == p.Lx) ? 0 : p.x + 1;
-        int xm = (p.x == 0) ? p.Lx - 1 : p.x - 1;
-        int yp = (p.y + 1 == p.Ly) ? 0 : p.y + 1;
-        int ym = (p.y == 0) ? p.Ly - 1 : p.y - 1;
-        f(0, base + xp * p.hy + (p.y >> 1), R.sq_code[0]);
-        f(1, base + xm * p.hy + (p.y >> 1), R.sq_code[1]);
-        f(2, base + p.x * p.hy + (yp >> 1), R.sq_code[2]);
-        f(3, base + p.x * p.hy + (ym >> 1), R.sq_code[3]);
+        const int c = v >= R.half;
+        const int k = v - c * R.half;
+        const int x = k / R.hy;
+        sq_links(R, c, x, k - x * R.hy, f);
     } else {
         int d = R.deg[v];
         for (int l = 0; l < d; ++l)
@@ -82,6 +81,23 @@ __device__ __forceinline__ int link_class(const Rep &R, int v, int l)
     if (GEOM == MCS_GEOM_SQUARE) return R.sq_cls[l];
     return R.lcls[(size_t)l * R.N + v];
 }
+
+// Walks the colour-local indices k = k0, k0+step, ... of a square lattice
+// keeping (x, yh) without divisions.
+struct SqWalk {
+    int x, yh, dx, dy, hy;
+    __device__ __forceinline__ void init(int k0, int step, int hy_)
+    {
+        hy = hy_;
+        x = k0 / hy; yh = k0 - x * hy;
+        dx = step / hy; dy = step - dx * hy;
+    }
+    __device__ __forceinline__ void next()
+    {
+        yh += dy; x += dx;
+        if (yh >= hy) { yh -= hy; ++x; }
+    }
+};
 
 // ------------------------------------------------------------------ spins
 struct Spins {
@@ -102,14 +118,13 @@ __device__ __forceinline__ Spins spins_global(const Rep &R)
 // threshold is ceil(exp(corr) * 2^32) (2^32 when corr >= 0); the trial is
 // accepted iff the Philox word is below it -- the same decision as
 // exp(corr) > w * 2^-32 of the reference rule with U = w * 2^-32.
-template <int GEOM>
-__device__ __forceinline__ void ising_trial(const Rep &R, const IsEntry *__restrict__ itab, signed char *s, int v,
-                                            uint32_t w, int (&dn)[MCS_MAXC], int (&dm)[MCS_MAXT])
+template <class LINKS>
+__device__ __forceinline__ bool ising_trial(const Rep &R, const IsEntry *__restrict__ itab, signed char *s, int v,
+                                            int t, uint32_t w, LINKS &&links, int (&dn)[MCS_MAXC], int (&dm)[MCS_MAXT])
 {
     int si = s[v];
-    int t = R.stype ? R.stype[v] : 0;
     int idx = R.ibase[t];
-    for_links<GEOM>(R, v, [&](int, int j, int code) { if (s[j] > 0) idx += code; });
+    links([&](int, int j, int code) { if (s[j] > 0) idx += code; });
     const IsEntry e = itab[idx];
     unsigned long long thr = e.thr[si > 0];
     if ((unsigned long long)w < thr) {
@@ -121,7 +136,9 @@ __device__ __forceinline__ void ising_trial(const Rep &R, const IsEntry *__restr
         dn[3] += si * (int)(signed char)((nc >> 24) & 0xff);
 #pragma unroll
         for (int q = 0; q < MCS_MAXT; ++q) dm[q] += (q == t) ? si : 0;
+        return true;
     }
+    return false;
 }
 
 // ------------------------------------------------------------------ O(n) trial
@@ -144,13 +161,13 @@ __device__ __forceinline__ void on_direction(const uint4 &w, float &r0, float &r
     }
 }
 
-template <int DIM, int GEOM>
-__device__ __forceinline__ void on_field(const Rep &R, const float *__restrict__ jt, const Spins &S, int v,
+template <int DIM, class LINKS>
+__device__ __forceinline__ void on_field(const Rep &R, const float *__restrict__ jt, const Spins &S, LINKS &&links,
                                          float &h0, float &h1, float &h2)
 {
     h0 = h1 = h2 = 0.f;
     const bool full = R.fullJ;
-    for_links<GEOM>(R, v, [&](int, int j, int code) {
+    links([&](int, int j, int code) {
         const float *M = jt + 9 * code;
         float a = S.x[j], b = S.y[j];
         float c = (DIM == 3) ? S.z[j] : 0.f;
@@ -170,13 +187,15 @@ __device__ __forceinline__ void on_field(const Rep &R, const float *__restrict__
     });
 }
 
-// returns true when accepted; dE (table units, before beta) in *dEout
-template <int DIM, int GEOM>
+// returns true when accepted; dE (table units, before beta) in *dEout.
+// dc: site class (anisotropy vector and |S|).
+template <int DIM, class LINKS>
 __device__ __forceinline__ bool on_trial(const Rep &R, const float *__restrict__ jt, const float *__restrict__ dt,
-                                         const Spins &S, int v, const uint4 &w, float beta, float h, float *dEout)
+                                         const Spins &S, int v, int dc, const uint4 &w, float beta, float h,
+                                         LINKS &&links, float *dEout)
 {
     float h0, h1, h2;
-    on_field<DIM, GEOM>(R, jt, S, v, h0, h1, h2);
+    on_field<DIM>(R, jt, S, links, h0, h1, h2);
     float r0, r1, r2;
     on_direction<DIM>(w, r0, r1, r2);
     float s0 = S.x[v], s1 = S.y[v];
@@ -185,9 +204,8 @@ __device__ __forceinline__ bool on_trial(const Rep &R, const float *__restrict__
     float f = -2.f * sr;
     float d0 = f * r0, d1 = f * r1, d2 = f * r2;
     float dE = d0 * h0 + d1 * h1 + d2 * h2;
+    const float *D = dt + 4 * dc;
     if (R.has_d) {
-        int dc = R.stype ? R.stype[v] : 0;
-        const float *D = dt + 4 * dc;
         dE += D[0] * (d0 * (2.f * s0 + d0)) + D[1] * (d1 * (2.f * s1 + d1));
         if (DIM == 3) dE += D[2] * (d2 * (2.f * s2 + d2));
     }
@@ -200,8 +218,7 @@ __device__ __forceinline__ bool on_trial(const Rep &R, const float *__restrict__
         // back onto |s| = S so that the length cannot random-walk
         float n0 = s0 + d0, n1 = s1 + d1, n2 = s2 + d2;
         float len2 = n0 * n0 + n1 * n1 + n2 * n2;
-        float Sabs = dt[4 * (R.stype ? R.stype[v] : 0) + 3];
-        float k = len2 > 0.f ? Sabs * rsqrtf(len2) : 1.f;
+        float k = len2 > 0.f ? D[3] * rsqrtf(len2) : 1.f;
         S.x[v] = n0 * k;
         S.y[v] = n1 * k;
         if (DIM == 3) S.z[v] = n2 * k;
@@ -324,123 +341,132 @@ __device__ __forceinline__ double on_signed_area(const Rep &R, const Spins &S, i
 // ------------------------------------------------------------------ O(n) frame over a virtual index range
 // Every thread of the block calls this; vb..ve is the index range of this block
 // (resident: 0..max list length).  Results in Fout (shared, F_NON doubles),
-// valid after return.  red: shared scratch [32*12] doubles.  efull: also sum
-// the full energy (bond and onsite parts).
+// valid after return.  red: shared scratch [MCS_RED] doubles.  efull: also sum
+// the full energy (bond and onsite parts).  majc: optional shared cache of the
+// block spins of the chosen sites ([n_rorb][3]); filled here when given, and
+// only usable when the block covers the whole lattice.
+#define MCS_RED (32 * 16 + 32)
 template <int DIM, int GEOM>
 __device__ void on_frame(const Rep &R, const float *jt, const float *dt, const Spins &S, int vb, int ve,
-                         bool efull, double *red, double *Fout)
+                         bool efull, double *red, double *Fout, float *majc)
 {
     const int tid = threadIdx.x, bd = blockDim.x;
-    // pass 1: correlated pairs
+    const bool full = R.fullJ;
+    if (majc) {
+        for (int v = tid; v < R.n_rorb; v += bd) {
+            float mx, my, mz;
+            on_majority<DIM>(R, S, __ldg(&R.rorb[v]), mx, my, mz);
+            majc[3 * v] = mx; majc[3 * v + 1] = my; majc[3 * v + 2] = mz;
+        }
+        __syncthreads();
+    }
+    auto maj = [&](int site, float &mx, float &my, float &mz) {
+        if (majc) {
+            int r = R.rindex[site];
+            mx = majc[3 * r]; my = majc[3 * r + 1]; mz = majc[3 * r + 2];
+        } else {
+            on_majority<DIM>(R, S, site, mx, my, mz);
+        }
+    };
+    // pass A: every site (total spin, full energy on re-checks) and circuits
     {
-        float a[7] = {0, 0, 0, 0, 0, 0, 0};
-        int e = min(ve, R.nlat);
+        float a[6] = {0, 0, 0, 0, 0, 0};
+        const int e = min(ve, R.N);
+        for (int v = vb + tid; v < e; v += bd) {
+            float sx = S.x[v], sy = S.y[v], sz = DIM == 3 ? S.z[v] : 0.f;
+            a[0] += sx; a[1] += sy; a[2] += sz;
+            if (efull) {
+                float h0, h1, h2;
+                on_field<DIM>(R, jt, S, [&](auto &&f) { for_links<GEOM>(R, v, f); }, h0, h1, h2);
+                a[3] += sx * h0 + sy * h1 + sz * h2;
+                a[4] += on_onsite<DIM>(R, dt, S, v);
+            }
+        }
+        if (DIM == 3) {
+            const int ec = min(ve, R.ncirc);
+            for (int v = vb + tid; v < ec; v += bd)
+                a[5] += (float)on_signed_area(R, S, __ldg(&R.circ[3 * v]), __ldg(&R.circ[3 * v + 1]), __ldg(&R.circ[3 * v + 2]));
+        }
+        double d[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) d[k] = a[k];
+        block_sum<6>(d, red, red + 32 * 16);
+        if (tid < 3) Fout[F_TOT + tid] = red[32 * 16 + tid];
+        if (tid == 3) Fout[F_EFB] = red[32 * 16 + 3];
+        if (tid == 4) Fout[F_EFO] = red[32 * 16 + 4];
+        if (tid == 5) Fout[F_Q] = red[32 * 16 + 5];
+        __syncthreads();
+    }
+    // pass G: orbital groups, four at a time
+    for (int g0 = 0; g0 < R.ngroup; g0 += 4) {
+        float a[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        const int e = min(ve, R.N);
+        for (int v = vb + tid; v < e; v += bd) {
+            int m = R.gmask[v] >> g0;
+            if (!(m & 15)) continue;
+            float x = S.x[v], y = S.y[v], z = DIM == 3 ? S.z[v] : 0.f;
+#pragma unroll
+            for (int g = 0; g < 4; ++g)
+                if (m & (1 << g)) { a[3 * g] += x; a[3 * g + 1] += y; a[3 * g + 2] += z; }
+        }
+        double d[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) d[k] = a[k];
+        block_sum<12>(d, red, red + 32 * 16);
+        if (tid < 12 && g0 + tid / 3 < MCS_MAXG) Fout[F_G + 3 * g0 + tid] = red[32 * 16 + tid];
+        __syncthreads();
+    }
+    // pass B: correlated pairs on both lattices, renormalised energy
+    {
+        float a[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) a[k] = 0.f;
+        const int e = min(ve, R.nlat);
         for (int v = vb + tid; v < e; v += bd) {
             int p = __ldg(&R.cpair[2 * v]), q = __ldg(&R.cpair[2 * v + 1]);
             float px = S.x[p], py = S.y[p], pz = DIM == 3 ? S.z[p] : 0.f;
             float qx = S.x[q], qy = S.y[q], qz = DIM == 3 ? S.z[q] : 0.f;
             a[0] += px; a[1] += py; a[2] += pz; a[3] += qx; a[4] += qy; a[5] += qz;
             a[6] += px * qx + py * qy + pz * qz;
-        }
-        double d[7];
-#pragma unroll
-        for (int k = 0; k < 7; ++k) d[k] = a[k];
-        block_sum<7>(d, red, Fout + F_SI);
-    }
-    // pass 2: all sites (total spin, full energy on re-checks)
-    {
-        float a[5] = {0, 0, 0, 0, 0};
-        int e = min(ve, R.N);
-        for (int v = vb + tid; v < e; v += bd) {
-            a[0] += S.x[v]; a[1] += S.y[v];
-            if (DIM == 3) a[2] += S.z[v];
-            if (efull) {
-                float h0, h1, h2;
-                on_field<DIM, GEOM>(R, jt, S, v, h0, h1, h2);
-                float sz = DIM == 3 ? S.z[v] : 0.f;
-                a[3] += S.x[v] * h0 + S.y[v] * h1 + sz * h2;
-                a[4] += on_onsite<DIM>(R, dt, S, v);
-            }
-        }
-        double d[5];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) d[k] = a[k];
-        double o[5];
-        block_sum<5>(d, red, red + 32 * 5);
-        if (tid < 5) o[0] = 0;  // silence
-        if (tid == 0) {
-            Fout[F_TOT] = red[32 * 5 + 0]; Fout[F_TOT + 1] = red[32 * 5 + 1]; Fout[F_TOT + 2] = red[32 * 5 + 2];
-            Fout[F_EFB] = red[32 * 5 + 3]; Fout[F_EFO] = red[32 * 5 + 4];
-        }
-        __syncthreads();
-    }
-    // pass 2b: orbital groups
-    if (R.ngroup > 0) {
-        for (int g0 = 0; g0 < R.ngroup; g0 += 4) {
-            float a[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-            int e = min(ve, R.N);
-            for (int v = vb + tid; v < e; v += bd) {
-                int m = R.gmask[v] >> g0;
-                if (!(m & 15)) continue;
-                float x = S.x[v], y = S.y[v], z = DIM == 3 ? S.z[v] : 0.f;
-#pragma unroll
-                for (int g = 0; g < 4; ++g)
-                    if (m & (1 << g)) { a[3 * g] += x; a[3 * g + 1] += y; a[3 * g + 2] += z; }
-            }
-            double d[12];
-#pragma unroll
-            for (int k = 0; k < 12; ++k) d[k] = a[k];
-            block_sum<12>(d, red, red + 32 * 12);
-            if (tid < 12 && g0 + tid / 3 < MCS_MAXG) Fout[F_G + 3 * g0 + tid] = red[32 * 12 + tid];
-            __syncthreads();
-        }
-    }
-    // pass 3: renormalised lattice
-    {
-        float a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-        const bool full = R.fullJ;
-        int e = min(ve, R.nlat);
-        for (int v = vb + tid; v < e; v += bd) {
-            int p = __ldg(&R.cpair[2 * v]), q = __ldg(&R.cpair[2 * v + 1]);
             bool cp = R.rindex[p] >= 0, cq = R.rindex[q] >= 0;
-            float px = 0, py = 0, pz = 0, qx = 0, qy = 0, qz = 0;
-            if (cp) { on_majority<DIM>(R, S, p, px, py, pz); a[0] += px; a[1] += py; a[2] += pz; }
-            if (cq) { on_majority<DIM>(R, S, q, qx, qy, qz); a[3] += qx; a[4] += qy; a[5] += qz; }
-            if (cp && cq) a[6] += px * qx + py * qy + pz * qz;
+            float mpx = 0, mpy = 0, mpz = 0, mqx = 0, mqy = 0, mqz = 0;
+            if (cp) { maj(p, mpx, mpy, mpz); a[7] += mpx; a[8] += mpy; a[9] += mpz; }
+            if (cq) {
+                if (q == p) { mqx = mpx; mqy = mpy; mqz = mpz; }
+                else maj(q, mqx, mqy, mqz);
+                a[10] += mqx; a[11] += mqy; a[12] += mqz;
+            }
+            if (cp && cq) a[13] += mpx * mqx + mpy * mqy + mpz * mqz;
         }
-        e = min(ve, R.n_rorb);
-        for (int v = vb + tid; v < e; v += bd) {
+        const int er = min(ve, R.n_rorb);
+        for (int v = vb + tid; v < er; v += bd) {
             int j = __ldg(&R.rorb[v]);
             float mx, my, mz;
-            on_majority<DIM>(R, S, j, mx, my, mz);
+            if (majc) { mx = majc[3 * v]; my = majc[3 * v + 1]; mz = majc[3 * v + 2]; }
+            else on_majority<DIM>(R, S, j, mx, my, mz);
             float corr = 0.f;
             int d = R.rdeg[v];
             for (int l = 0; l < d; ++l) {
                 int t = __ldg(&R.rlink[(size_t)v * R.zmax + l]);
                 if (t < 0) continue;
                 float tx, ty, tz;
-                on_majority<DIM>(R, S, t, tx, ty, tz);
+                if (R.rindex[t] >= 0) maj(t, tx, ty, tz);
+                else { tx = ty = tz = 0.f; }
                 corr += on_jdot<DIM>(jt + 9 * R.rjc[(size_t)v * R.zmax + l], full, mx, my, mz, tx, ty, tz);
             }
-            a[7] += corr;
-            a[8] += on_onsite<DIM>(R, dt, S, j);
+            a[14] += corr;
+            a[15] += on_onsite<DIM>(R, dt, S, j);
         }
-        double dd[9];
+        double d[16];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) dd[k] = a[k];
-        block_sum<9>(dd, red, Fout + F_SIR);
+        for (int k = 0; k < 16; ++k) d[k] = a[k];
+        block_sum<16>(d, red, red + 32 * 16);
+        if (tid < 7) Fout[F_SI + tid] = red[32 * 16 + tid];
+        else if (tid < 14) Fout[F_SIR + tid - 7] = red[32 * 16 + tid];
+        else if (tid == 14) Fout[F_ERB] = red[32 * 16 + 14];
+        else if (tid == 15) Fout[F_ERO] = red[32 * 16 + 15];
+        __syncthreads();
     }
-    // pass 4: topological charge over circuits (Heisenberg)
-    if (DIM == 3 && R.ncirc > 0) {
-        double q[1] = {0.0};
-        int e = min(ve, R.ncirc);
-        for (int v = vb + tid; v < e; v += bd)
-            q[0] += on_signed_area(R, S, __ldg(&R.circ[3 * v]), __ldg(&R.circ[3 * v + 1]), __ldg(&R.circ[3 * v + 2]));
-        block_sum<1>(q, red, Fout + F_Q);
-    } else if (tid == 0) {
-        Fout[F_Q] = 0.0;
-    }
-    __syncthreads();
 }
 
 // Fold one measurement frame into the FP64 accumulators (one thread).

@@ -123,6 +123,7 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r)
     memset(&R, 0, sizeof R);
     R.model = m.model; R.dim = m.dim; R.geom = m.geom; R.alg = m.alg;
     R.N = m.N; R.zmax = m.zmax; R.ncol = m.ncol; R.Ly = m.Ly;
+    R.Lx = m.Lx; R.hy = m.Ly / 2; R.half = m.N / 2;
     for (int d = 0; d < 4; ++d) { R.sq_code[d] = m.sq_code[d]; R.sq_cls[d] = m.sq_cls[d]; }
     for (int c = 0; c <= m.ncol; ++c) R.col_start[c] = m.col_start[c];
     if (m.geom == MCS_GEOM_ELL) {

@@ -71,6 +71,7 @@ struct Rep {
     // ---- geometry
     int model, dim, geom, alg;
     int N, zmax, ncol, Ly;          // Ly: square lattice side along y (N = Lx*Ly)
+    int Lx, hy, half;               // square: Lx, Ly/2, N/2
     int sq_code[4];                 // square: link code for +x, -x, +y, -y
     int sq_cls[4];                  // square Ising: class of +x, -x, +y, -y
     int col_start[65];              // colour ranges in sweep-index space

@@ -22,12 +22,15 @@ namespace mcs {
 
 static __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
-#define MCS_RED_DOUBLES (32 * 12 + 16)
+#define MCS_RED_DOUBLES MCS_RED
 
 struct SmemLayout {
-    size_t spins, tables, red, F, redl, Fi, total;
+    size_t spins, tables, stype, majc, red, F, redl, Fi, total;
 };
-__host__ __device__ inline SmemLayout smem_layout(const Rep &R)
+// Shared-memory plan of a resident replica.  The block-spin cache of the
+// renormalised lattice is included only when it fits (flag returned in majc
+// != 0).
+__host__ __device__ inline SmemLayout smem_layout(const Rep &R, size_t limit = 232448)
 {
     SmemLayout L;
     size_t off = 0;
@@ -37,10 +40,16 @@ __host__ __device__ inline SmemLayout smem_layout(const Rep &R)
     L.tables = off;
     if (R.dim == 1) off += align16((size_t)R.nite * sizeof(IsEntry));
     else off += align16((size_t)R.njc * 9 * sizeof(float) + (size_t)R.ndc * 4 * sizeof(float));
+    L.stype = off;
+    bool need_st = R.dim == 1 ? R.ntype > 1 : R.ndc > 1;
+    if (need_st) off += align16((size_t)R.N);
     L.red = off; off += MCS_RED_DOUBLES * sizeof(double);
     L.F = off; off += F_NON * sizeof(double);
     L.redl = off; off += 32 * (MCS_MAXT + MCS_MAXC + 1) * sizeof(long long);
     L.Fi = off; off += 16 * sizeof(long long);
+    L.majc = 0;
+    size_t mbytes = align16((size_t)R.n_rorb * 3 * sizeof(float));
+    if (R.dim > 1 && off + mbytes <= limit) { L.majc = off; off += mbytes; }
     L.total = off;
     return L;
 }
@@ -79,11 +88,16 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
     double *F = (double *)(smem + L.F);
     long long *redl = (long long *)(smem + L.redl);
     long long *Fi = (long long *)(smem + L.Fi);
+    float *majc = L.majc ? (float *)(smem + L.majc) : nullptr;
     Spins S;
     Spins G = spins_global(R);
     IsEntry *itab = (IsEntry *)(smem + L.tables);
     float *jt = (float *)(smem + L.tables);
     float *dt = jt + R.njc * 9;
+    const bool multi = DIM == 1 ? R.ntype > 1 : R.ndc > 1;
+    unsigned char *st = multi ? (unsigned char *)(smem + L.stype) : nullptr;
+    if (multi)
+        for (int v = tid; v < N; v += bd) st[v] = R.stype[v];
     if (DIM == 1) {
         S.s = (signed char *)(smem + L.spins);
         for (int v = tid; v < N; v += bd) S.s[v] = G.s[v];
@@ -154,25 +168,46 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
             const int c0 = R.col_start[c], nc = R.col_start[c + 1] - c0;
             if (DIM == 1) {
                 const int nq = (nc + 3) >> 2;
+                SqWalk wk;
+                if (GEOM == MCS_GEOM_SQUARE) wk.init(4 * tid, 4 * bd, R.hy);
                 for (int q = tid; q < nq; q += bd) {
                     uint4 w = philox_t((uint32_t)q, t, (uint32_t)c, R.seed);
-                    uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+                    const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+                    int x = 0, yh = 0;
+                    if (GEOM == MCS_GEOM_SQUARE) { x = wk.x; yh = wk.yh; }
 #pragma unroll
                     for (int e = 0; e < 4; ++e) {
-                        int k = 4 * q + e;
+                        const int k = 4 * q + e;
                         if (k < nc) {
-                            int before = dm[0] + dm[1] + dm[2] + dm[3];
-                            ising_trial<GEOM>(R, itab, S.s, c0 + k, ws[e], dn, dm);
-                            nacc += (dm[0] + dm[1] + dm[2] + dm[3]) != before;
+                            const int v = c0 + k;
+                            const int ty = multi ? st[v] : 0;
+                            bool a;
+                            if (GEOM == MCS_GEOM_SQUARE)
+                                a = ising_trial(R, itab, S.s, v, ty, ws[e], [&](auto &&f) { sq_links(R, c, x, yh, f); }, dn, dm);
+                            else
+                                a = ising_trial(R, itab, S.s, v, ty, ws[e], [&](auto &&f) { for_links<GEOM>(R, v, f); }, dn, dm);
+                            nacc += a;
                         }
+                        if (GEOM == MCS_GEOM_SQUARE) { if (++yh == R.hy) { yh = 0; ++x; } }
                     }
+                    if (GEOM == MCS_GEOM_SQUARE) wk.next();
                 }
             } else {
                 float dEf = 0.f;
+                SqWalk wk;
+                if (GEOM == MCS_GEOM_SQUARE) wk.init(tid, bd, R.hy);
                 for (int k = tid; k < nc; k += bd) {
+                    const int v = c0 + k;
                     uint4 w = philox_t((uint32_t)k, t, (uint32_t)c, R.seed);
+                    const int dc = multi ? st[v] : 0;
                     float dE;
-                    if (on_trial<DIM, GEOM>(R, jt, dt, S, c0 + k, w, beta, h, &dE)) { dEf += dE; ++nacc; }
+                    bool a;
+                    if (GEOM == MCS_GEOM_SQUARE)
+                        a = on_trial<DIM>(R, jt, dt, S, v, dc, w, beta, h, [&](auto &&f) { sq_links(R, c, wk.x, wk.yh, f); }, &dE);
+                    else
+                        a = on_trial<DIM>(R, jt, dt, S, v, dc, w, beta, h, [&](auto &&f) { for_links<GEOM>(R, v, f); }, &dE);
+                    if (a) { dEf += dE; ++nacc; }
+                    if (GEOM == MCS_GEOM_SQUARE) wk.next();
                 }
                 dEd += (double)dEf;
             }
@@ -189,7 +224,7 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
                 }
             } else {
                 const bool efull = (m % R.recheck) == 0;
-                on_frame<DIM, GEOM>(R, jt, dt, S, 0, max(max(N, R.nlat), max(R.n_rorb, R.ncirc)), efull, red, F);
+                on_frame<DIM, GEOM>(R, jt, dt, S, 0, max(max(N, R.nlat), max(R.n_rorb, R.ncirc)), efull, red, F, majc);
                 if (tid == 0) {
                     if (efull) {
                         double Ef = F[F_EFB] / 2 + F[F_EFO];
@@ -245,21 +280,30 @@ __global__ void __launch_bounds__(256) k_tiled_sweep(Rep *reps, const Item *item
     const int c = colour, c0 = R.col_start[c];
     Spins S = spins_global(R);
     const int tid = threadIdx.x;
+    const bool multi = DIM == 1 ? R.ntype > 1 : R.ndc > 1;
     if (DIM == 1) {
         int dn[MCS_MAXC] = {0, 0, 0, 0}, dm[MCS_MAXT] = {0, 0, 0, 0};
         long long nacc = 0;
         const int k0 = it.begin + 4 * tid;
         if (k0 < it.end) {
             uint4 w = philox_t((uint32_t)(k0 >> 2), t, (uint32_t)c, R.seed);
-            uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+            const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+            int x = 0, yh = 0;
+            if (GEOM == MCS_GEOM_SQUARE) { x = k0 / R.hy; yh = k0 - x * R.hy; }
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
-                int k = k0 + e;
+                const int k = k0 + e;
                 if (k < it.end) {
-                    int before = dm[0] + dm[1] + dm[2] + dm[3];
-                    ising_trial<GEOM>(R, R.itab, S.s, c0 + k, ws[e], dn, dm);
-                    nacc += (dm[0] + dm[1] + dm[2] + dm[3]) != before;
+                    const int v = c0 + k;
+                    const int ty = multi ? R.stype[v] : 0;
+                    bool a;
+                    if (GEOM == MCS_GEOM_SQUARE)
+                        a = ising_trial(R, R.itab, S.s, v, ty, ws[e], [&](auto &&f) { sq_links(R, c, x, yh, f); }, dn, dm);
+                    else
+                        a = ising_trial(R, R.itab, S.s, v, ty, ws[e], [&](auto &&f) { for_links<GEOM>(R, v, f); }, dn, dm);
+                    nacc += a;
                 }
+                if (GEOM == MCS_GEOM_SQUARE) { if (++yh == R.hy) { yh = 0; ++x; } }
             }
         }
         long long v[9] = {dn[0], dn[1], dn[2], dn[3], dm[0], dm[1], dm[2], dm[3], nacc};
@@ -270,9 +314,18 @@ __global__ void __launch_bounds__(256) k_tiled_sweep(Rep *reps, const Item *item
         double nacc = 0;
         const int k = it.begin + tid;
         if (k < it.end) {
+            const int v = c0 + k;
             uint4 w = philox_t((uint32_t)k, t, (uint32_t)c, R.seed);
+            const int dc = multi ? R.stype[v] : 0;
             float dE;
-            if (on_trial<DIM, GEOM>(R, R.jtab, R.dtab, S, c0 + k, w, R.beta, R.h, &dE)) { dEf = dE; nacc = 1; }
+            bool a;
+            if (GEOM == MCS_GEOM_SQUARE) {
+                const int x = k / R.hy, yh = k - x * R.hy;
+                a = on_trial<DIM>(R, R.jtab, R.dtab, S, v, dc, w, R.beta, R.h, [&](auto &&f) { sq_links(R, c, x, yh, f); }, &dE);
+            } else {
+                a = on_trial<DIM>(R, R.jtab, R.dtab, S, v, dc, w, R.beta, R.h, [&](auto &&f) { for_links<GEOM>(R, v, f); }, &dE);
+            }
+            if (a) { dEf = dE; nacc = 1; }
         }
         double v[2] = {(double)dEf, nacc};
         block_sum<2>(v, red, red + 64);
@@ -306,7 +359,7 @@ __global__ void __launch_bounds__(256) k_tiled_measure(Rep *reps, const Item *it
         const bool efull = (R.m % R.recheck) == 0;
         for (int k = threadIdx.x; k < F_NON; k += blockDim.x) F[k] = 0.0;
         __syncthreads();
-        on_frame<DIM, GEOM>(R, R.jtab, R.dtab, S, it.begin, it.end, efull, red, F);
+        on_frame<DIM, GEOM>(R, R.jtab, R.dtab, S, it.begin, it.end, efull, red, F, nullptr);
         for (int k = threadIdx.x; k < F_NON; k += blockDim.x) out[k] = F[k];
     }
 }
@@ -420,7 +473,7 @@ __global__ void __launch_bounds__(1024) k_init(Rep *reps, const int *ids)
     } else {
         for (int k = threadIdx.x; k < F_NON; k += blockDim.x) F[k] = 0.0;
         __syncthreads();
-        on_frame<DIM, GEOM>(R, R.jtab, R.dtab, S, 0, vmax, true, red, F);
+        on_frame<DIM, GEOM>(R, R.jtab, R.dtab, S, 0, vmax, true, red, F, nullptr);
         if (threadIdx.x == 0) R.acc[A_ECUR] = F[F_EFB] / 2 + F[F_EFO];
     }
 }
