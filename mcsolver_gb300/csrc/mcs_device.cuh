@@ -397,12 +397,16 @@ __device__ void on_frame(const Rep &R, const float *jt, const float *dt, const S
         if (tid == 5) Fout[F_Q] = red[32 * 16 + 5];
         __syncthreads();
     }
-    // pass G: orbital groups, four at a time
+    // pass G: orbital groups, four at a time; a group that holds every site
+    // is the total spin of pass A
+    if (tid < 3 * MCS_MAXG && (R.gall >> (tid / 3)) & 1) Fout[F_G + tid] = Fout[F_TOT + tid % 3];
     for (int g0 = 0; g0 < R.ngroup; g0 += 4) {
+        const int keep = ~(R.gall >> g0) & 15;
+        if (!keep) continue;
         float a[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         const int e = min(ve, R.N);
         for (int v = vb + tid; v < e; v += bd) {
-            int m = R.gmask[v] >> g0;
+            int m = (R.gmask[v] >> g0) & keep;
             if (!(m & 15)) continue;
             float x = S.x[v], y = S.y[v], z = DIM == 3 ? S.z[v] : 0.f;
 #pragma unroll
@@ -413,8 +417,54 @@ __device__ void on_frame(const Rep &R, const float *jt, const float *dt, const S
 #pragma unroll
         for (int k = 0; k < 12; ++k) d[k] = a[k];
         block_sum<12>(d, red, red + 32 * 16);
-        if (tid < 12 && g0 + tid / 3 < MCS_MAXG) Fout[F_G + 3 * g0 + tid] = red[32 * 16 + tid];
+        if (tid < 12 && g0 + tid / 3 < MCS_MAXG && ((keep >> (tid / 3)) & 1)) Fout[F_G + 3 * g0 + tid] = red[32 * 16 + tid];
         __syncthreads();
+    }
+    // pass B (site-centric): when every correlated pair is (v, v) and each site
+    // appears once, walk the sites instead of the pair and chosen-site lists.
+    if (R.pair_identity) {
+        float a[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) a[k] = 0.f;
+        const int e = min(ve, R.N);
+        for (int v = vb + tid; v < e; v += bd) {
+            const int fl = R.sflag[v];
+            if (!fl) continue;
+            float px = S.x[v], py = S.y[v], pz = DIM == 3 ? S.z[v] : 0.f;
+            if (fl & 1) { a[0] += px; a[1] += py; a[2] += pz; a[3] += px * px + py * py + pz * pz; }
+            if (fl & 2) {
+                const int r = R.rindex[v];
+                float mx, my, mz;
+                if (majc) { mx = majc[3 * r]; my = majc[3 * r + 1]; mz = majc[3 * r + 2]; }
+                else on_majority<DIM>(R, S, v, mx, my, mz);
+                if (fl & 1) { a[4] += mx; a[5] += my; a[6] += mz; a[7] += mx * mx + my * my + mz * mz; }
+                float corr = 0.f;
+                const int d = R.rdeg[r];
+                for (int l = 0; l < d; ++l) {
+                    const int tr = __ldg(&R.rtgt[(size_t)r * R.zmax + l]);  // cache slot of the target
+                    if (tr < 0) continue;
+                    float tx, ty, tz;
+                    if (majc) { tx = majc[3 * tr]; ty = majc[3 * tr + 1]; tz = majc[3 * tr + 2]; }
+                    else on_majority<DIM>(R, S, __ldg(&R.rorb[tr]), tx, ty, tz);
+                    corr += on_jdot<DIM>(jt + 9 * R.rjc[(size_t)r * R.zmax + l], full, mx, my, mz, tx, ty, tz);
+                }
+                a[8] += corr;
+                a[9] += on_onsite<DIM>(R, dt, S, v);
+            }
+        }
+        double d[10];
+#pragma unroll
+        for (int k = 0; k < 10; ++k) d[k] = a[k];
+        block_sum<10>(d, red, red + 32 * 16);
+        const double *o = red + 32 * 16;
+        if (tid < 3) { Fout[F_SI + tid] = o[tid]; Fout[F_SJ + tid] = o[tid]; }
+        if (tid == 3) Fout[F_SIJ] = o[3];
+        if (tid >= 4 && tid < 7) { Fout[F_SIR + tid - 4] = o[tid]; Fout[F_SJR + tid - 4] = o[tid]; }
+        if (tid == 7) Fout[F_SIJR] = o[7];
+        if (tid == 8) Fout[F_ERB] = o[8];
+        if (tid == 9) Fout[F_ERO] = o[9];
+        __syncthreads();
+        return;
     }
     // pass B: correlated pairs on both lattices, renormalised energy
     {

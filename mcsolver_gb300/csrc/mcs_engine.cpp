@@ -93,6 +93,7 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r)
     else o_rK = A.addv(m.rK);
     size_t o_rdeg = A.addv(m.rdeg), o_rindex = A.addv(m.rindex), o_circ = A.addv(m.circ);
     size_t o_slen = A.addv(m.slen), o_sval = A.addv(m.sval), o_gmask = A.addv(m.gmask);
+    size_t o_sflag = A.addv(m.sflag), o_rtgt = A.addv(m.rtgt);
     int spad = (m.N + 31) & ~31;
     size_t o_spins;
     if (m.dim == 1) o_spins = A.addv(m.init_sigma);
@@ -160,6 +161,10 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r)
     R.slen = (const float *)(b + o_slen); R.sval = (const float *)(b + o_sval);
     R.ngroup = m.ngroup; R.gmask = (const unsigned char *)(b + o_gmask);
     R.ci = m.ci; R.cj = m.cj; R.cij = m.cij;
+    R.pair_identity = m.pair_identity;
+    R.gall = m.gall;
+    R.sflag = (const unsigned char *)(b + o_sflag);
+    R.rtgt = (const int *)(b + o_rtgt);
     R.units_thermal = m.units_thermal; R.units_total = m.units_total; R.nsweep = m.nsweep; R.upm = m.upm;
     R.frames = m.frames; R.frame_every = m.frame_every;
     R.recheck = r->recheck;
@@ -325,13 +330,15 @@ int Batch::add(const mcs_problem *p, const mcs_options *o, int *idx)
 
 static int choose_schedule(const Replica &r, int requested, int max_smem)
 {
+    if (r.hm.alg == 1) {                     // Wolff: shared-memory or global state
+        int g = 0;
+        wolff_smem_bytes(r.rep, &g);
+        return g ? 5 : 4;
+    }
     if (requested == 1) return 1;            // plain
     if (requested == 3) return 3;            // tiled
     long long need = resident_smem_bytes(r.rep);
-    if (r.hm.alg == 0) {
-        if (need <= max_smem) return 2;
-        return 3;
-    }
+    if (need <= max_smem) return 2;
     return 3;
 }
 
@@ -424,10 +431,6 @@ int Batch::prepare()
     for (int i = 0; i < nrep; ++i) {
         Replica &r = *replicas[i];
         r.schedule = choose_schedule(r, r.requested_schedule, max_smem);
-        if (r.hm.alg == 1) {
-            set_error("Wolff updates are not built in this engine version");
-            return MCS_EUNSUPPORTED;
-        }
         host[i] = r.rep;
     }
     CUDA_TRY(cudaMalloc(&d_reps, nrep * sizeof(Rep)));
@@ -448,7 +451,7 @@ int Batch::prepare()
             }
     }
     // groups
-    for (int kind : {2, 3, 1})
+    for (int kind : {2, 3, 1, 4, 5})
         for (int d = 1; d <= 3; ++d)
             for (int g = 0; g <= 1; ++g) {
                 std::vector<int> ids;
@@ -476,7 +479,14 @@ int Batch::prepare()
                         for (int c = 0; c < r.hm.ncol; ++c)
                             maxcs = std::max(maxcs, r.hm.col_start[c + 1] - r.hm.col_start[c]);
                     }
-                    if (kind == 2) {
+                    if (kind == 4 || kind == 5) {
+                        int gs = 0;
+                        G->smem = 0;
+                        for (int id : set) G->smem = std::max<size_t>(G->smem, (size_t)wolff_smem_bytes(replicas[id]->rep, &gs));
+                        G->threads = threads_override > 0 ? threads_override : 512;
+                        G->chunk = 1 << 20;
+                        if (chunk_override > 0) G->chunk = chunk_override;
+                    } else if (kind == 2) {
                         int work = d == 1 ? (maxcs + 3) / 4 : maxcs;
                         G->threads = std::min(1024, std::max(64, ((work + 31) / 32) * 32));
                         if (threads_override > 0) G->threads = threads_override;
@@ -503,7 +513,15 @@ int Batch::advance(long long units)
         Group &G = *Gp;
         long long todo = std::min(units, G.max_units - G.done_units);
         if (todo <= 0) continue;
-        if (G.kind == 2) {
+        if (G.kind == 4 || G.kind == 5) {
+            for (long long u = 0; u < todo; u += G.chunk) {
+                long long n = std::min(G.chunk, todo - u);
+                cudaError_t e = launch_wolff(G.dim, G.geom, d_reps, G.d_ids, (int)G.ids.size(), G.threads, G.smem, n,
+                                             G.kind == 5, stream);
+                if (e != cudaSuccess) { set_error(std::string("wolff launch: ") + cudaGetErrorString(e)); return MCS_ECUDA; }
+                launches++;
+            }
+        } else if (G.kind == 2) {
             for (long long u = 0; u < todo; u += G.chunk) {
                 long long n = std::min(G.chunk, todo - u);
                 cudaError_t e = launch_resident_metro(G.dim, G.geom, d_reps, G.d_ids, (int)G.ids.size(), G.threads, G.smem, n, stream);

@@ -107,7 +107,11 @@ struct Rep {
     const float *slen;                           // [N] |S| (circuit normalisation)
     const float *sval;                           // [N] signed S (majority scaling)
     int ngroup; const unsigned char *gmask;      // [N]
+    int gall;                                    // bitmask of groups that hold every site
     int ci, cj, cij;                             // chosen counts of the pair lists
+    int pair_identity;                           // every pair is (v, v), each site at most once
+    const unsigned char *sflag;                  // [N] bit0: site is a pair member, bit1: chosen
+    const int *rtgt;                             // [n_rorb*zmax] index in rorb of the l-th renormalised target (-1)
     // ---- program
     long long units_thermal, units_total, nsweep;
     int upm;                                     // units per measurement
@@ -149,6 +153,9 @@ namespace mcs {
 // shared memory a resident replica needs (bytes), or -1 if it cannot be resident
 long long resident_smem_bytes(const Rep &r);
 int resident_max_smem();
+long long wolff_smem_bytes(const Rep &r, int *gstate);
+cudaError_t launch_wolff(int dim, int geom, Rep *reps, const int *ids, int nrep, int threads, size_t smem,
+                         long long max_units, int gstate, cudaStream_t st);
 cudaError_t launch_resident_metro(int dim, int geom, Rep *reps, const int *ids, int nrep, int threads,
                                   size_t smem, long long max_units, cudaStream_t st);
 cudaError_t launch_tiled_sweep(int dim, int geom, Rep *reps, const Item *items, int nitems, int colour,

@@ -17,6 +17,7 @@
 
 #include "mcs_device.cuh"
 #include "mcs_internal.h"
+#include "mcs_wolff.cuh"
 
 namespace mcs {
 
@@ -478,6 +479,161 @@ __global__ void __launch_bounds__(1024) k_init(Rep *reps, const int *ids)
     }
 }
 
+// ======================================================================= Wolff
+struct WolffLayout {
+    size_t spins, tables, stype, bits, queue, red, F, redl, Fi, sh, total;
+    int gstate;     // 1: spins, bits and queue live in global memory
+    int q16;
+};
+__host__ __device__ inline WolffLayout wolff_layout(const Rep &R, size_t limit = 232448)
+{
+    WolffLayout L;
+    for (int g = 0; g < 2; ++g) {
+        size_t off = 0;
+        L.gstate = g;
+        L.spins = off;
+        if (!g) {
+            if (R.dim == 1) off += align16((size_t)R.N);
+            else off += align16((size_t)R.dim * R.N * sizeof(float));
+        }
+        L.tables = off;
+        if (R.dim == 1) off += align16((size_t)R.nite * sizeof(IsEntry));
+        else off += align16((size_t)R.njc * 9 * sizeof(float) + (size_t)R.ndc * 4 * sizeof(float));
+        L.stype = off;
+        if (!g) off += align16((size_t)R.N);
+        L.bits = off;
+        if (!g) off += align16(((size_t)R.N + 31) / 32 * 4);
+        L.queue = off;
+        L.q16 = !g && R.N <= 65536;
+        if (!g) off += align16((size_t)R.N * (L.q16 ? 2 : 4));
+        L.red = off; off += MCS_RED_DOUBLES * sizeof(double);
+        L.F = off; off += F_NON * sizeof(double);
+        L.redl = off; off += 32 * (MCS_MAXT + MCS_MAXC + 1) * sizeof(long long);
+        L.Fi = off; off += 16 * sizeof(long long);
+        L.sh = off; off += 64;
+        L.total = off;
+        if (L.total <= limit) return L;
+    }
+    return L;
+}
+long long resident_wolff_smem_bytes(const Rep &r) { return (long long)wolff_layout(r).total; }
+
+template <int DIM, int GEOM>
+__global__ void __launch_bounds__(512) k_wolff(Rep *reps, const int *ids, long long max_units, int gstate)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ Rep R;
+    Rep *Rg = reps + ids[blockIdx.x];
+    load_rep(R, Rg);
+    if (R.u >= R.units_total) return;
+    WolffLayout L = wolff_layout(R);
+    if (gstate) {  // the host decided: keep the state in global memory
+        L = wolff_layout(R, 0);
+    }
+    const int tid = threadIdx.x, bd = blockDim.x, N = R.N;
+    double *red = (double *)(smem + L.red);
+    double *F = (double *)(smem + L.F);
+    long long *redl = (long long *)(smem + L.redl);
+    long long *Fi = (long long *)(smem + L.Fi);
+    int *sh = (int *)(smem + L.sh);
+    float *shf = (float *)(sh + 8);
+    const unsigned char *st = R.stype;
+    if (!L.gstate) {
+        unsigned char *sts = (unsigned char *)(smem + L.stype);
+        for (int v = tid; v < N; v += bd) sts[v] = R.stype[v];
+        st = sts;
+    }
+    IsEntry *itab = (IsEntry *)(smem + L.tables);
+    float *jt = (float *)(smem + L.tables);
+    float *dt = jt + R.njc * 9;
+    Spins G = spins_global(R);
+    Spins S = G;
+    WolffMem W;
+    if (L.gstate) {
+        W.bits = R.wbits; W.queue = R.wqueue; W.q16 = nullptr;
+    } else {
+        W.bits = (unsigned int *)(smem + L.bits);
+        W.queue = (int *)(smem + L.queue);
+        W.q16 = L.q16 ? (unsigned short *)(smem + L.queue) : nullptr;
+        for (int k = tid; k < (N + 31) / 32; k += bd) W.bits[k] = 0u;
+        if (DIM == 1) {
+            S.s = (signed char *)(smem + L.spins);
+            for (int v = tid; v < N; v += bd) S.s[v] = G.s[v];
+        } else {
+            S.x = (float *)(smem + L.spins);
+            S.y = S.x + N;
+            S.z = S.y + N;
+            for (int v = tid; v < N; v += bd) {
+                S.x[v] = G.x[v]; S.y[v] = G.y[v];
+                if (DIM == 3) S.z[v] = G.z[v];
+            }
+        }
+    }
+    if (DIM == 1) for (int k = tid; k < R.nite; k += bd) itab[k] = R.itab[k];
+    else {
+        for (int k = tid; k < R.njc * 9; k += bd) jt[k] = R.jtab[k];
+        for (int k = tid; k < R.ndc * 4; k += bd) dt[k] = R.dtab[k];
+    }
+    __syncthreads();
+    double dEd = 0.0;
+    long long dnacc = 0;
+    int dn[MCS_MAXC] = {0, 0, 0, 0}, dm[MCS_MAXT] = {0, 0, 0, 0};
+    long long u = R.u;
+    const long long uend = min(R.units_total, u + max_units);
+    for (; u < uend; ++u) {
+        if (tid == 0) R.u = u;
+        __syncthreads();
+        wolff_cluster<DIM, GEOM>(R, jt, dt, itab, st, S, W, R.u0 + u, sh, shf, red, F, redl, Fi, dEd, dnacc, dn, dm);
+        if (measures_after(R, u)) {
+            const long long m = R.m;
+            if (DIM == 1) {
+                is_frame<GEOM>(R, itab, S.s, 0, max(N, max(R.nlat, R.n_rorb)), m, red, F, redl, Fi);
+                if (tid == 0) is_accumulate(R, F, Fi, S.s[R.last_site], m);
+            } else {
+                if (tid == 0) { R.acc[A_ECUR] += dEd; dEd = 0.0; }
+                const bool efull = (m % R.recheck) == 0;
+                on_frame<DIM, GEOM>(R, jt, dt, S, 0, max(max(N, R.nlat), max(R.n_rorb, R.ncirc)), efull, red, F, nullptr);
+                if (tid == 0) {
+                    if (efull) {
+                        double Ef = F[F_EFB] / 2 + F[F_EFO];
+                        double d = fabs(R.acc[A_ECUR] - Ef);
+                        if (d > R.acc[A_DRIFT]) R.acc[A_DRIFT] = d;
+                        R.acc[A_ECUR] = Ef;
+                    }
+                    on_accumulate<DIM>(R, F, R.acc[A_ECUR], m);
+                }
+            }
+            if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) {
+                float *fb = R.frame_buf + (size_t)R.frames_written * N * 3;
+                for (int v = tid; v < N; v += bd) {
+                    if (DIM == 1) { fb[3 * v] = (float)(R.Stype[st[v]] * S.s[v]); fb[3 * v + 1] = 0; fb[3 * v + 2] = 0; }
+                    else { fb[3 * v] = S.x[v]; fb[3 * v + 1] = S.y[v]; fb[3 * v + 2] = DIM == 3 ? S.z[v] : 0.f; }
+                }
+            }
+            __syncthreads();
+            if (tid == 0) {
+                if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) R.frames_written++;
+                R.m = m + 1;
+            }
+            __syncthreads();
+        }
+    }
+    if (DIM > 1 && tid == 0) R.acc[A_ECUR] += dEd;
+    if (!L.gstate)
+        for (int v = tid; v < N; v += bd) {
+            if (DIM == 1) G.s[v] = S.s[v];
+            else {
+                G.x[v] = S.x[v]; G.y[v] = S.y[v];
+                if (DIM == 3) G.z[v] = S.z[v];
+            }
+        }
+    if (tid == 0) {
+        Rg->u = uend;
+        Rg->m = R.m;
+        Rg->frames_written = R.frames_written;
+    }
+}
+
 // ======================================================================= launchers
 template <int DIM, int GEOM>
 static cudaError_t set_smem_attr(size_t smem)
@@ -559,4 +715,38 @@ cudaError_t launch_init_state_dg(int dim, int geom, Rep *reps, const int *ids, i
     return cudaGetLastError();
 }
 
+
+template <int DIM, int GEOM>
+static cudaError_t set_wolff_attr(size_t smem)
+{
+    static size_t done = 0;
+    if (smem > 48 * 1024 && smem > done) {
+        cudaError_t e = cudaFuncSetAttribute(k_wolff<DIM, GEOM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        done = smem;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_wolff(int dim, int geom, Rep *reps, const int *ids, int nrep, int threads, size_t smem,
+                         long long max_units, int gstate, cudaStream_t st)
+{
+    if (nrep <= 0) return cudaSuccess;
+#define CALL_W(D, G)                                                                     \
+    {                                                                                    \
+        cudaError_t e = set_wolff_attr<D, G>(smem);                                      \
+        if (e != cudaSuccess) return e;                                                  \
+        k_wolff<D, G><<<nrep, threads, smem, st>>>(reps, ids, max_units, gstate);        \
+    }
+    MCS_DISPATCH(dim, geom, CALL_W);
+#undef CALL_W
+    return cudaGetLastError();
+}
+
+long long wolff_smem_bytes(const Rep &r, int *gstate)
+{
+    WolffLayout L = wolff_layout(r);
+    if (gstate) *gstate = L.gstate;
+    return (long long)L.total;
+}
 }  // namespace mcs

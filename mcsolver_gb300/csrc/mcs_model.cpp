@@ -431,6 +431,22 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
             else m->rK[(size_t)v * z + l] = p->link_strength[(size_t)j * z + l];
         }
     }
+    m->rtgt.assign((size_t)p->n_rorb * std::max(z, 1), -1);
+    for (int v = 0; v < p->n_rorb; ++v)
+        for (int l = 0; l < std::max(z, 1); ++l) {
+            int t = m->rlink[(size_t)v * std::max(z, 1) + l];
+            m->rtgt[(size_t)v * std::max(z, 1) + l] = t < 0 ? -1 : m->rindex[t];
+        }
+    m->sflag.assign(N, 0);
+    m->pair_identity = 1;
+    for (int v = 0; v < p->n_lat; ++v) {
+        int a = m->cpair[2 * v], b = m->cpair[2 * v + 1];
+        if (a != b || (m->sflag[a] & 1)) m->pair_identity = 0;
+        m->sflag[a] |= 1;
+    }
+    for (int v = 0; v < p->n_rorb; ++v) m->sflag[m->rorb[v]] |= 2;
+    if (!m->pair_identity)
+        for (int k = 0; k < N; ++k) m->sflag[k] &= 2;
     m->ci = m->cj = m->cij = 0;
     for (int v = 0; v < p->n_lat; ++v) {
         bool a = m->rindex[m->cpair[2 * v]] >= 0, b = m->rindex[m->cpair[2 * v + 1]] >= 0;
@@ -447,6 +463,12 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
             if (id < 0) break;
             m->gmask[pos[id]] |= (uint8_t)(1u << g);
         }
+    m->gall = 0;
+    for (int g = 0; g < m->ngroup; ++g) {
+        bool all = true;
+        for (int k = 0; k < N && all; ++k) all = (m->gmask[k] >> g) & 1;
+        if (all) m->gall |= 1 << g;
+    }
     m->slen.resize(N);
     m->sval.resize(N);
     for (int k = 0; k < N; ++k) { m->slen[k] = (float)fabs(p->init_spin[sites[k]]); m->sval[k] = (float)p->init_spin[sites[k]]; }

@@ -48,6 +48,10 @@ struct HostModel {
     std::vector<double> rK;
     std::vector<uint8_t> rdeg, gmask;
     std::vector<float> slen, sval;
+    std::vector<uint8_t> sflag;
+    std::vector<int> rtgt;
+    int pair_identity = 0;
+    int gall = 0;
     int nlat = 0, n_rorb = 0, ncl = 0, ncirc = 0, ngroup = 0;
     int ci = 0, cj = 0, cij = 0;
     // program

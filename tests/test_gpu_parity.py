@@ -101,7 +101,7 @@ def test_on_resident_and_tiled_trajectories_agree(engine, model):
     np.testing.assert_allclose(np.array(a[:27]), np.array(b[:27]), rtol=1e-6, atol=1e-7)
 
 
-STAT = [n for n in C.golden()["cases"] if n.startswith("stat_") and "wolff" not in n]
+STAT = [n for n in C.golden()["cases"] if n.startswith("stat_")]
 
 
 @pytest.mark.parametrize("name", STAT)
