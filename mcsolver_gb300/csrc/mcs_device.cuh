@@ -249,6 +249,28 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double *red, double *o
     }
     __syncthreads();
 }
+// FP32 inside a warp (32 per-thread partials), FP64 across the warps: the
+// device's FP64 rate is a small fraction of its FP32 rate, so per-lane FP64
+// arithmetic is kept out of the reduction tree.
+template <int K>
+__device__ __forceinline__ void block_sum_f(float (&v)[K], double *red, double *out)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        float x = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) red[wid * K + k] = (double)x;
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double a = 0.0;
+        for (int w = 0; w < nw; ++w) a += red[w * K + threadIdx.x];
+        out[threadIdx.x] = a;
+    }
+    __syncthreads();
+}
 template <int K>
 __device__ __forceinline__ void block_sum_ll(long long (&v)[K], long long *red, long long *out)
 {
@@ -387,10 +409,7 @@ __device__ void on_frame(const Rep &R, const float *jt, const float *dt, const S
             for (int v = vb + tid; v < ec; v += bd)
                 a[5] += (float)on_signed_area(R, S, __ldg(&R.circ[3 * v]), __ldg(&R.circ[3 * v + 1]), __ldg(&R.circ[3 * v + 2]));
         }
-        double d[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) d[k] = a[k];
-        block_sum<6>(d, red, red + 32 * 16);
+        block_sum_f<6>(a, red, red + 32 * 16);
         if (tid < 3) Fout[F_TOT + tid] = red[32 * 16 + tid];
         if (tid == 3) Fout[F_EFB] = red[32 * 16 + 3];
         if (tid == 4) Fout[F_EFO] = red[32 * 16 + 4];
@@ -413,10 +432,7 @@ __device__ void on_frame(const Rep &R, const float *jt, const float *dt, const S
             for (int g = 0; g < 4; ++g)
                 if (m & (1 << g)) { a[3 * g] += x; a[3 * g + 1] += y; a[3 * g + 2] += z; }
         }
-        double d[12];
-#pragma unroll
-        for (int k = 0; k < 12; ++k) d[k] = a[k];
-        block_sum<12>(d, red, red + 32 * 16);
+        block_sum_f<12>(a, red, red + 32 * 16);
         if (tid < 12 && g0 + tid / 3 < MCS_MAXG && ((keep >> (tid / 3)) & 1)) Fout[F_G + 3 * g0 + tid] = red[32 * 16 + tid];
         __syncthreads();
     }
@@ -452,10 +468,7 @@ __device__ void on_frame(const Rep &R, const float *jt, const float *dt, const S
                 a[9] += on_onsite<DIM>(R, dt, S, v);
             }
         }
-        double d[10];
-#pragma unroll
-        for (int k = 0; k < 10; ++k) d[k] = a[k];
-        block_sum<10>(d, red, red + 32 * 16);
+        block_sum_f<12>(a, red, red + 32 * 16);
         const double *o = red + 32 * 16;
         if (tid < 3) { Fout[F_SI + tid] = o[tid]; Fout[F_SJ + tid] = o[tid]; }
         if (tid == 3) Fout[F_SIJ] = o[3];
@@ -507,10 +520,7 @@ __device__ void on_frame(const Rep &R, const float *jt, const float *dt, const S
             a[14] += corr;
             a[15] += on_onsite<DIM>(R, dt, S, j);
         }
-        double d[16];
-#pragma unroll
-        for (int k = 0; k < 16; ++k) d[k] = a[k];
-        block_sum<16>(d, red, red + 32 * 16);
+        block_sum_f<16>(a, red, red + 32 * 16);
         if (tid < 7) Fout[F_SI + tid] = red[32 * 16 + tid];
         else if (tid < 14) Fout[F_SIR + tid - 7] = red[32 * 16 + tid];
         else if (tid == 14) Fout[F_ERB] = red[32 * 16 + 14];
@@ -597,6 +607,19 @@ __device__ __forceinline__ double is_majority(const Rep &R, const signed char *s
     return ((double)word * (1.0 / 4294967296.0) > 0.5) ? a : -a;
 }
 
+// Majority sign (single spin length): sign of the sum of the block's signs.
+__device__ __forceinline__ int is_majority_sign(const Rep &R, const signed char *s, int v, const uint4 &w, int slot)
+{
+    int avg = 0;
+    int r = R.rindex[v];
+    if (r >= 0)
+        for (int k = 0; k < R.ncl; ++k) avg += s[__ldg(&R.rcl[(size_t)r * R.ncl + k])];
+    if (avg > 0) return 1;
+    if (avg < 0) return -1;
+    uint32_t word = (slot & 3) == 0 ? w.x : (slot & 3) == 1 ? w.y : (slot & 3) == 2 ? w.z : w.w;
+    return ((double)word * (1.0 / 4294967296.0) > 0.5) ? 1 : -1;
+}
+
 // Ising frame over [vb, ve): pairs, renormalised energy, per-type sign sums,
 // full per-class directed bond sums.  Fd (4 doubles) and Fi (MAXT+MAXC ints).
 template <int GEOM>
@@ -604,6 +627,63 @@ __device__ void is_frame(const Rep &R, const IsEntry *itab, const signed char *s
                          double *red, double *Fd, long long *redl, long long *Fi)
 {
     const int tid = threadIdx.x, bd = blockDim.x;
+    if (R.is_fast) {
+        // one spin length S0 and <= 4 renormalised coupling values: every sum
+        // of the frame is an integer times a constant
+        long long c[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) c[k] = 0;
+        int e = min(ve, R.nlat);
+        for (int v = vb + tid; v < e; v += bd) {
+            int p = __ldg(&R.cpair[2 * v]), q = __ldg(&R.cpair[2 * v + 1]);
+            int sp = s[p], sq = s[q];
+            c[0] += sp; c[1] += sq; c[2] += sp * sq;
+        }
+        e = min(ve, R.n_rorb);
+        for (int v = vb + tid; v < e; v += bd) {
+            const int j = __ldg(&R.rorb[v]);
+            uint4 w = philox_t((uint32_t)j, m, 0x3000u, R.seed);
+            const int mj = is_majority_sign(R, s, j, w, 0);
+            const int d = R.rdeg[v];
+            for (int l = 0; l < d; ++l) {
+                const int slot = 1 + l;
+                if ((slot & 3) == 0) w = philox_t((uint32_t)j, m, 0x3000u + (uint32_t)(slot >> 2), R.seed);
+                const int t = __ldg(&R.rlink[(size_t)v * R.zmax + l]);
+                if (t < 0) continue;
+                const int mt = is_majority_sign(R, s, t, w, slot);
+                const int k = R.rkc[(size_t)v * R.zmax + l];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) c[3 + q] += (q == k) ? mj * mt : 0;
+            }
+            c[7] += s[j];
+        }
+        e = min(ve, R.N);
+        for (int v = vb + tid; v < e; v += bd) {
+            int si = s[v];
+            int idx = R.ibase[0];
+            for_links<GEOM>(R, v, [&](int, int j, int code) { if (s[j] > 0) idx += code; });
+            int nc = itab[idx].nc;
+            c[8] += si;
+            c[12] += si * (int)(signed char)(nc & 0xff);
+            c[13] += si * (int)(signed char)((nc >> 8) & 0xff);
+            c[14] += si * (int)(signed char)((nc >> 16) & 0xff);
+            c[15] += si * (int)(signed char)((nc >> 24) & 0xff);
+        }
+        block_sum_ll<16>(c, redl, redl + 32 * 16);
+        const long long *o = redl + 32 * 16;
+        if (tid == 0) {
+            const double S0 = R.Stype[0];
+            Fd[0] = S0 * (double)o[0];
+            Fd[1] = S0 * (double)o[1];
+            Fd[2] = S0 * S0 * (double)o[2];
+            double er = 0;
+            for (int k = 0; k < 4; ++k) er += R.rKv[k] * (double)o[3 + k];
+            Fd[3] = S0 * S0 * er / 2 - R.hd * S0 * (double)o[7];
+        }
+        if (tid < 8) Fi[tid] = o[8 + tid];
+        __syncthreads();
+        return;
+    }
     double a[4] = {0, 0, 0, 0};
     int e = min(ve, R.nlat);
     for (int v = vb + tid; v < e; v += bd) {

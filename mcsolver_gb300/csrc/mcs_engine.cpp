@@ -91,6 +91,7 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r)
     size_t o_rjc = 0, o_rK = 0;
     if (m.dim > 1) o_rjc = A.addv(m.rjc);
     else o_rK = A.addv(m.rK);
+    size_t o_rkc = m.dim == 1 ? A.addv(m.rkc) : 0;
     size_t o_rdeg = A.addv(m.rdeg), o_rindex = A.addv(m.rindex), o_circ = A.addv(m.circ);
     size_t o_slen = A.addv(m.slen), o_sval = A.addv(m.sval), o_gmask = A.addv(m.gmask);
     size_t o_sflag = A.addv(m.sflag), o_rtgt = A.addv(m.rtgt);
@@ -154,7 +155,12 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r)
     R.n_rorb = m.n_rorb; R.ncl = m.ncl;
     R.rorb = (const int *)(b + o_rorb); R.rcl = (const int *)(b + o_rcl); R.rlink = (const int *)(b + o_rlink);
     if (m.dim > 1) R.rjc = (const unsigned short *)(b + o_rjc);
-    else R.rK = (const double *)(b + o_rK);
+    else {
+        R.rK = (const double *)(b + o_rK);
+        R.rkc = (const unsigned char *)(b + o_rkc);
+        R.is_fast = m.is_fast;
+        for (int k = 0; k < 4; ++k) R.rKv[k] = m.rKv[k];
+    }
     R.rdeg = (const unsigned char *)(b + o_rdeg);
     R.rindex = (const int *)(b + o_rindex);
     R.ncirc = m.ncirc; R.circ = (const int *)(b + o_circ);

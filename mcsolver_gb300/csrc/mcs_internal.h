@@ -101,6 +101,9 @@ struct Rep {
     const int *rlink;                            // [n_rorb*zmax] (-1 = none)
     const unsigned short *rjc;                   // O(n) [n_rorb*zmax]: J class of the link
     const double *rK;                            // Ising [n_rorb*zmax]: link strength
+    const unsigned char *rkc;                    // Ising [n_rorb*zmax]: class of rK (fast path)
+    double rKv[4];                               // Ising: the <= 4 distinct rK values
+    int is_fast;                                 // Ising: one spin length and <= 4 rK values
     const unsigned char *rdeg;                   // [n_rorb]: nlink of the chosen site
     const int *rindex;                           // [N]: index in rorb or -1
     int ncirc; const int *circ;                  // [3*ncirc]

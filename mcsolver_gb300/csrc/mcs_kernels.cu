@@ -46,7 +46,7 @@ __host__ __device__ inline SmemLayout smem_layout(const Rep &R, size_t limit = 2
     if (need_st) off += align16((size_t)R.N);
     L.red = off; off += MCS_RED_DOUBLES * sizeof(double);
     L.F = off; off += F_NON * sizeof(double);
-    L.redl = off; off += 32 * (MCS_MAXT + MCS_MAXC + 1) * sizeof(long long);
+    L.redl = off; off += (32 * 16 + 16) * sizeof(long long);
     L.Fi = off; off += 16 * sizeof(long long);
     L.majc = 0;
     size_t mbytes = align16((size_t)R.n_rorb * 3 * sizeof(float));
@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(256) k_tiled_measure(Rep *reps, const Item *it
 {
     __shared__ double red[MCS_RED_DOUBLES];
     __shared__ double F[F_NON];
-    __shared__ long long redl[32 * 9];
+    __shared__ long long redl[32 * 16 + 16];
     __shared__ long long Fi[16];
     const Item it = items[blockIdx.x];
     const Rep &R = reps[it.rep];
@@ -459,7 +459,7 @@ __global__ void __launch_bounds__(1024) k_init(Rep *reps, const int *ids)
 {
     __shared__ double red[MCS_RED_DOUBLES];
     __shared__ double F[F_NON];
-    __shared__ long long redl[32 * 9];
+    __shared__ long long redl[32 * 16 + 16];
     __shared__ long long Fi[16];
     Rep &R = reps[ids[blockIdx.x]];
     if (R.dim != (DIM == 1 ? 1 : DIM) || R.geom != GEOM) return;
@@ -508,7 +508,7 @@ __host__ __device__ inline WolffLayout wolff_layout(const Rep &R, size_t limit =
         if (!g) off += align16((size_t)R.N * (L.q16 ? 2 : 4));
         L.red = off; off += MCS_RED_DOUBLES * sizeof(double);
         L.F = off; off += F_NON * sizeof(double);
-        L.redl = off; off += 32 * (MCS_MAXT + MCS_MAXC + 1) * sizeof(long long);
+        L.redl = off; off += (32 * 16 + 16) * sizeof(long long);
         L.Fi = off; off += 16 * sizeof(long long);
         L.sh = off; off += 64;
         L.total = off;

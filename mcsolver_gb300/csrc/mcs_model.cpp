@@ -447,6 +447,27 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
     for (int v = 0; v < p->n_rorb; ++v) m->sflag[m->rorb[v]] |= 2;
     if (!m->pair_identity)
         for (int k = 0; k < N; ++k) m->sflag[k] &= 2;
+    if (dim == 1) {
+        // integer fast path of the Ising frame: one |S| and <= 4 rK values
+        std::map<double, int> kc;
+        m->rkc.assign(m->rK.size(), 0);
+        bool ok = m->ntype == 1;
+        for (int v = 0; v < p->n_rorb && ok; ++v)
+            for (int l = 0; l < m->rdeg[v]; ++l) {
+                double k = m->rK[(size_t)v * std::max(z, 1) + l];
+                auto it = kc.find(k);
+                int c;
+                if (it == kc.end()) {
+                    c = (int)kc.size();
+                    if (c >= 4) { ok = false; break; }
+                    kc[k] = c;
+                    m->rKv[c] = k;
+                } else c = it->second;
+                m->rkc[(size_t)v * std::max(z, 1) + l] = (uint8_t)c;
+            }
+        for (int k = 0; k < N && ok; ++k) ok = fabs(p->init_spin[k]) == fabs(p->init_spin[0]);
+        m->is_fast = ok ? 1 : 0;
+    }
     m->ci = m->cj = m->cij = 0;
     for (int v = 0; v < p->n_lat; ++v) {
         bool a = m->rindex[m->cpair[2 * v]] >= 0, b = m->rindex[m->cpair[2 * v + 1]] >= 0;

@@ -46,6 +46,9 @@ struct HostModel {
     std::vector<int> cpair, rorb, rcl, rlink, rindex, circ;
     std::vector<uint16_t> rjc;
     std::vector<double> rK;
+    std::vector<uint8_t> rkc;
+    double rKv[4] = {0, 0, 0, 0};
+    int is_fast = 0;
     std::vector<uint8_t> rdeg, gmask;
     std::vector<float> slen, sval;
     std::vector<uint8_t> sflag;
