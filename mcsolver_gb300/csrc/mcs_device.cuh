@@ -346,6 +346,21 @@ __device__ __forceinline__ float on_onsite(const Rep &R, const float *dt, const 
 // Berg-Luescher solid angle with atan (not atan2), +-pi when |re| < 1e-6.
 __device__ __forceinline__ double on_signed_area(const Rep &R, const Spins &S, int a, int b, int c)
 {
+    if (R.uniform_len) {
+        // |S| the same everywhere: s_i.s_j/|S|^2 and s1.(s2 x s3)/|S|^3 share one scale
+        const float ax = S.x[a], ay = S.y[a], az = S.z[a];
+        const float bx = S.x[b], by = S.y[b], bz = S.z[b];
+        const float cx = S.x[c], cy = S.y[c], cz = S.z[c];
+        const float l = R.slen[0], il2 = 1.f / (l * l);
+        const float s1s2 = (ax * bx + ay * by + az * bz) * il2;
+        const float s2s3 = (bx * cx + by * cy + bz * cz) * il2;
+        const float s3s1 = (cx * ax + cy * ay + cz * az) * il2;
+        const float kx = by * cz - bz * cy, ky = bz * cx - bx * cz, kz = bx * cy - by * cx;
+        const float re = 1.f + s1s2 + s2s3 + s3s1;
+        const float im = (ax * kx + ay * ky + az * kz) * R.inv_len3;
+        if (fabsf(re) < 1e-6f) return im > 0.f ? MCS_PI_REF : -MCS_PI_REF;
+        return 2.0 * (double)atanf(__fdividef(im, re));
+    }
     float l1 = R.slen[a], l2 = R.slen[b], l3 = R.slen[c];
     float ax = S.x[a], ay = S.y[a], az = S.z[a];
     float bx = S.x[b], by = S.y[b], bz = S.z[b];
@@ -390,13 +405,16 @@ __device__ void on_frame(const Rep &R, const float *jt, const float *dt, const S
             on_majority<DIM>(R, S, site, mx, my, mz);
         }
     };
-    // pass A: every site (total spin, full energy on re-checks) and circuits
+    // pass A: every site (total spin, full energy on re-checks, and the
+    // correlated-pair sums when every pair is (v, v)) and circuits
     {
-        float a[6] = {0, 0, 0, 0, 0, 0};
+        float a[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         const int e = min(ve, R.N);
+        const bool pid = R.pair_identity;
         for (int v = vb + tid; v < e; v += bd) {
             float sx = S.x[v], sy = S.y[v], sz = DIM == 3 ? S.z[v] : 0.f;
             a[0] += sx; a[1] += sy; a[2] += sz;
+            if (pid && (R.sflag[v] & 1)) { a[6] += sx; a[7] += sy; a[8] += sz; a[9] += sx * sx + sy * sy + sz * sz; }
             if (efull) {
                 float h0, h1, h2;
                 on_field<DIM>(R, jt, S, [&](auto &&f) { for_links<GEOM>(R, v, f); }, h0, h1, h2);
@@ -409,11 +427,14 @@ __device__ void on_frame(const Rep &R, const float *jt, const float *dt, const S
             for (int v = vb + tid; v < ec; v += bd)
                 a[5] += (float)on_signed_area(R, S, __ldg(&R.circ[3 * v]), __ldg(&R.circ[3 * v + 1]), __ldg(&R.circ[3 * v + 2]));
         }
-        block_sum_f<6>(a, red, red + 32 * 16);
-        if (tid < 3) Fout[F_TOT + tid] = red[32 * 16 + tid];
-        if (tid == 3) Fout[F_EFB] = red[32 * 16 + 3];
-        if (tid == 4) Fout[F_EFO] = red[32 * 16 + 4];
-        if (tid == 5) Fout[F_Q] = red[32 * 16 + 5];
+        block_sum_f<10>(a, red, red + 32 * 16);
+        const double *o = red + 32 * 16;
+        if (tid < 3) Fout[F_TOT + tid] = o[tid];
+        if (tid == 3) Fout[F_EFB] = o[3];
+        if (tid == 4) Fout[F_EFO] = o[4];
+        if (tid == 5) Fout[F_Q] = o[5];
+        if (pid && tid >= 6 && tid < 9) { Fout[F_SI + tid - 6] = o[tid]; Fout[F_SJ + tid - 6] = o[tid]; }
+        if (pid && tid == 9) Fout[F_SIJ] = o[9];
         __syncthreads();
     }
     // pass G: orbital groups, four at a time; a group that holds every site
@@ -436,46 +457,38 @@ __device__ void on_frame(const Rep &R, const float *jt, const float *dt, const S
         if (tid < 12 && g0 + tid / 3 < MCS_MAXG && ((keep >> (tid / 3)) & 1)) Fout[F_G + 3 * g0 + tid] = red[32 * 16 + tid];
         __syncthreads();
     }
-    // pass B (site-centric): when every correlated pair is (v, v) and each site
-    // appears once, walk the sites instead of the pair and chosen-site lists.
+    // pass B (chosen-site walk): when every correlated pair is (v, v) the pair
+    // sums came from pass A; the renormalised sums walk the chosen sites.
     if (R.pair_identity) {
-        float a[12];
+        float a[8];
 #pragma unroll
-        for (int k = 0; k < 12; ++k) a[k] = 0.f;
-        const int e = min(ve, R.N);
-        for (int v = vb + tid; v < e; v += bd) {
-            const int fl = R.sflag[v];
-            if (!fl) continue;
-            float px = S.x[v], py = S.y[v], pz = DIM == 3 ? S.z[v] : 0.f;
-            if (fl & 1) { a[0] += px; a[1] += py; a[2] += pz; a[3] += px * px + py * py + pz * pz; }
-            if (fl & 2) {
-                const int r = R.rindex[v];
-                float mx, my, mz;
-                if (majc) { mx = majc[3 * r]; my = majc[3 * r + 1]; mz = majc[3 * r + 2]; }
-                else on_majority<DIM>(R, S, v, mx, my, mz);
-                if (fl & 1) { a[4] += mx; a[5] += my; a[6] += mz; a[7] += mx * mx + my * my + mz * mz; }
-                float corr = 0.f;
-                const int d = R.rdeg[r];
-                for (int l = 0; l < d; ++l) {
-                    const int tr = __ldg(&R.rtgt[(size_t)r * R.zmax + l]);  // cache slot of the target
-                    if (tr < 0) continue;
-                    float tx, ty, tz;
-                    if (majc) { tx = majc[3 * tr]; ty = majc[3 * tr + 1]; tz = majc[3 * tr + 2]; }
-                    else on_majority<DIM>(R, S, __ldg(&R.rorb[tr]), tx, ty, tz);
-                    corr += on_jdot<DIM>(jt + 9 * R.rjc[(size_t)r * R.zmax + l], full, mx, my, mz, tx, ty, tz);
-                }
-                a[8] += corr;
-                a[9] += on_onsite<DIM>(R, dt, S, v);
+        for (int k = 0; k < 8; ++k) a[k] = 0.f;
+        const int e = min(ve, R.n_rorb);
+        for (int r = vb + tid; r < e; r += bd) {
+            const int v = __ldg(&R.rorb[r]);
+            float mx, my, mz;
+            if (majc) { mx = majc[3 * r]; my = majc[3 * r + 1]; mz = majc[3 * r + 2]; }
+            else on_majority<DIM>(R, S, v, mx, my, mz);
+            if (R.sflag[v] & 1) { a[0] += mx; a[1] += my; a[2] += mz; a[3] += mx * mx + my * my + mz * mz; }
+            float corr = 0.f;
+            const int d = R.rdeg[r];
+            for (int l = 0; l < d; ++l) {
+                const int tr = __ldg(&R.rtgt[(size_t)r * R.zmax + l]);  // chosen index of the target
+                if (tr < 0) continue;
+                float tx, ty, tz;
+                if (majc) { tx = majc[3 * tr]; ty = majc[3 * tr + 1]; tz = majc[3 * tr + 2]; }
+                else on_majority<DIM>(R, S, __ldg(&R.rorb[tr]), tx, ty, tz);
+                corr += on_jdot<DIM>(jt + 9 * R.rjc[(size_t)r * R.zmax + l], full, mx, my, mz, tx, ty, tz);
             }
+            a[4] += corr;
+            a[5] += on_onsite<DIM>(R, dt, S, v);
         }
-        block_sum_f<12>(a, red, red + 32 * 16);
+        block_sum_f<8>(a, red, red + 32 * 16);
         const double *o = red + 32 * 16;
-        if (tid < 3) { Fout[F_SI + tid] = o[tid]; Fout[F_SJ + tid] = o[tid]; }
-        if (tid == 3) Fout[F_SIJ] = o[3];
-        if (tid >= 4 && tid < 7) { Fout[F_SIR + tid - 4] = o[tid]; Fout[F_SJR + tid - 4] = o[tid]; }
-        if (tid == 7) Fout[F_SIJR] = o[7];
-        if (tid == 8) Fout[F_ERB] = o[8];
-        if (tid == 9) Fout[F_ERO] = o[9];
+        if (tid < 3) { Fout[F_SIR + tid] = o[tid]; Fout[F_SJR + tid] = o[tid]; }
+        if (tid == 3) Fout[F_SIJR] = o[3];
+        if (tid == 4) Fout[F_ERB] = o[4];
+        if (tid == 5) Fout[F_ERO] = o[5];
         __syncthreads();
         return;
     }
@@ -535,45 +548,46 @@ template <int DIM>
 __device__ void on_accumulate(Rep &R, const double *F, double E, long long m)
 {
     double *acc = R.acc;
-    const double nl = (double)R.nlat;
+    const double inl = R.inv_nl;
     double tx = F[F_TOT], ty = F[F_TOT + 1], tz = DIM == 3 ? F[F_TOT + 2] : 0.0;
     double dx = tx, dy = ty, dz = tz;
     double len = sqrt(dx * dx + dy * dy + dz * dz);
-    if (len >= 1e-5) { dx /= len; dy /= len; dz /= len; }
+    if (len >= 1e-5) { double il = 1.0 / len; dx *= il; dy *= il; dz *= il; }
     double six = F[F_SI], siy = F[F_SI + 1], siz = DIM == 3 ? F[F_SI + 2] : 0.0;
     double sjx = F[F_SJ], sjy = F[F_SJ + 1], sjz = DIM == 3 ? F[F_SJ + 2] : 0.0;
-    acc[A_SIZ] += (dx * six + dy * siy + dz * siz) / nl;
-    acc[A_SJZ] += (dx * sjx + dy * sjy + dz * sjz) / nl;
-    acc[A_STZ] += (dx * tx + dy * ty + dz * tz) / nl;
-    acc[A_SIH] += (DIM == 3 ? siz : six) / nl;
-    acc[A_SJH] += (DIM == 3 ? sjz : sjx) / nl;
-    acc[A_STH] += (DIM == 3 ? tz : tx) / nl;
-    double M = (DIM == 3) ? sqrt(tx * tx + ty * ty + tz * tz) / nl : sqrt(six * six + siy * siy) / nl;
-    acc[A_M2] += M * M;
-    acc[A_M4] += M * M * M * M;
+    acc[A_SIZ] += (dx * six + dy * siy + dz * siz) * inl;
+    acc[A_SJZ] += (dx * sjx + dy * sjy + dz * sjz) * inl;
+    acc[A_STZ] += (dx * tx + dy * ty + dz * tz) * inl;
+    acc[A_SIH] += (DIM == 3 ? siz : six) * inl;
+    acc[A_SJH] += (DIM == 3 ? sjz : sjx) * inl;
+    acc[A_STH] += (DIM == 3 ? tz : tx) * inl;
+    double M = (DIM == 3) ? sqrt(tx * tx + ty * ty + tz * tz) * inl : sqrt(six * six + siy * siy) * inl;
+    const double M2 = M * M;
+    acc[A_M2] += M2;
+    acc[A_M4] += M2 * M2;
     acc[A_MTOT] += M;
     acc[A_MDM] += acc[A_MPREV] * M;
     acc[A_MPREV] = M;
-    acc[A_SI] += fabs(six / nl); acc[A_SI + 1] += fabs(siy / nl); acc[A_SI + 2] += fabs(siz / nl);
-    acc[A_SJ] += fabs(sjx / nl); acc[A_SJ + 1] += fabs(sjy / nl); acc[A_SJ + 2] += fabs(sjz / nl);
-    acc[A_SIJ] += F[F_SIJ] / nl;
-    double e = E / R.N;
+    acc[A_SI] += fabs(six * inl); acc[A_SI + 1] += fabs(siy * inl); acc[A_SI + 2] += fabs(siz * inl);
+    acc[A_SJ] += fabs(sjx * inl); acc[A_SJ + 1] += fabs(sjy * inl); acc[A_SJ + 2] += fabs(sjz * inl);
+    acc[A_SIJ] += F[F_SIJ] * inl;
+    double e = E * R.inv_N;
     acc[A_E] += e;
     acc[A_E2] += e * e;
     for (int k = 0; k < 3; ++k) {
-        acc[A_SIR + k] += fabs(F[F_SIR + k] / R.ci);
-        acc[A_SJR + k] += fabs(F[F_SJR + k] / R.cj);
+        acc[A_SIR + k] += fabs(F[F_SIR + k] * R.inv_ci);
+        acc[A_SJR + k] += fabs(F[F_SJR + k] * R.inv_cj);
     }
-    acc[A_SIJR] += F[F_SIJR] / R.cij;
-    double er = (F[F_ERB] / 2 + F[F_ERO]) / R.n_rorb;
+    acc[A_SIJR] += F[F_SIJR] * R.inv_cij;
+    double er = (F[F_ERB] * 0.5 + F[F_ERO]) * R.inv_nr;
     acc[A_ER] += er;
     acc[A_ER2] += er * er;
-    if (DIM == 3) acc[A_Q] += F[F_Q] / MCS_PI_REF / 4;
+    if (DIM == 3) acc[A_Q] += F[F_Q] * (1.0 / (MCS_PI_REF * 4));
     const int G = R.ngroup;
     if (G > 0) {
         double gx[MCS_MAXG + 1], gy[MCS_MAXG + 1], gz[MCS_MAXG + 1];
         for (int g = 0; g < G; ++g) { gx[g] = F[F_G + 3 * g]; gy[g] = F[F_G + 3 * g + 1]; gz[g] = DIM == 3 ? F[F_G + 3 * g + 2] : 0.0; }
-        gx[G] = tx / nl; gy[G] = ty / nl; gz[G] = tz / nl;
+        gx[G] = tx * inl; gy[G] = ty * inl; gz[G] = tz * inl;
         for (int a = 0; a <= G; ++a)
             for (int b = 0; b <= G; ++b) {
                 double d = gx[a] * gx[b] + gy[a] * gy[b] + gz[a] * gz[b];
@@ -583,7 +597,7 @@ __device__ void on_accumulate(Rep &R, const double *F, double E, long long m)
     }
     if (R.series) {
         double *s = R.series + (size_t)m * MCS_NSER;
-        s[0] = e; s[1] = M; s[2] = er; s[3] = F[F_SIJ] / nl;
+        s[0] = e; s[1] = M; s[2] = er; s[3] = F[F_SIJ] * inl;
     }
 }
 
@@ -765,23 +779,23 @@ __device__ void is_accumulate(Rep &R, const double *Fd, const long long *Fi, int
     double ts = Mtrue - R.ts_const;
     if (R.ts_wolff_last) ts -= R.Stype[R.stype ? R.stype[R.last_site] : 0] * (double)last_sign;
     acc[B_STOT] += ts;
-    double M = Fd[0] / nl;
+    double M = Fd[0] * R.inv_nl;
     acc[B_M2] += M * M;
     acc[B_M4] += M * M * M * M;
     acc[B_MTOT] += M;
     acc[B_MDM] += acc[B_MPREV] * M;
     acc[B_MPREV] = M;
-    acc[B_SI] += fabs(Fd[0]) / nl;
-    acc[B_SJ] += fabs(Fd[1]) / nl;
-    acc[B_SIJ] += Fd[2] / nl;
-    double e = e_rep / R.N, er = Fd[3] / R.n_rorb;
+    acc[B_SI] += fabs(Fd[0]) * R.inv_nl;
+    acc[B_SJ] += fabs(Fd[1]) * R.inv_nl;
+    acc[B_SIJ] += Fd[2] * R.inv_nl;
+    double e = e_rep * R.inv_N, er = Fd[3] * R.inv_nr;
     acc[B_E] += e;
     acc[B_ER] += er;
     acc[B_E2] += e * e;
     acc[B_ER2] += er * er;
     if (R.series) {
         double *s = R.series + (size_t)m * MCS_NSER;
-        s[0] = e; s[1] = M; s[2] = er; s[3] = Fd[2] / nl;
+        s[0] = e; s[1] = M; s[2] = er; s[3] = Fd[2] * R.inv_nl;
     }
 }
 

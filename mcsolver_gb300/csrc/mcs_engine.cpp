@@ -167,6 +167,15 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r)
     R.slen = (const float *)(b + o_slen); R.sval = (const float *)(b + o_sval);
     R.ngroup = m.ngroup; R.gmask = (const unsigned char *)(b + o_gmask);
     R.ci = m.ci; R.cj = m.cj; R.cij = m.cij;
+    R.inv_nl = 1.0 / m.nlat; R.inv_N = 1.0 / m.N;
+    R.inv_ci = 1.0 / m.ci; R.inv_cj = 1.0 / m.cj; R.inv_cij = 1.0 / m.cij; R.inv_nr = 1.0 / m.n_rorb;
+    R.nacc = (int)replica_acc_count(m);
+    {
+        bool uni = true;
+        for (int k = 0; k < m.N && uni; ++k) uni = m.slen[k] == m.slen[0];
+        R.uniform_len = uni && m.slen[0] > 0;
+        R.inv_len3 = R.uniform_len ? 1.0f / (m.slen[0] * m.slen[0] * m.slen[0]) : 0.f;
+    }
     R.pair_identity = m.pair_identity;
     R.gall = m.gall;
     R.sflag = (const unsigned char *)(b + o_sflag);

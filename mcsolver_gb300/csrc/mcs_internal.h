@@ -112,6 +112,10 @@ struct Rep {
     int ngroup; const unsigned char *gmask;      // [N]
     int gall;                                    // bitmask of groups that hold every site
     int ci, cj, cij;                             // chosen counts of the pair lists
+    double inv_nl, inv_N, inv_ci, inv_cj, inv_cij, inv_nr;  // reciprocals of the divisors above
+    int nacc;                                    // FP64 accumulators in acc[]
+    int uniform_len;                             // every |S| equal (circuit fast path)
+    float inv_len3;                              // 1/|S|^3 when uniform_len
     int pair_identity;                           // every pair is (v, v), each site at most once
     const unsigned char *sflag;                  // [N] bit0: site is a pair member, bit1: chosen
     const int *rtgt;                             // [n_rorb*zmax] index in rorb of the l-th renormalised target (-1)

@@ -26,7 +26,7 @@ static __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~
 #define MCS_RED_DOUBLES MCS_RED
 
 struct SmemLayout {
-    size_t spins, tables, stype, majc, red, F, redl, Fi, total;
+    size_t spins, tables, stype, majc, red, F, redl, Fi, acc, total;
 };
 // Shared-memory plan of a resident replica.  The block-spin cache of the
 // renormalised lattice is included only when it fits (flag returned in majc
@@ -48,6 +48,7 @@ __host__ __device__ inline SmemLayout smem_layout(const Rep &R, size_t limit = 2
     L.F = off; off += F_NON * sizeof(double);
     L.redl = off; off += (32 * 16 + 16) * sizeof(long long);
     L.Fi = off; off += 16 * sizeof(long long);
+    L.acc = off; off += align16((size_t)R.nacc * sizeof(double) + C_NINT * sizeof(long long));
     L.majc = 0;
     size_t mbytes = align16((size_t)R.n_rorb * 3 * sizeof(float));
     if (R.dim > 1 && off + mbytes <= limit) { L.majc = off; off += mbytes; }
@@ -63,6 +64,25 @@ int resident_max_smem()
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     return v;
+}
+
+// The FP64 accumulators and the Ising integer counters of a replica are kept
+// in shared memory for the life of a launch (thread 0 updates them at every
+// measurement) and written back at its end.
+__device__ __forceinline__ void acc_to_smem(Rep &R, unsigned char *buf)
+{
+    double *a = (double *)buf;
+    long long *ic = (long long *)(a + R.nacc);
+    for (int k = threadIdx.x; k < R.nacc; k += blockDim.x) a[k] = R.acc[k];
+    for (int k = threadIdx.x; k < C_NINT; k += blockDim.x) ic[k] = R.icnt[k];
+    __syncthreads();
+    if (threadIdx.x == 0) { R.acc = a; R.icnt = ic; }
+    __syncthreads();
+}
+__device__ __forceinline__ void acc_to_global(const Rep &R, const Rep *Rg)
+{
+    for (int k = threadIdx.x; k < R.nacc; k += blockDim.x) Rg->acc[k] = R.acc[k];
+    for (int k = threadIdx.x; k < C_NINT; k += blockDim.x) Rg->icnt[k] = R.icnt[k];
 }
 
 // copy the replica descriptor into shared memory with all threads
@@ -115,6 +135,7 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
         for (int k = tid; k < R.ndc * 4; k += bd) dt[k] = R.dtab[k];
     }
     __syncthreads();
+    acc_to_smem(R, smem + L.acc);
 
     int dn[MCS_MAXC] = {0, 0, 0, 0}, dm[MCS_MAXT] = {0, 0, 0, 0};
     long long nacc = 0;
@@ -252,6 +273,7 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
         }
     }
     fold();
+    acc_to_global(R, Rg);
     for (int v = tid; v < N; v += bd) {
         if (DIM == 1) G.s[v] = S.s[v];
         else {
@@ -481,7 +503,7 @@ __global__ void __launch_bounds__(1024) k_init(Rep *reps, const int *ids)
 
 // ======================================================================= Wolff
 struct WolffLayout {
-    size_t spins, tables, stype, bits, queue, red, F, redl, Fi, sh, total;
+    size_t spins, tables, stype, bits, queue, red, F, redl, Fi, sh, acc, total;
     int gstate;     // 1: spins, bits and queue live in global memory
     int q16;
 };
@@ -511,6 +533,7 @@ __host__ __device__ inline WolffLayout wolff_layout(const Rep &R, size_t limit =
         L.redl = off; off += (32 * 16 + 16) * sizeof(long long);
         L.Fi = off; off += 16 * sizeof(long long);
         L.sh = off; off += 64;
+        L.acc = off; off += align16((size_t)R.nacc * sizeof(double) + C_NINT * sizeof(long long));
         L.total = off;
         if (L.total <= limit) return L;
     }
@@ -575,6 +598,7 @@ __global__ void __launch_bounds__(512) k_wolff(Rep *reps, const int *ids, long l
         for (int k = tid; k < R.ndc * 4; k += bd) dt[k] = R.dtab[k];
     }
     __syncthreads();
+    acc_to_smem(R, smem + L.acc);
     double dEd = 0.0;
     long long dnacc = 0;
     int dn[MCS_MAXC] = {0, 0, 0, 0}, dm[MCS_MAXT] = {0, 0, 0, 0};
@@ -619,6 +643,8 @@ __global__ void __launch_bounds__(512) k_wolff(Rep *reps, const int *ids, long l
         }
     }
     if (DIM > 1 && tid == 0) R.acc[A_ECUR] += dEd;
+    __syncthreads();
+    acc_to_global(R, Rg);
     if (!L.gstate)
         for (int v = tid; v < N; v += bd) {
             if (DIM == 1) G.s[v] = S.s[v];
