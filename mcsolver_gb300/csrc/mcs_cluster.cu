@@ -1,0 +1,429 @@
+// mcs_cluster.cu -- cluster schedule of the Metropolis sweep (square lattice, XY / Heisenberg).
+//
+// One replica is split by rows over a thread-block cluster of C CTAs (C = 2, 4
+// or 8).  CTA r owns rows [r*RP, (r+1)*RP) of both colours (RP = Lx/C, even)
+// and keeps one ghost row on each side:
+//
+//   local index (c, xl, yh) = c*(RP+2)*hy + (xl+1)*hy + yh,   xl in [-1, RP]
+//
+// A colour phase updates the CTA's own sites of that colour from local data
+// only; a cluster barrier follows, then each CTA pulls the two boundary rows
+// of the colour just updated from its neighbours' shared memory (DSMEM) into
+// its ghost rows.  Measurements reduce per-CTA partial sums through DSMEM into
+// rank 0, which owns the replica's FP64 accumulators for the launch.  The
+// per-site update, the Philox counters and the measurement sums are the ones
+// of the other schedules, so the spin trajectory is the same.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include "mcs_device.cuh"
+#include "mcs_internal.h"
+
+namespace cg = cooperative_groups;
+
+namespace mcs {
+
+static __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+#define CL_NV 28
+#define CL_PART 32
+#define CL_RED (32 * CL_NV + 32)
+
+struct ClusterLayout {
+    size_t spins, tables, majc, part, red, F, acc, total;
+    int rows, hy, nloc, nchosen;
+};
+
+__host__ __device__ inline ClusterLayout cluster_layout(const Rep &R, int C)
+{
+    ClusterLayout L;
+    const int RP = R.Lx / C;
+    L.rows = RP + 2;
+    L.hy = R.hy;
+    L.nloc = 2 * L.rows * L.hy;
+    L.nchosen = (RP / 2) * (R.Ly / 2);
+    size_t off = 0;
+    L.spins = off; off += a16((size_t)R.dim * L.nloc * sizeof(float));
+    L.tables = off; off += a16((size_t)R.njc * 9 * sizeof(float) + (size_t)R.ndc * 4 * sizeof(float));
+    L.majc = off; off += a16((size_t)L.nchosen * 3 * sizeof(float));
+    L.part = off; off += CL_PART * sizeof(double);
+    L.red = off; off += CL_RED * sizeof(double);
+    L.F = off; off += F_NON * sizeof(double);
+    L.acc = off; off += a16((size_t)R.nacc * sizeof(double) + C_NINT * sizeof(long long));
+    L.total = off;
+    return L;
+}
+
+// Square-lattice neighbours of an owned site in local coordinates.
+template <class F>
+__device__ __forceinline__ void cl_links(const Rep &R, int rows, int c, int xl, int yh, F &&f)
+{
+    const int Ly = R.Ly, hy = R.hy;
+    const int x = xl;  // parity of the global row equals the parity of xl (RP even)
+    const int y = 2 * yh + ((x + c) & 1);
+    const int base = (1 - c) * rows * hy;
+    const int yp = (y + 1 == Ly) ? 0 : y + 1;
+    const int ym = (y == 0) ? Ly - 1 : y - 1;
+    f(0, base + (xl + 2) * hy + yh, R.sq_code[0]);
+    f(1, base + xl * hy + yh, R.sq_code[1]);
+    f(2, base + (xl + 1) * hy + (yp >> 1), R.sq_code[2]);
+    f(3, base + (xl + 1) * hy + (ym >> 1), R.sq_code[3]);
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(1024) k_cluster_metro(Rep *reps, const int *ids, long long max_units, int C)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ Rep R;
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    Rep *Rg = reps + ids[blockIdx.x / C];
+    {
+        const int *s = (const int *)Rg;
+        int *d = (int *)&R;
+        for (int i = threadIdx.x; i < (int)(sizeof(Rep) / 4); i += blockDim.x) d[i] = s[i];
+    }
+    __syncthreads();
+    // every CTA of the cluster reads the same descriptor: the early exit is uniform over the cluster
+    if (R.u >= R.units_total) return;
+    const ClusterLayout L = cluster_layout(R, C);
+    const int tid = threadIdx.x, bd = blockDim.x;
+    const int hy = L.hy, rows = L.rows, RP = rows - 2, x0 = rank * RP, nloc = L.nloc;
+    const int half = R.half;
+    float *sp = (float *)(smem + L.spins);
+    Spins S;
+    S.x = sp; S.y = sp + nloc; S.z = sp + 2 * nloc;
+    float *jt = (float *)(smem + L.tables);
+    float *dt = jt + R.njc * 9;
+    float *majc = (float *)(smem + L.majc);
+    double *part = (double *)(smem + L.part);
+    double *red = (double *)(smem + L.red);
+    double *F = (double *)(smem + L.F);
+    Spins G = spins_global(R);
+    // own rows and ghost rows from global memory
+    for (int i = tid; i < nloc; i += bd) {
+        const int c = i / (rows * hy);
+        const int rem = i - c * rows * hy;
+        const int xl = rem / hy - 1, yh = rem - (xl + 1) * hy;
+        int x = x0 + xl;
+        if (x < 0) x += R.Lx;
+        if (x >= R.Lx) x -= R.Lx;
+        const int v = c * half + x * hy + yh;
+        S.x[i] = G.x[v]; S.y[i] = G.y[v];
+        if (DIM == 3) S.z[i] = G.z[v];
+    }
+    for (int k = tid; k < R.njc * 9; k += bd) jt[k] = R.jtab[k];
+    for (int k = tid; k < R.ndc * 4; k += bd) dt[k] = R.dtab[k];
+    if (rank == 0) {
+        double *a = (double *)(smem + L.acc);
+        for (int k = tid; k < R.nacc; k += bd) a[k] = R.acc[k];
+        __syncthreads();
+        if (tid == 0) R.acc = a;
+    }
+    __syncthreads();
+    cl.sync();
+
+    const float beta = R.beta, h = R.h;
+    double dEd = 0.0;
+    long long nacc = 0;
+    const int nown = RP * hy;  // own sites per colour
+    const int rprev = (rank + C - 1) % C, rnext = (rank + 1) % C;
+    float *prev_sp = cl.map_shared_rank(sp, rprev);
+    float *next_sp = cl.map_shared_rank(sp, rnext);
+
+    // partial sums of one measurement -> rank 0 (fixed rank order)
+    auto measure = [&](long long m, bool efull) {
+        // block spins of the own chosen sites
+        const int r0 = rank * L.nchosen;
+        for (int q = tid; q < L.nchosen; q += bd) {
+            const int pr = q / (R.Ly / 2);           // even-row index inside the CTA
+            const int yc = q - pr * (R.Ly / 2);
+            const int xl = 2 * pr, y = 2 * yc;     // chosen: even x, even y
+            const int yh = y >> 1;
+            // cluster (x,y), (x,y+1), (x+1,y), (x+1,y+1) for Lz = 1
+            const int y1 = (y + 1 == R.Ly) ? 0 : y + 1;
+            const int c00 = (xl + y) & 1, c01 = (xl + y1) & 1, c10 = (xl + 1 + y) & 1, c11 = (xl + 1 + y1) & 1;
+            const int i00 = c00 * rows * hy + (xl + 1) * hy + yh;
+            const int i01 = c01 * rows * hy + (xl + 1) * hy + (y1 >> 1);
+            const int i10 = c10 * rows * hy + (xl + 2) * hy + yh;
+            const int i11 = c11 * rows * hy + (xl + 2) * hy + (y1 >> 1);
+            float mx = S.x[i00] + S.x[i01] + S.x[i10] + S.x[i11];
+            float my = S.y[i00] + S.y[i01] + S.y[i10] + S.y[i11];
+            float mz = DIM == 3 ? S.z[i00] + S.z[i01] + S.z[i10] + S.z[i11] : 0.f;
+            v_norm_ref(mx, my, mz);
+            const float sv = R.sval[R.rorb[r0 + q]];
+            majc[3 * q] = mx * sv; majc[3 * q + 1] = my * sv; majc[3 * q + 2] = mz * sv;
+        }
+        __syncthreads();
+        cl.sync();
+        const bool full = R.fullJ;
+        // partial layout: 0-2 total spin, 3-5 pair sum, 6 pair s.s, 7/8 full
+        // energy bond/onsite, 9 solid angles, 10-12 block-spin pair sum,
+        // 13 block s.s, 14/15 renormalised bond/onsite, 16-27 four groups
+        float a[CL_NV];
+#pragma unroll
+        for (int k = 0; k < CL_NV; ++k) a[k] = 0.f;
+        // pass A over own sites: total spin, pair sums, groups, full energy
+        for (int c = 0; c < 2; ++c)
+            for (int kk = tid; kk < nown; kk += bd) {
+                const int xl = kk / hy, yh = kk - xl * hy;
+                const int li = c * rows * hy + (xl + 1) * hy + yh;
+                const int v = c * half + (x0 + xl) * hy + yh;
+                const float sx = S.x[li], sy = S.y[li], sz = DIM == 3 ? S.z[li] : 0.f;
+                a[0] += sx; a[1] += sy; a[2] += sz;
+                if (R.sflag[v] & 1) { a[3] += sx; a[4] += sy; a[5] += sz; a[6] += sx * sx + sy * sy + sz * sz; }
+                if (efull) {
+                    float h0, h1, h2;
+                    on_field<DIM>(R, jt, S, [&](auto &&f) { cl_links(R, rows, c, xl, yh, f); }, h0, h1, h2);
+                    a[7] += sx * h0 + sy * h1 + sz * h2;
+                    float e = 0.f;
+                    if (R.has_d) {
+                        e = dt[0] * sx * sx + dt[1] * sy * sy;
+                        if (DIM == 3) e += dt[2] * sz * sz;
+                    }
+                    a[8] += e - h * ((DIM == 3) ? sz : sx);
+                }
+                const int gm = R.ngroup ? (R.gmask[v] & ~R.gall) : 0;
+                if (gm) {
+#pragma unroll
+                    for (int g = 0; g < 4; ++g)
+                        if (gm & (1 << g)) { a[16 + 3 * g] += sx; a[17 + 3 * g] += sy; a[18 + 3 * g] += sz; }
+                }
+            }
+        // circuits of the cells this CTA owns (Heisenberg): circuit (cell, q)
+        // has index cell*per + q and its sites lie in rows x and x+1
+        if (DIM == 3 && R.ncirc > 0) {
+            const int per = R.ncirc / R.N;
+            for (int c = 0; c < 2; ++c)
+                for (int kk = tid; kk < nown; kk += bd) {
+                    const int xl = kk / hy, yh = kk - xl * hy;
+                    const int xg = x0 + xl, yg = 2 * yh + ((xg + c) & 1);
+                    for (int q = 0; q < per; ++q) {
+                        const int ci = (xg * R.Ly + yg) * per + q;
+                        const int tv[3] = {__ldg(&R.circ[3 * ci]), __ldg(&R.circ[3 * ci + 1]), __ldg(&R.circ[3 * ci + 2])};
+                        int li3[3];
+#pragma unroll
+                        for (int e3 = 0; e3 < 3; ++e3) {
+                            const int w = tv[e3];
+                            const int cc = w >= half;
+                            const int k2 = w - cc * half;
+                            const int xw = k2 / hy, yy = k2 - xw * hy;
+                            int xl2 = xw - x0;
+                            if (xl2 < -1) xl2 += R.Lx;
+                            if (xl2 > RP) xl2 -= R.Lx;
+                            li3[e3] = cc * rows * hy + (xl2 + 1) * hy + yy;
+                        }
+                        const int ia = li3[0], ib = li3[1], ic = li3[2];
+                        const float ax = S.x[ia], ay = S.y[ia], az = S.z[ia];
+                        const float bx = S.x[ib], by = S.y[ib], bz = S.z[ib];
+                        const float cx = S.x[ic], cy = S.y[ic], cz = S.z[ic];
+                        const float l = R.slen[0], il2 = 1.f / (l * l);
+                        const float s1s2 = (ax * bx + ay * by + az * bz) * il2;
+                        const float s2s3 = (bx * cx + by * cy + bz * cz) * il2;
+                        const float s3s1 = (cx * ax + cy * ay + cz * az) * il2;
+                        const float kx = by * cz - bz * cy, ky = bz * cx - bx * cz, kz = bx * cy - by * cx;
+                        const float re = 1.f + s1s2 + s2s3 + s3s1;
+                        const float im = (ax * kx + ay * ky + az * kz) * R.inv_len3;
+                        a[9] += (fabsf(re) < 1e-6f) ? (im > 0.f ? (float)MCS_PI_REF : -(float)MCS_PI_REF)
+                                                    : 2.f * atanf(__fdividef(im, re));
+                    }
+                }
+        }
+        // pass B over own chosen sites
+        for (int q = tid; q < L.nchosen; q += bd) {
+            const int r = r0 + q;
+            const int v = R.rorb[r];
+            const float mx = majc[3 * q], my = majc[3 * q + 1], mz = majc[3 * q + 2];
+            if (R.sflag[v] & 1) { a[10] += mx; a[11] += my; a[12] += mz; a[13] += mx * mx + my * my + mz * mz; }
+            float corr = 0.f;
+            const int d = R.rdeg[r];
+            for (int l = 0; l < d; ++l) {
+                const int tr = __ldg(&R.rtgt[(size_t)r * R.zmax + l]);
+                if (tr < 0) continue;
+                const int owner = tr / L.nchosen;
+                const float *mc = owner == rank ? majc : cl.map_shared_rank(majc, owner);
+                const int lq = tr - owner * L.nchosen;
+                corr += on_jdot<DIM>(jt + 9 * R.rjc[(size_t)r * R.zmax + l], full, mx, my, mz, mc[3 * lq], mc[3 * lq + 1], mc[3 * lq + 2]);
+            }
+            a[14] += corr;
+            // onsite energy of the actual spin
+            const int cc = v >= half;
+            const int k2 = v - cc * half;
+            const int xg = k2 / hy, yy = k2 - xg * hy;
+            const int li = cc * rows * hy + (xg - x0 + 1) * hy + yy;
+            const float sx = S.x[li], sy = S.y[li], sz = DIM == 3 ? S.z[li] : 0.f;
+            float e = 0.f;
+            if (R.has_d) {
+                e = dt[0] * sx * sx + dt[1] * sy * sy;
+                if (DIM == 3) e += dt[2] * sz * sz;
+            }
+            a[15] += e - h * ((DIM == 3) ? sz : sx);
+        }
+        block_sum_f<CL_NV>(a, red, red + 32 * CL_NV);
+        if (tid < CL_NV) part[tid] = red[32 * CL_NV + tid];
+        if (tid == 0) { part[CL_NV] = dEd; part[CL_NV + 1] = (double)nacc; }
+        dEd = 0.0;
+        nacc = 0;
+        __syncthreads();
+        cl.sync();
+        if (rank == 0) {
+            if (tid < CL_NV + 2) {
+                double s = 0.0;
+                for (int q = 0; q < C; ++q) s += cl.map_shared_rank(part, q)[tid];
+                red[tid] = s;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                const double *o = red;
+                for (int k = 0; k < F_NON; ++k) F[k] = 0.0;
+                for (int k = 0; k < 3; ++k) {
+                    F[F_TOT + k] = o[k];
+                    F[F_SI + k] = F[F_SJ + k] = o[3 + k];
+                    F[F_SIR + k] = F[F_SJR + k] = o[10 + k];
+                }
+                F[F_SIJ] = o[6];
+                F[F_EFB] = o[7]; F[F_EFO] = o[8]; F[F_Q] = o[9];
+                F[F_SIJR] = o[13];
+                F[F_ERB] = o[14]; F[F_ERO] = o[15];
+                for (int g = 0; g < R.ngroup; ++g) {
+                    const bool all = (R.gall >> g) & 1;
+                    for (int k = 0; k < 3; ++k) F[F_G + 3 * g + k] = all ? o[k] : o[16 + 3 * g + k];
+                }
+                R.acc[A_ECUR] += o[CL_NV];
+                R.stats[S_ACCEPT] += (long long)o[CL_NV + 1];
+                if (efull) {
+                    double Ef = F[F_EFB] / 2 + F[F_EFO];
+                    double d = fabs(R.acc[A_ECUR] - Ef);
+                    if (d > R.acc[A_DRIFT]) R.acc[A_DRIFT] = d;
+                    R.acc[A_ECUR] = Ef;
+                }
+                on_accumulate<DIM>(R, F, R.acc[A_ECUR], m);
+            }
+        }
+        // spin frame: every CTA writes its own rows
+        if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) {
+            float *fb = R.frame_buf + (size_t)R.frames_written * R.N * 3;
+            for (int c = 0; c < 2; ++c)
+                for (int kk = tid; kk < nown; kk += bd) {
+                    const int xl = kk / hy, yh = kk - xl * hy;
+                    const int li = c * rows * hy + (xl + 1) * hy + yh;
+                    const int v = c * half + (x0 + xl) * hy + yh;
+                    fb[3 * v] = S.x[li]; fb[3 * v + 1] = S.y[li]; fb[3 * v + 2] = DIM == 3 ? S.z[li] : 0.f;
+                }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) R.frames_written++;
+            R.m = m + 1;
+        }
+        __syncthreads();
+    };
+
+    long long u = R.u;
+    const long long uend = min(R.units_total, u + max_units);
+    for (; u < uend; ++u) {
+        const long long t = R.u0 + u;
+        for (int c = 0; c < 2; ++c) {
+            float dEf = 0.f;
+            SqWalk wk;
+            wk.init(tid, bd, hy);
+            for (int kk = tid; kk < nown; kk += bd) {
+                const int xl = wk.x, yh = wk.yh;
+                const int li = c * rows * hy + (xl + 1) * hy + yh;
+                const int k = (x0 + xl) * hy + yh;  // colour-local index of the whole lattice
+                uint4 w = philox_t((uint32_t)k, t, (uint32_t)c, R.seed);
+                float dE;
+                if (on_trial<DIM>(R, jt, dt, S, li, 0, w, beta, h, [&](auto &&f) { cl_links(R, rows, c, xl, yh, f); }, &dE)) {
+                    dEf += dE;
+                    ++nacc;
+                }
+                wk.next();
+            }
+            dEd += (double)dEf;
+            cl.sync();
+            // ghost rows of colour c: row -1 <- previous CTA's row RP-1, row RP <- next CTA's row 0
+            const int cb = c * rows * hy;
+            for (int i = tid; i < 2 * hy; i += bd) {
+                const int side = i >= hy, yh = i - side * hy;
+                const int dst = cb + (side ? (RP + 1) : 0) * hy + yh;
+                const int src = cb + (side ? 1 : RP) * hy + yh;
+                const float *base = side ? next_sp : prev_sp;
+                S.x[dst] = base[src];
+                S.y[dst] = base[nloc + src];
+                if (DIM == 3) S.z[dst] = base[2 * nloc + src];
+            }
+            __syncthreads();
+        }
+        // the ghost rows must be complete in every CTA before the next colour
+        // phase reads them, and no CTA may overwrite a row a neighbour still copies
+        cl.sync();
+        if (measures_after(R, u)) measure(R.m, (R.m % R.recheck) == 0);
+    }
+    // fold the energy change since the last measurement
+    if (tid == 0) { part[CL_NV] = dEd; part[CL_NV + 1] = (double)nacc; }
+    __syncthreads();
+    cl.sync();
+    if (rank == 0 && tid == 0) {
+        double s = 0.0, na = 0.0;
+        for (int q = 0; q < C; ++q) { s += cl.map_shared_rank(part, q)[CL_NV]; na += cl.map_shared_rank(part, q)[CL_NV + 1]; }
+        R.acc[A_ECUR] += s;
+        R.stats[S_ACCEPT] += (long long)na;
+    }
+    cl.sync();
+    // own rows back to global memory
+    for (int c = 0; c < 2; ++c)
+        for (int kk = tid; kk < nown; kk += bd) {
+            const int xl = kk / hy, yh = kk - xl * hy;
+            const int li = c * rows * hy + (xl + 1) * hy + yh;
+            const int v = c * half + (x0 + xl) * hy + yh;
+            G.x[v] = S.x[li]; G.y[v] = S.y[li];
+            if (DIM == 3) G.z[v] = S.z[li];
+        }
+    if (rank == 0) {
+        __syncthreads();
+        for (int k = tid; k < R.nacc; k += bd) Rg->acc[k] = R.acc[k];
+        if (tid == 0) {
+            R.stats[S_VISITS] += (uend - R.u) * (long long)R.N;
+            Rg->u = uend;
+            Rg->m = R.m;
+            Rg->frames_written = R.frames_written;
+        }
+    }
+}
+
+long long cluster_smem_bytes(const Rep &r, int C) { return (long long)cluster_layout(r, C).total; }
+
+template <int DIM>
+static cudaError_t launch_cluster_t(Rep *reps, const int *ids, int nrep, int C, int threads, size_t smem,
+                                    long long max_units, cudaStream_t st)
+{
+    static size_t done = 0;
+    if (smem > done) {
+        cudaError_t e = cudaFuncSetAttribute(k_cluster_metro<DIM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        done = smem;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nrep * C, 1, 1);
+    cfg.blockDim = dim3(threads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_cluster_metro<DIM>, reps, ids, max_units, C);
+}
+
+cudaError_t launch_cluster_metro(int dim, Rep *reps, const int *ids, int nrep, int C, int threads, size_t smem,
+                                 long long max_units, cudaStream_t st)
+{
+    if (nrep <= 0) return cudaSuccess;
+    if (dim == 2) return launch_cluster_t<2>(reps, ids, nrep, C, threads, smem, max_units, st);
+    return launch_cluster_t<3>(reps, ids, nrep, C, threads, smem, max_units, st);
+}
+
+}  // namespace mcs

@@ -11,6 +11,7 @@
 //                    graphs (the one-solve-per-launch-sequence baseline).
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdlib.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -313,6 +314,8 @@ Batch::~Batch()
     if (stream2) cudaStreamDestroy(stream2);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    if (ev_a) cudaEventDestroy(ev_a);
+    if (ev_b) cudaEventDestroy(ev_b);
 }
 
 int Batch::init(int dev)
@@ -329,6 +332,8 @@ int Batch::ensure_streams()
     CUDA_TRY(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreate(&ev0));
     CUDA_TRY(cudaEventCreate(&ev1));
+    CUDA_TRY(cudaEventCreate(&ev_a));
+    CUDA_TRY(cudaEventCreate(&ev_b));
     return MCS_OK;
 }
 
@@ -353,7 +358,10 @@ static int choose_schedule(const Replica &r, int requested, int max_smem)
     if (requested == 1) return 1;            // plain
     if (requested == 3) return 3;            // tiled
     long long need = resident_smem_bytes(r.rep);
+    if (requested == 2) return need <= max_smem ? 2 : 3;
+    if (requested == 6 && r.hm.cluster_ok) return 6;
     if (need <= max_smem) return 2;
+    if (r.hm.cluster_ok) return 6;
     return 3;
 }
 
@@ -420,6 +428,14 @@ int Batch::setup_tiled(Group &G)
     return MCS_OK;
 }
 
+cudaError_t Batch::launch_group(Group &G, int C, int threads, long long units, cudaStream_t s)
+{
+    if (C <= 1) return launch_resident_metro(G.dim, G.geom, d_reps, G.d_ids, (int)G.ids.size(), threads, G.smem, units, s);
+    size_t sm = 0;
+    for (int id : G.ids) sm = std::max<size_t>(sm, (size_t)cluster_smem_bytes(replicas[id]->rep, C));
+    return launch_cluster_metro(G.dim, d_reps, G.d_ids, (int)G.ids.size(), C, threads, sm, units, s);
+}
+
 cudaError_t Batch::tiled_unit(Group &G, cudaStream_t s, long long *nl)
 {
     for (int c = 0; c < G.maxcol; ++c) {
@@ -442,10 +458,12 @@ int Batch::prepare()
     const int nrep = (int)replicas.size();
     if (nrep == 0) { prepared = true; return MCS_OK; }
     const int max_smem = resident_max_smem();
+    if (const char *e = getenv("MCSGPU_CLUSTER")) cluster_override = atoi(e);
+    if (const char *e = getenv("MCSGPU_NO_AUTOTUNE")) no_autotune = atoi(e);
     std::vector<Rep> host(nrep);
     for (int i = 0; i < nrep; ++i) {
         Replica &r = *replicas[i];
-        r.schedule = choose_schedule(r, r.requested_schedule, max_smem);
+        r.schedule = choose_schedule(r, cluster_override > 1 ? 6 : r.requested_schedule, max_smem);
         host[i] = r.rep;
     }
     CUDA_TRY(cudaMalloc(&d_reps, nrep * sizeof(Rep)));
@@ -466,7 +484,7 @@ int Batch::prepare()
             }
     }
     // groups
-    for (int kind : {2, 3, 1, 4, 5})
+    for (int kind : {2, 6, 3, 1, 4, 5})
         for (int d = 1; d <= 3; ++d)
             for (int g = 0; g <= 1; ++g) {
                 std::vector<int> ids;
@@ -501,12 +519,41 @@ int Batch::prepare()
                         G->threads = threads_override > 0 ? threads_override : 512;
                         G->chunk = 1 << 20;
                         if (chunk_override > 0) G->chunk = chunk_override;
-                    } else if (kind == 2) {
+                    } else if (kind == 2 || kind == 6) {
                         int work = d == 1 ? (maxcs + 3) / 4 : maxcs;
                         G->threads = std::min(1024, std::max(64, ((work + 31) / 32) * 32));
                         if (threads_override > 0) G->threads = threads_override;
                         G->chunk = std::max<long long>(1, (1LL << 28) / std::max<long long>(1, maxn));
                         if (chunk_override > 0) G->chunk = chunk_override;
+                        // candidate configurations for the autotuner
+                        bool all_cl = g == MCS_GEOM_SQUARE && d > 1;
+                        int Lx = 0;
+                        for (int id : set) {
+                            all_cl &= replicas[id]->hm.cluster_ok != 0;
+                            if (Lx == 0) Lx = replicas[id]->hm.Lx;
+                            all_cl &= replicas[id]->hm.Lx == Lx;
+                        }
+                        if (kind == 2) G->candidates.push_back({1, G->threads});
+                        if (all_cl && cluster_override != 1) {
+                            for (int C : {2, 4, 8}) {
+                                if (cluster_override > 1 && C != cluster_override) continue;
+                                if (Lx % C || (Lx / C) % 2 || Lx / C < 2) continue;
+                                size_t sm = 0;
+                                for (int id : set) sm = std::max<size_t>(sm, (size_t)cluster_smem_bytes(replicas[id]->rep, C));
+                                if ((int)sm > max_smem) continue;
+                                for (int th : {512, 1024}) G->candidates.push_back({C, th});
+                            }
+                            G->can_cluster = 1;
+                        }
+                        if (G->candidates.empty()) G->candidates.push_back({1, G->threads});
+                        if (G->candidates.size() == 1 || no_autotune) {
+                            G->C = G->candidates[0].first;
+                            G->threads = G->candidates[0].second;
+                            if (no_autotune && G->can_cluster && kind == 6) {
+                                G->C = G->candidates[0].first; G->threads = G->candidates[0].second;
+                            }
+                            G->tuned = 1;
+                        }
                     } else {
                         int rc = setup_tiled(*G);
                         if (rc != MCS_OK) return rc;
@@ -536,11 +583,36 @@ int Batch::advance(long long units)
                 if (e != cudaSuccess) { set_error(std::string("wolff launch: ") + cudaGetErrorString(e)); return MCS_ECUDA; }
                 launches++;
             }
-        } else if (G.kind == 2) {
-            for (long long u = 0; u < todo; u += G.chunk) {
+        } else if (G.kind == 2 || G.kind == 6) {
+            long long u = 0;
+            // autotuner: time each candidate (cluster size, block size) on a
+            // few real units and keep the fastest
+            if (!G.tuned) {
+                const long long probe = std::max<long long>(1, std::min<long long>(4, todo / (2 * (long long)G.candidates.size() + 1)));
+                G.cand_ms.assign(G.candidates.size(), 1e30);
+                for (size_t ci = 0; ci < G.candidates.size() && u + probe <= todo; ++ci) {
+                    int C = G.candidates[ci].first, th = G.candidates[ci].second;
+                    CUDA_TRY(cudaEventRecord(ev_a, stream));
+                    cudaError_t e = launch_group(G, C, th, probe, stream);
+                    if (e != cudaSuccess) { cudaGetLastError(); continue; }
+                    CUDA_TRY(cudaEventRecord(ev_b, stream));
+                    CUDA_TRY(cudaEventSynchronize(ev_b));
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, ev_a, ev_b);
+                    G.cand_ms[ci] = ms / probe;
+                    launches++;
+                    u += probe;
+                }
+                size_t best = 0;
+                for (size_t ci = 1; ci < G.candidates.size(); ++ci) if (G.cand_ms[ci] < G.cand_ms[best]) best = ci;
+                G.C = G.candidates[best].first;
+                G.threads = G.candidates[best].second;
+                G.tuned = 1;
+            }
+            for (; u < todo; u += G.chunk) {
                 long long n = std::min(G.chunk, todo - u);
-                cudaError_t e = launch_resident_metro(G.dim, G.geom, d_reps, G.d_ids, (int)G.ids.size(), G.threads, G.smem, n, stream);
-                if (e != cudaSuccess) { set_error(std::string("resident launch: ") + cudaGetErrorString(e)); return MCS_ECUDA; }
+                cudaError_t e = launch_group(G, G.C, G.threads, n, stream);
+                if (e != cudaSuccess) { set_error(std::string("resident/cluster launch: ") + cudaGetErrorString(e)); return MCS_ECUDA; }
                 launches++;
             }
         } else if (G.kind == 3 && todo >= 8) {

@@ -23,7 +23,7 @@ struct Replica {
     size_t bytes = 0;
     size_t acc_off = 0, icnt_off = 0, stats_off = 0, series_off = 0, frames_off = 0, spins_off = 0;
     size_t nacc = 0;
-    int schedule = 0;        // 1 plain, 2 resident, 3 tiled
+    int schedule = 0;        // 1 plain, 2 resident, 3 tiled, 4/5 Wolff, 6 cluster
     int requested_schedule = 0;
     int record_series = 0;
     int recheck = 32;
@@ -44,10 +44,15 @@ struct Group {
     std::vector<int> ids;
     int *d_ids = nullptr;
     long long max_units = 0, done_units = 0;
-    // resident
+    // resident / cluster
     int threads = 0;
     size_t smem = 0;
     long long chunk = 0;
+    int C = 1;                 // cluster size (1 = resident kernel)
+    int tuned = 0;             // autotuner has chosen (C, threads)
+    int can_cluster = 0;
+    std::vector<std::pair<int, int>> candidates;  // (C, threads)
+    std::vector<double> cand_ms;
     // tiled
     int maxcol = 0, nmeas = 0;
     std::vector<size_t> cofs;
@@ -75,7 +80,9 @@ struct Batch {
     std::vector<std::unique_ptr<Group>> groups;
     double last_ms = 0;
     cudaStream_t stream = nullptr, stream2 = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_a = nullptr, ev_b = nullptr;
+    int cluster_override = 0;   // 1: never cluster; 2/4/8: only that size
+    int no_autotune = 0;
     double device_ms = 0;
     long long site_updates = 0;
     long long launches = 0;
@@ -93,6 +100,7 @@ struct Batch {
     int result(int i, mcs_result *res);
     int setup_tiled(Group &G);
     cudaError_t tiled_unit(Group &G, cudaStream_t s, long long *nl);
+    cudaError_t launch_group(Group &G, int C, int threads, long long units, cudaStream_t s);
 };
 
 }  // namespace mcs

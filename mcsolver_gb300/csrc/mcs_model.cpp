@@ -494,6 +494,37 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
     m->sval.resize(N);
     for (int k = 0; k < N; ++k) { m->slen[k] = (float)fabs(p->init_spin[sites[k]]); m->sval[k] = (float)p->init_spin[sites[k]]; }
 
+    // ---------------------------------------------------------------- cluster schedule eligibility
+    // square lattice, pairs (v, v), chosen sites = even rows x even columns in
+    // site order with the four-site block (x,y),(x,y+1),(x+1,y),(x+1,y+1),
+    // circuits listed cell by cell inside rows x and x+1, one site class.
+    m->cluster_ok = 0;
+    if (m->geom == MCS_GEOM_SQUARE && dim > 1 && m->pair_identity && m->ndc == 1 && m->ncl == 4) {
+        const int Lx = m->Lx, Ly = m->Ly;
+        bool ok = p->n_rorb == (Lx / 2) * (Ly / 2);
+        for (int r = 0; r < p->n_rorb && ok; ++r) {
+            int x = 2 * (r / (Ly / 2)), y = 2 * (r % (Ly / 2));
+            if (p->r_orb[r] != x * Ly + y) { ok = false; break; }
+            int want[4] = {x * Ly + y, x * Ly + (y + 1) % Ly, ((x + 1) % Lx) * Ly + y, ((x + 1) % Lx) * Ly + (y + 1) % Ly};
+            for (int k = 0; k < 4; ++k)
+                if (p->r_cluster[(size_t)r * 4 + k] != want[k]) { ok = false; break; }
+        }
+        if (ok && m->ncirc > 0) {
+            ok = (m->ncirc % N) == 0;
+            int per = ok ? m->ncirc / N : 0;
+            for (int ci = 0; ci < m->ncirc && ok; ++ci) {
+                int cell = ci / per, x = cell / Ly;
+                for (int k = 0; k < 3; ++k) {
+                    int xs = p->circuits[3 * ci + k] / Ly;
+                    if (xs != x && xs != (x + 1) % Lx) { ok = false; break; }
+                }
+            }
+            for (int k = 0; k < N && ok; ++k) ok = m->slen[k] == m->slen[0] && m->slen[0] > 0;
+        }
+        for (int g = 4; g < m->ngroup && ok; ++g) ok = (m->gall >> g) & 1;
+        m->cluster_ok = ok ? 1 : 0;
+    }
+
     // ---------------------------------------------------------------- program
     if (p->algorithm == 0) {
         m->upm = (int)std::min<long long>((p->ninterval + N - 1) / N, 1 << 30);

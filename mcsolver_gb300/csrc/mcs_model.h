@@ -55,6 +55,7 @@ struct HostModel {
     std::vector<int> rtgt;
     int pair_identity = 0;
     int gall = 0;
+    int cluster_ok = 0;     // the row-split cluster schedule can run this replica
     int nlat = 0, n_rorb = 0, ncl = 0, ncirc = 0, ngroup = 0;
     int ci = 0, cj = 0, cij = 0;
     // program
