@@ -746,7 +746,7 @@ __device__ void is_frame(const Rep &R, const IsEntry *itab, const signed char *s
 }
 
 // Fold one Ising measurement (one thread).  isingLib.c:388-431.
-__device__ void is_accumulate(Rep &R, const double *Fd, const long long *Fi, int last_sign, long long m)
+__device__ inline void is_accumulate(Rep &R, const double *Fd, const long long *Fi, int last_sign, long long m)
 {
     double *acc = R.acc;
     long long *ic = R.icnt;
