@@ -261,7 +261,12 @@ __global__ void __launch_bounds__(1024) k_cluster_metro(Rep *reps, const int *id
         }
         block_sum_f<CL_NV>(a, red, red + 32 * CL_NV);
         if (tid < CL_NV) part[tid] = red[32 * CL_NV + tid];
-        if (tid == 0) { part[CL_NV] = dEd; part[CL_NV + 1] = (double)nacc; }
+        __syncthreads();
+        {
+            double de[2] = {dEd, (double)nacc};
+            block_sum<2>(de, red, red + 64);
+            if (tid == 0) { part[CL_NV] = red[64]; part[CL_NV + 1] = red[65]; }
+        }
         dEd = 0.0;
         nacc = 0;
         __syncthreads();
@@ -360,7 +365,11 @@ __global__ void __launch_bounds__(1024) k_cluster_metro(Rep *reps, const int *id
         if (measures_after(R, u)) measure(R.m, (R.m % R.recheck) == 0);
     }
     // fold the energy change since the last measurement
-    if (tid == 0) { part[CL_NV] = dEd; part[CL_NV + 1] = (double)nacc; }
+    {
+        double de[2] = {dEd, (double)nacc};
+        block_sum<2>(de, red, red + 64);
+        if (tid == 0) { part[CL_NV] = red[64]; part[CL_NV + 1] = red[65]; }
+    }
     __syncthreads();
     cl.sync();
     if (rank == 0 && tid == 0) {
