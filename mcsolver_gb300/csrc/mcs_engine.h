@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -81,6 +82,7 @@ struct Batch {
     double last_ms = 0;
     cudaStream_t stream = nullptr, stream2 = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_a = nullptr, ev_b = nullptr;
+    std::mutex add_mutex;       // mcs_batch_add may be called from several threads
     int cluster_override = 0;   // 1: never cluster; 2/4/8: only that size
     int no_autotune = 0;
     double device_ms = 0;

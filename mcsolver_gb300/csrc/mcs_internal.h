@@ -128,6 +128,7 @@ struct Rep {
     int ts_wolff_last;                           // Ising Wolff: totSpin excludes the last site
     int last_site;                               // sweep index of original site N-1
     int offset_energy;                           // Ising Metropolis offset semantics
+    int rinit;                                   // draw the initial state from Philox (a, 0, 0, 0x5000)
     // ---- state
     void *spins;                                 // Ising int8[N]; O(n) float[dim][spad] (or double)
     int spad;

@@ -487,6 +487,22 @@ __global__ void __launch_bounds__(1024) k_init(Rep *reps, const int *ids)
     if (R.dim != (DIM == 1 ? 1 : DIM) || R.geom != GEOM) return;
     Spins S = spins_global(R);
     const int vmax = max(max(R.N, R.nlat), max(R.n_rorb, R.ncirc));
+    if (R.rinit) {
+        // random initial state keyed by the sweep index: Ising sign, XY angle, Heisenberg sphere
+        for (int v = threadIdx.x; v < R.N; v += blockDim.x) {
+            const uint4 w = philox((uint32_t)v, 0u, 0u, 0x5000u, R.seed);
+            if (DIM == 1) {
+                S.s[v] = (w.x & 1) ? 1 : -1;
+            } else {
+                float r0, r1, r2;
+                on_direction<DIM>(w, r0, r1, r2);
+                const float a = R.slen[v];
+                S.x[v] = r0 * a; S.y[v] = r1 * a;
+                if (DIM == 3) S.z[v] = r2 * a;
+            }
+        }
+        __syncthreads();
+    }
     if (DIM == 1) {
         is_frame<GEOM>(R, R.itab, S.s, 0, vmax, 0, red, F, redl, Fi);
         if (threadIdx.x == 0) {

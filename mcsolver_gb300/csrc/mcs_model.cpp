@@ -17,11 +17,45 @@
 #include <string.h>
 
 #include <algorithm>
+#include <array>
 #include <map>
 #include <set>
+#include <string>
+#include <unordered_map>
 #include <utility>
 
 namespace mcs {
+
+// De-duplication of K-double keys (bitwise equality).  Most lattices repeat a
+// handful of values in long runs, so the previous hit and a short linear scan
+// answer almost every lookup; a hash map covers the rest.
+template <int K>
+struct ClassTable {
+    std::vector<std::array<double, K>> keys;
+    std::unordered_map<std::string, int> map;
+    int last = -1;
+    int find_or_add(const double *v)
+    {
+        if (last >= 0 && memcmp(keys[last].data(), v, sizeof(double) * K) == 0) return last;
+        if (keys.size() <= 16) {
+            for (size_t c = 0; c < keys.size(); ++c)
+                if (memcmp(keys[c].data(), v, sizeof(double) * K) == 0) return last = (int)c;
+        } else {
+            auto it = map.find(std::string((const char *)v, sizeof(double) * K));
+            if (it != map.end()) return last = it->second;
+        }
+        std::array<double, K> a;
+        memcpy(a.data(), v, sizeof(double) * K);
+        keys.push_back(a);
+        int c = (int)keys.size() - 1;
+        if (keys.size() == 17)
+            for (size_t q = 0; q < keys.size(); ++q)
+                map[std::string((const char *)keys[q].data(), sizeof(double) * K)] = (int)q;
+        else if (keys.size() > 17)
+            map[std::string((const char *)v, sizeof(double) * K)] = c;
+        return last = c;
+    }
+};
 
 void philox_host(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, unsigned long long seed, uint32_t out[4])
 {
@@ -165,23 +199,21 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
     std::vector<int> linkcls((size_t)N * std::max(z, 1), 0);
     if (dim > 1) {
         const bool ign = p->ignore_offdiag > 0;
-        std::map<std::vector<double>, int> cls;
-        std::vector<std::vector<double>> tab;
+        ClassTable<9> cls;
         bool anyoff = false;
         for (int i = 0; i < N; ++i)
             for (int l = 0; l < p->nlink[i]; ++l) {
                 const double *J = p->link_strength + ((size_t)i * z + l) * 9;
-                std::vector<double> v(J, J + 9);
+                double v[9];
+                memcpy(v, J, sizeof v);
                 if (ign) v[3] = v[4] = v[5] = v[6] = v[7] = v[8] = 0.0;
                 if (dim == 2) v[2] = v[4] = v[5] = v[7] = v[8] = 0.0;  // XY reads xx,yy,xy,yx (xyLib.c:150-153)
                 for (int k = 3; k < 9; ++k) anyoff |= v[k] != 0.0;
-                auto it = cls.find(v);
-                int c;
-                if (it == cls.end()) { c = (int)tab.size(); cls[v] = c; tab.push_back(v); }
-                else c = it->second;
-                linkcls[(size_t)i * z + l] = c;
+                linkcls[(size_t)i * z + l] = cls.find_or_add(v);
             }
-        if (tab.size() > 65535) FAIL(MCS_EUNSUPPORTED, "too many distinct exchange matrices");
+        if (cls.keys.size() > 65535) FAIL(MCS_EUNSUPPORTED, "too many distinct exchange matrices");
+        std::vector<std::vector<double>> tab;
+        for (auto &k : cls.keys) tab.push_back(std::vector<double>(k.begin(), k.end()));
         if (tab.empty()) tab.push_back(std::vector<double>(9, 0.0));
         m->njc = (int)tab.size();
         m->fullJ = anyoff ? 1 : 0;
@@ -190,23 +222,21 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
         for (size_t c = 0; c < tab.size(); ++c)
             for (int k = 0; k < 9; ++k) { m->jtab[9 * c + k] = (float)tab[c][k]; m->jtab64[9 * c + k] = tab[c][k]; }
         // site classes: anisotropy vector and spin length |S|
-        std::map<std::vector<double>, int> dcls;
-        std::vector<std::vector<double>> dt;
+        ClassTable<4> dcls;
         m->stype.assign(N, 0);
         bool anyd = false;
         for (int k = 0; k < N; ++k) {
             int i = sites[k];
-            std::vector<double> v(p->init_d + 3 * (size_t)i, p->init_d + 3 * (size_t)i + 3);
+            double v[4] = {p->init_d[3 * (size_t)i], p->init_d[3 * (size_t)i + 1], p->init_d[3 * (size_t)i + 2],
+                           fabs(p->init_spin[i])};
             if (dim == 2) v[2] = 0.0;
-            for (double x : v) anyd |= x != 0.0;
-            v.push_back(fabs(p->init_spin[i]));
-            auto it = dcls.find(v);
-            int c;
-            if (it == dcls.end()) { c = (int)dt.size(); dcls[v] = c; dt.push_back(v); }
-            else c = it->second;
+            anyd |= v[0] != 0.0 || v[1] != 0.0 || v[2] != 0.0;
+            int c = dcls.find_or_add(v);
             if (c > 255) FAIL(MCS_EUNSUPPORTED, "more than 256 distinct (anisotropy, spin length) site classes");
             m->stype[k] = (uint8_t)c;
         }
+        std::vector<std::vector<double>> dt;
+        for (auto &k : dcls.keys) dt.push_back(std::vector<double>(k.begin(), k.end()));
         m->ndc = (int)dt.size();
         m->has_d = anyd ? 1 : 0;
         m->dtab.resize(4 * dt.size());
@@ -214,18 +244,16 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
             for (int k = 0; k < 4; ++k) m->dtab[4 * c + k] = (float)dt[c][k];
     } else {
         // Ising: classes of Q = K |s_i| |s_j|, site types (|s_i|, class counts)
-        std::map<double, int> qcls;
-        std::vector<double> qv;
+        ClassTable<1> qcls;
         for (int i = 0; i < N; ++i)
             for (int l = 0; l < p->nlink[i]; ++l) {
                 int j = p->linked_orb[(size_t)i * z + l];
                 double q = p->link_strength[(size_t)i * z + l] * fabs(p->init_spin[i]) * fabs(p->init_spin[j]);
-                auto it = qcls.find(q);
-                int c;
-                if (it == qcls.end()) { c = (int)qv.size(); qcls[q] = c; qv.push_back(q); }
-                else c = it->second;
-                linkcls[(size_t)i * z + l] = c;
+                linkcls[(size_t)i * z + l] = qcls.find_or_add(&q);
+                if (qcls.keys.size() > MCS_MAXC) break;
             }
+        std::vector<double> qv;
+        for (auto &k : qcls.keys) qv.push_back(k[0]);
         if (qv.size() > MCS_MAXC) FAIL(MCS_EUNSUPPORTED, "Ising model with more than 4 distinct coupling values");
         if (qv.empty()) qv.push_back(0.0);
         m->nclass = (int)qv.size();
@@ -389,16 +417,17 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
                 m->lcls[(size_t)l * N + k] = (uint8_t)c;
             }
         }
-    } else {
+    } else if (m->geom != MCS_GEOM_SQUARE) {
         m->lcode.assign((size_t)std::max(z, 1) * N, 0);
         for (int k = 0; k < N; ++k) {
             int i = sites[k];
             for (int l = 0; l < p->nlink[i]; ++l) m->lcode[(size_t)l * N + k] = (uint16_t)linkcls[(size_t)i * z + l];
         }
     }
-    m->nbr.assign((size_t)std::max(z, 1) * N, 0);
-    m->deg.assign(N, 0);
-    for (int k = 0; k < N; ++k) {
+    if (m->geom == MCS_GEOM_SQUARE && dim > 1) m->lcode.clear();  // neighbours and classes are arithmetic
+    m->nbr.assign(m->geom == MCS_GEOM_SQUARE ? 0 : (size_t)std::max(z, 1) * N, 0);
+    m->deg.assign(m->geom == MCS_GEOM_SQUARE ? 0 : N, 0);
+    for (int k = 0; k < N && m->geom != MCS_GEOM_SQUARE; ++k) {
         int i = sites[k];
         m->deg[k] = (uint8_t)p->nlink[i];
         for (int l = 0; l < p->nlink[i]; ++l) m->nbr[(size_t)l * N + k] = pos[p->linked_orb[(size_t)i * z + l]];
@@ -542,17 +571,13 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
     m->offset_energy = (o && o->absolute_energy) ? 0 : 1;
 
     // ---------------------------------------------------------------- initial state
+    m->device_random_init = rnd ? 1 : 0;  // drawn on the device by the initial-state kernel
     if (dim == 1) {
         m->init_sigma.resize(N);
         double M0 = 0, first = 0;
         for (int k = 0; k < N; ++k) {
             int i = sites[k];
             int8_t sg = p->init_spin[i] < 0 ? -1 : 1;
-            if (rnd) {
-                uint32_t w[4];
-                philox_host((uint32_t)k, 0, 0, 0x5000u, m->seed, w);
-                sg = (w[0] & 1) ? 1 : -1;
-            }
             m->init_sigma[k] = sg;
             M0 += fabs(p->init_spin[i]) * sg;
         }
@@ -573,16 +598,15 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
         }
     } else {
         m->init_vec.assign((size_t)3 * N, 0.f);
-        m->init_vec64.assign((size_t)3 * N, 0.0);
         for (int k = 0; k < N; ++k) {
             int i = sites[k];
             double S0 = p->init_spin[i];
             double v[3] = {S0, 0, 0}, d[3];
             uint32_t w[4];
-            if (rnd) {
-                philox_host((uint32_t)k, 0, 0, 0x5000u, m->seed, w);
-                eng_dir(dim, w[0], w[1], d);
-                v[0] = d[0]; v[1] = d[1]; v[2] = d[2];
+            if (rnd || p->flunc == 0.0) {
+                // (S,0,0) normalised and scaled back is (S,0,0); random states are drawn on the device
+                m->init_vec[k] = (float)S0;
+                continue;
             } else {
                 philox_host((uint32_t)k, 0, 0, 0x4000u, m->seed, w);
                 eng_dir(dim, w[0], w[1], d);
@@ -594,7 +618,6 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
             double a = fabs(S0);
             for (int c = 0; c < 3; ++c) {
                 double x = (c < dim) ? v[c] * a : 0.0;
-                m->init_vec64[(size_t)c * N + k] = x;
                 m->init_vec[(size_t)c * N + k] = (float)x;
             }
         }

@@ -68,7 +68,7 @@ struct HostModel {
     // initial state (sweep order)
     std::vector<int8_t> init_sigma;      // Ising
     std::vector<float> init_vec;         // O(n) [dim][N]
-    std::vector<double> init_vec64;
+    int device_random_init = 0;          // draw the initial state on the device
     unsigned long long seed = 0;
 };
 
