@@ -174,6 +174,30 @@ int mcs_server_poll(mcs_server *s, uint64_t ticket, mcs_result *result);
 int mcs_server_stats(mcs_server *s, int32_t *active, int32_t *queued, uint64_t *bytes_in_use, int64_t *site_updates);
 void mcs_server_destroy(mcs_server *s);
 
+/* ---- allocation-free sweeps ------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc --
+ * a framework that owns all device memory through its own allocator, a process
+ * that reserved the GPU's memory up front, code inside another library's
+ * allocation scope -- this entry point allocates nothing (no device, no pinned
+ * host memory).  The caller passes device pointers:
+ *   d_sigma  [Lx*Ly] int8 spins +-1 of a periodic square lattice, site order
+ *            x*Ly + y, updated in place;
+ *   d_sums   [nsweeps][2] int64, written after each sweep: the sum of the
+ *            spins and the sum of s_i*s_j over the 2*Lx*Ly bonds.
+ * K = J/T and h = H/T follow the reference's sign convention (K < 0 is a
+ * ferromagnet; the acceptance rule is isingLib.c:242-252).  The sweeps are the
+ * Ising Metropolis sweeps of mcs_solve(): same colour order, same Philox words
+ * (sweep index sweep0 + k), same integer thresholds, so the spins equal those
+ * mcs_solve() produces for the same lattice, couplings and seed.
+ * Scratch: a fixed 64 KiB array in device memory owned by the library (held by
+ * every GPU that loads it until exit), which limits the lattice to 8,388,608
+ * sites (larger lattices are rejected with MCS_EINVAL).  The first call on a
+ * device looks up that array's address; make it before any stream capture.
+ * Calls that overlap on the GPU share the array and race: issue them on one
+ * stream, one after the other.  Lx, Ly even and >= 4. */
+int mcs_ising_square_noalloc(int8_t *d_sigma, int32_t Lx, int32_t Ly, double K, double h, uint64_t seed,
+                             int64_t sweep0, int32_t nsweeps, int64_t *d_sums, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -87,7 +87,7 @@ ABI_FUNCTIONS = [
     "mcs_batch_result", "mcs_batch_stats", "mcs_batch_memory", "mcs_batch_destroy",
     "mcs_pt_create", "mcs_pt_run", "mcs_pt_result", "mcs_pt_stats", "mcs_pt_destroy",
     "mcs_server_create", "mcs_server_submit", "mcs_server_step", "mcs_server_poll", "mcs_server_stats",
-    "mcs_server_destroy",
+    "mcs_server_destroy", "mcs_ising_square_noalloc",
 ]
 
 
@@ -112,6 +112,10 @@ def lib():
         L.mcs_batch_memory.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
         L.mcs_batch_destroy.argtypes = [ctypes.c_void_p]
         L.mcs_batch_destroy.restype = None
+        L.mcs_ising_square_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                               ctypes.c_double, ctypes.c_uint64, ctypes.c_int64, ctypes.c_int32,
+                                               ctypes.c_void_p, ctypes.c_void_p]
+        L.mcs_ising_square_noalloc.restype = ctypes.c_int
         _lib = L
     return _lib
 
