@@ -112,6 +112,13 @@ def lib():
         L.mcs_batch_memory.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
         L.mcs_batch_destroy.argtypes = [ctypes.c_void_p]
         L.mcs_batch_destroy.restype = None
+        L.mcs_pt_create.argtypes = [ctypes.POINTER(McsProblem), ctypes.POINTER(McsOptions), _f64p, ctypes.c_int32,
+                                     ctypes.POINTER(ctypes.c_void_p)]
+        L.mcs_pt_run.argtypes = [ctypes.c_void_p]
+        L.mcs_pt_result.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(McsResult)]
+        L.mcs_pt_stats.argtypes = [ctypes.c_void_p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int64)]
+        L.mcs_pt_destroy.argtypes = [ctypes.c_void_p]
+        L.mcs_pt_destroy.restype = None
         L.mcs_ising_square_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                                ctypes.c_double, ctypes.c_uint64, ctypes.c_int64, ctypes.c_int32,
                                                ctypes.c_void_p, ctypes.c_void_p]
@@ -315,6 +322,50 @@ class Batch:
     def close(self):
         if self._h:
             lib().mcs_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ParallelTempering:
+    """Replica exchange over a ladder of inverse temperatures.
+
+    ``args`` is an MCMainFunction tuple whose couplings, anisotropy and field
+    are PHYSICAL (build it at T = 1); ``betas[k]`` = 1/T_k.  Energies in the
+    results are physical too."""
+
+    def __init__(self, model: str, args, betas, seed: int = 1, device: int = 0, record_series: bool = False):
+        self.P = args if isinstance(args, Problem) else Problem(model, args)
+        self.nt = len(betas)
+        self._betas = np.ascontiguousarray(betas, dtype=np.float64)
+        self._series = record_series
+        o = make_options(seed=seed, device=device, record_series=record_series)
+        self._h = ctypes.c_void_p()
+        _check(lib().mcs_pt_create(ctypes.byref(self.P.struct), ctypes.byref(o),
+                                   self._betas.ctypes.data_as(_f64p), self.nt, ctypes.byref(self._h)))
+
+    def run(self):
+        _check(lib().mcs_pt_run(self._h))
+
+    def result(self, k: int):
+        rb = _ResultBuf(self.P, self._series)
+        _check(lib().mcs_pt_result(self._h, k, ctypes.byref(rb.r)))
+        return rb.unpack(self.P)
+
+    def stats(self):
+        acc = np.zeros(max(1, self.nt - 1))
+        ms = ctypes.c_double()
+        su = ctypes.c_int64()
+        _check(lib().mcs_pt_stats(self._h, acc.ctypes.data_as(_f64p), ctypes.byref(ms), ctypes.byref(su)))
+        return {"swap_acceptance": acc, "device_ms": ms.value, "site_updates": su.value}
+
+    def close(self):
+        if self._h:
+            lib().mcs_pt_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

@@ -799,3 +799,133 @@ int mcs_batch_memory(mcs_batch *b, uint64_t *device_bytes, uint64_t *readback_by
 void mcs_batch_destroy(mcs_batch *b) { delete b; }
 
 }  // extern "C"
+
+// ====================================================================== parallel tempering
+struct mcs_pt {
+    mcs::Batch b;
+    int nt = 0;
+    std::vector<double> betas;
+    int *d_perm = nullptr;
+    long long *d_acc = nullptr, *d_att = nullptr;
+    unsigned long long seed = 0;
+    double ms = 0;
+    bool ran = false;
+    ~mcs_pt()
+    {
+        if (d_perm) cudaFree(d_perm);
+        if (d_acc) cudaFree(d_acc);
+        if (d_att) cudaFree(d_att);
+    }
+};
+
+extern "C" int mcs_pt_create(const mcs_problem *problem, const mcs_options *options, const double *betas,
+                             int32_t n_temps, mcs_pt **out)
+{
+    if (!problem || !betas || !out || n_temps < 2) { set_error("parallel tempering needs a problem and >= 2 temperatures"); return MCS_EINVAL; }
+    if (problem->model == MCS_ISING) { set_error("parallel tempering is built for the XY and Heisenberg models"); return MCS_EUNSUPPORTED; }
+    if (problem->algorithm != MCS_METROPOLIS) { set_error("parallel tempering runs Metropolis sweeps"); return MCS_EUNSUPPORTED; }
+    for (int k = 0; k < n_temps; ++k)
+        if (!(betas[k] > 0)) { set_error("betas must be positive"); return MCS_EINVAL; }
+    mcs_options def;
+    memset(&def, 0, sizeof def);
+    if (!options) options = &def;
+    std::unique_ptr<mcs_pt> pt(new mcs_pt());
+    int rc = pt->b.init(options->device);
+    if (rc != MCS_OK) return rc;
+    pt->nt = n_temps;
+    pt->seed = options->seed;
+    for (int k = 0; k < n_temps; ++k) {
+        mcs_options o = *options;
+        o.seed = options->seed + 0x9E3779B97F4A7C15ULL * (unsigned long long)(k + 1);
+        if (o.schedule == 0) o.schedule = 2;
+        int idx = 0;
+        rc = pt->b.add(problem, &o, &idx);
+        if (rc != MCS_OK) return rc;
+        pt->b.replicas[idx]->rep.beta = (float)betas[k];
+        pt->betas.push_back(betas[k]);
+    }
+    if (pt->b.replicas[0]->hm.upm != 1) { set_error("parallel tempering measures after every sweep (ninterval = N)"); return MCS_EINVAL; }
+    *out = pt.release();
+    return MCS_OK;
+}
+
+extern "C" int mcs_pt_run(mcs_pt *pt)
+{
+    if (!pt) return MCS_EINVAL;
+    Batch &b = pt->b;
+    int rc = b.prepare();
+    if (rc != MCS_OK) return rc;
+    if (b.groups.size() != 1) { set_error("parallel tempering replicas must form one kernel group"); return MCS_EINVAL; }
+    Group &G = *b.groups[0];
+    int C = 1, threads = G.threads;
+    if (G.kind == 6 && !G.candidates.empty()) { C = G.candidates[0].first; threads = G.candidates[0].second; }
+    const int nt = pt->nt;
+    CUDA_TRY(cudaMalloc(&pt->d_perm, nt * sizeof(int)));
+    CUDA_TRY(cudaMalloc(&pt->d_acc, nt * sizeof(long long)));
+    CUDA_TRY(cudaMalloc(&pt->d_att, nt * sizeof(long long)));
+    std::vector<int> perm(nt);
+    for (int k = 0; k < nt; ++k) perm[k] = k;
+    CUDA_TRY(cudaMemcpy(pt->d_perm, perm.data(), nt * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemset(pt->d_acc, 0, nt * sizeof(long long)));
+    CUDA_TRY(cudaMemset(pt->d_att, 0, nt * sizeof(long long)));
+    const long long total = G.max_units;
+    auto sweep = [&](cudaStream_t s) -> cudaError_t {
+        cudaError_t e = b.launch_group(G, C, threads, 1, s);
+        if (e != cudaSuccess) return e;
+        return launch_pt_exchange(b.d_reps, nt, pt->d_perm, pt->seed ^ 0x5054ULL, pt->d_acc, pt->d_att, s);
+    };
+    CUDA_TRY(cudaEventRecord(b.ev0, b.stream));
+    const int K = 32;
+    long long u = 0;
+    if (total >= 2 * K) {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        CUDA_TRY(cudaStreamBeginCapture(b.stream2, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < K && e == cudaSuccess; ++k) e = sweep(b.stream2);
+        cudaError_t e2 = cudaStreamEndCapture(b.stream2, &graph);
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            set_error(std::string("parallel tempering capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+            return MCS_ECUDA;
+        }
+        CUDA_TRY(cudaGraphInstantiate(&exec, graph, 0));
+        for (; u + K <= total; u += K) CUDA_TRY(cudaGraphLaunch(exec, b.stream));
+        cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(graph);
+    }
+    for (; u < total; ++u) CUDA_TRY(sweep(b.stream));
+    CUDA_TRY(cudaEventRecord(b.ev1, b.stream));
+    CUDA_TRY(cudaStreamSynchronize(b.stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, b.ev0, b.ev1);
+    pt->ms = ms;
+    b.device_ms = ms;
+    G.done_units = total;
+    rc = b.collect();
+    pt->ran = rc == MCS_OK;
+    return rc;
+}
+
+extern "C" int mcs_pt_result(mcs_pt *pt, int32_t k, mcs_result *result)
+{
+    if (!pt || !pt->ran) { set_error("parallel tempering has not been run"); return MCS_EINVAL; }
+    if (k < 0 || k >= pt->nt) { set_error("temperature index out of range"); return MCS_EINVAL; }
+    // the accumulators of temperature k live in the arena allocated for replica k
+    return pt->b.result(k, result);
+}
+
+extern "C" int mcs_pt_stats(mcs_pt *pt, double *swap_acceptance, double *device_ms, int64_t *site_updates)
+{
+    if (!pt || !pt->ran) { set_error("parallel tempering has not been run"); return MCS_EINVAL; }
+    std::vector<long long> a(pt->nt), t(pt->nt);
+    CUDA_TRY(cudaMemcpy(a.data(), pt->d_acc, pt->nt * sizeof(long long), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(t.data(), pt->d_att, pt->nt * sizeof(long long), cudaMemcpyDeviceToHost));
+    if (swap_acceptance)
+        for (int k = 0; k + 1 < pt->nt; ++k) swap_acceptance[k] = t[k] ? (double)a[k] / (double)t[k] : 0.0;
+    if (device_ms) *device_ms = pt->ms;
+    if (site_updates) *site_updates = pt->b.site_updates;
+    return MCS_OK;
+}
+
+extern "C" void mcs_pt_destroy(mcs_pt *pt) { delete pt; }

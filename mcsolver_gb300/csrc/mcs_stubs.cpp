@@ -5,18 +5,12 @@
 #include "mcs_engine.h"
 
 extern "C" {
-struct mcs_pt { int unused; };
 struct mcs_server { int unused; };
 static int unsupported(const char *what)
 {
     mcs::set_error(std::string(what) + " is not built in this engine version");
     return MCS_EUNSUPPORTED;
 }
-int mcs_pt_create(const mcs_problem *, const mcs_options *, const double *, int32_t, mcs_pt **) { return unsupported("parallel tempering"); }
-int mcs_pt_run(mcs_pt *) { return unsupported("parallel tempering"); }
-int mcs_pt_result(mcs_pt *, int32_t, mcs_result *) { return unsupported("parallel tempering"); }
-int mcs_pt_stats(mcs_pt *, double *, double *, int64_t *) { return unsupported("parallel tempering"); }
-void mcs_pt_destroy(mcs_pt *) {}
 int mcs_server_create(int32_t, uint64_t, int32_t, mcs_server **) { return unsupported("server"); }
 int mcs_server_submit(mcs_server *, const mcs_problem *, const mcs_options *, uint64_t *) { return unsupported("server"); }
 int mcs_server_step(mcs_server *, int32_t *) { return unsupported("server"); }
