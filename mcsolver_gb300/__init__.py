@@ -119,6 +119,15 @@ def lib():
         L.mcs_pt_stats.argtypes = [ctypes.c_void_p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int64)]
         L.mcs_pt_destroy.argtypes = [ctypes.c_void_p]
         L.mcs_pt_destroy.restype = None
+        L.mcs_server_create.argtypes = [ctypes.c_int32, ctypes.c_uint64, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]
+        L.mcs_server_submit.argtypes = [ctypes.c_void_p, ctypes.POINTER(McsProblem), ctypes.POINTER(McsOptions),
+                                        ctypes.POINTER(ctypes.c_uint64)]
+        L.mcs_server_step.argtypes = [ctypes.c_void_p, _i32p]
+        L.mcs_server_poll.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(McsResult)]
+        L.mcs_server_stats.argtypes = [ctypes.c_void_p, _i32p, _i32p, ctypes.POINTER(ctypes.c_uint64),
+                                       ctypes.POINTER(ctypes.c_int64)]
+        L.mcs_server_destroy.argtypes = [ctypes.c_void_p]
+        L.mcs_server_destroy.restype = None
         L.mcs_ising_square_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                                ctypes.c_double, ctypes.c_uint64, ctypes.c_int64, ctypes.c_int32,
                                                ctypes.c_void_p, ctypes.c_void_p]
@@ -366,6 +375,61 @@ class ParallelTempering:
     def close(self):
         if self._h:
             lib().mcs_pt_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching request loop: submit solves as they arrive, call
+    step() to let the device work, poll() for finished results."""
+
+    def __init__(self, hbm_budget_bytes: int = 8 << 30, max_slots: int = 512, device: int = 0):
+        self._h = ctypes.c_void_p()
+        _check(lib().mcs_server_create(device, int(hbm_budget_bytes), int(max_slots), ctypes.byref(self._h)))
+        self._problems = {}
+
+    def submit(self, model: str, args, **opt) -> int:
+        P = args if isinstance(args, Problem) else Problem(model, args)
+        o = make_options(**opt)
+        t = ctypes.c_uint64()
+        _check(lib().mcs_server_submit(self._h, ctypes.byref(P.struct), ctypes.byref(o), ctypes.byref(t)))
+        self._problems[t.value] = P
+        return t.value
+
+    def step(self) -> int:
+        n = ctypes.c_int32()
+        _check(lib().mcs_server_step(self._h, ctypes.byref(n)))
+        return n.value
+
+    def poll(self, ticket: int):
+        """The result tuple and extras when done, else None."""
+        P = self._problems[ticket]
+        rb = _ResultBuf(P, False)
+        rb.r.frames = None
+        rc = lib().mcs_server_poll(self._h, ticket, ctypes.byref(rb.r))
+        if rc == 1:
+            return None
+        _check(rc)
+        del self._problems[ticket]
+        P.frames = 0
+        return rb.unpack(P)
+
+    def stats(self):
+        a = ctypes.c_int32()
+        q = ctypes.c_int32()
+        b = ctypes.c_uint64()
+        su = ctypes.c_int64()
+        _check(lib().mcs_server_stats(self._h, ctypes.byref(a), ctypes.byref(q), ctypes.byref(b), ctypes.byref(su)))
+        return {"active": a.value, "queued": q.value, "bytes_in_use": b.value, "site_updates": su.value}
+
+    def close(self):
+        if self._h:
+            lib().mcs_server_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

@@ -74,7 +74,7 @@ def build(force: bool = False, verbose: bool = False) -> dict:
     cuda = _cuda_home(nvcc)
     jobs = []
     objs = []
-    for f in ("mcs_kernels.cu", "mcs_cluster.cu", "mcs_noalloc.cu", "mcs_pt.cu", "mcs_model.cpp", "mcs_engine.cpp", "mcs_stubs.cpp"):
+    for f in ("mcs_kernels.cu", "mcs_cluster.cu", "mcs_noalloc.cu", "mcs_pt.cu", "mcs_model.cpp", "mcs_engine.cpp", "mcs_server.cpp"):
         o = os.path.join(OBJ, f + ".o")
         objs.append(o)
         cmd = [nvcc] + NVCC_FLAGS + ["-x", "cu" if f.endswith(".cu") else "c++", "-c", os.path.join(SRC, f), "-o", o]

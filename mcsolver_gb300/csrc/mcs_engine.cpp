@@ -44,7 +44,7 @@ const std::string &get_error() { return g_err; }
 
 // ------------------------------------------------------------------ arena builder
 struct ArenaBuilder {
-    std::vector<unsigned char> host;
+    std::vector<unsigned char> host = std::vector<unsigned char>(256, 0);  // offset 0 is never used
     size_t add(const void *data, size_t bytes)
     {
         size_t off = (host.size() + 255) & ~(size_t)255;
@@ -68,12 +68,11 @@ size_t replica_acc_count(const HostModel &m)
     return A_GRP + (size_t)(G + 1) * (G + 1) + (G + 1);
 }
 
-int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r)
+int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool upload)
 {
     std::string err;
     int rc = compile_model(p, o, &r->hm, &err);
     if (rc != MCS_OK) { set_error(err); return rc; }
-    CUDA_TRY(cudaSetDevice(r->device));
     const HostModel &m = r->hm;
     r->record_series = o && o->record_series;
     r->requested_schedule = o ? o->schedule : 0;
@@ -120,22 +119,8 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r)
         o_wq = A.add(nullptr, (size_t)m.N * sizeof(int));
     }
     r->bytes = A.host.size();
-    CUDA_TRY(cudaMalloc(&r->arena, r->bytes));
-    {
-        // stage through page-locked memory (one buffer per calling thread, kept for reuse)
-        static thread_local void *pinned = nullptr;
-        static thread_local size_t pinned_n = 0;
-        if (pinned_n < r->bytes) {
-            if (pinned) cudaFreeHost(pinned);
-            pinned = nullptr;
-            pinned_n = 0;
-            CUDA_TRY(cudaMallocHost(&pinned, r->bytes));
-            pinned_n = r->bytes;
-        }
-        memcpy(pinned, A.host.data(), r->bytes);
-        CUDA_TRY(cudaMemcpy(r->arena, pinned, r->bytes, cudaMemcpyHostToDevice));
-    }
-    unsigned char *b = (unsigned char *)r->arena;
+    // the descriptor holds arena offsets until upload_replica() relocates them
+    auto P = [](size_t off) { return (void *)(uintptr_t)off; };
     Rep &R = r->rep;
     memset(&R, 0, sizeof R);
     R.model = m.model; R.dim = m.dim; R.geom = m.geom; R.alg = m.alg;
@@ -144,18 +129,18 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r)
     for (int d = 0; d < 4; ++d) { R.sq_code[d] = m.sq_code[d]; R.sq_cls[d] = m.sq_cls[d]; }
     for (int c = 0; c <= m.ncol; ++c) R.col_start[c] = m.col_start[c];
     if (m.geom == MCS_GEOM_ELL) {
-        R.nbr = (const int *)(b + o_nbr);
-        R.lcode = (const unsigned short *)(b + o_lcode);
-        R.deg = (const unsigned char *)(b + o_deg);
+        R.nbr = (const int *)P(o_nbr);
+        R.lcode = (const unsigned short *)P(o_lcode);
+        R.deg = (const unsigned char *)P(o_deg);
     }
-    if (m.dim == 1) R.lcls = (const unsigned char *)(b + o_lcls);
-    R.stype = (const unsigned char *)(b + o_stype);
+    if (m.dim == 1) R.lcls = (const unsigned char *)P(o_lcls);
+    R.stype = (const unsigned char *)P(o_stype);
     if (m.dim > 1) {
-        R.jtab = (const float *)(b + o_jt); R.jtab64 = (const double *)(b + o_jt64);
+        R.jtab = (const float *)P(o_jt); R.jtab64 = (const double *)P(o_jt64);
         R.njc = m.njc; R.fullJ = m.fullJ;
-        R.dtab = (const float *)(b + o_dt); R.ndc = m.ndc; R.has_d = m.has_d;
+        R.dtab = (const float *)P(o_dt); R.ndc = m.ndc; R.has_d = m.has_d;
     } else {
-        R.itab = (const IsEntry *)(b + o_it); R.nite = (int)m.itab.size(); R.ntype = m.ntype;
+        R.itab = (const IsEntry *)P(o_it); R.nite = (int)m.itab.size(); R.ntype = m.ntype;
         for (int t = 0; t < MCS_MAXT; ++t) { R.ibase[t] = m.ibase[t]; R.Stype[t] = m.Stype[t]; }
         for (int c = 0; c < MCS_MAXC; ++c) {
             R.Q[c] = m.Q[c];
@@ -166,21 +151,21 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r)
     R.beta = 1.0f; R.h = (float)m.h; R.hd = m.h;
     R.fp64 = 0;
     R.seed = m.seed;
-    R.nlat = m.nlat; R.cpair = (const int *)(b + o_cp);
+    R.nlat = m.nlat; R.cpair = (const int *)P(o_cp);
     R.n_rorb = m.n_rorb; R.ncl = m.ncl;
-    R.rorb = (const int *)(b + o_rorb); R.rcl = (const int *)(b + o_rcl); R.rlink = (const int *)(b + o_rlink);
-    if (m.dim > 1) R.rjc = (const unsigned short *)(b + o_rjc);
+    R.rorb = (const int *)P(o_rorb); R.rcl = (const int *)P(o_rcl); R.rlink = (const int *)P(o_rlink);
+    if (m.dim > 1) R.rjc = (const unsigned short *)P(o_rjc);
     else {
-        R.rK = (const double *)(b + o_rK);
-        R.rkc = (const unsigned char *)(b + o_rkc);
+        R.rK = (const double *)P(o_rK);
+        R.rkc = (const unsigned char *)P(o_rkc);
         R.is_fast = m.is_fast;
         for (int k = 0; k < 4; ++k) R.rKv[k] = m.rKv[k];
     }
-    R.rdeg = (const unsigned char *)(b + o_rdeg);
-    R.rindex = (const int *)(b + o_rindex);
-    R.ncirc = m.ncirc; R.circ = (const int *)(b + o_circ);
-    R.slen = (const float *)(b + o_slen); R.sval = (const float *)(b + o_sval);
-    R.ngroup = m.ngroup; R.gmask = (const unsigned char *)(b + o_gmask);
+    R.rdeg = (const unsigned char *)P(o_rdeg);
+    R.rindex = (const int *)P(o_rindex);
+    R.ncirc = m.ncirc; R.circ = (const int *)P(o_circ);
+    R.slen = (const float *)P(o_slen); R.sval = (const float *)P(o_sval);
+    R.ngroup = m.ngroup; R.gmask = (const unsigned char *)P(o_gmask);
     R.ci = m.ci; R.cj = m.cj; R.cij = m.cij;
     R.inv_nl = 1.0 / m.nlat; R.inv_N = 1.0 / m.N;
     R.inv_ci = 1.0 / m.ci; R.inv_cj = 1.0 / m.cj; R.inv_cij = 1.0 / m.cij; R.inv_nr = 1.0 / m.n_rorb;
@@ -193,25 +178,59 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r)
     }
     R.pair_identity = m.pair_identity;
     R.gall = m.gall;
-    R.sflag = (const unsigned char *)(b + o_sflag);
-    R.rtgt = (const int *)(b + o_rtgt);
+    R.sflag = (const unsigned char *)P(o_sflag);
+    R.rtgt = (const int *)P(o_rtgt);
     R.units_thermal = m.units_thermal; R.units_total = m.units_total; R.nsweep = m.nsweep; R.upm = m.upm;
     R.frames = m.frames; R.frame_every = m.frame_every;
     R.recheck = r->recheck;
     R.ts_const = m.ts_const; R.ts_wolff_last = m.ts_wolff_last; R.last_site = m.last_site;
     R.offset_energy = m.offset_energy;
     R.rinit = m.device_random_init;
-    R.spins = b + o_spins; R.spad = spad;
-    R.acc = (double *)(b + o_acc);
-    R.series = r->record_series ? (double *)(b + o_series) : nullptr;
-    R.frame_buf = m.frames > 0 ? (float *)(b + o_frames) : nullptr;
-    R.icnt = (long long *)(b + o_icnt);
-    R.stats = (long long *)(b + o_stats);
-    if (m.alg == 1) { R.wbits = (unsigned *)(b + o_wbits); R.wqueue = (int *)(b + o_wq); }
+    R.spins = P(o_spins); R.spad = spad;
+    R.acc = (double *)P(o_acc);
+    R.series = r->record_series ? (double *)P(o_series) : nullptr;
+    R.frame_buf = m.frames > 0 ? (float *)P(o_frames) : nullptr;
+    R.icnt = (long long *)P(o_icnt);
+    R.stats = (long long *)P(o_stats);
+    if (m.alg == 1) { R.wbits = (unsigned *)P(o_wbits); R.wqueue = (int *)P(o_wq); }
     R.u0 = 0; R.u = 0; R.m = 0;
     r->acc_off = o_acc; r->icnt_off = o_icnt; r->stats_off = o_stats; r->series_off = o_series;
     r->frames_off = o_frames; r->spins_off = o_spins;
     r->nacc = nacc;
+    r->staging = std::move(A.host);
+    if (upload) return upload_replica(r);
+    return MCS_OK;
+}
+
+// Device allocation, upload (through page-locked memory) and relocation of
+// the descriptor's arena offsets to device pointers.
+int upload_replica(Replica *r)
+{
+    if (r->arena) return MCS_OK;
+    CUDA_TRY(cudaSetDevice(r->device));
+    CUDA_TRY(cudaMalloc(&r->arena, r->bytes));
+    {
+        static thread_local void *pinned = nullptr;
+        static thread_local size_t pinned_n = 0;
+        if (pinned_n < r->bytes) {
+            if (pinned) cudaFreeHost(pinned);
+            pinned = nullptr;
+            pinned_n = 0;
+            CUDA_TRY(cudaMallocHost(&pinned, r->bytes));
+            pinned_n = r->bytes;
+        }
+        memcpy(pinned, r->staging.data(), r->bytes);
+        CUDA_TRY(cudaMemcpy(r->arena, pinned, r->bytes, cudaMemcpyHostToDevice));
+    }
+    const uintptr_t base = (uintptr_t)r->arena;
+    Rep &R = r->rep;
+#define RELOC(f) if (R.f) R.f = (decltype(R.f))((uintptr_t)R.f + base)
+    RELOC(nbr); RELOC(lcode); RELOC(lcls); RELOC(deg); RELOC(stype); RELOC(jtab); RELOC(jtab64); RELOC(dtab);
+    RELOC(itab); RELOC(cpair); RELOC(rorb); RELOC(rcl); RELOC(rlink); RELOC(rjc); RELOC(rK); RELOC(rkc);
+    RELOC(rdeg); RELOC(rindex); RELOC(circ); RELOC(slen); RELOC(sval); RELOC(gmask); RELOC(sflag); RELOC(rtgt);
+    RELOC(spins); RELOC(acc); RELOC(series); RELOC(frame_buf); RELOC(icnt); RELOC(stats); RELOC(wbits); RELOC(wqueue);
+#undef RELOC
+    std::vector<unsigned char>().swap(r->staging);
     return MCS_OK;
 }
 
@@ -356,7 +375,7 @@ int Batch::add(const mcs_problem *p, const mcs_options *o, int *idx)
 {
     std::unique_ptr<Replica> r(new Replica());
     r->device = device;
-    int rc = build_replica(p, o, r.get());
+    int rc = build_replica(p, o, r.get(), true);
     if (rc != MCS_OK) return rc;
     std::lock_guard<std::mutex> lock(add_mutex);
     if (prepared) { set_error("batch already prepared: add replicas before the first run or advance"); return MCS_EINVAL; }
@@ -487,18 +506,20 @@ int Batch::prepare()
     CUDA_TRY(cudaMemcpy(d_reps, host.data(), nrep * sizeof(Rep), cudaMemcpyHostToDevice));
     // initial energies / exact sums
     {
-        std::vector<int> all(nrep);
-        for (int i = 0; i < nrep; ++i) all[i] = i;
-        CUDA_TRY(cudaMalloc(&d_all, nrep * sizeof(int)));
-        CUDA_TRY(cudaMemcpy(d_all, all.data(), nrep * sizeof(int), cudaMemcpyHostToDevice));
-        for (int d = 1; d <= 3; ++d)
+        std::vector<int> all;
+        for (int i = 0; i < nrep; ++i)
+            if (!replicas[i]->initialized) all.push_back(i);
+        CUDA_TRY(cudaMalloc(&d_all, std::max<size_t>(1, all.size()) * sizeof(int)));
+        if (!all.empty()) CUDA_TRY(cudaMemcpy(d_all, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice));
+        for (int d = 1; d <= 3 && !all.empty(); ++d)
             for (int g = 0; g <= 1; ++g) {
                 bool any = false;
-                for (auto &r : replicas) any |= (r->hm.dim == d && r->hm.geom == g);
+                for (int i : all) any |= (replicas[i]->hm.dim == d && replicas[i]->hm.geom == g);
                 if (!any) continue;
-                CUDA_TRY(launch_init_state_dg(d, g, d_reps, d_all, nrep, stream));
+                CUDA_TRY(launch_init_state_dg(d, g, d_reps, d_all, (int)all.size(), stream));
                 launches++;
             }
+        for (int i : all) replicas[i]->initialized = true;
     }
     // groups
     for (int kind : {2, 6, 3, 1, 4, 5})
@@ -523,7 +544,7 @@ int Batch::prepare()
                     int maxcs = 0;
                     for (int id : set) {
                         Replica &r = *replicas[id];
-                        G->max_units = std::max(G->max_units, r.hm.units_total);
+                        G->max_units = std::max(G->max_units, r.hm.units_total - r.rep.u);
                         maxn = std::max<long long>(maxn, r.hm.N);
                         G->smem = std::max<size_t>(G->smem, (size_t)resident_smem_bytes(r.rep));
                         for (int c = 0; c < r.hm.ncol; ++c)
@@ -678,6 +699,11 @@ int Batch::collect()
     std::vector<Rep> host(nrep);
     if (nrep) CUDA_TRY(cudaMemcpy(host.data(), d_reps, nrep * sizeof(Rep), cudaMemcpyDeviceToHost));
     final_reps = host;
+    for (int i = 0; i < nrep; ++i) {  // progress travels with the replica
+        replicas[i]->rep.u = host[i].u;
+        replicas[i]->rep.m = host[i].m;
+        replicas[i]->rep.frames_written = host[i].frames_written;
+    }
     site_updates = 0;
     for (int i = 0; i < nrep; ++i) {
         long long st[S_NSTAT];

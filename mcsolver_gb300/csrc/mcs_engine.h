@@ -29,10 +29,13 @@ struct Replica {
     int record_series = 0;
     int recheck = 32;
     int device = 0;
+    bool initialized = false;          // initial-state kernel has run
+    std::vector<unsigned char> staging; // host image of the arena until upload
     ~Replica();
 };
 
-int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r);
+int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool upload);
+int upload_replica(Replica *r);
 int replica_results(Replica *r, const Rep &Rfinal, mcs_result *res);
 int replica_spins(Replica *r, std::vector<double> &out);
 int replica_set_spins(Replica *r, const double *in);
