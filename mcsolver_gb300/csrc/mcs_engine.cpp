@@ -489,6 +489,7 @@ cudaError_t Batch::tiled_unit(Group &G, cudaStream_t s, long long *nl)
 int Batch::prepare()
 {
     if (prepared) return MCS_OK;
+    cudaGetLastError();  // a failed call of an earlier batch must not be reported here
     int src = ensure_streams();
     if (src != MCS_OK) return src;
     const int nrep = (int)replicas.size();
@@ -563,25 +564,35 @@ int Batch::prepare()
                         if (threads_override > 0) G->threads = threads_override;
                         G->chunk = std::max<long long>(1, (1LL << 28) / std::max<long long>(1, maxn));
                         if (chunk_override > 0) G->chunk = chunk_override;
-                        // candidate configurations for the autotuner
+                        // candidate configurations for the autotuner: the resident
+                        // kernel, and every cluster size that divides each replica's
+                        // rows into even slabs that fit in shared memory
                         bool all_cl = g == MCS_GEOM_SQUARE && d > 1;
-                        int Lx = 0;
-                        for (int id : set) {
-                            all_cl &= replicas[id]->hm.cluster_ok != 0;
-                            if (Lx == 0) Lx = replicas[id]->hm.Lx;
-                            all_cl &= replicas[id]->hm.Lx == Lx;
-                        }
+                        for (int id : set) all_cl &= replicas[id]->hm.cluster_ok != 0;
                         if (kind == 2) G->candidates.push_back({1, G->threads});
                         if (all_cl && cluster_override != 1) {
                             for (int C : {2, 4, 8}) {
                                 if (cluster_override > 1 && C != cluster_override) continue;
-                                if (Lx % C || (Lx / C) % 2 || Lx / C < 2) continue;
+                                bool ok = true;
                                 size_t sm = 0;
-                                for (int id : set) sm = std::max<size_t>(sm, (size_t)cluster_smem_bytes(replicas[id]->rep, C));
-                                if ((int)sm > max_smem) continue;
+                                for (int id : set) {
+                                    const int Lx = replicas[id]->hm.Lx;
+                                    ok &= Lx % C == 0 && (Lx / C) % 2 == 0 && Lx / C >= 2;
+                                    sm = std::max<size_t>(sm, (size_t)cluster_smem_bytes(replicas[id]->rep, C));
+                                }
+                                if (!ok || (int)sm > max_smem) continue;
                                 for (int th : {512, 1024}) G->candidates.push_back({C, th});
                             }
                             G->can_cluster = 1;
+                        }
+                        if (G->candidates.empty() && kind == 6) {
+                            // no cluster size fits: run these replicas on the tiled schedule
+                            G->kind = 3;
+                            for (int id : set) replicas[id]->schedule = 3;
+                            int rc = setup_tiled(*G);
+                            if (rc != MCS_OK) return rc;
+                            groups.push_back(std::move(G));
+                            continue;
                         }
                         if (G->candidates.empty()) G->candidates.push_back({1, G->threads});
                         if (G->candidates.size() == 1 || no_autotune) {

@@ -33,7 +33,8 @@ def _close(model, a, b):
     np.testing.assert_allclose(np.array(a[:n]), np.array(b[:n]), rtol=1e-9 if model == "ising" else 1e-6, atol=1e-9)
 
 
-def test_server_results_equal_alone_with_overlapping_arrivals(engine):
+def test_server_results_equal_alone_with_overlapping_arrivals(engine, monkeypatch):
+    monkeypatch.setenv("MCSGPU_SERVER_CHUNK", "8")   # short steps, so that arrivals overlap
     reqs = _reqs()
     srv = engine.Server(hbm_budget_bytes=1 << 30, max_slots=64)
     tickets = {}
@@ -65,7 +66,8 @@ def test_server_results_equal_alone_with_overlapping_arrivals(engine):
     srv.close()
 
 
-def test_server_budget_queues_requests(engine):
+def test_server_budget_queues_requests(engine, monkeypatch):
+    monkeypatch.setenv("MCSGPU_SERVER_CHUNK", "8")
     reqs = _reqs()[:4]
     srv = engine.Server(hbm_budget_bytes=600_000, max_slots=2)
     ts = [srv.submit(m, a, seed=s) for m, a, s in reqs]
