@@ -29,8 +29,11 @@ def _reqs():
 
 
 def _close(model, a, b):
+    # O(n): the same trajectory; FP32 per-thread partials summed in another
+    # order leave ~1e-8 absolute noise on quantities near zero (e.g. Q)
     n = 10 if model == "ising" else 27
-    np.testing.assert_allclose(np.array(a[:n]), np.array(b[:n]), rtol=1e-9 if model == "ising" else 1e-6, atol=1e-9)
+    np.testing.assert_allclose(np.array(a[:n]), np.array(b[:n]), rtol=1e-9 if model == "ising" else 1e-6,
+                               atol=1e-9 if model == "ising" else 1e-6)
 
 
 def test_server_results_equal_alone_with_overlapping_arrivals(engine, monkeypatch):
