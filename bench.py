@@ -265,6 +265,153 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------- other configurations
+def _plain_rate(eng, model, args, seed):
+    r, ex = eng.solve(model, args, seed=seed, schedule="plain", random_init=True)
+    return ex["site_updates"], ex["device_ms"] / 1000.0
+
+
+def run_served(args):
+    """Served stream: Poisson arrivals (mean 200 req/s, seeded) of mixed
+    Ising / XY / Heisenberg (DMI, field) square-lattice solves, L log-uniform in
+    32..512, random (T, H) in each model's range, nthermal / nsweep as given;
+    requests are submitted when they arrive and the server admits them as
+    slots and its HBM budget allow."""
+    import numpy as np
+
+    import mcsolver_gb300 as eng
+    from mcsolver_gb300 import build as b
+    from mcsolver_gb300.lattice import square_args_fast
+    b.build()
+    rng = np.random.default_rng(5)
+    n = args.requests
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=n))
+    reqs = []
+    for k in range(n):
+        model = ["ising", "xy", "heisenberg"][rng.integers(3)]
+        L = int(round(math.exp(rng.uniform(math.log(32), math.log(512)))))
+        L += L % 2
+        if model == "ising":
+            T, H = rng.uniform(1.5, 3.5), 0.0
+            a = square_args_fast("ising", L, T, nthermal=args.nthermal, nsweep=args.nsweep, arrays=True)
+        elif model == "xy":
+            T, H = rng.uniform(0.5, 1.5), 0.0
+            a = square_args_fast("xy", L, T, nthermal=args.nthermal, nsweep=args.nsweep, arrays=True)
+        else:
+            T, H = rng.uniform(0.05, 1.0), rng.uniform(0.0, 0.6)
+            a = square_args_fast("heisenberg", L, T, h=H, dmi=0.4, nthermal=args.nthermal, nsweep=args.nsweep,
+                                 arrays=True)
+        reqs.append((model, eng.Problem(model, a), L, T, H))
+    srv = eng.Server(hbm_budget_bytes=64 << 30, max_slots=4096)
+    lat, upd, pending = [], 0, {}
+    t0 = time.time()
+    nxt = 0
+    while nxt < n or pending:
+        now = time.time() - t0
+        while nxt < n and arrivals[nxt] <= now:
+            model, P, L, T, H = reqs[nxt]
+            pending[srv.submit(model, P, seed=7000 + nxt, random_init=True)] = arrivals[nxt]
+            nxt += 1
+        if not pending:
+            time.sleep(max(0.0, arrivals[nxt] - now))
+            continue
+        srv.step()
+        now = time.time() - t0
+        for t in list(pending):
+            r = srv.poll(t)
+            if r is not None:
+                lat.append(now - pending.pop(t))
+                upd += r[1]["site_updates"]
+    makespan = time.time() - t0
+    srv.close()
+    # one solve per launch sequence, host-driven, for a sample of the same requests
+    ps, pt = 0, 0.0
+    for k in range(min(args.plain_sample, n)):
+        model, P, L, T, H = reqs[k]
+        u, s = _plain_rate(eng, model, P, 7000 + k)
+        ps += u
+        pt += s
+    lat = np.array(lat)
+    print(json.dumps({"workload": "served_stream", "requests": n, "rate_req_s": args.rate,
+                      "nthermal": args.nthermal, "nsweep": args.nsweep, "makespan_s": makespan,
+                      "solves_per_s": n / makespan, "site_updates_per_s": upd / makespan,
+                      "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+                      "plain_site_updates_per_s": ps / pt if pt > 0 else None,
+                      "served_over_plain": (upd / makespan) / (ps / pt) if pt > 0 else None,
+                      "plain_sample": min(args.plain_sample, n)}))
+
+
+def run_batched4(args):
+    """Batched grid: square Heisenberg with DMI (0.4 |J|, J = -1) and field,
+    16 temperatures 0.05..1.0 (clamped to 0.1 as mcMain does) x 16 fields
+    0..0.6 = 256 replicas of uneven sizes L in {64, 96, 128, 192, 256}, two
+    circuits per cell, all in one launch sequence."""
+    import numpy as np
+
+    import mcsolver_gb300 as eng
+    from mcsolver_gb300 import build as b
+    from mcsolver_gb300.lattice import rescale_args, square_args_fast
+    b.build()
+    sizes = [64, 96, 128, 192, 256]
+    base = {L: square_args_fast("heisenberg", L, 1.0, dmi=0.4, nthermal=args.nthermal, nsweep=args.nsweep, arrays=True)
+            for L in sizes}
+    Ts = np.linspace(0.05, 1.0, 16)
+    Hs = np.linspace(0.0, 0.6, 16)
+    bt = eng.Batch()
+    k = 0
+    total = 0
+    jobs = []
+    for iT, T in enumerate(Ts):
+        for iH, H in enumerate(Hs):
+            L = sizes[k % len(sizes)]
+            jobs.append((L, rescale_args("heisenberg", base[L], T, h=H)))
+            k += 1
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as pool:
+        list(pool.map(lambda kj: bt.add("heisenberg", kj[1][1], seed=11 + kj[0], random_init=True), enumerate(jobs)))
+    for L, a in jobs:
+        total += L * L * (args.nthermal + args.nsweep)
+    bt.prepare()
+    t = time.time()
+    bt.run()
+    wall = time.time() - t
+    st = bt.stats()
+    bt.close()
+    u, s = _plain_rate(eng, "heisenberg", jobs[2][1], 99)
+    print(json.dumps({"workload": "batched_heisenberg_dmi_256_uneven", "replicas": len(jobs), "sizes": sizes,
+                      "nthermal": args.nthermal, "nsweep": args.nsweep, "site_updates": st["site_updates"],
+                      "device_ms": st["device_ms"], "wall_s": wall,
+                      "site_updates_per_s": st["site_updates"] / (st["device_ms"] / 1000.0),
+                      "plain_site_updates_per_s_L128": u / s,
+                      "batched_over_plain": (st["site_updates"] / (st["device_ms"] / 1000.0)) / (u / s)}))
+
+
+def run_pt(args):
+    """Parallel tempering: honeycomb Heisenberg (2 sites/cell), 1NN Kitaev-type
+    J = diag(-1.5,-1.5,-1.8) with Jxy = Jyx = 0.3, 2NN -0.3, Az = -0.5, 64x64
+    cells, 64 replicas at geometric temperatures 5..50 K, exchange every sweep."""
+    import numpy as np
+
+    import mcsolver_gb300 as eng
+    from mcsolver_gb300 import build as b
+    from mcsolver_gb300.lattice import honeycomb_args
+    b.build()
+    phys = honeycomb_args("heisenberg", 64, 1.0, nthermal=args.nthermal, nsweep=args.nsweep)
+    betas = 1.0 / np.geomspace(5.0, 50.0, 64)
+    pt = eng.ParallelTempering("heisenberg", phys, betas, seed=3)
+    t = time.time()
+    pt.run()
+    wall = time.time() - t
+    st = pt.stats()
+    pt.close()
+    print(json.dumps({"workload": "pt_honeycomb_heisenberg_64x64_64T", "replicas": 64,
+                      "sweeps": args.nthermal + args.nsweep, "site_updates": st["site_updates"],
+                      "device_ms": st["device_ms"], "wall_s": wall,
+                      "site_updates_per_s": st["site_updates"] / (st["device_ms"] / 1000.0),
+                      "swap_acceptance_min": float(np.min(st["swap_acceptance"])),
+                      "swap_acceptance_max": float(np.max(st["swap_acceptance"]))}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -275,7 +422,19 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--workload", default="headline", choices=["headline", "served", "batched4", "pt"])
+    ap.add_argument("--requests", type=int, default=48)
+    ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--nthermal", type=int, default=1000)
+    ap.add_argument("--nsweep", type=int, default=5000)
+    ap.add_argument("--plain-sample", type=int, default=4)
     args = ap.parse_args()
+    if args.workload == "served":
+        return run_served(args)
+    if args.workload == "batched4":
+        return run_batched4(args)
+    if args.workload == "pt":
+        return run_pt(args)
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         if rank == 0:

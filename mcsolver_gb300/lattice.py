@@ -188,17 +188,122 @@ def honeycomb_args(model, L, T, nthermal=10, nsweep=10, tau=0, algo=0, h=0.0):
 
 
 
-def rescale_args(model, args, T, T0=1.0):
+def rescale_args(model, args, T, T0=1.0, h=None):
     """The tuple of the same lattice at temperature T from one built at T0:
-    couplings, anisotropy and field scale as 1/T (mcMain.py:21-31)."""
+    couplings, anisotropy and field scale as 1/T (mcMain.py:21-31).  numpy
+    array entries stay arrays.  h, when given, replaces the field (physical)."""
     T = max(T, 0.1)
     f = T0 / T
     a = list(args)
+    if isinstance(a[1], np.ndarray):
+        if model == "ising":
+            a[7] = a[7] * f
+            a[10] = a[10] * f if h is None else h / T
+        else:
+            a[2] = a[2] * f
+            a[8] = a[8] * f
+            a[16] = a[16] * f if h is None else h / T
+        return tuple(a)
     if model == "ising":
         a[7] = tuple((np.asarray(a[7], dtype=float) * f).tolist())
         a[10] = a[10] * f
     else:
         a[2] = tuple((np.asarray(a[2], dtype=float) * f).tolist())
         a[8] = tuple((np.asarray(a[8], dtype=float) * f).tolist())
-        a[16] = a[16] * f
+        a[16] = a[16] * f if h is None else h / T
+    if model == "ising" and h is not None:
+        a[10] = h / T
     return tuple(a)
+
+
+def _square_link_order(Lx, Ly, step):
+    """Targets and directions of the links of every site of a periodic square
+    lattice (one orbital, bonds along [1 0 0] and [0 1 0]) in the order
+    Lattice.establishLinking appends them (Lattice.py:247-271): as the target
+    of the bonds from (x-step, y) and (x, y-step) when those sources are
+    visited before the site itself, then its own two bonds, then the targets
+    from sources visited later.  Returns (targets[N,4], fwd[N,4]) where fwd is
+    True for a link the site owns (strength J) and False for an inverse one."""
+    x = np.repeat(np.arange(Lx), Ly)
+    y = np.tile(np.arange(Ly), Lx)
+    sid = lambda a, b: (a % Lx) * Ly + (b % Ly)
+    tA = sid(x - step, y)          # inverse of bond 0 from (x-step, y)
+    tB = sid(x, y - step)          # inverse of bond 1 from (x, y-step)
+    tF0 = sid(x + step, y)         # own bond 0
+    tF1 = sid(x, y + step)         # own bond 1
+    early_a = x >= step            # source (x-step, y) visited before (x, y)
+    early_b = y >= step
+    N = Lx * Ly
+    tg = np.zeros((N, 4), dtype=np.int64)
+    fw = np.zeros((N, 4), dtype=bool)
+    # the four cases of which inverse links come before the site's own
+    c11 = early_a & early_b
+    c01 = ~early_a & early_b
+    c10 = early_a & ~early_b
+    c00 = ~early_a & ~early_b
+    for mask, order in ((c11, ("A", "B", "F0", "F1")), (c01, ("B", "F0", "F1", "A")),
+                        (c10, ("A", "F0", "F1", "B")), (c00, ("F0", "F1", "B", "A"))):
+        for k, name in enumerate(order):
+            t = {"A": tA, "B": tB, "F0": tF0, "F1": tF1}[name]
+            tg[mask, k] = t[mask]
+            fw[mask, k] = name.startswith("F")
+    return tg, fw
+
+
+def square_args_fast(model, L, T, J=-1.0, h=0.0, dmi=0.0, D=None, nthermal=10, nsweep=10, tau=0, algo=0,
+                     frames=0, circuits=True, arrays=False):
+    """The tuple of ``square_args`` (same values, same order) built with numpy
+    array operations; for large lattices and served requests.  L even, >= 6.
+    arrays=True returns numpy arrays in place of the inner tuples (for the
+    C ABI, which takes buffers; the drop-in modules take tuples)."""
+    if arrays:
+        return _square_fast(model, L, T, J, h, dmi, D, nthermal, nsweep, tau, algo, frames, circuits, True)
+    return _square_fast(model, L, T, J, h, dmi, D, nthermal, nsweep, tau, algo, frames, circuits, False)
+
+
+def _square_fast(model, L, T, J, h, dmi, D, nthermal, nsweep, tau, algo, frames, circuits, arrays):
+    if L < 6 or L % 2:
+        return square_args(model, L, T, J=J, h=h, dmi=dmi, D=D, nthermal=nthermal, nsweep=nsweep, tau=tau,
+                           algo=algo, frames=frames, circuits=circuits)
+    T = max(T, 0.1)
+    Lx = Ly = L
+    N = L * L
+    tg, fw = _square_link_order(Lx, Ly, 1)
+    rtg, _ = _square_link_order(Lx, Ly, 2)
+    x = np.repeat(np.arange(Lx), Ly)
+    y = np.tile(np.arange(Ly), Lx)
+    dirx = np.zeros((N, 4), dtype=bool)   # link along x (bond 0) or y (bond 1)
+    sid = lambda a, b: (a % Lx) * Ly + (b % Ly)
+    dirx[:] = (tg == sid(x + 1, y)[:, None]) | (tg == sid(x - 1, y)[:, None])
+    chosen = (x % 2 == 0) & (y % 2 == 0)
+    rorb = np.nonzero(chosen)[0]
+    rcl = np.stack([sid(x, y), sid(x, y + 1), sid(x + 1, y), sid(x + 1, y + 1)], axis=1)[rorb]
+    rlk = rtg[rorb]
+    tau = N if tau <= 0 else tau
+    cp = np.stack([np.arange(N), np.arange(N)], axis=1).reshape(-1)
+    out = (lambda a: np.ascontiguousarray(a).reshape(-1)) if arrays else (lambda a: tuple(np.asarray(a).reshape(-1).tolist()))
+    if model == "ising":
+        K = J / T
+        ls = np.full((N, 4), K)
+        return (algo, out(np.ones(N)), nthermal, nsweep, tau, 4, out(np.full(N, 4)), out(ls), out(tg), out(cp), h / T,
+                out(rorb), out(rcl), out(rlk), frames)
+    bx = np.asarray(J9(J, J, J, xz=dmi, zx=-dmi), dtype=float) / T
+    by = np.asarray(J9(J, J, J, yz=dmi, zy=-dmi), dtype=float) / T
+    inv = lambda b: np.array([b[0], b[1], b[2], b[6], b[7], b[8], b[3], b[4], b[5]])
+    ls = np.zeros((N, 4, 9))
+    for k in range(4):
+        ls[:, k, :] = np.where((dirx[:, k] & fw[:, k])[:, None], bx, 0) + \
+            np.where((dirx[:, k] & ~fw[:, k])[:, None], inv(bx), 0) + \
+            np.where((~dirx[:, k] & fw[:, k])[:, None], by, 0) + \
+            np.where((~dirx[:, k] & ~fw[:, k])[:, None], inv(by), 0)
+    Dv = np.asarray(D or [0, 0, 0], dtype=float) / T
+    initD = np.tile(Dv, N)
+    circ = np.zeros(0, dtype=np.int64)
+    if circuits and model == "heisenberg":
+        c = []
+        for circuit in SQ_CIRCUITS:
+            c.append(np.stack([sid(x + ov[0], y + ov[1]) for (o, ov) in circuit], axis=1))
+        circ = np.stack(c, axis=1)
+    ign = 0 if dmi != 0 else 1
+    return (algo, out(np.ones(N)), out(initD), nthermal, nsweep, tau, 4, out(np.full(N, 4)), out(ls), out(tg),
+            out(circ), out(cp), 1, N, out(np.arange(N)), 0.0, h / T, out(rorb), out(rcl), out(rlk), frames, ign)

@@ -107,3 +107,21 @@ def test_reference_crashes_are_documented_cases():
                 nthermal=1, nsweep=1, tau=0, algo="Metropolis")
     args = rh.capture_args(spec)
     assert -1 in args[13]
+
+
+@pytest.mark.parametrize("model", ["ising", "xy", "heisenberg"])
+@pytest.mark.parametrize("L", [6, 8, 12])
+def test_vectorised_builder_equals_reference_order(model, L):
+    """mcsolver_gb300.lattice.square_args_fast reproduces the reference-order
+    tuples of square_args (itself checked against the reference's own
+    marshalling above) value for value, as tuples and as arrays."""
+    from mcsolver_gb300.lattice import square_args_fast
+    kw = dict(h=0.2, nthermal=3, nsweep=4)
+    if model != "ising":
+        kw.update(D=[0, 0, -0.1], dmi=0.4 if model == "heisenberg" else 0.0)
+    a = C.square_args(model, L, 0.7, **kw)
+    for arrays in (False, True):
+        b = square_args_fast(model, L, 0.7, arrays=arrays, **kw)
+        assert len(a) == len(b)
+        for x, y in zip(a, b):
+            np.testing.assert_array_equal(np.asarray(x, float), np.asarray(y, float))
