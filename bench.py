@@ -172,13 +172,15 @@ def run_ours(args):
             times.append(batch.advance(S))
         wall = time.time() - wall0
     launches = batch.stats()["launches"] - l0
+    sched = batch.schedules()
     batch.close()
     per_step_updates = NTEMP * L * L * S
     dev_s = sum(times) / 1000.0
     value = per_step_updates * K / dev_s
     ms_per_step = sum(times) / K
-    # roofline of the resident Metropolis kernel (one launch per step):
+    # roofline of the Metropolis kernel the autotuner chose (one launch per step):
     # algorithmic bytes = lattice read + written once per sweep, FP32 (x,y) = 16 B / site update
+    kname = "k_cluster_metro<2>" if sched[0][1] > 1 else "k_resident_metro<2,SQUARE>"
     alg_bytes = 16.0 * per_step_updates
     achieved = alg_bytes / (ms_per_step / 1000.0) / 1e9
     traffic = None
@@ -230,13 +232,15 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f32 update / f64 accumulate", "data": "synthetic",
         "config": {"workload": WORKLOAD, "model": "XY", "L": L, "n_temperatures": NTEMP, "T_range_K": [0.5, 1.5],
                    "algorithm": "Metropolis", "sweeps_per_step": S, "measurement": "every sweep (tau=N)",
-                   "replicas": NTEMP, "l2": "flushed between steps (256 MB write)", "schedule": "resident"},
+                   "replicas": NTEMP, "l2": "flushed between steps (256 MB write)",
+                   "schedule": [{"schedule": g[0], "ctas_per_replica": g[1], "threads": g[2], "replicas": g[3]}
+                                for g in sched]},
         "e2e": {"value": e2e_value, "unit": "site_updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "C ABI mcs_batch_* from host arrays: create, compile+upload 32 replicas (16 host threads, "
                         "pinned staging), run, read every result back"},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "kernel": "k_resident_metro<2,SQUARE>",
+                     "traffic": traffic, "kernel": kname,
                      "note": "lattice is shared-memory resident inside a launch; HBM is touched once per launch"},
         "cpu_baseline": cpu,
         "plain_engine": plain,
@@ -274,9 +278,16 @@ def _plain_rate(eng, model, args, seed):
 def run_served(args):
     """Served stream: Poisson arrivals (mean 200 req/s, seeded) of mixed
     Ising / XY / Heisenberg (DMI, field) square-lattice solves, L log-uniform in
-    32..512, random (T, H) in each model's range, nthermal / nsweep as given;
-    requests are submitted when they arrive and the server admits them as
-    slots and its HBM budget allow."""
+    32..512 (even), random (T, H) in each model's range, nthermal / nsweep as
+    given.  The client marshals each request's arrays before the run (as
+    mcsolver builds its tuples); inside the timed run a dispatcher submits each
+    request at its arrival time to a pool of submit threads (host compile runs
+    there, beside the device work), and the main thread steps the server and
+    polls.  Latency = completion - arrival."""
+    import queue
+    import threading
+    from concurrent.futures import ThreadPoolExecutor
+
     import numpy as np
 
     import mcsolver_gb300 as eng
@@ -301,44 +312,68 @@ def run_served(args):
             T, H = rng.uniform(0.05, 1.0), rng.uniform(0.0, 0.6)
             a = square_args_fast("heisenberg", L, T, h=H, dmi=0.4, nthermal=args.nthermal, nsweep=args.nsweep,
                                  arrays=True)
-        reqs.append((model, eng.Problem(model, a), L, T, H))
+        reqs.append((model, eng.Problem(model, a), L))
     srv = eng.Server(hbm_budget_bytes=64 << 30, max_slots=4096)
+    submitted = queue.Queue()
+    pool = ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1))
+
+    def submit(k, t_arr):
+        model, P, L = reqs[k]
+        submitted.put((srv.submit(model, P, seed=7000 + k, random_init=True), t_arr))
+
+    def dispatch(t0):
+        for k in range(n):
+            d = t0 + arrivals[k] - time.time()
+            if d > 0:
+                time.sleep(d)
+            pool.submit(submit, k, t0 + arrivals[k])
+
     lat, upd, pending = [], 0, {}
     t0 = time.time()
-    nxt = 0
-    while nxt < n or pending:
-        now = time.time() - t0
-        while nxt < n and arrivals[nxt] <= now:
-            model, P, L, T, H = reqs[nxt]
-            pending[srv.submit(model, P, seed=7000 + nxt, random_init=True)] = arrivals[nxt]
-            nxt += 1
+    th = threading.Thread(target=dispatch, args=(t0,))
+    th.start()
+    finished = 0
+    while finished < n:
+        while True:
+            try:
+                t, ta = submitted.get_nowait()
+            except queue.Empty:
+                break
+            pending[t] = ta
         if not pending:
-            time.sleep(max(0.0, arrivals[nxt] - now))
+            time.sleep(0.0005)
             continue
         srv.step()
-        now = time.time() - t0
+        now = time.time()
         for t in list(pending):
             r = srv.poll(t)
             if r is not None:
                 lat.append(now - pending.pop(t))
                 upd += r[1]["site_updates"]
+                finished += 1
     makespan = time.time() - t0
+    th.join()
+    pool.shutdown()
     srv.close()
-    # one solve per launch sequence, host-driven, for a sample of the same requests
+    # the plain engine (one solve at a time, host-driven launches per sweep) on a seeded sample
+    pick = rng.choice(n, size=min(args.plain_sample, n), replace=False)
     ps, pt = 0, 0.0
-    for k in range(min(args.plain_sample, n)):
-        model, P, L, T, H = reqs[k]
-        u, s = _plain_rate(eng, model, P, 7000 + k)
+    for k in pick:
+        model, P, L = reqs[k]
+        u, s = _plain_rate(eng, model, P, 7000 + int(k))
         ps += u
         pt += s
     lat = np.array(lat)
+    Ls = np.array([r[2] for r in reqs])
     print(json.dumps({"workload": "served_stream", "requests": n, "rate_req_s": args.rate,
-                      "nthermal": args.nthermal, "nsweep": args.nsweep, "makespan_s": makespan,
+                      "nthermal": args.nthermal, "nsweep": args.nsweep,
+                      "L_range": [int(Ls.min()), int(Ls.max())], "site_updates": int(upd),
+                      "makespan_s": makespan, "last_arrival_s": float(arrivals[-1]),
                       "solves_per_s": n / makespan, "site_updates_per_s": upd / makespan,
                       "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
                       "plain_site_updates_per_s": ps / pt if pt > 0 else None,
                       "served_over_plain": (upd / makespan) / (ps / pt) if pt > 0 else None,
-                      "plain_sample": min(args.plain_sample, n)}))
+                      "plain_sample": [int(Ls[k]) for k in pick]}))
 
 
 def run_batched4(args):
@@ -396,7 +431,8 @@ def run_pt(args):
     from mcsolver_gb300 import build as b
     from mcsolver_gb300.lattice import honeycomb_args
     b.build()
-    phys = honeycomb_args("heisenberg", 64, 1.0, nthermal=args.nthermal, nsweep=args.nsweep)
+    nth = args.pt_sweeps // 5
+    phys = honeycomb_args("heisenberg", 64, 1.0, nthermal=nth, nsweep=args.pt_sweeps - nth)
     betas = 1.0 / np.geomspace(5.0, 50.0, 64)
     pt = eng.ParallelTempering("heisenberg", phys, betas, seed=3)
     t = time.time()
@@ -405,7 +441,7 @@ def run_pt(args):
     st = pt.stats()
     pt.close()
     print(json.dumps({"workload": "pt_honeycomb_heisenberg_64x64_64T", "replicas": 64,
-                      "sweeps": args.nthermal + args.nsweep, "site_updates": st["site_updates"],
+                      "sweeps": args.pt_sweeps, "site_updates": st["site_updates"],
                       "device_ms": st["device_ms"], "wall_s": wall,
                       "site_updates_per_s": st["site_updates"] / (st["device_ms"] / 1000.0),
                       "swap_acceptance_min": float(np.min(st["swap_acceptance"])),
@@ -427,7 +463,8 @@ def main():
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--nthermal", type=int, default=1000)
     ap.add_argument("--nsweep", type=int, default=5000)
-    ap.add_argument("--plain-sample", type=int, default=4)
+    ap.add_argument("--plain-sample", type=int, default=6)
+    ap.add_argument("--pt-sweeps", type=int, default=50000)
     args = ap.parse_args()
     if args.workload == "served":
         return run_served(args)

@@ -143,6 +143,14 @@ int mcs_batch_stats(mcs_batch *b, double *device_ms, int64_t *site_updates, int3
 /* Device bytes the batch holds (uploaded from the host) and bytes read back
  * per result collection. */
 int mcs_batch_memory(mcs_batch *b, uint64_t *device_bytes, uint64_t *readback_bytes);
+/* Schedule of launch group `group` (0-based) after preparation: *kind 1 plain,
+ * 2 resident (one CTA per replica), 3 tiled (global memory, graphs),
+ * 4 Wolff in shared memory, 5 Wolff in global memory, 6 thread-block cluster;
+ * *cluster = CTAs per replica, *threads per CTA, *replicas in the group.
+ * Returns MCS_EINVAL when `group` is out of range (no counterpart in the
+ * reference, which has one schedule). */
+int mcs_batch_schedule(mcs_batch *b, int32_t group, int32_t *kind, int32_t *cluster, int32_t *threads,
+                       int32_t *replicas);
 void mcs_batch_destroy(mcs_batch *b);
 
 /* ---- parallel tempering over a temperature ladder (one model) ------------- */
@@ -163,11 +171,14 @@ void mcs_pt_destroy(mcs_pt *pt);
 typedef struct mcs_server mcs_server;
 /* hbm_budget_bytes: device memory the server may hold for request state. */
 int mcs_server_create(int32_t device, uint64_t hbm_budget_bytes, int32_t max_slots, mcs_server **out);
-/* Queue one solve; *ticket identifies it.  Admission happens in mcs_server_step
- * when slots and memory allow. */
+/* Queue one solve; *ticket identifies it.  The problem is compiled on the
+ * calling thread before this returns (its arrays may be freed afterwards).
+ * Admission happens in mcs_server_step when slots and memory allow.
+ * submit, poll and stats may run on any threads concurrently with step. */
 int mcs_server_submit(mcs_server *s, const mcs_problem *problem, const mcs_options *options, uint64_t *ticket);
 /* Advance the device by one tick (admit, run a chunk of sweeps on every active
- * slot, retire finished ones).  Returns the number of requests completed. */
+ * slot, stopping at the next completion, retire finished ones).  *completed
+ * receives the number of requests completed.  One step at a time. */
 int mcs_server_step(mcs_server *s, int32_t *completed);
 /* 0 = done (result filled, ticket released), 1 = pending. */
 int mcs_server_poll(mcs_server *s, uint64_t ticket, mcs_result *result);

@@ -84,7 +84,7 @@ _lib = None
 ABI_FUNCTIONS = [
     "mcs_solve", "mcs_last_error", "mcs_abi_version", "mcs_build_info",
     "mcs_batch_create", "mcs_batch_add", "mcs_batch_run", "mcs_batch_prepare", "mcs_batch_advance",
-    "mcs_batch_result", "mcs_batch_stats", "mcs_batch_memory", "mcs_batch_destroy",
+    "mcs_batch_result", "mcs_batch_stats", "mcs_batch_memory", "mcs_batch_schedule", "mcs_batch_destroy",
     "mcs_pt_create", "mcs_pt_run", "mcs_pt_result", "mcs_pt_stats", "mcs_pt_destroy",
     "mcs_server_create", "mcs_server_submit", "mcs_server_step", "mcs_server_poll", "mcs_server_stats",
     "mcs_server_destroy", "mcs_ising_square_noalloc",
@@ -110,6 +110,7 @@ def lib():
         L.mcs_batch_result.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(McsResult)]
         L.mcs_batch_stats.argtypes = [ctypes.c_void_p, _f64p, ctypes.POINTER(ctypes.c_int64), _i32p]
         L.mcs_batch_memory.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+        L.mcs_batch_schedule.argtypes = [ctypes.c_void_p, ctypes.c_int32, _i32p, _i32p, _i32p, _i32p]
         L.mcs_batch_destroy.argtypes = [ctypes.c_void_p]
         L.mcs_batch_destroy.restype = None
         L.mcs_pt_create.argtypes = [ctypes.POINTER(McsProblem), ctypes.POINTER(McsOptions), _f64p, ctypes.c_int32,
@@ -263,8 +264,9 @@ class _ResultBuf:
 
 def solve(model: str, args: tuple, seed: int = 1, schedule: str = "auto", record_series: bool = False,
           absolute_energy: bool = False, random_init: bool = False, recheck_every: int = 0, device: int = 0):
-    """One solve through the C ABI; returns (reference result tuple, extras)."""
-    P = Problem(model, args)
+    """One solve through the C ABI; returns (reference result tuple, extras).
+    ``args`` is the MCMainFunction tuple or a prebuilt Problem."""
+    P = args if isinstance(args, Problem) else Problem(model, args)
     o = make_options(seed, schedule, absolute_energy, recheck_every, record_series, random_init, device)
     rb = _ResultBuf(P, record_series)
     _check(lib().mcs_solve(ctypes.byref(P.struct), ctypes.byref(o), ctypes.byref(rb.r)))
@@ -321,6 +323,20 @@ class Batch:
         nl = ctypes.c_int32()
         _check(lib().mcs_batch_stats(self._h, ctypes.byref(ms), ctypes.byref(su), ctypes.byref(nl)))
         return {"device_ms": ms.value, "site_updates": su.value, "launches": nl.value}
+
+    SCHEDULES = {1: "plain", 2: "resident", 3: "tiled", 4: "wolff_shared", 5: "wolff_global", 6: "cluster"}
+
+    def schedules(self):
+        """[(schedule name, CTAs per replica, threads per CTA, replicas)] per launch group."""
+        out = []
+        g = 0
+        while True:
+            k, c, t, n = (ctypes.c_int32() for _ in range(4))
+            if lib().mcs_batch_schedule(self._h, g, ctypes.byref(k), ctypes.byref(c), ctypes.byref(t),
+                                        ctypes.byref(n)) != 0:
+                return out
+            out.append((self.SCHEDULES.get(k.value, str(k.value)), c.value, t.value, n.value))
+            g += 1
 
     def memory(self):
         dev = ctypes.c_uint64()

@@ -302,7 +302,10 @@ __global__ void __launch_bounds__(1024) k_cluster_metro(Rep *reps, const int *id
                     if (d > R.acc[A_DRIFT]) R.acc[A_DRIFT] = d;
                     R.acc[A_ECUR] = Ef;
                 }
-                on_accumulate<DIM>(R, F, R.acc[A_ECUR], m);
+            }
+            if (tid < 32) {
+                __syncwarp();
+                on_accumulate_lanes<DIM>(R, F, R.acc[A_ECUR], m, tid, 32);
             }
         }
         // spin frame: every CTA writes its own rows

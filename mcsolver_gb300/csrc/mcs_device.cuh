@@ -251,18 +251,37 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double *red, double *o
 }
 // FP32 inside a warp (32 per-thread partials), FP64 across the warps: the
 // device's FP64 rate is a small fraction of its FP32 rate, so per-lane FP64
-// arithmetic is kept out of the reduction tree.
+// arithmetic is kept out of the reduction tree.  Inside the warp the K values
+// are reduced by recursive halving (reduce-scatter): at each xor step a lane
+// keeps half of its values, adds the partner's copy of that half and sends the
+// other half, so K values cost about K shuffles instead of 5 K; afterwards
+// lane l holds the warp's sum of value l.
 template <int K>
 __device__ __forceinline__ void block_sum_f(float (&v)[K], double *red, double *out)
 {
+    static_assert(K >= 1 && K <= 32, "block_sum_f reduces at most 32 values");
+    constexpr int P = K <= 1 ? 1 : K <= 2 ? 2 : K <= 4 ? 4 : K <= 8 ? 8 : K <= 16 ? 16 : 32;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    float x[P];
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-        float x = v[k];
+    for (int k = 0; k < P; ++k) x[k] = k < K ? v[k] : 0.f;
+    // halving steps over the value set: widths P/2, P/4, ..., 1 at lane bits log2(P)-1 .. 0
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) red[wid * K + k] = (double)x;
+    for (int w = P / 2; w >= 1; w >>= 1) {
+        const bool up = (lane & w) != 0;
+#pragma unroll
+        for (int j = 0; j < w; ++j) {
+            const float send = up ? x[j] : x[j + w];
+            const float keep = up ? x[j + w] : x[j];
+            x[j] = keep + __shfl_xor_sync(0xffffffffu, send, w);
+        }
     }
+    // lanes that differ above bit log2(P) hold partial sums of the same value
+    float y = x[0];
+#pragma unroll
+    for (int o = P; o < 32; o <<= 1) y += __shfl_xor_sync(0xffffffffu, y, o);
+    const int idx = lane & (P - 1);
+    if (lane < P && idx < K) red[wid * K + idx] = (double)y;
     __syncthreads();
     if (threadIdx.x < K) {
         double a = 0.0;
@@ -542,63 +561,98 @@ __device__ void on_frame(const Rep &R, const float *jt, const float *dt, const S
     }
 }
 
-// Fold one measurement frame into the FP64 accumulators (one thread).
-// Follows heisenbergLib.c:678-830 / xyLib.c:606-757 in FP64.
+// Fold one measurement frame into the FP64 accumulators.  Follows
+// heisenbergLib.c:678-830 / xyLib.c:606-757 in FP64.  The work is split into
+// independent items over `nl` lanes (lane < nl; every lane computes the few
+// shared scalars itself), so a warp folds a frame in the latency of one item
+// rather than of the whole list; nl = 1 is the serial fold.  The lanes must
+// see F and R.acc[A_ECUR] (shared memory) before the call.
 template <int DIM>
-__device__ void on_accumulate(Rep &R, const double *F, double E, long long m)
+__device__ void on_accumulate_lanes(Rep &R, const double *F, double E, long long m, int lane, int nl)
 {
     double *acc = R.acc;
     const double inl = R.inv_nl;
-    double tx = F[F_TOT], ty = F[F_TOT + 1], tz = DIM == 3 ? F[F_TOT + 2] : 0.0;
-    double dx = tx, dy = ty, dz = tz;
-    double len = sqrt(dx * dx + dy * dy + dz * dz);
-    if (len >= 1e-5) { double il = 1.0 / len; dx *= il; dy *= il; dz *= il; }
-    double six = F[F_SI], siy = F[F_SI + 1], siz = DIM == 3 ? F[F_SI + 2] : 0.0;
-    double sjx = F[F_SJ], sjy = F[F_SJ + 1], sjz = DIM == 3 ? F[F_SJ + 2] : 0.0;
-    acc[A_SIZ] += (dx * six + dy * siy + dz * siz) * inl;
-    acc[A_SJZ] += (dx * sjx + dy * sjy + dz * sjz) * inl;
-    acc[A_STZ] += (dx * tx + dy * ty + dz * tz) * inl;
-    acc[A_SIH] += (DIM == 3 ? siz : six) * inl;
-    acc[A_SJH] += (DIM == 3 ? sjz : sjx) * inl;
-    acc[A_STH] += (DIM == 3 ? tz : tx) * inl;
-    double M = (DIM == 3) ? sqrt(tx * tx + ty * ty + tz * tz) * inl : sqrt(six * six + siy * siy) * inl;
-    const double M2 = M * M;
-    acc[A_M2] += M2;
-    acc[A_M4] += M2 * M2;
-    acc[A_MTOT] += M;
-    acc[A_MDM] += acc[A_MPREV] * M;
-    acc[A_MPREV] = M;
-    acc[A_SI] += fabs(six * inl); acc[A_SI + 1] += fabs(siy * inl); acc[A_SI + 2] += fabs(siz * inl);
-    acc[A_SJ] += fabs(sjx * inl); acc[A_SJ + 1] += fabs(sjy * inl); acc[A_SJ + 2] += fabs(sjz * inl);
-    acc[A_SIJ] += F[F_SIJ] * inl;
-    double e = E * R.inv_N;
-    acc[A_E] += e;
-    acc[A_E2] += e * e;
-    for (int k = 0; k < 3; ++k) {
-        acc[A_SIR + k] += fabs(F[F_SIR + k] * R.inv_ci);
-        acc[A_SJR + k] += fabs(F[F_SJR + k] * R.inv_cj);
-    }
-    acc[A_SIJR] += F[F_SIJR] * R.inv_cij;
-    double er = (F[F_ERB] * 0.5 + F[F_ERO]) * R.inv_nr;
-    acc[A_ER] += er;
-    acc[A_ER2] += er * er;
-    if (DIM == 3) acc[A_Q] += F[F_Q] * (1.0 / (MCS_PI_REF * 4));
+    const double tx = F[F_TOT], ty = F[F_TOT + 1], tz = DIM == 3 ? F[F_TOT + 2] : 0.0;
+    const double six = F[F_SI], siy = F[F_SI + 1], siz = DIM == 3 ? F[F_SI + 2] : 0.0;
+    const double sjx = F[F_SJ], sjy = F[F_SJ + 1], sjz = DIM == 3 ? F[F_SJ + 2] : 0.0;
     const int G = R.ngroup;
-    if (G > 0) {
-        double gx[MCS_MAXG + 1], gy[MCS_MAXG + 1], gz[MCS_MAXG + 1];
-        for (int g = 0; g < G; ++g) { gx[g] = F[F_G + 3 * g]; gy[g] = F[F_G + 3 * g + 1]; gz[g] = DIM == 3 ? F[F_G + 3 * g + 2] : 0.0; }
-        gx[G] = tx * inl; gy[G] = ty * inl; gz[G] = tz * inl;
-        for (int a = 0; a <= G; ++a)
-            for (int b = 0; b <= G; ++b) {
-                double d = gx[a] * gx[b] + gy[a] * gy[b] + gz[a] * gz[b];
-                acc[A_GRP + a * (G + 1) + b] += d;
-                if (a == b) acc[A_GRP + (G + 1) * (G + 1) + a] += d * d;
+    const int nitem = 12 + (G > 0 ? (G + 1) * (G + 1) : 0);
+    for (int it = lane; it < nitem; it += nl) {
+        switch (it) {
+        case 0: {
+            double dx = tx, dy = ty, dz = tz;
+            const double len = sqrt(dx * dx + dy * dy + dz * dz);
+            if (len >= 1e-5) { const double il = 1.0 / len; dx *= il; dy *= il; dz *= il; }
+            acc[A_SIZ] += (dx * six + dy * siy + dz * siz) * inl;
+            acc[A_SJZ] += (dx * sjx + dy * sjy + dz * sjz) * inl;
+            acc[A_STZ] += (dx * tx + dy * ty + dz * tz) * inl;
+            break;
+        }
+        case 1:
+            acc[A_SIH] += (DIM == 3 ? siz : six) * inl;
+            acc[A_SJH] += (DIM == 3 ? sjz : sjx) * inl;
+            acc[A_STH] += (DIM == 3 ? tz : tx) * inl;
+            break;
+        case 2: {
+            const double M = (DIM == 3) ? sqrt(tx * tx + ty * ty + tz * tz) * inl : sqrt(six * six + siy * siy) * inl;
+            const double M2 = M * M;
+            acc[A_M2] += M2;
+            acc[A_M4] += M2 * M2;
+            acc[A_MTOT] += M;
+            acc[A_MDM] += acc[A_MPREV] * M;
+            acc[A_MPREV] = M;
+            if (R.series) {
+                double *sr = R.series + (size_t)m * MCS_NSER;
+                const double e = E * R.inv_N;
+                sr[0] = e; sr[1] = M; sr[2] = (F[F_ERB] * 0.5 + F[F_ERO]) * R.inv_nr; sr[3] = F[F_SIJ] * inl;
             }
+            break;
+        }
+        case 3: acc[A_SI] += fabs(six * inl); acc[A_SI + 1] += fabs(siy * inl); acc[A_SI + 2] += fabs(siz * inl); break;
+        case 4: acc[A_SJ] += fabs(sjx * inl); acc[A_SJ + 1] += fabs(sjy * inl); acc[A_SJ + 2] += fabs(sjz * inl); break;
+        case 5: acc[A_SIJ] += F[F_SIJ] * inl; break;
+        case 6: {
+            const double e = E * R.inv_N;
+            acc[A_E] += e;
+            acc[A_E2] += e * e;
+            break;
+        }
+        case 7:
+            for (int k = 0; k < 3; ++k) {
+                acc[A_SIR + k] += fabs(F[F_SIR + k] * R.inv_ci);
+                acc[A_SJR + k] += fabs(F[F_SJR + k] * R.inv_cj);
+            }
+            break;
+        case 8: acc[A_SIJR] += F[F_SIJR] * R.inv_cij; break;
+        case 9: {
+            const double er = (F[F_ERB] * 0.5 + F[F_ERO]) * R.inv_nr;
+            acc[A_ER] += er;
+            acc[A_ER2] += er * er;
+            break;
+        }
+        case 10:
+            if (DIM == 3) acc[A_Q] += F[F_Q] * (1.0 / (MCS_PI_REF * 4));
+            break;
+        case 11: break;
+        default: {
+            // spin.spin between groups a and b (group G is the whole lattice / N)
+            const int idx = it - 12, ga = idx / (G + 1), gb = idx - ga * (G + 1);
+            const double ax = ga < G ? F[F_G + 3 * ga] : tx * inl, ay = ga < G ? F[F_G + 3 * ga + 1] : ty * inl;
+            const double az = DIM == 3 ? (ga < G ? F[F_G + 3 * ga + 2] : tz * inl) : 0.0;
+            const double bx = gb < G ? F[F_G + 3 * gb] : tx * inl, by = gb < G ? F[F_G + 3 * gb + 1] : ty * inl;
+            const double bz = DIM == 3 ? (gb < G ? F[F_G + 3 * gb + 2] : tz * inl) : 0.0;
+            const double d = ax * bx + ay * by + az * bz;
+            acc[A_GRP + idx] += d;
+            if (ga == gb) acc[A_GRP + (G + 1) * (G + 1) + ga] += d * d;
+        }
+        }
     }
-    if (R.series) {
-        double *s = R.series + (size_t)m * MCS_NSER;
-        s[0] = e; s[1] = M; s[2] = er; s[3] = F[F_SIJ] * inl;
-    }
+}
+
+template <int DIM>
+__device__ __forceinline__ void on_accumulate(Rep &R, const double *F, double E, long long m)
+{
+    on_accumulate_lanes<DIM>(R, F, E, m, 0, 1);
 }
 
 // ------------------------------------------------------------------ Ising frame

@@ -350,6 +350,9 @@ Batch::~Batch()
     if (ev1) cudaEventDestroy(ev1);
     if (ev_a) cudaEventDestroy(ev_a);
     if (ev_b) cudaEventDestroy(ev_b);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    for (cudaStream_t g : gstreams) cudaStreamDestroy(g);
+    for (cudaEvent_t e : gevents) cudaEventDestroy(e);
 }
 
 int Batch::init(int dev)
@@ -368,6 +371,7 @@ int Batch::ensure_streams()
     CUDA_TRY(cudaEventCreate(&ev1));
     CUDA_TRY(cudaEventCreate(&ev_a));
     CUDA_TRY(cudaEventCreate(&ev_b));
+    CUDA_TRY(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
     return MCS_OK;
 }
 
@@ -486,6 +490,116 @@ cudaError_t Batch::tiled_unit(Group &G, cudaStream_t s, long long *nl)
     return e;
 }
 
+// Load balancing.  A launch of the resident kernel lasts as long as its
+// largest replica (one CTA each), so one big replica among small ones leaves
+// most SMs idle.  The balancer estimates the device time of a placement as
+//     max( longest per-replica critical path, total SM-seconds / #SMs )
+// with, per replica of c site updates,
+//     resident:   critical c / r_cta,            SM-seconds c / r_cta
+//     cluster C:  critical c / (e C r_cta),      SM-seconds c / (e r_cta)
+//     tiled:      critical 0,                    SM-seconds c #SMs / r_dev(S)
+// (r_cta = one CTA's rate, e = cluster efficiency, r_dev(S) = the tiled
+// schedule's whole-device rate for S sites in flight, r_max S / (S + S_half):
+// short launches are latency-bound; rates measured on GB300 for square
+// lattices), and
+// moves the replicas on the critical path one step (resident -> cluster 2 ->
+// 4 -> 8 -> tiled; resident -> tiled where the cluster kernel does not apply)
+// while the estimate falls.  With the autotuner on, cluster sizes stay the
+// autotuner's choice and only the move to tiled is decided here.
+void Batch::place_replicas(int max_smem)
+{
+    int nsm = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || nsm < 1) {
+        cudaGetLastError();
+        nsm = 1;
+    }
+    static const double r_cta[4] = {0, 0.40e9, 0.85e9, 0.65e9};   // by spin dimension
+    static const double r_max[4] = {0, 2.5e10, 1.8e10, 0.86e10};
+    static const double s_half[4] = {0, 6.0e5, 1.0e6, 5.3e5};
+    const double e = 0.8;
+    struct P { int i; int opt; double c; std::vector<int> opts; };
+    std::vector<P> ps;
+    for (int i = 0; i < (int)replicas.size(); ++i) {
+        Replica &r = *replicas[i];
+        r.pref_C = 0;
+        if (r.requested_schedule != 0 || r.hm.alg != 0 || !(r.schedule == 2 || r.schedule == 6)) continue;
+        P q;
+        q.i = i;
+        q.c = (double)r.hm.N * (double)std::max<long long>(1, r.hm.units_total - r.rep.u);
+        // options in order: 1 = resident, 2/4/8 = cluster, 0 = tiled
+        const bool clusterable = r.hm.cluster_ok && r.hm.geom == MCS_GEOM_SQUARE && r.hm.dim > 1 && cluster_override != 1;
+        if (clusterable && !no_autotune) {
+            // the autotuner picks its cluster size; counted here as a cluster of 4
+            q.opts.push_back(-1);
+            q.opt = 0;
+            ps.push_back(q);
+            continue;
+        }
+        if (resident_smem_bytes(r.rep) <= max_smem) q.opts.push_back(1);
+        if (clusterable)
+            for (int C : {2, 4, 8}) {
+                const int Lx = r.hm.Lx;
+                if (Lx % C || (Lx / C) % 2 || cluster_smem_bytes(r.rep, C) > max_smem) continue;
+                if (cluster_override > 1 && C != cluster_override) continue;
+                q.opts.push_back(C);
+            }
+        if (r.hm.N >= 8192 || q.opts.empty()) q.opts.push_back(0);
+        q.opt = 0;
+        ps.push_back(q);
+    }
+    if (ps.empty()) return;
+    auto crit = [&](const P &q) {
+        const int o = q.opts[q.opt], d = replicas[q.i]->hm.dim;
+        if (o < 0) return q.c / (e * 4 * r_cta[d]);
+        return o == 0 ? 0.0 : (o == 1 ? q.c / r_cta[d] : q.c / (e * o * r_cta[d]));
+    };
+    double tiled_sites[4] = {0, 0, 0, 0};
+    auto smsec = [&](const P &q) {
+        const int o = q.opts[q.opt], d = replicas[q.i]->hm.dim;
+        if (o < 0) return q.c / (e * r_cta[d]);
+        if (o == 0) {
+            const double S = std::max(1.0, tiled_sites[d]);
+            return q.c * nsm / (r_max[d] * S / (S + s_half[d]));
+        }
+        return o == 1 ? q.c / r_cta[d] : q.c / (e * r_cta[d]);
+    };
+    auto estimate = [&]() {
+        for (int d = 0; d < 4; ++d) tiled_sites[d] = 0;
+        for (auto &q : ps)
+            if (q.opts[q.opt] == 0) tiled_sites[replicas[q.i]->hm.dim] += replicas[q.i]->hm.N;
+        double m = 0, t = 0;
+        for (auto &q : ps) { m = std::max(m, crit(q)); t += smsec(q); }
+        return std::max(m, t / nsm);
+    };
+    double best = estimate();
+    for (int it = 0; it < 64; ++it) {
+        double m = 0;
+        for (auto &q : ps) m = std::max(m, crit(q));
+        if (m <= 0) break;
+        std::vector<int> moved;
+        bool stuck = false;
+        for (int k = 0; k < (int)ps.size(); ++k) {
+            P &q = ps[k];
+            if (crit(q) < 0.95 * m) continue;
+            if (q.opt + 1 >= (int)q.opts.size()) { stuck = true; break; }
+            ++q.opt;
+            moved.push_back(k);
+        }
+        const double now = stuck ? best + 1 : estimate();
+        if (now < best) { best = now; continue; }
+        for (int k : moved) --ps[k].opt;
+        break;
+    }
+    for (auto &q : ps) {
+        Replica &r = *replicas[q.i];
+        const int o = q.opts[q.opt];
+        if (o < 0) continue;
+        if (o == 0) r.schedule = 3;
+        else if (o == 1) r.schedule = 2;
+        else if (no_autotune) { r.schedule = 6; r.pref_C = o; }
+    }
+}
+
 int Batch::prepare()
 {
     if (prepared) return MCS_OK;
@@ -501,8 +615,9 @@ int Batch::prepare()
     for (int i = 0; i < nrep; ++i) {
         Replica &r = *replicas[i];
         r.schedule = choose_schedule(r, cluster_override > 1 ? 6 : r.requested_schedule, max_smem);
-        host[i] = r.rep;
     }
+    if (balance) place_replicas(max_smem);
+    for (int i = 0; i < nrep; ++i) host[i] = replicas[i]->rep;
     CUDA_TRY(cudaMalloc(&d_reps, nrep * sizeof(Rep)));
     CUDA_TRY(cudaMemcpy(d_reps, host.data(), nrep * sizeof(Rep), cudaMemcpyHostToDevice));
     // initial energies / exact sums
@@ -522,19 +637,29 @@ int Batch::prepare()
             }
         for (int i : all) replicas[i]->initialized = true;
     }
-    // groups
+    // groups; every replica joins exactly one (a cluster group that falls
+    // back to the tiled schedule keeps its replicas)
+    std::vector<char> grouped(nrep, 0);
     for (int kind : {2, 6, 3, 1, 4, 5})
         for (int d = 1; d <= 3; ++d)
             for (int g = 0; g <= 1; ++g) {
                 std::vector<int> ids;
                 for (int i = 0; i < nrep; ++i) {
                     Replica &r = *replicas[i];
-                    if (r.schedule == kind && r.hm.dim == d && r.hm.geom == g) ids.push_back(i);
+                    if (!grouped[i] && r.schedule == kind && r.hm.dim == d && r.hm.geom == g) ids.push_back(i);
                 }
+                for (int i : ids) grouped[i] = 1;
                 if (ids.empty()) continue;
                 std::vector<std::vector<int>> sets;
                 if (kind == 1) for (int id : ids) sets.push_back({id});
-                else sets.push_back(ids);
+                else if (kind == 6) {
+                    // one launch configuration per group: split by the balancer's cluster size
+                    for (int C : {0, 2, 4, 8}) {
+                        std::vector<int> sub;
+                        for (int id : ids) if (replicas[id]->pref_C == C) sub.push_back(id);
+                        if (!sub.empty()) sets.push_back(sub);
+                    }
+                } else sets.push_back(ids);
                 for (auto &set : sets) {
                     std::unique_ptr<Group> G(new Group());
                     G->kind = kind; G->dim = d; G->geom = g; G->ids = set;
@@ -571,8 +696,10 @@ int Batch::prepare()
                         for (int id : set) all_cl &= replicas[id]->hm.cluster_ok != 0;
                         if (kind == 2) G->candidates.push_back({1, G->threads});
                         if (all_cl && cluster_override != 1) {
+                            const int pc = kind == 6 ? replicas[set[0]]->pref_C : 0;
                             for (int C : {2, 4, 8}) {
                                 if (cluster_override > 1 && C != cluster_override) continue;
+                                if (pc > 0 && C != pc) continue;
                                 bool ok = true;
                                 size_t sm = 0;
                                 for (int id : set) {
@@ -610,6 +737,8 @@ int Batch::prepare()
                     groups.push_back(std::move(G));
                 }
             }
+    for (int i = 0; i < nrep; ++i)
+        if (!grouped[i]) { set_error("internal: replica without a kernel group"); return MCS_EINVAL; }
     prepared = true;
     return MCS_OK;
 }
@@ -619,60 +748,79 @@ int Batch::advance(long long units)
     int rc = prepare();
     if (rc != MCS_OK) return rc;
     if (replicas.empty()) return MCS_OK;
+    const bool multi = groups.size() > 1;
+    while (multi && gstreams.size() < groups.size()) {
+        cudaStream_t gs = nullptr;
+        CUDA_TRY(cudaStreamCreateWithFlags(&gs, cudaStreamNonBlocking));
+        gstreams.push_back(gs);
+        cudaEvent_t ge = nullptr;
+        CUDA_TRY(cudaEventCreateWithFlags(&ge, cudaEventDisableTiming));
+        gevents.push_back(ge);
+    }
     CUDA_TRY(cudaEventRecord(ev0, stream));
-    for (auto &Gp : groups) {
-        Group &G = *Gp;
-        long long todo = std::min(units, G.max_units - G.done_units);
+    // 1. autotuner: time each candidate (cluster size, block size) of an
+    //    untuned group on a few real units, alone on the batch stream, and keep
+    //    the fastest
+    std::vector<long long> pre(groups.size(), 0);
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+        Group &G = *groups[gi];
+        const long long todo = std::min(units, G.max_units - G.done_units);
+        if (todo <= 0 || !(G.kind == 2 || G.kind == 6) || G.tuned) continue;
+        long long u = 0;
+        const long long probe = std::max<long long>(1, std::min<long long>(4, todo / (2 * (long long)G.candidates.size() + 1)));
+        G.cand_ms.assign(G.candidates.size(), 1e30);
+        for (size_t ci = 0; ci < G.candidates.size() && u + probe <= todo; ++ci) {
+            int C = G.candidates[ci].first, th = G.candidates[ci].second;
+            CUDA_TRY(cudaEventRecord(ev_a, stream));
+            cudaError_t e = launch_group(G, C, th, probe, stream);
+            if (e != cudaSuccess) { cudaGetLastError(); continue; }
+            CUDA_TRY(cudaEventRecord(ev_b, stream));
+            CUDA_TRY(cudaEventSynchronize(ev_b));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev_a, ev_b);
+            G.cand_ms[ci] = ms / probe;
+            launches++;
+            u += probe;
+        }
+        size_t best = 0;
+        for (size_t ci = 1; ci < G.candidates.size(); ++ci) if (G.cand_ms[ci] < G.cand_ms[best]) best = ci;
+        G.C = G.candidates[best].first;
+        G.threads = G.candidates[best].second;
+        G.tuned = 1;
+        pre[gi] = u;
+    }
+    // 2. the rest: each group on its own stream, side by side on the device
+    if (multi) CUDA_TRY(cudaEventRecord(ev_fork, stream));
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+        Group &G = *groups[gi];
+        const long long todo = std::min(units, G.max_units - G.done_units);
         if (todo <= 0) continue;
+        cudaStream_t gs = multi ? gstreams[gi] : stream;
+        if (multi) CUDA_TRY(cudaStreamWaitEvent(gs, ev_fork, 0));
         if (G.kind == 4 || G.kind == 5) {
             for (long long u = 0; u < todo; u += G.chunk) {
                 long long n = std::min(G.chunk, todo - u);
                 cudaError_t e = launch_wolff(G.dim, G.geom, d_reps, G.d_ids, (int)G.ids.size(), G.threads, G.smem, n,
-                                             G.kind == 5, stream);
+                                             G.kind == 5, gs);
                 if (e != cudaSuccess) { set_error(std::string("wolff launch: ") + cudaGetErrorString(e)); return MCS_ECUDA; }
                 launches++;
             }
         } else if (G.kind == 2 || G.kind == 6) {
-            long long u = 0;
-            // autotuner: time each candidate (cluster size, block size) on a
-            // few real units and keep the fastest
-            if (!G.tuned) {
-                const long long probe = std::max<long long>(1, std::min<long long>(4, todo / (2 * (long long)G.candidates.size() + 1)));
-                G.cand_ms.assign(G.candidates.size(), 1e30);
-                for (size_t ci = 0; ci < G.candidates.size() && u + probe <= todo; ++ci) {
-                    int C = G.candidates[ci].first, th = G.candidates[ci].second;
-                    CUDA_TRY(cudaEventRecord(ev_a, stream));
-                    cudaError_t e = launch_group(G, C, th, probe, stream);
-                    if (e != cudaSuccess) { cudaGetLastError(); continue; }
-                    CUDA_TRY(cudaEventRecord(ev_b, stream));
-                    CUDA_TRY(cudaEventSynchronize(ev_b));
-                    float ms = 0;
-                    cudaEventElapsedTime(&ms, ev_a, ev_b);
-                    G.cand_ms[ci] = ms / probe;
-                    launches++;
-                    u += probe;
-                }
-                size_t best = 0;
-                for (size_t ci = 1; ci < G.candidates.size(); ++ci) if (G.cand_ms[ci] < G.cand_ms[best]) best = ci;
-                G.C = G.candidates[best].first;
-                G.threads = G.candidates[best].second;
-                G.tuned = 1;
-            }
-            for (; u < todo; u += G.chunk) {
+            for (long long u = pre[gi]; u < todo; u += G.chunk) {
                 long long n = std::min(G.chunk, todo - u);
-                cudaError_t e = launch_group(G, G.C, G.threads, n, stream);
+                cudaError_t e = launch_group(G, G.C, G.threads, n, gs);
                 if (e != cudaSuccess) { set_error(std::string("resident/cluster launch: ") + cudaGetErrorString(e)); return MCS_ECUDA; }
                 launches++;
             }
         } else if (G.kind == 3 && todo >= 8) {
             if (!G.exec) {
-                G.K = (int)std::min<long long>(32, std::max<long long>(1, todo));
+                G.K = (int)std::min<long long>(32, std::max<long long>(1, std::max(todo, G.max_units - G.done_units)));
                 long long nl = 0;
                 CUDA_TRY(cudaStreamBeginCapture(stream2, cudaStreamCaptureModeThreadLocal));
                 for (int k = 0; k < G.K; ++k) {
                     cudaError_t e = tiled_unit(G, stream2, &nl);
                     if (e != cudaSuccess) {
-                        cudaGraph_t g0;
+                        cudaGraph_t g0 = nullptr;
                         cudaStreamEndCapture(stream2, &g0);
                         if (g0) cudaGraphDestroy(g0);
                         set_error(std::string("capture: ") + cudaGetErrorString(e));
@@ -685,14 +833,18 @@ int Batch::advance(long long units)
             }
             long long u = 0;
             for (; u + G.K <= todo; u += G.K) {
-                CUDA_TRY(cudaGraphLaunch(G.exec, stream));
+                CUDA_TRY(cudaGraphLaunch(G.exec, gs));
                 launches += G.per_graph;
             }
-            for (; u < todo; ++u) CUDA_TRY(tiled_unit(G, stream, &launches));
+            for (; u < todo; ++u) CUDA_TRY(tiled_unit(G, gs, &launches));
         } else {
-            for (long long u = 0; u < todo; ++u) CUDA_TRY(tiled_unit(G, stream, &launches));
+            for (long long u = 0; u < todo; ++u) CUDA_TRY(tiled_unit(G, gs, &launches));
         }
         G.done_units += todo;
+        if (multi) {
+            CUDA_TRY(cudaEventRecord(gevents[gi], gs));
+            CUDA_TRY(cudaStreamWaitEvent(stream, gevents[gi], 0));
+        }
     }
     CUDA_TRY(cudaEventRecord(ev1, stream));
     cudaError_t e = cudaStreamSynchronize(stream);
@@ -704,17 +856,36 @@ int Batch::advance(long long units)
     return MCS_OK;
 }
 
-int Batch::collect()
+int Batch::sync_descriptors()
 {
     const int nrep = (int)replicas.size();
+    if (!prepared || !d_reps || nrep == 0) return MCS_OK;
     std::vector<Rep> host(nrep);
-    if (nrep) CUDA_TRY(cudaMemcpy(host.data(), d_reps, nrep * sizeof(Rep), cudaMemcpyDeviceToHost));
-    final_reps = host;
+    CUDA_TRY(cudaMemcpy(host.data(), d_reps, nrep * sizeof(Rep), cudaMemcpyDeviceToHost));
     for (int i = 0; i < nrep; ++i) {  // progress travels with the replica
         replicas[i]->rep.u = host[i].u;
         replicas[i]->rep.m = host[i].m;
         replicas[i]->rep.frames_written = host[i].frames_written;
     }
+    final_reps.swap(host);
+    return MCS_OK;
+}
+
+void Batch::release_groups()
+{
+    groups.clear();
+    if (d_reps) cudaFree(d_reps);
+    if (d_all) cudaFree(d_all);
+    d_reps = nullptr;
+    d_all = nullptr;
+    prepared = false;
+}
+
+int Batch::collect()
+{
+    const int nrep = (int)replicas.size();
+    int rc = sync_descriptors();
+    if (rc != MCS_OK) return rc;
     site_updates = 0;
     for (int i = 0; i < nrep; ++i) {
         long long st[S_NSTAT];
@@ -821,6 +992,18 @@ int mcs_batch_stats(mcs_batch *b, double *device_ms, int64_t *site_updates, int3
     if (launches) *launches = (int32_t)b->b.launches;
     return MCS_OK;
 }
+int mcs_batch_schedule(mcs_batch *b, int32_t group, int32_t *kind, int32_t *cluster, int32_t *threads,
+                       int32_t *replicas)
+{
+    if (!b) return MCS_EINVAL;
+    if (group < 0 || group >= (int32_t)b->b.groups.size()) { set_error("group index out of range"); return MCS_EINVAL; }
+    const Group &G = *b->b.groups[group];
+    if (kind) *kind = G.kind;
+    if (cluster) *cluster = G.C;
+    if (threads) *threads = G.threads;
+    if (replicas) *replicas = (int32_t)G.ids.size();
+    return MCS_OK;
+}
 int mcs_batch_memory(mcs_batch *b, uint64_t *device_bytes, uint64_t *readback_bytes)
 {
     if (!b) return MCS_EINVAL;
@@ -868,6 +1051,7 @@ extern "C" int mcs_pt_create(const mcs_problem *problem, const mcs_options *opti
     if (!options) options = &def;
     std::unique_ptr<mcs_pt> pt(new mcs_pt());
     int rc = pt->b.init(options->device);
+    pt->b.balance = 0;  // the exchange kernel needs every temperature in one kernel group
     if (rc != MCS_OK) return rc;
     pt->nt = n_temps;
     pt->seed = options->seed;

@@ -30,6 +30,7 @@ struct Replica {
     int recheck = 32;
     int device = 0;
     bool initialized = false;          // initial-state kernel has run
+    int pref_C = 0;                    // cluster size chosen by the load balancer (0: none)
     std::vector<unsigned char> staging; // host image of the arena until upload
     ~Replica();
 };
@@ -84,10 +85,13 @@ struct Batch {
     std::vector<std::unique_ptr<Group>> groups;
     double last_ms = 0;
     cudaStream_t stream = nullptr, stream2 = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_a = nullptr, ev_b = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_a = nullptr, ev_b = nullptr, ev_fork = nullptr;
     std::mutex add_mutex;       // mcs_batch_add may be called from several threads
     int cluster_override = 0;   // 1: never cluster; 2/4/8: only that size
     int no_autotune = 0;
+    int balance = 1;            // place replicas by the load balancer (off for parallel tempering)
+    std::vector<cudaStream_t> gstreams;  // one stream per group: groups run side by side
+    std::vector<cudaEvent_t> gevents;
     double device_ms = 0;
     long long site_updates = 0;
     long long launches = 0;
@@ -101,9 +105,12 @@ struct Batch {
     int prepare();                 // upload descriptors, initial energies, build groups
     int advance(long long units);  // every replica runs up to `units` more units
     int collect();                 // read back descriptors and counters
+    int sync_descriptors();        // read back descriptors: progress travels with each replica
+    void release_groups();         // drop groups and descriptor arrays; the next advance re-prepares
     int run();                     // prepare + advance to completion + collect
     int result(int i, mcs_result *res);
     int setup_tiled(Group &G);
+    void place_replicas(int max_smem);
     cudaError_t tiled_unit(Group &G, cudaStream_t s, long long *nl);
     cudaError_t launch_group(Group &G, int C, int threads, long long units, cudaStream_t s);
 };

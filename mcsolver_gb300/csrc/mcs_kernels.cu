@@ -247,14 +247,15 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
             } else {
                 const bool efull = (m % R.recheck) == 0;
                 on_frame<DIM, GEOM>(R, jt, dt, S, 0, max(max(N, R.nlat), max(R.n_rorb, R.ncirc)), efull, red, F, majc);
-                if (tid == 0) {
-                    if (efull) {
-                        double Ef = F[F_EFB] / 2 + F[F_EFO];
-                        double d = fabs(R.acc[A_ECUR] - Ef);
-                        if (d > R.acc[A_DRIFT]) R.acc[A_DRIFT] = d;
-                        R.acc[A_ECUR] = Ef;
-                    }
-                    on_accumulate<DIM>(R, F, R.acc[A_ECUR], m);
+                if (tid == 0 && efull) {
+                    double Ef = F[F_EFB] / 2 + F[F_EFO];
+                    double d = fabs(R.acc[A_ECUR] - Ef);
+                    if (d > R.acc[A_DRIFT]) R.acc[A_DRIFT] = d;
+                    R.acc[A_ECUR] = Ef;
+                }
+                if (tid < 32) {
+                    __syncwarp();
+                    on_accumulate_lanes<DIM>(R, F, R.acc[A_ECUR], m, tid, 32);
                 }
             }
             if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) {
@@ -442,16 +443,17 @@ __global__ void __launch_bounds__(256) k_tiled_finalize(Rep *reps, const int *id
                 for (int k = 0; k < MCS_MAXT + MCS_MAXC; ++k) Fi[k] = (long long)F[4 + k];
                 signed char *s = (signed char *)R.spins;
                 is_accumulate(R, F, Fi, s[R.last_site], m);
-            } else {
-                if ((m % R.recheck) == 0) {
-                    double Ef = F[F_EFB] / 2 + F[F_EFO];
-                    double d = fabs(R.acc[A_ECUR] - Ef);
-                    if (d > R.acc[A_DRIFT]) R.acc[A_DRIFT] = d;
-                    R.acc[A_ECUR] = Ef;
-                }
-                if (DIM == 2) on_accumulate<2>(R, F, R.acc[A_ECUR], m);
-                else on_accumulate<3>(R, F, R.acc[A_ECUR], m);
+            } else if ((m % R.recheck) == 0) {
+                double Ef = F[F_EFB] / 2 + F[F_EFO];
+                double d = fabs(R.acc[A_ECUR] - Ef);
+                if (d > R.acc[A_DRIFT]) R.acc[A_DRIFT] = d;
+                R.acc[A_ECUR] = Ef;
             }
+        }
+        if (DIM > 1 && tid < 32) {
+            __syncwarp();
+            if (DIM == 2) on_accumulate_lanes<2>(R, F, R.acc[A_ECUR], m, tid, 32);
+            else on_accumulate_lanes<3>(R, F, R.acc[A_ECUR], m, tid, 32);
         }
         if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) {
             float *fb = R.frame_buf + (size_t)R.frames_written * R.N * 3;

@@ -258,26 +258,23 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
         if (qv.empty()) qv.push_back(0.0);
         m->nclass = (int)qv.size();
         for (int c = 0; c < m->nclass; ++c) m->Q[c] = qv[c];
-        std::map<std::vector<double>, int> tmap;
+        ClassTable<1 + MCS_MAXC> tcls;
         std::vector<std::vector<int>> tcount;
         std::vector<double> tS;
         m->stype.assign(N, 0);
         for (int k = 0; k < N; ++k) {
             int i = sites[k];
-            std::vector<double> key(1 + MCS_MAXC, 0.0);
+            double key[1 + MCS_MAXC] = {};
             key[0] = fabs(p->init_spin[i]);
             for (int l = 0; l < p->nlink[i]; ++l) key[1 + linkcls[(size_t)i * z + l]] += 1.0;
-            auto it = tmap.find(key);
-            int t;
-            if (it == tmap.end()) {
-                t = (int)tS.size();
-                tmap[key] = t;
+            const int t = tcls.find_or_add(key);
+            if (t >= MCS_MAXT) FAIL(MCS_EUNSUPPORTED, "Ising model with more than 4 site types");
+            if (t == (int)tS.size()) {
                 tS.push_back(key[0]);
                 std::vector<int> cnt(MCS_MAXC, 0);
                 for (int c = 0; c < MCS_MAXC; ++c) cnt[c] = (int)key[1 + c];
                 tcount.push_back(cnt);
-            } else t = it->second;
-            if (t >= MCS_MAXT) FAIL(MCS_EUNSUPPORTED, "Ising model with more than 4 site types");
+            }
             m->stype[k] = (uint8_t)t;
         }
         m->ntype = (int)tS.size();
@@ -329,18 +326,19 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
                 }
                 m->wthr[c][sg] = thr;
             }
-        // exactness of the incremental bookkeeping: no self links, symmetric couplings
+        // exactness of the incremental bookkeeping: no self links, and every
+        // directed link i->j of class c has a reverse link j->i of class c
         bool ok = true;
-        std::multiset<std::pair<std::pair<int, int>, int>> fw;
         for (int i = 0; i < N && ok; ++i)
-            for (int l = 0; l < p->nlink[i]; ++l) {
-                int j = p->linked_orb[(size_t)i * z + l];
+            for (int l = 0; l < p->nlink[i] && ok; ++l) {
+                const int j = p->linked_orb[(size_t)i * z + l];
+                const int c = linkcls[(size_t)i * z + l];
                 if (j == i) { ok = false; break; }
-                fw.insert({{i, j}, linkcls[(size_t)i * z + l]});
+                bool rev = false;
+                for (int q = 0; q < p->nlink[j] && !rev; ++q)
+                    rev = p->linked_orb[(size_t)j * z + q] == i && linkcls[(size_t)j * z + q] == c;
+                ok = rev;
             }
-        if (ok)
-            for (auto &e : fw)
-                if (fw.find({{e.first.second, e.first.first}, e.second}) == fw.end()) { ok = false; break; }
         m->exact_ok = ok ? 1 : 0;
     }
 

@@ -1,12 +1,17 @@
 // mcs_server.cpp -- continuous-batching request loop (C ABI mcs_server_*).
 //
-// submit(): compiles the request on the host (validation, colouring, tables,
-//           the arena image) and queues it; nothing touches the device yet.
+// submit(): compiles the request on the caller's thread (validation,
+//           colouring, tables, the arena image) and queues it; nothing touches
+//           the device yet.  submit() and poll() may be called from any number
+//           of threads while another thread runs step(): they hold the queue
+//           lock only to insert or look up, never across device work.
 // step():   1. admits queued requests in arrival order while a slot is free and
 //              the HBM budget holds the request's arena (allocation + upload);
-//           2. advances every active request by a chunk of units in one batched
-//              launch sequence (the kernels of mcs_batch_*), so requests that
-//              arrived at different times run side by side on the device;
+//           2. advances every active request in one persistent batch: its
+//              launch groups (and captured graphs) are rebuilt only when the
+//              set of active requests changes, and each step runs as many
+//              units as the chunk allows but never past the next completion,
+//              so a finished request is retired at once;
 //           3. retires requests that reached their last unit: results are kept
 //              for poll(), the arena is freed and its bytes return to the budget.
 // A request's spin trajectory depends only on its own problem and seed, so its
@@ -14,12 +19,14 @@
 #include <cuda_runtime.h>
 #include <string.h>
 
+#include <algorithm>
 #include <chrono>
 #include <deque>
 #include <memory>
 #include <mutex>
 #include <string>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "../../include/mcsgpu.h"
@@ -33,16 +40,22 @@ struct mcs_server {
     int max_slots = 0;
     uint64_t next_ticket = 1;
     long long chunk = 50;
-    std::deque<std::pair<uint64_t, std::unique_ptr<Replica>>> queue;
-    std::vector<std::pair<uint64_t, std::unique_ptr<Replica>>> active;
     struct Done {
         mcs_result r;
         std::vector<double> groups;
     };
+    // guarded by qmu: the queue, finished results, tickets not yet finished, counters
+    std::mutex qmu;
+    std::deque<std::pair<uint64_t, std::unique_ptr<Replica>>> queue;
     std::unordered_map<uint64_t, Done> done;
+    std::unordered_set<uint64_t> pending;
     uint64_t in_use = 0;
     long long site_updates = 0;
-    std::mutex mu;
+    int n_active = 0;
+    // guarded by smu: the device side (one step at a time)
+    std::mutex smu;
+    Batch batch;                       // replicas = active requests
+    std::vector<uint64_t> tickets;     // ticket of batch.replicas[i]
 };
 
 extern "C" int mcs_server_create(int32_t device, uint64_t hbm_budget_bytes, int32_t max_slots, mcs_server **out)
@@ -52,6 +65,8 @@ extern "C" int mcs_server_create(int32_t device, uint64_t hbm_budget_bytes, int3
     s->device = device;
     s->budget = hbm_budget_bytes;
     s->max_slots = max_slots;
+    s->batch.init(device);
+    s->batch.no_autotune = 1;  // membership changes often; the first candidate of each group runs
     if (const char *e = getenv("MCSGPU_SERVER_CHUNK")) s->chunk = std::max(1LL, atoll(e));
     *out = s;
     return MCS_OK;
@@ -68,9 +83,10 @@ extern "C" int mcs_server_submit(mcs_server *s, const mcs_problem *problem, cons
     int rc = build_replica(problem, options, r.get(), false);
     if (rc != MCS_OK) return rc;
     if (r->bytes + sizeof(Rep) > s->budget) { set_error("request larger than the server's HBM budget"); return MCS_ENOMEM; }
-    std::lock_guard<std::mutex> lock(s->mu);
+    std::lock_guard<std::mutex> lock(s->qmu);
     const uint64_t t = s->next_ticket++;
     s->queue.emplace_back(t, std::move(r));
+    s->pending.insert(t);
     if (ticket) *ticket = t;
     return MCS_OK;
 }
@@ -78,69 +94,107 @@ extern "C" int mcs_server_submit(mcs_server *s, const mcs_problem *problem, cons
 extern "C" int mcs_server_step(mcs_server *s, int32_t *completed)
 {
     if (!s) return MCS_EINVAL;
-    std::lock_guard<std::mutex> lock(s->mu);
+    std::lock_guard<std::mutex> slock(s->smu);
     if (completed) *completed = 0;
+    Batch &b = s->batch;
     // 1. admission by slots and HBM budget, in arrival order
-    while (!s->queue.empty() && (int)s->active.size() < s->max_slots) {
-        Replica &r = *s->queue.front().second;
-        const uint64_t need = r.bytes + sizeof(Rep);
-        if (s->in_use + need > s->budget) break;
-        int rc = upload_replica(&r);
-        if (rc != MCS_OK) return rc;
-        s->in_use += need;
-        s->active.push_back(std::move(s->queue.front()));
-        s->queue.pop_front();
-    }
-    if (s->active.empty()) return MCS_OK;
-    // 2. one chunk of units for every active request
-    Batch b;
-    b.init(s->device);
-    b.no_autotune = 1;
-    std::vector<uint64_t> tickets;
-    for (auto &a : s->active) {
-        tickets.push_back(a.first);
-        b.replicas.push_back(std::move(a.second));
-    }
-    s->active.clear();
-    int rc = b.advance(s->chunk);
-    if (rc == MCS_OK) rc = b.collect();
-    // 3. retire finished requests, keep the rest
-    int ndone = 0;
-    for (size_t i = 0; i < b.replicas.size(); ++i) {
-        std::unique_ptr<Replica> r = std::move(b.replicas[i]);
-        if (rc == MCS_OK && r->rep.u >= r->hm.units_total) {
-            mcs_server::Done d;
-            memset(&d.r, 0, sizeof d.r);
-            const int G = r->hm.ngroup;
-            d.groups.assign((size_t)(G + 1) * (G + 1) + (G + 1), 0.0);
-            d.r.group_values = d.groups.data();
-            d.r.group_capacity = (int)d.groups.size();
-            int rr = replica_results(r.get(), r->rep, &d.r);
-            d.r.group_values = nullptr;
-            d.r.frames = nullptr;
-            d.r.series = nullptr;
-            if (rr != MCS_OK) return rr;
-            s->site_updates += d.r.site_updates;
-            s->in_use -= r->bytes + sizeof(Rep);
-            s->done.emplace(tickets[i], std::move(d));
-            ++ndone;
-        } else {
-            s->active.emplace_back(tickets[i], std::move(r));
+    std::vector<std::pair<uint64_t, std::unique_ptr<Replica>>> admit;
+    {
+        std::lock_guard<std::mutex> lock(s->qmu);
+        int slots = s->max_slots - (int)b.replicas.size();
+        while (!s->queue.empty() && slots > 0) {
+            Replica &r = *s->queue.front().second;
+            const uint64_t need = r.bytes + sizeof(Rep);
+            if (s->in_use + need > s->budget) break;
+            s->in_use += need;
+            admit.push_back(std::move(s->queue.front()));
+            s->queue.pop_front();
+            --slots;
         }
     }
-    b.replicas.clear();
-    if (completed) *completed = ndone;
-    return rc;
+    if (!admit.empty()) {
+        // progress of the running requests goes back to their host descriptors
+        // before the groups are rebuilt around the new set
+        int rc = b.sync_descriptors();
+        if (rc != MCS_OK) return rc;
+        b.release_groups();
+        for (auto &a : admit) {
+            rc = upload_replica(a.second.get());
+            if (rc != MCS_OK) {
+                std::lock_guard<std::mutex> lock(s->qmu);
+                s->in_use -= a.second->bytes + sizeof(Rep);
+                s->pending.erase(a.first);
+                return rc;
+            }
+            s->tickets.push_back(a.first);
+            b.replicas.push_back(std::move(a.second));
+        }
+        std::lock_guard<std::mutex> lock(s->qmu);
+        s->n_active = (int)b.replicas.size();
+    }
+    if (b.replicas.empty()) return MCS_OK;
+    // 2. one chunk of units, ending at the next completion at the latest
+    long long units = s->chunk;
+    for (auto &r : b.replicas) units = std::min(units, std::max(1LL, r->hm.units_total - r->rep.u));
+    int rc = b.advance(units);
+    if (rc != MCS_OK) return rc;
+    for (auto &r : b.replicas) r->rep.u = std::min(r->hm.units_total, r->rep.u + units);
+    // 3. retire finished requests
+    bool any = false;
+    for (auto &r : b.replicas) any |= r->rep.u >= r->hm.units_total;
+    if (!any) return MCS_OK;
+    rc = b.sync_descriptors();
+    if (rc != MCS_OK) return rc;
+    std::vector<std::pair<uint64_t, mcs_server::Done>> fin;
+    std::vector<std::unique_ptr<Replica>> keep;
+    std::vector<uint64_t> keep_t;
+    uint64_t freed = 0;
+    long long su = 0;
+    for (size_t i = 0; i < b.replicas.size(); ++i) {
+        std::unique_ptr<Replica> &r = b.replicas[i];
+        if (r->rep.u < r->hm.units_total) {
+            keep.push_back(std::move(r));
+            keep_t.push_back(s->tickets[i]);
+            continue;
+        }
+        mcs_server::Done d;
+        memset(&d.r, 0, sizeof d.r);
+        const int G = r->hm.ngroup;
+        d.groups.assign((size_t)(G + 1) * (G + 1) + (G + 1), 0.0);
+        d.r.group_values = d.groups.data();
+        d.r.group_capacity = (int)d.groups.size();
+        int rr = replica_results(r.get(), r->rep, &d.r);
+        d.r.group_values = nullptr;
+        d.r.frames = nullptr;
+        d.r.series = nullptr;
+        if (rr != MCS_OK) return rr;
+        su += d.r.site_updates;
+        freed += r->bytes + sizeof(Rep);
+        fin.emplace_back(s->tickets[i], std::move(d));
+    }
+    b.release_groups();
+    b.replicas.swap(keep);
+    s->tickets.swap(keep_t);
+    keep.clear();  // frees the retired arenas
+    std::lock_guard<std::mutex> lock(s->qmu);
+    for (auto &f : fin) {
+        s->pending.erase(f.first);
+        s->done.emplace(f.first, std::move(f.second));
+    }
+    s->site_updates += su;
+    s->in_use -= freed;
+    s->n_active = (int)b.replicas.size();
+    if (completed) *completed = (int32_t)fin.size();
+    return MCS_OK;
 }
 
 extern "C" int mcs_server_poll(mcs_server *s, uint64_t ticket, mcs_result *result)
 {
     if (!s) return MCS_EINVAL;
-    std::lock_guard<std::mutex> lock(s->mu);
+    std::lock_guard<std::mutex> lock(s->qmu);
     auto it = s->done.find(ticket);
     if (it == s->done.end()) {
-        for (auto &q : s->queue) if (q.first == ticket) return 1;
-        for (auto &a : s->active) if (a.first == ticket) return 1;
+        if (s->pending.count(ticket)) return 1;
         set_error("unknown ticket");
         return MCS_ENOTFOUND;
     }
@@ -166,12 +220,20 @@ extern "C" int mcs_server_stats(mcs_server *s, int32_t *active, int32_t *queued,
                                 int64_t *site_updates)
 {
     if (!s) return MCS_EINVAL;
-    std::lock_guard<std::mutex> lock(s->mu);
-    if (active) *active = (int32_t)s->active.size();
+    std::lock_guard<std::mutex> lock(s->qmu);
+    if (active) *active = (int32_t)s->n_active;
     if (queued) *queued = (int32_t)s->queue.size();
     if (bytes_in_use) *bytes_in_use = s->in_use;
     if (site_updates) *site_updates = s->site_updates;
     return MCS_OK;
 }
 
-extern "C" void mcs_server_destroy(mcs_server *s) { delete s; }
+extern "C" void mcs_server_destroy(mcs_server *s)
+{
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> slock(s->smu);
+        s->batch.release_groups();
+    }
+    delete s;
+}

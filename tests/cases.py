@@ -33,7 +33,7 @@ def golden_case(name):
 
 
 from mcsolver_gb300.lattice import (  # noqa: E402,F401
-    HC_POS, J9, SQ_CIRCUITS, honeycomb_args, lattice_args, square_args)
+    HC_POS, J9, SQ_CIRCUITS, honeycomb_args, lattice_args, square_args, square_args_fast)
 
 
 def flat(t):

@@ -46,3 +46,38 @@ def test_cluster_matches_resident(engine, name, model, mk, csize):
     n = 27
     np.testing.assert_allclose(np.array(b[:n]), np.array(a[:n]), rtol=1e-5, atol=1e-6)
     assert eb["site_updates"] == ea["site_updates"]
+
+
+def test_replica_too_large_for_any_cluster_runs_once_on_tiles(engine):
+    """XY L=512: 2 MB of spins fit neither one CTA nor a cluster of 8; the
+    cluster group falls back to the tiled schedule and the replica must join
+    that one group only (two groups would sweep it twice, side by side)."""
+    args = C.square_args_fast("xy", 512, 0.9, nthermal=2, nsweep=4, frames=4)
+    a, ea = engine.solve("xy", args, seed=5, schedule="tiled", random_init=True)
+    b, eb = engine.solve("xy", args, seed=5, random_init=True)
+    assert eb["site_updates"] == ea["site_updates"] == 512 * 512 * 6
+    np.testing.assert_allclose(eb["frames"], ea["frames"], atol=2e-5)
+    np.testing.assert_allclose(np.array(b[:27]), np.array(a[:27]), rtol=1e-6, atol=1e-6)
+
+
+def test_balanced_batch_equals_alone(engine):
+    """A large Ising replica among small ones is moved to the tiled schedule
+    by the load balancer (its groups run on their own streams beside the
+    resident group); Ising spin trajectories are bit-exact across schedules,
+    so the integer counts are equal and the FP64 averages agree to their
+    summation order (1e-12)."""
+    probs = [C.square_args_fast("ising", 256, 2.3, nthermal=4, nsweep=8)]
+    probs += [C.square_args("ising", 16 + 4 * k, 2.0 + 0.1 * k, nthermal=4, nsweep=8) for k in range(6)]
+    b = engine.Batch()
+    for k, a in enumerate(probs):
+        b.add("ising", a, seed=40 + k, random_init=True)
+    b.prepare()
+    kinds = [g[0] for g in b.schedules()]
+    assert "tiled" in kinds and "resident" in kinds
+    b.run()
+    got = [b.result(k) for k in range(len(probs))]
+    b.close()
+    for k, a in enumerate(probs):
+        alone, ex = engine.solve("ising", a, seed=40 + k, schedule="resident", random_init=True)
+        np.testing.assert_allclose(np.array(got[k][0][:10]), np.array(alone[:10]), rtol=1e-12, atol=1e-12)
+        assert got[k][1]["accepted"] == ex["accepted"] and got[k][1]["site_updates"] == ex["site_updates"]

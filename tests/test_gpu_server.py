@@ -3,6 +3,8 @@
 * requests of mixed models and sizes submitted while others are already on
   the device give the same results as each solved alone (Ising to 1e-9,
   O(n) to 1e-6 relative: same spin trajectory, FP64 sums in another order);
+* submits from several threads while the main thread steps the server
+  (host compile beside device work) lose nothing and change nothing;
 * a small HBM budget queues requests without losing any;
 * a batch of replicas of uneven lattice sizes (square Heisenberg with DMI,
   field and circuits, L in {64, 96, 128, 192, 256}) matches solves alone.
@@ -63,6 +65,48 @@ def test_server_results_equal_alone_with_overlapping_arrivals(engine, monkeypatc
     assert len(got) == len(tickets)
     for t, (m, a, s) in tickets.items():
         alone, _ = engine.solve(m, a, seed=s)
+        _close(m, got[t][0], alone)
+    st = srv.stats()
+    assert st["active"] == 0 and st["queued"] == 0 and st["bytes_in_use"] == 0
+    srv.close()
+
+
+def test_server_threaded_submits_while_stepping(engine, monkeypatch):
+    import threading
+    from concurrent.futures import ThreadPoolExecutor
+
+    monkeypatch.setenv("MCSGPU_SERVER_CHUNK", "5")
+    reqs = _reqs()
+    srv = engine.Server(hbm_budget_bytes=1 << 30, max_slots=64)
+    tickets, lock = {}, threading.Lock()
+
+    def sub(k):
+        m, a, s = reqs[k]
+        t = srv.submit(m, a, seed=s + 100, random_init=(k % 2 == 0))
+        with lock:
+            tickets[t] = k
+
+    pool = ThreadPoolExecutor(max_workers=4)
+    futs = [pool.submit(sub, k) for k in range(len(reqs))]
+    got = {}
+    for _ in range(5000):
+        srv.step()
+        with lock:
+            live = list(tickets)
+        for t in live:
+            if t not in got:
+                r = srv.poll(t)
+                if r is not None:
+                    got[t] = r
+        if len(got) == len(reqs):
+            break
+    for f in futs:
+        f.result()
+    pool.shutdown()
+    assert len(got) == len(reqs)
+    for t, k in tickets.items():
+        m, a, s = reqs[k]
+        alone, _ = engine.solve(m, a, seed=s + 100, random_init=(k % 2 == 0))
         _close(m, got[t][0], alone)
     st = srv.stats()
     assert st["active"] == 0 and st["queued"] == 0 and st["bytes_in_use"] == 0
