@@ -26,8 +26,13 @@ namespace mcs {
 static __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 #define CL_NV 28
-#define CL_PART 32
-#define CL_RED (32 * CL_NV + 32)
+// per-CTA partial slot of one measurement: CL_NV frame sums, then the energy
+// change and the accepted count since the previous measurement, the full-energy
+// flag and the measurement index; two slots (measurement parity) and a third
+// for the energy change after the last measurement of a launch
+#define CL_SLOT 32
+#define CL_PART (3 * CL_SLOT)
+#define CL_RED (32 * CL_SLOT + 32)
 
 struct ClusterLayout {
     size_t spins, tables, majc, part, red, F, acc, total;
@@ -48,7 +53,7 @@ __host__ __device__ inline ClusterLayout cluster_layout(const Rep &R, int C)
     L.majc = off; off += a16((size_t)L.nchosen * 3 * sizeof(float));
     L.part = off; off += CL_PART * sizeof(double);
     L.red = off; off += CL_RED * sizeof(double);
-    L.F = off; off += F_NON * sizeof(double);
+    L.F = off; off += (F_NON + CL_SLOT) * sizeof(double);
     L.acc = off; off += a16((size_t)R.nacc * sizeof(double) + C_NINT * sizeof(long long));
     L.total = off;
     return L;
@@ -70,8 +75,51 @@ __device__ __forceinline__ void cl_links(const Rep &R, int rows, int c, int xl, 
     f(3, base + (xl + 1) * hy + (ym >> 1), R.sq_code[3]);
 }
 
+// Fold partial slot `slot` of every CTA of the cluster (fixed rank order) into
+// the FP64 accumulators of rank 0.  Called by the 32 lanes of rank 0's warp 0;
+// kept out of line so that its registers do not add to the sweep loop's.
 template <int DIM>
-__global__ void __launch_bounds__(1024) k_cluster_metro(Rep *reps, const int *ids, long long max_units, int C)
+__device__ __noinline__ void cluster_fold(Rep &R, double *part, double *F, double *Fo, int C, int slot, int lane)
+{
+    cg::cluster_group cl = cg::this_cluster();
+    double o = 0.0;
+    for (int q = 0; q < C; ++q) o += cl.map_shared_rank(part, q)[slot * CL_SLOT + lane];
+    Fo[lane] = o;
+    __syncwarp();
+    const bool efull = Fo[CL_NV + 2] != 0.0;
+    if (lane == 0) {
+        for (int k = 0; k < F_NON; ++k) F[k] = 0.0;
+        for (int k = 0; k < 3; ++k) {
+            F[F_TOT + k] = Fo[k];
+            F[F_SI + k] = F[F_SJ + k] = Fo[3 + k];
+            F[F_SIR + k] = F[F_SJR + k] = Fo[10 + k];
+        }
+        F[F_SIJ] = Fo[6];
+        F[F_EFB] = Fo[7]; F[F_EFO] = Fo[8]; F[F_Q] = Fo[9];
+        F[F_SIJR] = Fo[13];
+        F[F_ERB] = Fo[14]; F[F_ERO] = Fo[15];
+        for (int g = 0; g < R.ngroup; ++g) {
+            const bool all = (R.gall >> g) & 1;
+            for (int k = 0; k < 3; ++k) F[F_G + 3 * g + k] = all ? Fo[k] : Fo[16 + 3 * g + k];
+        }
+        R.acc[A_ECUR] += Fo[CL_NV];
+        R.stats[S_ACCEPT] += (long long)Fo[CL_NV + 1];
+        if (efull) {
+            double Ef = F[F_EFB] / 2 + F[F_EFO];
+            double d = fabs(R.acc[A_ECUR] - Ef);
+            if (d > R.acc[A_DRIFT]) R.acc[A_DRIFT] = d;
+            R.acc[A_ECUR] = Ef;
+        }
+    }
+    __syncwarp();
+    on_accumulate_lanes<DIM>(R, F, R.acc[A_ECUR], (long long)Fo[CL_NV + 3], lane, 32);
+    __syncwarp();
+}
+
+// NT: block size the kernel is compiled for (256, 512 or 1024 threads; the
+// register budget per thread follows from it)
+template <int DIM, int NT>
+__global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids, long long max_units, int C)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ Rep R;
@@ -131,7 +179,17 @@ __global__ void __launch_bounds__(1024) k_cluster_metro(Rep *reps, const int *id
     float *prev_sp = cl.map_shared_rank(sp, rprev);
     float *next_sp = cl.map_shared_rank(sp, rnext);
 
-    // partial sums of one measurement -> rank 0 (fixed rank order)
+    // Measurements.  Every CTA reduces its own sites into its partial slot
+    // part[m & 1]; rank 0 folds measurement m into the FP64 accumulators while
+    // measurement m + 1 runs (after that measurement's first cluster barrier,
+    // when every slot of m is complete), so a measurement costs one cluster
+    // barrier.  The fold of the launch's last measurement runs at launch end.
+    long long mloc = R.m;
+    int fw = R.frames_written;
+    int pending = -1;  // slot of a measurement not yet folded
+    double *Fo = F + F_NON;  // [CL_SLOT] rank sums of one slot (rank 0)
+    // rank 0, warp 0: fold slot `slot` (fixed rank order)
+    auto fold = [&](int slot) { cluster_fold<DIM>(R, part, F, Fo, C, slot, tid); };
     auto measure = [&](long long m, bool efull) {
         // block spins of the own chosen sites
         const int r0 = rank * L.nchosen;
@@ -151,18 +209,19 @@ __global__ void __launch_bounds__(1024) k_cluster_metro(Rep *reps, const int *id
             float my = S.y[i00] + S.y[i01] + S.y[i10] + S.y[i11];
             float mz = DIM == 3 ? S.z[i00] + S.z[i01] + S.z[i10] + S.z[i11] : 0.f;
             v_norm_ref(mx, my, mz);
-            const float sv = R.sval[R.rorb[r0 + q]];
+            const float sv = R.meas_regular ? R.sval0 : R.sval[R.rorb[r0 + q]];
             majc[3 * q] = mx * sv; majc[3 * q + 1] = my * sv; majc[3 * q + 2] = mz * sv;
         }
         __syncthreads();
         cl.sync();
+        if (rank == 0 && tid < 32 && pending >= 0) fold(pending);
         const bool full = R.fullJ;
         // partial layout: 0-2 total spin, 3-5 pair sum, 6 pair s.s, 7/8 full
         // energy bond/onsite, 9 solid angles, 10-12 block-spin pair sum,
         // 13 block s.s, 14/15 renormalised bond/onsite, 16-27 four groups
-        float a[CL_NV];
+        float a[32];  // CL_NV values, padded to the warp width for the halving sum
 #pragma unroll
-        for (int k = 0; k < CL_NV; ++k) a[k] = 0.f;
+        for (int k = 0; k < 32; ++k) a[k] = 0.f;
         // pass A over own sites: total spin, pair sums, groups, full energy
         for (int c = 0; c < 2; ++c)
             for (int kk = tid; kk < nown; kk += bd) {
@@ -171,7 +230,7 @@ __global__ void __launch_bounds__(1024) k_cluster_metro(Rep *reps, const int *id
                 const int v = c * half + (x0 + xl) * hy + yh;
                 const float sx = S.x[li], sy = S.y[li], sz = DIM == 3 ? S.z[li] : 0.f;
                 a[0] += sx; a[1] += sy; a[2] += sz;
-                if (R.sflag[v] & 1) { a[3] += sx; a[4] += sy; a[5] += sz; a[6] += sx * sx + sy * sy + sz * sz; }
+                if (R.meas_regular || (R.sflag[v] & 1)) { a[3] += sx; a[4] += sy; a[5] += sz; a[6] += sx * sx + sy * sy + sz * sz; }
                 if (efull) {
                     float h0, h1, h2;
                     on_field<DIM>(R, jt, S, [&](auto &&f) { cl_links(R, rows, c, xl, yh, f); }, h0, h1, h2);
@@ -183,7 +242,7 @@ __global__ void __launch_bounds__(1024) k_cluster_metro(Rep *reps, const int *id
                     }
                     a[8] += e - h * ((DIM == 3) ? sz : sx);
                 }
-                const int gm = R.ngroup ? (R.gmask[v] & ~R.gall) : 0;
+                const int gm = (R.ngroup && !R.meas_regular) ? (R.gmask[v] & ~R.gall) : 0;
                 if (gm) {
 #pragma unroll
                     for (int g = 0; g < 4; ++g)
@@ -229,7 +288,38 @@ __global__ void __launch_bounds__(1024) k_cluster_metro(Rep *reps, const int *id
                     }
                 }
         }
-        // pass B over own chosen sites
+        // pass B over own chosen sites; regular lattices by arithmetic (block
+        // (xr, yb) links to its four neighbour blocks), others from the lists
+        if (R.meas_regular) {
+            const int hb = R.Ly >> 1, nbx = R.Lx >> 1;
+            for (int q = tid; q < L.nchosen; q += bd) {
+                const int r = r0 + q;
+                const int xr = r / hb, yb = r - xr * hb;
+                const float mx = majc[3 * q], my = majc[3 * q + 1], mz = majc[3 * q + 2];
+                a[10] += mx; a[11] += my; a[12] += mz; a[13] += mx * mx + my * my + mz * mz;
+                const int tg[4] = {(xr + 1 == nbx ? 0 : xr + 1) * hb + yb, (xr == 0 ? nbx - 1 : xr - 1) * hb + yb,
+                                   xr * hb + (yb + 1 == hb ? 0 : yb + 1), xr * hb + (yb == 0 ? hb - 1 : yb - 1)};
+                float corr = 0.f;
+#pragma unroll
+                for (int d = 0; d < 4; ++d) {
+                    const int tr = tg[d];
+                    const int owner = tr / L.nchosen;
+                    const float *mc = owner == rank ? majc : cl.map_shared_rank(majc, owner);
+                    const int lq = tr - owner * L.nchosen;
+                    corr += on_jdot<DIM>(jt + 9 * R.rdir_cls[d], full, mx, my, mz, mc[3 * lq], mc[3 * lq + 1], mc[3 * lq + 2]);
+                }
+                a[14] += corr;
+                // onsite energy of the actual spin at (2 xr, 2 yb): colour 0
+                const int li = (2 * xr - x0 + 1) * hy + yb;
+                const float sx = S.x[li], sy = S.y[li], sz = DIM == 3 ? S.z[li] : 0.f;
+                float e = 0.f;
+                if (R.has_d) {
+                    e = dt[0] * sx * sx + dt[1] * sy * sy;
+                    if (DIM == 3) e += dt[2] * sz * sz;
+                }
+                a[15] += e - h * ((DIM == 3) ? sz : sx);
+            }
+        } else
         for (int q = tid; q < L.nchosen; q += bd) {
             const int r = r0 + q;
             const int v = R.rorb[r];
@@ -259,58 +349,45 @@ __global__ void __launch_bounds__(1024) k_cluster_metro(Rep *reps, const int *id
             }
             a[15] += e - h * ((DIM == 3) ? sz : sx);
         }
-        block_sum_f<CL_NV>(a, red, red + 32 * CL_NV);
-        if (tid < CL_NV) part[tid] = red[32 * CL_NV + tid];
-        __syncthreads();
+        // warp sums (FP32 frame values by recursive halving, FP64 energy
+        // change and count), then the CTA's slot in FP64 across the warps
         {
-            double de[2] = {dEd, (double)nacc};
-            block_sum<2>(de, red, red + 64);
-            if (tid == 0) { part[CL_NV] = red[64]; part[CL_NV + 1] = red[65]; }
+            const int lane = tid & 31, wid = tid >> 5, nw = (bd + 31) >> 5;
+#pragma unroll
+            for (int w = 16; w >= 1; w >>= 1) {
+                const bool up = (lane & w) != 0;
+#pragma unroll
+                for (int j = 0; j < w; ++j) {
+                    const float send = up ? a[j] : a[j + w];
+                    const float keep = up ? a[j + w] : a[j];
+                    a[j] = keep + __shfl_xor_sync(0xffffffffu, send, w);
+                }
+            }
+            double de = dEd, na = (double)nacc;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                de += __shfl_xor_sync(0xffffffffu, de, o);
+                na += __shfl_xor_sync(0xffffffffu, na, o);
+            }
+            red[wid * CL_SLOT + lane] = lane < CL_NV ? (double)a[0] : (lane == CL_NV ? de : na);
+            __syncthreads();
+            const int slot = (int)(m & 1);
+            if (tid < CL_NV + 2) {
+                double s2 = 0.0;
+                for (int w = 0; w < nw; ++w) s2 += red[w * CL_SLOT + tid];
+                part[slot * CL_SLOT + tid] = s2;
+            } else if (tid == CL_NV + 2) {
+                part[slot * CL_SLOT + tid] = efull ? 1.0 : 0.0;
+            } else if (tid == CL_NV + 3) {
+                part[slot * CL_SLOT + tid] = (double)m;
+            }
+            pending = slot;
         }
         dEd = 0.0;
         nacc = 0;
-        __syncthreads();
-        cl.sync();
-        if (rank == 0) {
-            if (tid < CL_NV + 2) {
-                double s = 0.0;
-                for (int q = 0; q < C; ++q) s += cl.map_shared_rank(part, q)[tid];
-                red[tid] = s;
-            }
-            __syncthreads();
-            if (tid == 0) {
-                const double *o = red;
-                for (int k = 0; k < F_NON; ++k) F[k] = 0.0;
-                for (int k = 0; k < 3; ++k) {
-                    F[F_TOT + k] = o[k];
-                    F[F_SI + k] = F[F_SJ + k] = o[3 + k];
-                    F[F_SIR + k] = F[F_SJR + k] = o[10 + k];
-                }
-                F[F_SIJ] = o[6];
-                F[F_EFB] = o[7]; F[F_EFO] = o[8]; F[F_Q] = o[9];
-                F[F_SIJR] = o[13];
-                F[F_ERB] = o[14]; F[F_ERO] = o[15];
-                for (int g = 0; g < R.ngroup; ++g) {
-                    const bool all = (R.gall >> g) & 1;
-                    for (int k = 0; k < 3; ++k) F[F_G + 3 * g + k] = all ? o[k] : o[16 + 3 * g + k];
-                }
-                R.acc[A_ECUR] += o[CL_NV];
-                R.stats[S_ACCEPT] += (long long)o[CL_NV + 1];
-                if (efull) {
-                    double Ef = F[F_EFB] / 2 + F[F_EFO];
-                    double d = fabs(R.acc[A_ECUR] - Ef);
-                    if (d > R.acc[A_DRIFT]) R.acc[A_DRIFT] = d;
-                    R.acc[A_ECUR] = Ef;
-                }
-            }
-            if (tid < 32) {
-                __syncwarp();
-                on_accumulate_lanes<DIM>(R, F, R.acc[A_ECUR], m, tid, 32);
-            }
-        }
         // spin frame: every CTA writes its own rows
-        if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) {
-            float *fb = R.frame_buf + (size_t)R.frames_written * R.N * 3;
+        if (R.frames > 0 && (m % R.frame_every) == 0 && fw < R.frames) {
+            float *fb = R.frame_buf + (size_t)fw * R.N * 3;
             for (int c = 0; c < 2; ++c)
                 for (int kk = tid; kk < nown; kk += bd) {
                     const int xl = kk / hy, yh = kk - xl * hy;
@@ -318,13 +395,8 @@ __global__ void __launch_bounds__(1024) k_cluster_metro(Rep *reps, const int *id
                     const int v = c * half + (x0 + xl) * hy + yh;
                     fb[3 * v] = S.x[li]; fb[3 * v + 1] = S.y[li]; fb[3 * v + 2] = DIM == 3 ? S.z[li] : 0.f;
                 }
+            ++fw;
         }
-        __syncthreads();
-        if (tid == 0) {
-            if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) R.frames_written++;
-            R.m = m + 1;
-        }
-        __syncthreads();
     };
 
     long long u = R.u;
@@ -365,21 +437,31 @@ __global__ void __launch_bounds__(1024) k_cluster_metro(Rep *reps, const int *id
         // the ghost rows must be complete in every CTA before the next colour
         // phase reads them, and no CTA may overwrite a row a neighbour still copies
         cl.sync();
-        if (measures_after(R, u)) measure(R.m, (R.m % R.recheck) == 0);
+        if (measures_after(R, u)) {
+            measure(mloc, (mloc % R.recheck) == 0);
+            ++mloc;
+        }
     }
-    // fold the energy change since the last measurement
+    // the energy change after the last measurement -> slot 2
     {
         double de[2] = {dEd, (double)nacc};
         block_sum<2>(de, red, red + 64);
-        if (tid == 0) { part[CL_NV] = red[64]; part[CL_NV + 1] = red[65]; }
+        if (tid == 0) { part[2 * CL_SLOT + CL_NV] = red[64]; part[2 * CL_SLOT + CL_NV + 1] = red[65]; }
     }
     __syncthreads();
     cl.sync();
-    if (rank == 0 && tid == 0) {
-        double s = 0.0, na = 0.0;
-        for (int q = 0; q < C; ++q) { s += cl.map_shared_rank(part, q)[CL_NV]; na += cl.map_shared_rank(part, q)[CL_NV + 1]; }
-        R.acc[A_ECUR] += s;
-        R.stats[S_ACCEPT] += (long long)na;
+    if (rank == 0) {
+        if (tid < 32 && pending >= 0) fold(pending);
+        if (tid == 0) {
+            double s = 0.0, na = 0.0;
+            for (int q = 0; q < C; ++q) {
+                const double *pq = cl.map_shared_rank(part, q) + 2 * CL_SLOT;
+                s += pq[CL_NV];
+                na += pq[CL_NV + 1];
+            }
+            R.acc[A_ECUR] += s;
+            R.stats[S_ACCEPT] += (long long)na;
+        }
     }
     cl.sync();
     // own rows back to global memory
@@ -397,27 +479,27 @@ __global__ void __launch_bounds__(1024) k_cluster_metro(Rep *reps, const int *id
         if (tid == 0) {
             R.stats[S_VISITS] += (uend - R.u) * (long long)R.N;
             Rg->u = uend;
-            Rg->m = R.m;
-            Rg->frames_written = R.frames_written;
+            Rg->m = mloc;
+            Rg->frames_written = fw;
         }
     }
 }
 
 long long cluster_smem_bytes(const Rep &r, int C) { return (long long)cluster_layout(r, C).total; }
 
-template <int DIM>
-static cudaError_t launch_cluster_t(Rep *reps, const int *ids, int nrep, int C, int threads, size_t smem,
-                                    long long max_units, cudaStream_t st)
+template <int DIM, int NT>
+static cudaError_t launch_cluster_t(Rep *reps, const int *ids, int nrep, int C, size_t smem, long long max_units,
+                                    cudaStream_t st)
 {
     static size_t done = 0;
     if (smem > done) {
-        cudaError_t e = cudaFuncSetAttribute(k_cluster_metro<DIM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(k_cluster_metro<DIM, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         done = smem;
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nrep * C, 1, 1);
-    cfg.blockDim = dim3(threads, 1, 1);
+    cfg.blockDim = dim3(NT, 1, 1);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
@@ -427,15 +509,25 @@ static cudaError_t launch_cluster_t(Rep *reps, const int *ids, int nrep, int C, 
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_cluster_metro<DIM>, reps, ids, max_units, C);
+    return cudaLaunchKernelEx(&cfg, k_cluster_metro<DIM, NT>, reps, ids, max_units, C);
+}
+
+template <int DIM>
+static cudaError_t launch_cluster_d(Rep *reps, const int *ids, int nrep, int C, int threads, size_t smem,
+                                    long long max_units, cudaStream_t st)
+{
+    if (threads == 256) return launch_cluster_t<DIM, 256>(reps, ids, nrep, C, smem, max_units, st);
+    if (threads == 512) return launch_cluster_t<DIM, 512>(reps, ids, nrep, C, smem, max_units, st);
+    if (threads == 1024) return launch_cluster_t<DIM, 1024>(reps, ids, nrep, C, smem, max_units, st);
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_cluster_metro(int dim, Rep *reps, const int *ids, int nrep, int C, int threads, size_t smem,
                                  long long max_units, cudaStream_t st)
 {
     if (nrep <= 0) return cudaSuccess;
-    if (dim == 2) return launch_cluster_t<2>(reps, ids, nrep, C, threads, smem, max_units, st);
-    return launch_cluster_t<3>(reps, ids, nrep, C, threads, smem, max_units, st);
+    if (dim == 2) return launch_cluster_d<2>(reps, ids, nrep, C, threads, smem, max_units, st);
+    return launch_cluster_d<3>(reps, ids, nrep, C, threads, smem, max_units, st);
 }
 
 }  // namespace mcs

@@ -178,6 +178,9 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool u
     }
     R.pair_identity = m.pair_identity;
     R.gall = m.gall;
+    R.meas_regular = m.meas_regular;
+    R.sval0 = m.sval.empty() ? 0.f : m.sval[0];
+    for (int d = 0; d < 4; ++d) R.rdir_cls[d] = m.rdir_cls[d];
     R.sflag = (const unsigned char *)P(o_sflag);
     R.rtgt = (const int *)P(o_rtgt);
     R.units_thermal = m.units_thermal; R.units_total = m.units_total; R.nsweep = m.nsweep; R.upm = m.upm;
@@ -708,7 +711,7 @@ int Batch::prepare()
                                     sm = std::max<size_t>(sm, (size_t)cluster_smem_bytes(replicas[id]->rep, C));
                                 }
                                 if (!ok || (int)sm > max_smem) continue;
-                                for (int th : {512, 1024}) G->candidates.push_back({C, th});
+                                for (int th : {512, 256, 1024}) G->candidates.push_back({C, th});
                             }
                             G->can_cluster = 1;
                         }

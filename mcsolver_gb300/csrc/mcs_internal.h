@@ -119,6 +119,13 @@ struct Rep {
     int pair_identity;                           // every pair is (v, v), each site at most once
     const unsigned char *sflag;                  // [N] bit0: site is a pair member, bit1: chosen
     const int *rtgt;                             // [n_rorb*zmax] index in rorb of the l-th renormalised target (-1)
+    // regular square measurement (cluster schedule): every site is a (v, v)
+    // pair, one signed spin value sval0, every group holds every site, and each
+    // chosen block links to the blocks two sites away along +x, -x, +y, -y with
+    // exchange classes rdir_cls[0..3]; the frame then needs no index lists
+    int meas_regular;
+    float sval0;
+    int rdir_cls[4];
     // ---- program
     long long units_thermal, units_total, nsweep;
     int upm;                                     // units per measurement

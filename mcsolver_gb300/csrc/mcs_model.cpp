@@ -551,6 +551,36 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
         for (int g = 4; g < m->ngroup && ok; ++g) ok = (m->gall >> g) & 1;
         m->cluster_ok = ok ? 1 : 0;
     }
+    m->meas_regular = 0;
+    if (m->cluster_ok) {
+        const int Lx = m->Lx, Ly = m->Ly, hb = Ly / 2;
+        bool ok = m->ngroup == 0 || m->gall == (1 << m->ngroup) - 1;
+        for (int k = 0; k < N && ok; ++k) ok = (m->sflag[k] & 1) && m->sval[k] == m->sval[0];
+        int dc[4] = {-1, -1, -1, -1};
+        const int zz = std::max(z, 1);
+        for (int r = 0; r < p->n_rorb && ok; ++r) {
+            const int x = 2 * (r / hb), y = 2 * (r % hb);
+            if (m->rdeg[r] != 4) { ok = false; break; }
+            const int want[4] = {(((x + 2) % Lx) / 2) * hb + y / 2, (((x - 2 + Lx) % Lx) / 2) * hb + y / 2,
+                                 (x / 2) * hb + ((y + 2) % Ly) / 2, (x / 2) * hb + ((y - 2 + Ly) % Ly) / 2};
+            int seen = 0;
+            for (int l = 0; l < 4 && ok; ++l) {
+                const int t = m->rtgt[(size_t)r * zz + l];
+                int d = -1;
+                for (int q = 0; q < 4; ++q)
+                    if (t == want[q] && !(seen & (1 << q))) { d = q; break; }
+                if (d < 0) { ok = false; break; }
+                seen |= 1 << d;
+                const int cls = m->rjc[(size_t)r * zz + l];
+                if (dc[d] < 0) dc[d] = cls;
+                else if (dc[d] != cls) ok = false;
+            }
+        }
+        if (ok) {
+            m->meas_regular = 1;
+            for (int d = 0; d < 4; ++d) m->rdir_cls[d] = dc[d];
+        }
+    }
 
     // ---------------------------------------------------------------- program
     if (p->algorithm == 0) {

@@ -56,6 +56,8 @@ struct HostModel {
     int pair_identity = 0;
     int gall = 0;
     int cluster_ok = 0;     // the row-split cluster schedule can run this replica
+    int meas_regular = 0;   // cluster frame from arithmetic (see Rep::meas_regular)
+    int rdir_cls[4] = {0, 0, 0, 0};
     int nlat = 0, n_rorb = 0, ncl = 0, ncirc = 0, ngroup = 0;
     int ci = 0, cj = 0, cij = 0;
     // program
