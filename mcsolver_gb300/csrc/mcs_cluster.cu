@@ -75,45 +75,55 @@ __device__ __forceinline__ void cl_links(const Rep &R, int rows, int c, int xl, 
     f(3, base + (xl + 1) * hy + (ym >> 1), R.sq_code[3]);
 }
 
+// Index of the slot sum that feeds frame entry f (frame layout F_*), -1 for 0.
+__device__ __forceinline__ int cl_frame_src(int f, int ngroup, int gall)
+{
+    if (f >= F_G) {
+        const int g = (f - F_G) / 3, k = (f - F_G) - 3 * g;
+        if (g >= ngroup) return -1;
+        return ((gall >> g) & 1) ? k : 16 + 3 * g + k;
+    }
+    if (f < F_SJ) return 3 + (f - F_SI);
+    if (f < F_SIJ) return 3 + (f - F_SJ);
+    if (f == F_SIJ) return 6;
+    if (f < F_Q) return f - F_TOT;
+    if (f == F_Q) return 9;
+    if (f < F_SJR) return 10 + (f - F_SIR);
+    if (f < F_SIJR) return 10 + (f - F_SJR);
+    if (f == F_SIJR) return 13;
+    if (f == F_ERB) return 14;
+    if (f == F_ERO) return 15;
+    if (f == F_EFB) return 7;
+    return 8;  // F_EFO
+}
+
 // Fold partial slot `slot` of every CTA of the cluster (fixed rank order) into
 // the FP64 accumulators of rank 0.  Called by the 32 lanes of rank 0's warp 0;
 // kept out of line so that its registers do not add to the sweep loop's.
 template <int DIM>
-__device__ __noinline__ void cluster_fold(Rep &R, double *part, double *F, double *Fo, int C, int slot, int lane)
+__device__ __noinline__ void cluster_fold(Rep &R, double *part, double *Fo, float *fs, int C, int slot, int lane)
 {
     cg::cluster_group cl = cg::this_cluster();
     double o = 0.0;
     for (int q = 0; q < C; ++q) o += cl.map_shared_rank(part, q)[slot * CL_SLOT + lane];
     Fo[lane] = o;
     __syncwarp();
-    const bool efull = Fo[CL_NV + 2] != 0.0;
+    for (int f = lane; f < F_NON; f += 32) {
+        const int k = cl_frame_src(f, R.ngroup, R.gall);
+        fs[f] = k < 0 ? 0.f : (float)Fo[k];
+    }
     if (lane == 0) {
-        for (int k = 0; k < F_NON; ++k) F[k] = 0.0;
-        for (int k = 0; k < 3; ++k) {
-            F[F_TOT + k] = Fo[k];
-            F[F_SI + k] = F[F_SJ + k] = Fo[3 + k];
-            F[F_SIR + k] = F[F_SJR + k] = Fo[10 + k];
-        }
-        F[F_SIJ] = Fo[6];
-        F[F_EFB] = Fo[7]; F[F_EFO] = Fo[8]; F[F_Q] = Fo[9];
-        F[F_SIJR] = Fo[13];
-        F[F_ERB] = Fo[14]; F[F_ERO] = Fo[15];
-        for (int g = 0; g < R.ngroup; ++g) {
-            const bool all = (R.gall >> g) & 1;
-            for (int k = 0; k < 3; ++k) F[F_G + 3 * g + k] = all ? Fo[k] : Fo[16 + 3 * g + k];
-        }
         R.acc[A_ECUR] += Fo[CL_NV];
         R.stats[S_ACCEPT] += (long long)Fo[CL_NV + 1];
-        if (efull) {
-            double Ef = F[F_EFB] / 2 + F[F_EFO];
-            double d = fabs(R.acc[A_ECUR] - Ef);
+        if (Fo[CL_NV + 2] != 0.0) {  // full-energy re-check
+            const double Ef = Fo[7] / 2 + Fo[8];
+            const double d = fabs(R.acc[A_ECUR] - Ef);
             if (d > R.acc[A_DRIFT]) R.acc[A_DRIFT] = d;
             R.acc[A_ECUR] = Ef;
         }
     }
     __syncwarp();
-    on_accumulate_lanes<DIM>(R, F, R.acc[A_ECUR], (long long)Fo[CL_NV + 3], lane, 32);
-    __syncwarp();
+    on_accumulate_warp<DIM>(R, fs, R.acc[A_ECUR], (long long)Fo[CL_NV + 3], lane);
 }
 
 // NT: block size the kernel is compiled for (256, 512 or 1024 threads; the
@@ -189,7 +199,8 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
     int pending = -1;  // slot of a measurement not yet folded
     double *Fo = F + F_NON;  // [CL_SLOT] rank sums of one slot (rank 0)
     // rank 0, warp 0: fold slot `slot` (fixed rank order)
-    auto fold = [&](int slot) { cluster_fold<DIM>(R, part, F, Fo, C, slot, tid); };
+    __shared__ float fsx[F_NON + 32];
+    auto fold = [&](int slot) { cluster_fold<DIM>(R, part, Fo, fsx, C, slot, tid); };
     auto measure = [&](long long m, bool efull) {
         // block spins of the own chosen sites
         const int r0 = rank * L.nchosen;
@@ -397,8 +408,18 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
                 }
             ++fw;
         }
+        // a full-energy pass and the solid angles read ghost rows, which the
+        // neighbours' next colour phase overwrites: hold them back until every
+        // CTA is done reading
+        if (efull || (DIM == 3 && R.ncirc > 0)) cl.sync();
     };
 
+    // Sweeps.  A CTA that accepts a move on its first or last own row writes
+    // the new spin straight into the neighbouring CTA's ghost row as well
+    // (DSMEM store); sites that reject keep the value the ghost already holds.
+    // Colour phase c reads only colour 1-c ghosts and writes only colour-c
+    // ghosts, so one cluster barrier per colour both publishes the pushes and
+    // orders them before the next phase's reads.
     long long u = R.u;
     const long long uend = min(R.units_total, u + max_units);
     for (; u < uend; ++u) {
@@ -407,36 +428,49 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
             float dEf = 0.f;
             SqWalk wk;
             wk.init(tid, bd, hy);
-            for (int kk = tid; kk < nown; kk += bd) {
-                const int xl = wk.x, yh = wk.yh;
-                const int li = c * rows * hy + (xl + 1) * hy + yh;
-                const int k = (x0 + xl) * hy + yh;  // colour-local index of the whole lattice
-                uint4 w = philox_t((uint32_t)k, t, (uint32_t)c, R.seed);
+            const int cb = c * rows * hy;
+            // four sites per thread at a time: their Philox words are drawn
+            // first, as independent instruction streams, then the trials run
+            for (int kb = tid; kb < nown; kb += 4 * bd) {
+                uint4 ws[4];
+                int xs[4], ys[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    xs[e] = wk.x; ys[e] = wk.yh;
+                    // colour-local index of the whole lattice
+                    if (kb + e * bd < nown) ws[e] = philox_t((uint32_t)((x0 + xs[e]) * hy + ys[e]), t, (uint32_t)c, R.seed);
+                    wk.next();
+                }
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                if (kb + e * bd >= nown) break;
+                const int xl = xs[e], yh = ys[e];
+                const int li = cb + (xl + 1) * hy + yh;
+                const uint4 w = ws[e];
                 float dE;
                 if (on_trial<DIM>(R, jt, dt, S, li, 0, w, beta, h, [&](auto &&f) { cl_links(R, rows, c, xl, yh, f); }, &dE)) {
                     dEf += dE;
                     ++nacc;
+                    // own row 0 is the previous CTA's bottom ghost (local row RP+1),
+                    // own row RP-1 the next CTA's top ghost (local row 0)
+                    if (xl == 0) {
+                        const int g = cb + (RP + 1) * hy + yh;
+                        prev_sp[g] = S.x[li];
+                        prev_sp[nloc + g] = S.y[li];
+                        if (DIM == 3) prev_sp[2 * nloc + g] = S.z[li];
+                    }
+                    if (xl == RP - 1) {
+                        const int g = cb + yh;
+                        next_sp[g] = S.x[li];
+                        next_sp[nloc + g] = S.y[li];
+                        if (DIM == 3) next_sp[2 * nloc + g] = S.z[li];
+                    }
                 }
-                wk.next();
+              }
             }
             dEd += (double)dEf;
             cl.sync();
-            // ghost rows of colour c: row -1 <- previous CTA's row RP-1, row RP <- next CTA's row 0
-            const int cb = c * rows * hy;
-            for (int i = tid; i < 2 * hy; i += bd) {
-                const int side = i >= hy, yh = i - side * hy;
-                const int dst = cb + (side ? (RP + 1) : 0) * hy + yh;
-                const int src = cb + (side ? 1 : RP) * hy + yh;
-                const float *base = side ? next_sp : prev_sp;
-                S.x[dst] = base[src];
-                S.y[dst] = base[nloc + src];
-                if (DIM == 3) S.z[dst] = base[2 * nloc + src];
-            }
-            __syncthreads();
         }
-        // the ghost rows must be complete in every CTA before the next colour
-        // phase reads them, and no CTA may overwrite a row a neighbour still copies
-        cl.sync();
         if (measures_after(R, u)) {
             measure(mloc, (mloc % R.recheck) == 0);
             ++mloc;

@@ -655,6 +655,82 @@ __device__ __forceinline__ void on_accumulate(Rep &R, const double *F, double E,
     on_accumulate_lanes<DIM>(R, F, E, m, 0, 1);
 }
 
+// Fold one measurement frame with one warp, keeping the FP64 pipe out of the
+// per-measurement arithmetic (the device issues a warp's FP64 instruction over
+// many cycles): the observables of the frame are formed in FP32 from the
+// frame converted once (fs[0..F_NON), filled by the caller, one lane per
+// entry), and each FP64 accumulator then takes one FP64 add, all lanes at
+// once.  E = running energy (FP64).  fs: shared scratch of >= F_NON + 32
+// floats.  Same formulas as on_accumulate_lanes (heisenbergLib.c:678-830,
+// xyLib.c:606-757); the per-measurement values carry FP32 rounding (relative
+// 6e-8), the sums over measurements are FP64.
+template <int DIM>
+__device__ void on_accumulate_warp(Rep &R, float *fs, double E, long long m, int lane)
+{
+    double *acc = R.acc;
+    float *val = fs + F_NON;  // [32]: value added to acc[k], k < A_ECUR
+    if (lane == 0) {
+        const float inl = (float)R.inv_nl;
+        const float tx = fs[F_TOT], ty = fs[F_TOT + 1], tz = DIM == 3 ? fs[F_TOT + 2] : 0.f;
+        const float six = fs[F_SI], siy = fs[F_SI + 1], siz = DIM == 3 ? fs[F_SI + 2] : 0.f;
+        const float sjx = fs[F_SJ], sjy = fs[F_SJ + 1], sjz = DIM == 3 ? fs[F_SJ + 2] : 0.f;
+        float dx = tx, dy = ty, dz = tz;
+        const float len = sqrtf(dx * dx + dy * dy + dz * dz);
+        if (len >= 1e-5f) { dx /= len; dy /= len; dz /= len; }
+        val[A_SIZ] = (dx * six + dy * siy + dz * siz) * inl;
+        val[A_SJZ] = (dx * sjx + dy * sjy + dz * sjz) * inl;
+        val[A_STZ] = (dx * tx + dy * ty + dz * tz) * inl;
+        val[A_SIH] = (DIM == 3 ? siz : six) * inl;
+        val[A_SJH] = (DIM == 3 ? sjz : sjx) * inl;
+        val[A_STH] = (DIM == 3 ? tz : tx) * inl;
+        const float M = (DIM == 3) ? sqrtf(tx * tx + ty * ty + tz * tz) * inl : sqrtf(six * six + siy * siy) * inl;
+        const float M2 = M * M;
+        val[A_M2] = M2;
+        val[A_M4] = M2 * M2;
+        val[A_MTOT] = M;
+        val[A_MDM] = (float)acc[A_MPREV] * M;
+        acc[A_MPREV] = (double)M;
+        val[A_MPREV] = 0.f;
+        val[A_SI] = fabsf(six * inl); val[A_SI + 1] = fabsf(siy * inl); val[A_SI + 2] = fabsf(siz * inl);
+        val[A_SJ] = fabsf(sjx * inl); val[A_SJ + 1] = fabsf(sjy * inl); val[A_SJ + 2] = fabsf(sjz * inl);
+        val[A_SIJ] = fs[F_SIJ] * inl;
+        const float e = (float)(E * R.inv_N);
+        val[A_E] = e;
+        val[A_E2] = e * e;
+        const float ici = (float)R.inv_ci, icj = (float)R.inv_cj;
+        for (int k = 0; k < 3; ++k) {
+            val[A_SIR + k] = fabsf(fs[F_SIR + k] * ici);
+            val[A_SJR + k] = fabsf(fs[F_SJR + k] * icj);
+        }
+        val[A_SIJR] = fs[F_SIJR] * (float)R.inv_cij;
+        const float er = (fs[F_ERB] * 0.5f + fs[F_ERO]) * (float)R.inv_nr;
+        val[A_ER] = er;
+        val[A_ER2] = er * er;
+        val[A_Q] = DIM == 3 ? fs[F_Q] * (float)(1.0 / (MCS_PI_REF * 4)) : 0.f;
+        if (R.series) {
+            double *sr = R.series + (size_t)m * MCS_NSER;
+            sr[0] = e; sr[1] = M; sr[2] = er; sr[3] = val[A_SIJ];
+        }
+    }
+    __syncwarp();
+    if (lane < A_ECUR && lane != A_MPREV) acc[lane] += (double)val[lane];
+    const int G = R.ngroup;
+    if (G > 0) {
+        const float inl = (float)R.inv_nl;
+        for (int idx = lane; idx < (G + 1) * (G + 1); idx += 32) {
+            const int ga = idx / (G + 1), gb = idx - ga * (G + 1);
+            const float ax = ga < G ? fs[F_G + 3 * ga] : fs[F_TOT] * inl, ay = ga < G ? fs[F_G + 3 * ga + 1] : fs[F_TOT + 1] * inl;
+            const float az = DIM == 3 ? (ga < G ? fs[F_G + 3 * ga + 2] : fs[F_TOT + 2] * inl) : 0.f;
+            const float bx = gb < G ? fs[F_G + 3 * gb] : fs[F_TOT] * inl, by = gb < G ? fs[F_G + 3 * gb + 1] : fs[F_TOT + 1] * inl;
+            const float bz = DIM == 3 ? (gb < G ? fs[F_G + 3 * gb + 2] : fs[F_TOT + 2] * inl) : 0.f;
+            const float d = ax * bx + ay * by + az * bz;
+            acc[A_GRP + idx] += (double)d;
+            if (ga == gb) acc[A_GRP + (G + 1) * (G + 1) + ga] += (double)(d * d);
+        }
+    }
+    __syncwarp();
+}
+
 // ------------------------------------------------------------------ Ising frame
 // Majority sign of the block around v; tie -> Philox word of (a, m, slot).
 __device__ __forceinline__ double is_majority(const Rep &R, const signed char *s, int v, const uint4 &w, int slot)
@@ -804,7 +880,6 @@ __device__ inline void is_accumulate(Rep &R, const double *Fd, const long long *
 {
     double *acc = R.acc;
     long long *ic = R.icnt;
-    const double nl = (double)R.nlat;
     double Mtrue = 0;
     for (int t = 0; t < R.ntype; ++t) Mtrue += R.Stype[t] * (double)Fi[t];
     // exact check: incremental bookkeeping vs full recompute
