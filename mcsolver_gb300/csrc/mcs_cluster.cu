@@ -35,7 +35,7 @@ static __host__ __device__ inline size_t a16(size_t x) { return (x + 15) & ~(siz
 #define CL_RED (32 * CL_SLOT + 32)
 
 struct ClusterLayout {
-    size_t spins, tables, majc, part, red, F, acc, total;
+    size_t spins, tables, majc, part, red, acc, total;
     int rows, hy, nloc, nchosen;
 };
 
@@ -53,7 +53,6 @@ __host__ __device__ inline ClusterLayout cluster_layout(const Rep &R, int C)
     L.majc = off; off += a16((size_t)L.nchosen * 3 * sizeof(float));
     L.part = off; off += CL_PART * sizeof(double);
     L.red = off; off += CL_RED * sizeof(double);
-    L.F = off; off += (F_NON + CL_SLOT) * sizeof(double);
     L.acc = off; off += a16((size_t)R.nacc * sizeof(double) + C_NINT * sizeof(long long));
     L.total = off;
     return L;
@@ -97,33 +96,48 @@ __device__ __forceinline__ int cl_frame_src(int f, int ngroup, int gall)
     return 8;  // F_EFO
 }
 
-// Fold partial slot `slot` of every CTA of the cluster (fixed rank order) into
-// the FP64 accumulators of rank 0.  Called by the 32 lanes of rank 0's warp 0;
-// kept out of line so that its registers do not add to the sweep loop's.
-template <int DIM>
-__device__ __noinline__ void cluster_fold(Rep &R, double *part, double *Fo, float *fs, int C, int slot, int lane)
+// Measurement slots folded per batch by rank 0 (consecutive measurements).
+#define CL_RING 8
+
+// Rank 0, warp 0 (lane = slot entry): sum slot `slot` of every CTA of the
+// cluster in fixed rank order into one ring entry.
+__device__ __forceinline__ void cluster_gather(double *part, double *entry, int C, int slot, int lane)
 {
     cg::cluster_group cl = cg::this_cluster();
     double o = 0.0;
     for (int q = 0; q < C; ++q) o += cl.map_shared_rank(part, q)[slot * CL_SLOT + lane];
-    Fo[lane] = o;
+    entry[lane] = o;
+}
+
+// Rank 0, warp 0: fold the n ring entries (consecutive measurements) into the
+// FP64 accumulators: running energy in order (lane 0), then the frames
+// together.  Kept out of line so that its registers do not add to the sweep
+// loop's.
+template <int DIM>
+__device__ __noinline__ void cluster_fold_ring(Rep &R, const double *ring, int n, float *fs, double *Eb, int lane)
+{
     __syncwarp();
-    for (int f = lane; f < F_NON; f += 32) {
+    for (int idx = lane; idx < n * F_NON; idx += 32) {
+        const int j = idx / F_NON, f = idx - j * F_NON;
         const int k = cl_frame_src(f, R.ngroup, R.gall);
-        fs[f] = k < 0 ? 0.f : (float)Fo[k];
+        fs[j * MCS_FS_STRIDE + f] = k < 0 ? 0.f : (float)ring[j * CL_SLOT + k];
     }
     if (lane == 0) {
-        R.acc[A_ECUR] += Fo[CL_NV];
-        R.stats[S_ACCEPT] += (long long)Fo[CL_NV + 1];
-        if (Fo[CL_NV + 2] != 0.0) {  // full-energy re-check
-            const double Ef = Fo[7] / 2 + Fo[8];
-            const double d = fabs(R.acc[A_ECUR] - Ef);
-            if (d > R.acc[A_DRIFT]) R.acc[A_DRIFT] = d;
-            R.acc[A_ECUR] = Ef;
+        for (int j = 0; j < n; ++j) {
+            const double *o = ring + j * CL_SLOT;
+            R.acc[A_ECUR] += o[CL_NV];
+            R.stats[S_ACCEPT] += (long long)o[CL_NV + 1];
+            if (o[CL_NV + 2] != 0.0) {  // full-energy re-check
+                const double Ef = o[7] / 2 + o[8];
+                const double d = fabs(R.acc[A_ECUR] - Ef);
+                if (d > R.acc[A_DRIFT]) R.acc[A_DRIFT] = d;
+                R.acc[A_ECUR] = Ef;
+            }
+            Eb[j] = R.acc[A_ECUR];
         }
     }
     __syncwarp();
-    on_accumulate_warp<DIM>(R, fs, R.acc[A_ECUR], (long long)Fo[CL_NV + 3], lane);
+    on_accumulate_frames<DIM>(R, fs, Eb, (long long)ring[CL_NV + 3], n, lane);
 }
 
 // NT: block size the kernel is compiled for (256, 512 or 1024 threads; the
@@ -156,7 +170,6 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
     float *majc = (float *)(smem + L.majc);
     double *part = (double *)(smem + L.part);
     double *red = (double *)(smem + L.red);
-    double *F = (double *)(smem + L.F);
     Spins G = spins_global(R);
     // own rows and ghost rows from global memory
     for (int i = tid; i < nloc; i += bd) {
@@ -197,11 +210,27 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
     long long mloc = R.m;
     int fw = R.frames_written;
     int pending = -1;  // slot of a measurement not yet folded
-    double *Fo = F + F_NON;  // [CL_SLOT] rank sums of one slot (rank 0)
     // rank 0, warp 0: fold slot `slot` (fixed rank order)
-    __shared__ float fsx[F_NON + 32];
-    auto fold = [&](int slot) { cluster_fold<DIM>(R, part, Fo, fsx, C, slot, tid); };
-    auto measure = [&](long long m, bool efull) {
+    __shared__ double ring[CL_RING * CL_SLOT];
+    __shared__ float fsx[CL_RING * MCS_FS_STRIDE];
+    __shared__ double Eb[CL_RING];
+    int nring = 0;  // ring entries gathered and not yet folded (rank 0)
+    // rank 0, warp 0: gather the pending slot; fold when the ring is full
+    auto gather = [&](bool flush) {
+        if (pending >= 0) {
+            if (tid < 32) cluster_gather(part, ring + nring * CL_SLOT, C, pending, tid);
+            ++nring;
+        }
+        if (nring > 0 && (flush || nring == CL_RING)) {
+            if (tid < 32) cluster_fold_ring<DIM>(R, ring, nring, fsx, Eb, tid);
+            nring = 0;
+        }
+    };
+    // sums of pass A gathered by the sweep itself (regular lattices, no
+    // full-energy pass): each site's value right after its colour phase, in
+    // the order pass A would read them
+    float fa[4] = {0.f, 0.f, 0.f, 0.f};
+    auto measure = [&](long long m, bool efull, bool fused) {
         // block spins of the own chosen sites
         const int r0 = rank * L.nchosen;
         for (int q = tid; q < L.nchosen; q += bd) {
@@ -225,7 +254,7 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
         }
         __syncthreads();
         cl.sync();
-        if (rank == 0 && tid < 32 && pending >= 0) fold(pending);
+        if (rank == 0) gather(false);
         const bool full = R.fullJ;
         // partial layout: 0-2 total spin, 3-5 pair sum, 6 pair s.s, 7/8 full
         // energy bond/onsite, 9 solid angles, 10-12 block-spin pair sum,
@@ -233,8 +262,12 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
         float a[32];  // CL_NV values, padded to the warp width for the halving sum
 #pragma unroll
         for (int k = 0; k < 32; ++k) a[k] = 0.f;
+        if (fused) {
+            a[0] = fa[0]; a[1] = fa[1]; a[2] = fa[2];
+            a[3] = fa[0]; a[4] = fa[1]; a[5] = fa[2]; a[6] = fa[3];
+        }
         // pass A over own sites: total spin, pair sums, groups, full energy
-        for (int c = 0; c < 2; ++c)
+        for (int c = 0; c < (fused ? 0 : 2); ++c)
             for (int kk = tid; kk < nown; kk += bd) {
                 const int xl = kk / hy, yh = kk - xl * hy;
                 const int li = c * rows * hy + (xl + 1) * hy + yh;
@@ -424,6 +457,8 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
     const long long uend = min(R.units_total, u + max_units);
     for (; u < uend; ++u) {
         const long long t = R.u0 + u;
+        const bool fuse = R.meas_regular && measures_after(R, u) && (mloc % R.recheck) != 0;
+        fa[0] = fa[1] = fa[2] = fa[3] = 0.f;
         for (int c = 0; c < 2; ++c) {
             float dEf = 0.f;
             SqWalk wk;
@@ -466,13 +501,18 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
                         if (DIM == 3) next_sp[2 * nloc + g] = S.z[li];
                     }
                 }
+                if (fuse) {
+                    const float sx = S.x[li], sy = S.y[li], sz = DIM == 3 ? S.z[li] : 0.f;
+                    fa[0] += sx; fa[1] += sy; fa[2] += sz;
+                    fa[3] += sx * sx + sy * sy + sz * sz;
+                }
               }
             }
             dEd += (double)dEf;
             cl.sync();
         }
         if (measures_after(R, u)) {
-            measure(mloc, (mloc % R.recheck) == 0);
+            measure(mloc, (mloc % R.recheck) == 0, fuse);
             ++mloc;
         }
     }
@@ -485,7 +525,7 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
     __syncthreads();
     cl.sync();
     if (rank == 0) {
-        if (tid < 32 && pending >= 0) fold(pending);
+        gather(true);
         if (tid == 0) {
             double s = 0.0, na = 0.0;
             for (int q = 0; q < C; ++q) {

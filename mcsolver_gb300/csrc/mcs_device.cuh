@@ -655,25 +655,28 @@ __device__ __forceinline__ void on_accumulate(Rep &R, const double *F, double E,
     on_accumulate_lanes<DIM>(R, F, E, m, 0, 1);
 }
 
-// Fold one measurement frame with one warp, keeping the FP64 pipe out of the
-// per-measurement arithmetic (the device issues a warp's FP64 instruction over
-// many cycles): the observables of the frame are formed in FP32 from the
-// frame converted once (fs[0..F_NON), filled by the caller, one lane per
-// entry), and each FP64 accumulator then takes one FP64 add, all lanes at
-// once.  E = running energy (FP64).  fs: shared scratch of >= F_NON + 32
-// floats.  Same formulas as on_accumulate_lanes (heisenbergLib.c:678-830,
-// xyLib.c:606-757); the per-measurement values carry FP32 rounding (relative
-// 6e-8), the sums over measurements are FP64.
+// Fold n consecutive measurement frames (indices m0 .. m0+n-1, n <= 32) with
+// one warp, keeping the FP64 pipe out of the per-measurement arithmetic (the
+// device issues a warp's FP64 instruction over many cycles): the observables of
+// each frame are formed in FP32 -- frame j by lane j -- from the frame
+// converted once (filled by the caller: frame j at fs + j*MCS_FS_STRIDE,
+// entries 0..F_NON), and each FP64 accumulator then takes its n FP64 adds in
+// measurement order, all accumulators at once (one per lane).  E[j] = running
+// energy after frame j (FP64).  Same formulas as on_accumulate_lanes
+// (heisenbergLib.c:678-830, xyLib.c:606-757); the per-measurement values carry
+// FP32 rounding (relative 6e-8), the sums over measurements are FP64.
+#define MCS_FS_STRIDE (F_NON + 32)
 template <int DIM>
-__device__ void on_accumulate_warp(Rep &R, float *fs, double E, long long m, int lane)
+__device__ void on_accumulate_frames(Rep &R, float *fs, const double *E, long long m0, int n, int lane)
 {
     double *acc = R.acc;
-    float *val = fs + F_NON;  // [32]: value added to acc[k], k < A_ECUR
-    if (lane == 0) {
+    if (lane < n) {
+        const float *f = fs + lane * MCS_FS_STRIDE;
+        float *val = fs + lane * MCS_FS_STRIDE + F_NON;  // [32]: value added to acc[k], k < A_ECUR
         const float inl = (float)R.inv_nl;
-        const float tx = fs[F_TOT], ty = fs[F_TOT + 1], tz = DIM == 3 ? fs[F_TOT + 2] : 0.f;
-        const float six = fs[F_SI], siy = fs[F_SI + 1], siz = DIM == 3 ? fs[F_SI + 2] : 0.f;
-        const float sjx = fs[F_SJ], sjy = fs[F_SJ + 1], sjz = DIM == 3 ? fs[F_SJ + 2] : 0.f;
+        const float tx = f[F_TOT], ty = f[F_TOT + 1], tz = DIM == 3 ? f[F_TOT + 2] : 0.f;
+        const float six = f[F_SI], siy = f[F_SI + 1], siz = DIM == 3 ? f[F_SI + 2] : 0.f;
+        const float sjx = f[F_SJ], sjy = f[F_SJ + 1], sjz = DIM == 3 ? f[F_SJ + 2] : 0.f;
         float dx = tx, dy = ty, dz = tz;
         const float len = sqrtf(dx * dx + dy * dy + dz * dz);
         if (len >= 1e-5f) { dx /= len; dy /= len; dz /= len; }
@@ -688,44 +691,63 @@ __device__ void on_accumulate_warp(Rep &R, float *fs, double E, long long m, int
         val[A_M2] = M2;
         val[A_M4] = M2 * M2;
         val[A_MTOT] = M;
-        val[A_MDM] = (float)acc[A_MPREV] * M;
-        acc[A_MPREV] = (double)M;
         val[A_MPREV] = 0.f;
         val[A_SI] = fabsf(six * inl); val[A_SI + 1] = fabsf(siy * inl); val[A_SI + 2] = fabsf(siz * inl);
         val[A_SJ] = fabsf(sjx * inl); val[A_SJ + 1] = fabsf(sjy * inl); val[A_SJ + 2] = fabsf(sjz * inl);
-        val[A_SIJ] = fs[F_SIJ] * inl;
-        const float e = (float)(E * R.inv_N);
+        val[A_SIJ] = f[F_SIJ] * inl;
+        const float e = (float)(E[lane] * R.inv_N);
         val[A_E] = e;
         val[A_E2] = e * e;
         const float ici = (float)R.inv_ci, icj = (float)R.inv_cj;
         for (int k = 0; k < 3; ++k) {
-            val[A_SIR + k] = fabsf(fs[F_SIR + k] * ici);
-            val[A_SJR + k] = fabsf(fs[F_SJR + k] * icj);
+            val[A_SIR + k] = fabsf(f[F_SIR + k] * ici);
+            val[A_SJR + k] = fabsf(f[F_SJR + k] * icj);
         }
-        val[A_SIJR] = fs[F_SIJR] * (float)R.inv_cij;
-        const float er = (fs[F_ERB] * 0.5f + fs[F_ERO]) * (float)R.inv_nr;
+        val[A_SIJR] = f[F_SIJR] * (float)R.inv_cij;
+        const float er = (f[F_ERB] * 0.5f + f[F_ERO]) * (float)R.inv_nr;
         val[A_ER] = er;
         val[A_ER2] = er * er;
-        val[A_Q] = DIM == 3 ? fs[F_Q] * (float)(1.0 / (MCS_PI_REF * 4)) : 0.f;
+        val[A_Q] = DIM == 3 ? f[F_Q] * (float)(1.0 / (MCS_PI_REF * 4)) : 0.f;
         if (R.series) {
-            double *sr = R.series + (size_t)m * MCS_NSER;
+            double *sr = R.series + (size_t)(m0 + lane) * MCS_NSER;
             sr[0] = e; sr[1] = M; sr[2] = er; sr[3] = val[A_SIJ];
         }
     }
     __syncwarp();
-    if (lane < A_ECUR && lane != A_MPREV) acc[lane] += (double)val[lane];
+    if (lane == 0) {  // <M_{m-1} M_m> runs through the frames in order
+        float prev = (float)acc[A_MPREV];
+        for (int j = 0; j < n; ++j) {
+            float *val = fs + j * MCS_FS_STRIDE + F_NON;
+            const float M = val[A_MTOT];
+            val[A_MDM] = prev * M;
+            prev = M;
+        }
+        acc[A_MPREV] = (double)prev;
+    }
+    __syncwarp();
+    if (lane < A_ECUR && lane != A_MPREV) {
+        double a = acc[lane];
+        for (int j = 0; j < n; ++j) a += (double)fs[j * MCS_FS_STRIDE + F_NON + lane];
+        acc[lane] = a;
+    }
     const int G = R.ngroup;
     if (G > 0) {
         const float inl = (float)R.inv_nl;
         for (int idx = lane; idx < (G + 1) * (G + 1); idx += 32) {
             const int ga = idx / (G + 1), gb = idx - ga * (G + 1);
-            const float ax = ga < G ? fs[F_G + 3 * ga] : fs[F_TOT] * inl, ay = ga < G ? fs[F_G + 3 * ga + 1] : fs[F_TOT + 1] * inl;
-            const float az = DIM == 3 ? (ga < G ? fs[F_G + 3 * ga + 2] : fs[F_TOT + 2] * inl) : 0.f;
-            const float bx = gb < G ? fs[F_G + 3 * gb] : fs[F_TOT] * inl, by = gb < G ? fs[F_G + 3 * gb + 1] : fs[F_TOT + 1] * inl;
-            const float bz = DIM == 3 ? (gb < G ? fs[F_G + 3 * gb + 2] : fs[F_TOT + 2] * inl) : 0.f;
-            const float d = ax * bx + ay * by + az * bz;
-            acc[A_GRP + idx] += (double)d;
-            if (ga == gb) acc[A_GRP + (G + 1) * (G + 1) + ga] += (double)(d * d);
+            double a = acc[A_GRP + idx], a4 = ga == gb ? acc[A_GRP + (G + 1) * (G + 1) + ga] : 0.0;
+            for (int j = 0; j < n; ++j) {
+                const float *f = fs + j * MCS_FS_STRIDE;
+                const float ax = ga < G ? f[F_G + 3 * ga] : f[F_TOT] * inl, ay = ga < G ? f[F_G + 3 * ga + 1] : f[F_TOT + 1] * inl;
+                const float az = DIM == 3 ? (ga < G ? f[F_G + 3 * ga + 2] : f[F_TOT + 2] * inl) : 0.f;
+                const float bx = gb < G ? f[F_G + 3 * gb] : f[F_TOT] * inl, by = gb < G ? f[F_G + 3 * gb + 1] : f[F_TOT + 1] * inl;
+                const float bz = DIM == 3 ? (gb < G ? f[F_G + 3 * gb + 2] : f[F_TOT + 2] * inl) : 0.f;
+                const float d = ax * bx + ay * by + az * bz;
+                a += (double)d;
+                a4 += (double)(d * d);
+            }
+            acc[A_GRP + idx] = a;
+            if (ga == gb) acc[A_GRP + (G + 1) * (G + 1) + ga] = a4;
         }
     }
     __syncwarp();

@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ Rep R;
-    __shared__ float fsx[F_NON + 32];  // FP32 frame for the warp fold
+    __shared__ float fsx[MCS_FS_STRIDE];  // FP32 frame for the warp fold
     Rep *Rg = reps + ids[blockIdx.x];
     load_rep(R, Rg);
     if (R.u >= R.units_total) return;
@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
                     __syncwarp();
                     for (int f = tid; f < F_NON; f += 32) fsx[f] = (float)F[f];
                     __syncwarp();
-                    on_accumulate_warp<DIM>(R, fsx, R.acc[A_ECUR], m, tid);
+                    on_accumulate_frames<DIM>(R, fsx, &R.acc[A_ECUR], m, 1, tid);
                 }
             }
             if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) {
@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(256) k_tiled_finalize(Rep *reps, const int *id
 {
     __shared__ double red[MCS_RED_DOUBLES];
     __shared__ double F[F_NON];
-    __shared__ float fsx[F_NON + 32];  // FP32 frame for the warp fold
+    __shared__ float fsx[MCS_FS_STRIDE];  // FP32 frame for the warp fold
     __shared__ long long redl[32 * 9 + 9];
     __shared__ long long Fi[16];
     __shared__ int meas;
@@ -458,8 +458,8 @@ __global__ void __launch_bounds__(256) k_tiled_finalize(Rep *reps, const int *id
             __syncwarp();
             for (int f = tid; f < F_NON; f += 32) fsx[f] = (float)F[f];
             __syncwarp();
-            if (DIM == 2) on_accumulate_warp<2>(R, fsx, R.acc[A_ECUR], m, tid);
-            else on_accumulate_warp<3>(R, fsx, R.acc[A_ECUR], m, tid);
+            if (DIM == 2) on_accumulate_frames<2>(R, fsx, &R.acc[A_ECUR], m, 1, tid);
+            else on_accumulate_frames<3>(R, fsx, &R.acc[A_ECUR], m, 1, tid);
         }
         if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) {
             float *fb = R.frame_buf + (size_t)R.frames_written * R.N * 3;
