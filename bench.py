@@ -180,7 +180,7 @@ def run_ours(args):
     ms_per_step = sum(times) / K
     # roofline of the Metropolis kernel the autotuner chose (one launch per step):
     # algorithmic bytes = lattice read + written once per sweep, FP32 (x,y) = 16 B / site update
-    kname = "k_cluster_metro<2>" if sched[0][1] > 1 else "k_resident_metro<2,SQUARE>"
+    kname = ("k_cluster_metro<2,%d>" % sched[0][2]) if sched[0][0] == "cluster" else "k_resident_metro<2,SQUARE>"
     alg_bytes = 16.0 * per_step_updates
     achieved = alg_bytes / (ms_per_step / 1000.0) / 1e9
     traffic = None

@@ -327,7 +327,9 @@ class Batch:
     SCHEDULES = {1: "plain", 2: "resident", 3: "tiled", 4: "wolff_shared", 5: "wolff_global", 6: "cluster"}
 
     def schedules(self):
-        """[(schedule name, CTAs per replica, threads per CTA, replicas)] per launch group."""
+        """[(schedule name, CTAs per replica, threads per CTA, replicas)] per launch group
+        (after prepare; a resident group's cluster size is the autotuner's
+        choice once it has run)."""
         out = []
         g = 0
         while True:
@@ -335,7 +337,10 @@ class Batch:
             if lib().mcs_batch_schedule(self._h, g, ctypes.byref(k), ctypes.byref(c), ctypes.byref(t),
                                         ctypes.byref(n)) != 0:
                 return out
-            out.append((self.SCHEDULES.get(k.value, str(k.value)), c.value, t.value, n.value))
+            name = self.SCHEDULES.get(k.value, str(k.value))
+            if k.value == 2 and c.value >= 1:
+                name = "cluster"  # a resident group the autotuner moved to the cluster kernel
+            out.append((name, max(1, c.value), t.value, n.value))
             g += 1
 
     def memory(self):

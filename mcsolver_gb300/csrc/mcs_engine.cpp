@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -56,9 +57,37 @@ struct ArenaBuilder {
     template <class T> size_t addv(const std::vector<T> &v) { return add(v.empty() ? nullptr : v.data(), v.size() * sizeof(T)); }
 };
 
+// Arenas come from the device's default memory pool, kept cached by the
+// process (release threshold raised once per device): batches and served
+// requests allocate and free an arena each, and a pooled allocation costs a
+// fraction of a cudaMalloc.
+static std::mutex g_pool_mutex;
+static bool g_pool_ready[64];
+
+static int arena_alloc(int device, size_t bytes, void **out, cudaStream_t st)
+{
+    if (device >= 0 && device < 64) {
+        std::lock_guard<std::mutex> lock(g_pool_mutex);
+        if (!g_pool_ready[device]) {
+            cudaMemPool_t pool;
+            if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+                uint64_t thr = ~0ULL;
+                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+            }
+            cudaGetLastError();
+            g_pool_ready[device] = true;
+        }
+    }
+    CUDA_TRY(cudaMallocAsync(out, bytes, st));
+    return MCS_OK;
+}
+
 Replica::~Replica()
 {
-    if (arena) cudaFree(arena);
+    if (arena) {
+        cudaSetDevice(device);
+        cudaFreeAsync(arena, 0);
+    }
 }
 
 size_t replica_acc_count(const HostModel &m)
@@ -211,10 +240,17 @@ int upload_replica(Replica *r)
 {
     if (r->arena) return MCS_OK;
     CUDA_TRY(cudaSetDevice(r->device));
-    CUDA_TRY(cudaMalloc(&r->arena, r->bytes));
     {
         static thread_local void *pinned = nullptr;
         static thread_local size_t pinned_n = 0;
+        static thread_local cudaStream_t ust = nullptr;
+        static thread_local int ust_dev = -1;
+        if (ust_dev != r->device) {
+            if (ust) cudaStreamDestroy(ust);
+            ust = nullptr;
+            CUDA_TRY(cudaStreamCreateWithFlags(&ust, cudaStreamNonBlocking));
+            ust_dev = r->device;
+        }
         if (pinned_n < r->bytes) {
             if (pinned) cudaFreeHost(pinned);
             pinned = nullptr;
@@ -222,8 +258,11 @@ int upload_replica(Replica *r)
             CUDA_TRY(cudaMallocHost(&pinned, r->bytes));
             pinned_n = r->bytes;
         }
+        int rc = arena_alloc(r->device, r->bytes, &r->arena, ust);
+        if (rc != MCS_OK) return rc;
         memcpy(pinned, r->staging.data(), r->bytes);
-        CUDA_TRY(cudaMemcpy(r->arena, pinned, r->bytes, cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpyAsync(r->arena, pinned, r->bytes, cudaMemcpyHostToDevice, ust));
+        CUDA_TRY(cudaStreamSynchronize(ust));
     }
     const uintptr_t base = (uintptr_t)r->arena;
     Rep &R = r->rep;
@@ -238,15 +277,62 @@ int upload_replica(Replica *r)
 }
 
 // ------------------------------------------------------------------ results
+int fetch_result_blocks(const std::vector<Replica *> &rs, int device)
+{
+    if (rs.empty()) return MCS_OK;
+    CUDA_TRY(cudaSetDevice(device));
+    static thread_local void *pinned = nullptr;
+    static thread_local size_t pinned_n = 0;
+    static thread_local cudaStream_t rst = nullptr;
+    static thread_local int rst_dev = -1;
+    if (rst_dev != device) {
+        if (rst) cudaStreamDestroy(rst);
+        rst = nullptr;
+        CUDA_TRY(cudaStreamCreateWithFlags(&rst, cudaStreamNonBlocking));
+        rst_dev = device;
+    }
+    size_t total = 0;
+    std::vector<size_t> off(rs.size()), len(rs.size());
+    for (size_t i = 0; i < rs.size(); ++i) {
+        off[i] = total;
+        len[i] = rs[i]->stats_off + S_NSTAT * sizeof(long long) - rs[i]->acc_off;
+        total += (len[i] + 15) & ~(size_t)15;
+    }
+    if (pinned_n < total) {
+        if (pinned) cudaFreeHost(pinned);
+        pinned = nullptr;
+        pinned_n = 0;
+        CUDA_TRY(cudaMallocHost(&pinned, total));
+        pinned_n = total;
+    }
+    for (size_t i = 0; i < rs.size(); ++i)
+        CUDA_TRY(cudaMemcpyAsync((unsigned char *)pinned + off[i], (unsigned char *)rs[i]->arena + rs[i]->acc_off, len[i],
+                                 cudaMemcpyDeviceToHost, rst));
+    CUDA_TRY(cudaStreamSynchronize(rst));
+    for (size_t i = 0; i < rs.size(); ++i) {
+        rs[i]->rblock.assign((unsigned char *)pinned + off[i], (unsigned char *)pinned + off[i] + len[i]);
+        rs[i]->rblock_fresh = true;
+    }
+    return MCS_OK;
+}
+
 int replica_results(Replica *r, const Rep &Rfinal, mcs_result *res)
 {
     const HostModel &m = r->hm;
     std::vector<double> acc(r->nacc);
     std::vector<long long> icnt(C_NINT), stats(S_NSTAT);
     unsigned char *b = (unsigned char *)r->arena;
-    CUDA_TRY(cudaMemcpy(acc.data(), b + r->acc_off, acc.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    CUDA_TRY(cudaMemcpy(icnt.data(), b + r->icnt_off, icnt.size() * sizeof(long long), cudaMemcpyDeviceToHost));
-    CUDA_TRY(cudaMemcpy(stats.data(), b + r->stats_off, stats.size() * sizeof(long long), cudaMemcpyDeviceToHost));
+    if (!r->rblock_fresh) {
+        int rc = fetch_result_blocks({r}, r->device);
+        if (rc != MCS_OK) return rc;
+    }
+    {
+        // the block spans acc .. stats in the arena (consecutive regions)
+        const unsigned char *h = r->rblock.data();
+        memcpy(acc.data(), h, acc.size() * sizeof(double));
+        memcpy(icnt.data(), h + (r->icnt_off - r->acc_off), icnt.size() * sizeof(long long));
+        memcpy(stats.data(), h + (r->stats_off - r->acc_off), stats.size() * sizeof(long long));
+    }
     if (!res) return MCS_OK;
     double *g = res->group_values;
     int gcap = res->group_capacity;
@@ -343,6 +429,10 @@ int replica_set_spins(Replica *r, const double *in)
 // ------------------------------------------------------------------ batch execution
 Batch::~Batch()
 {
+    // work of this batch may still be queued (a prepared batch that never
+    // advanced); the arenas are freed stream-ordered on the default stream
+    if (stream) cudaStreamSynchronize(stream);
+    for (cudaStream_t g : gstreams) cudaStreamSynchronize(g);
     groups.clear();
     if (d_reps) cudaFree(d_reps);
     if (d_all) cudaFree(d_all);
@@ -473,7 +563,7 @@ int Batch::setup_tiled(Group &G)
 
 cudaError_t Batch::launch_group(Group &G, int C, int threads, long long units, cudaStream_t s)
 {
-    if (C <= 1) return launch_resident_metro(G.dim, G.geom, d_reps, G.d_ids, (int)G.ids.size(), threads, G.smem, units, s);
+    if (C <= 0) return launch_resident_metro(G.dim, G.geom, d_reps, G.d_ids, (int)G.ids.size(), threads, G.smem, units, s);
     size_t sm = 0;
     for (int id : G.ids) sm = std::max<size_t>(sm, (size_t)cluster_smem_bytes(replicas[id]->rep, C));
     return launch_cluster_metro(G.dim, d_reps, G.d_ids, (int)G.ids.size(), C, threads, sm, units, s);
@@ -693,14 +783,17 @@ int Batch::prepare()
                         G->chunk = std::max<long long>(1, (1LL << 28) / std::max<long long>(1, maxn));
                         if (chunk_override > 0) G->chunk = chunk_override;
                         // candidate configurations for the autotuner: the resident
-                        // kernel, and every cluster size that divides each replica's
-                        // rows into even slabs that fit in shared memory
+                        // kernel (C = 0), and every cluster size that divides each
+                        // replica's rows into even slabs that fit in shared memory
+                        // (C = 1: the cluster kernel on one CTA, whose measurement
+                        // needs no index lists on regular lattices)
                         bool all_cl = g == MCS_GEOM_SQUARE && d > 1;
                         for (int id : set) all_cl &= replicas[id]->hm.cluster_ok != 0;
-                        if (kind == 2) G->candidates.push_back({1, G->threads});
+                        if (kind == 2) G->candidates.push_back({0, G->threads});
                         if (all_cl && cluster_override != 1) {
                             const int pc = kind == 6 ? replicas[set[0]]->pref_C : 0;
-                            for (int C : {2, 4, 8}) {
+                            for (int C : {1, 2, 4, 8}) {
+                                if (C == 1 && kind != 2) continue;
                                 if (cluster_override > 1 && C != cluster_override) continue;
                                 if (pc > 0 && C != pc) continue;
                                 bool ok = true;
@@ -724,13 +817,15 @@ int Batch::prepare()
                             groups.push_back(std::move(G));
                             continue;
                         }
-                        if (G->candidates.empty()) G->candidates.push_back({1, G->threads});
+                        if (G->candidates.empty()) G->candidates.push_back({0, G->threads});
                         if (G->candidates.size() == 1 || no_autotune) {
-                            G->C = G->candidates[0].first;
-                            G->threads = G->candidates[0].second;
-                            if (no_autotune && G->can_cluster && kind == 6) {
-                                G->C = G->candidates[0].first; G->threads = G->candidates[0].second;
-                            }
+                            // without the autotuner: the first candidate, except that a
+                            // resident group runs the one-CTA cluster kernel when it can
+                            size_t pick = 0;
+                            for (size_t ci = 0; ci < G->candidates.size() && kind == 2; ++ci)
+                                if (G->candidates[ci].first == 1) { pick = ci; break; }
+                            G->C = G->candidates[pick].first;
+                            G->threads = G->candidates[pick].second;
                             G->tuned = 1;
                         }
                     } else {
@@ -746,11 +841,40 @@ int Batch::prepare()
     return MCS_OK;
 }
 
+// Autotuner results kept for the life of the process, keyed by the group's
+// shape (kind, model dimension, geometry, replica count and sizes, coupling
+// flags, measurement interval) and its candidate list, so that a batch of the
+// same shape -- the next request of a sweep over (T, H) grids, the next bench
+// step -- starts with the configuration found before instead of probing again.
+static std::mutex g_tune_mutex;
+static std::map<std::string, std::pair<int, int>> g_tune_cache;
+
+static std::string tune_key(const Batch &b, const Group &G)
+{
+    long long sumn = 0, maxn = 0, upm_lo = 1LL << 62, upm_hi = 0;
+    int flags = 0;
+    for (int id : G.ids) {
+        const Replica &r = *b.replicas[id];
+        sumn += r.hm.N;
+        maxn = std::max<long long>(maxn, r.hm.N);
+        upm_lo = std::min<long long>(upm_lo, r.hm.upm);
+        upm_hi = std::max<long long>(upm_hi, r.hm.upm);
+        flags |= (r.rep.fullJ ? 1 : 0) | (r.rep.has_d ? 2 : 0) | (r.hm.ncirc > 0 ? 4 : 0) | (r.hm.meas_regular ? 8 : 0) |
+                 (r.hm.ngroup > 0 ? 16 : 0);
+    }
+    std::string k = std::to_string(G.kind) + "/" + std::to_string(G.dim) + "/" + std::to_string(G.geom) + "/" +
+                    std::to_string(G.ids.size()) + "/" + std::to_string(sumn) + "/" + std::to_string(maxn) + "/" +
+                    std::to_string(upm_lo) + "-" + std::to_string(upm_hi) + "/" + std::to_string(flags) + "/";
+    for (auto &c : G.candidates) k += std::to_string(c.first) + "x" + std::to_string(c.second) + ",";
+    return k;
+}
+
 int Batch::advance(long long units)
 {
     int rc = prepare();
     if (rc != MCS_OK) return rc;
     if (replicas.empty()) return MCS_OK;
+    for (auto &r : replicas) r->rblock_fresh = false;
     const bool multi = groups.size() > 1;
     while (multi && gstreams.size() < groups.size()) {
         cudaStream_t gs = nullptr;
@@ -769,6 +893,17 @@ int Batch::advance(long long units)
         Group &G = *groups[gi];
         const long long todo = std::min(units, G.max_units - G.done_units);
         if (todo <= 0 || !(G.kind == 2 || G.kind == 6) || G.tuned) continue;
+        if (G.tune_key.empty()) G.tune_key = tune_key(*this, G);
+        if (!getenv("MCSGPU_NO_TUNE_CACHE")) {
+            std::lock_guard<std::mutex> lock(g_tune_mutex);
+            auto it = g_tune_cache.find(G.tune_key);
+            if (it != g_tune_cache.end()) {
+                G.C = it->second.first;
+                G.threads = it->second.second;
+                G.tuned = 1;
+                continue;
+            }
+        }
         long long u = 0;
         const long long probe = std::max<long long>(1, std::min<long long>(4, todo / (2 * (long long)G.candidates.size() + 1)));
         G.cand_ms.assign(G.candidates.size(), 1e30);
@@ -791,8 +926,19 @@ int Batch::advance(long long units)
         G.threads = G.candidates[best].second;
         G.tuned = 1;
         pre[gi] = u;
+        if (G.cand_ms[best] < 1e29) {
+            std::lock_guard<std::mutex> lock(g_tune_mutex);
+            g_tune_cache[G.tune_key] = {G.C, G.threads};
+        }
     }
     // 2. the rest: each group on its own stream, side by side on the device
+    // (MCSGPU_TRACE=1 prints each group's schedule and device time to stderr)
+    const bool trace = getenv("MCSGPU_TRACE") != nullptr;
+    std::vector<cudaEvent_t> tev;
+    if (trace) {
+        tev.resize(2 * groups.size(), nullptr);
+        for (auto &e : tev) CUDA_TRY(cudaEventCreate(&e));
+    }
     if (multi) CUDA_TRY(cudaEventRecord(ev_fork, stream));
     for (size_t gi = 0; gi < groups.size(); ++gi) {
         Group &G = *groups[gi];
@@ -800,6 +946,7 @@ int Batch::advance(long long units)
         if (todo <= 0) continue;
         cudaStream_t gs = multi ? gstreams[gi] : stream;
         if (multi) CUDA_TRY(cudaStreamWaitEvent(gs, ev_fork, 0));
+        if (trace) CUDA_TRY(cudaEventRecord(tev[2 * gi], gs));
         if (G.kind == 4 || G.kind == 5) {
             for (long long u = 0; u < todo; u += G.chunk) {
                 long long n = std::min(G.chunk, todo - u);
@@ -844,6 +991,7 @@ int Batch::advance(long long units)
             for (long long u = 0; u < todo; ++u) CUDA_TRY(tiled_unit(G, gs, &launches));
         }
         G.done_units += todo;
+        if (trace) CUDA_TRY(cudaEventRecord(tev[2 * gi + 1], gs));
         if (multi) {
             CUDA_TRY(cudaEventRecord(gevents[gi], gs));
             CUDA_TRY(cudaStreamWaitEvent(stream, gevents[gi], 0));
@@ -856,6 +1004,20 @@ int Batch::advance(long long units)
     cudaEventElapsedTime(&ms, ev0, ev1);
     device_ms += ms;
     last_ms = ms;
+    if (trace) {
+        for (size_t gi = 0; gi < groups.size(); ++gi) {
+            const Group &G = *groups[gi];
+            float gms = -1.f;
+            if (cudaEventQuery(tev[2 * gi + 1]) == cudaSuccess) cudaEventElapsedTime(&gms, tev[2 * gi], tev[2 * gi + 1]);
+            long long sites = 0, maxn = 0;
+            for (int id : G.ids) { sites += replicas[id]->hm.N; maxn = std::max<long long>(maxn, replicas[id]->hm.N); }
+            fprintf(stderr, "mcsgpu trace: group %zu kind %d dim %d C %d threads %d replicas %zu sites %lld max %lld: %.3f ms\n",
+                    gi, G.kind, G.dim, G.C, G.threads, G.ids.size(), sites, maxn, gms);
+        }
+        fprintf(stderr, "mcsgpu trace: advance %lld units: %.3f ms\n", units, ms);
+        cudaGetLastError();
+        for (auto &e : tev) if (e) cudaEventDestroy(e);
+    }
     return MCS_OK;
 }
 
@@ -889,11 +1051,16 @@ int Batch::collect()
     const int nrep = (int)replicas.size();
     int rc = sync_descriptors();
     if (rc != MCS_OK) return rc;
+    std::vector<Replica *> rs;
+    for (auto &r : replicas) rs.push_back(r.get());
+    rc = fetch_result_blocks(rs, device);
+    if (rc != MCS_OK) return rc;
     site_updates = 0;
     for (int i = 0; i < nrep; ++i) {
         long long st[S_NSTAT];
-        CUDA_TRY(cudaMemcpy(st, (unsigned char *)replicas[i]->arena + replicas[i]->stats_off, sizeof st, cudaMemcpyDeviceToHost));
-        site_updates += replicas[i]->hm.alg == 0 ? st[S_VISITS] : st[S_FLIPPED];
+        const Replica &r = *replicas[i];
+        memcpy(st, r.rblock.data() + (r.stats_off - r.acc_off), sizeof st);
+        site_updates += r.hm.alg == 0 ? st[S_VISITS] : st[S_FLIPPED];
     }
     return MCS_OK;
 }
@@ -1081,7 +1248,7 @@ extern "C" int mcs_pt_run(mcs_pt *pt)
     if (rc != MCS_OK) return rc;
     if (b.groups.size() != 1) { set_error("parallel tempering replicas must form one kernel group"); return MCS_EINVAL; }
     Group &G = *b.groups[0];
-    int C = 1, threads = G.threads;
+    int C = 0, threads = G.threads;
     if (G.kind == 6 && !G.candidates.empty()) { C = G.candidates[0].first; threads = G.candidates[0].second; }
     const int nt = pt->nt;
     CUDA_TRY(cudaMalloc(&pt->d_perm, nt * sizeof(int)));

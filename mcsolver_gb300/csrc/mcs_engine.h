@@ -32,12 +32,16 @@ struct Replica {
     bool initialized = false;          // initial-state kernel has run
     int pref_C = 0;                    // cluster size chosen by the load balancer (0: none)
     std::vector<unsigned char> staging; // host image of the arena until upload
+    std::vector<unsigned char> rblock;  // host copy of the result block (acc, icnt, stats)
+    bool rblock_fresh = false;          // rblock matches the device (set by a batched readback)
     ~Replica();
 };
 
 int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool upload);
 int upload_replica(Replica *r);
 int replica_results(Replica *r, const Rep &Rfinal, mcs_result *res);
+// Read the result blocks of many replicas with one synchronisation.
+int fetch_result_blocks(const std::vector<Replica *> &rs, int device);
 int replica_spins(Replica *r, std::vector<double> &out);
 int replica_set_spins(Replica *r, const double *in);
 size_t replica_acc_count(const HostModel &m);
@@ -53,10 +57,11 @@ struct Group {
     int threads = 0;
     size_t smem = 0;
     long long chunk = 0;
-    int C = 1;                 // cluster size (1 = resident kernel)
+    int C = 0;                 // CTAs per replica of the cluster kernel (0 = the resident kernel)
     int tuned = 0;             // autotuner has chosen (C, threads)
     int can_cluster = 0;
     std::vector<std::pair<int, int>> candidates;  // (C, threads)
+    std::string tune_key;      // autotuner cache key (group shape and candidates)
     std::vector<double> cand_ms;
     // tiled
     int maxcol = 0, nmeas = 0;

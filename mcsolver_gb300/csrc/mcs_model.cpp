@@ -93,6 +93,20 @@ static void eng_dir(int dim, uint32_t w0, uint32_t w1, double d[3])
         return (code);            \
     } while (0)
 
+// Bitwise equality of two 9-double coupling matrices (inline: this runs once
+// per link).
+static inline bool same_bits9(const double *a, const double *b)
+{
+    uint64_t d = 0;
+    for (int k = 0; k < 9; ++k) {
+        uint64_t x, y;
+        memcpy(&x, a + k, 8);
+        memcpy(&y, b + k, 8);
+        d |= x ^ y;
+    }
+    return d == 0;
+}
+
 int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std::string *err)
 {
     if (!p) FAIL(MCS_EINVAL, "null problem");
@@ -142,7 +156,108 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
     for (long long k = 0; k < (long long)p->n_group * p->max_group; ++k)
         if (p->group_list[k] >= N) FAIL(MCS_EINVAL, "orbital-group index out of range");
 
+    // ---------------------------------------------------------------- coupling classes
+    // O(n): exchange-matrix classes over all links (exact equality).
+    std::vector<int> linkcls((size_t)N * std::max(z, 1), 0);
+    if (dim > 1) {
+        const bool ign = p->ignore_offdiag > 0;
+        ClassTable<9> cls;
+        bool anyoff = false;
+        const double *prevJ = nullptr;  // a link equal to the previous one has its class
+        int prevc = 0;
+        for (int i = 0; i < N; ++i)
+            for (int l = 0; l < p->nlink[i]; ++l) {
+                const double *J = p->link_strength + ((size_t)i * z + l) * 9;
+                if (prevJ && same_bits9(J, prevJ)) {
+                    linkcls[(size_t)i * z + l] = prevc;
+                    continue;
+                }
+                double v[9];
+                memcpy(v, J, sizeof v);
+                if (ign) v[3] = v[4] = v[5] = v[6] = v[7] = v[8] = 0.0;
+                if (dim == 2) v[2] = v[4] = v[5] = v[7] = v[8] = 0.0;  // XY reads xx,yy,xy,yx (xyLib.c:150-153)
+                for (int k = 3; k < 9; ++k) anyoff |= v[k] != 0.0;
+                linkcls[(size_t)i * z + l] = prevc = cls.find_or_add(v);
+                prevJ = J;
+            }
+        if (cls.keys.size() > 65535) FAIL(MCS_EUNSUPPORTED, "too many distinct exchange matrices");
+        std::vector<std::vector<double>> tab;
+        for (auto &k : cls.keys) tab.push_back(std::vector<double>(k.begin(), k.end()));
+        if (tab.empty()) tab.push_back(std::vector<double>(9, 0.0));
+        m->njc = (int)tab.size();
+        m->fullJ = anyoff ? 1 : 0;
+        m->jtab.resize(9 * tab.size());
+        m->jtab64.resize(9 * tab.size());
+        for (size_t c = 0; c < tab.size(); ++c)
+            for (int k = 0; k < 9; ++k) { m->jtab[9 * c + k] = (float)tab[c][k]; m->jtab64[9 * c + k] = tab[c][k]; }
+    } else {
+        // Ising: classes of Q = K |s_i| |s_j|, site types (|s_i|, class counts)
+        ClassTable<1> qcls;
+        for (int i = 0; i < N; ++i)
+            for (int l = 0; l < p->nlink[i]; ++l) {
+                int j = p->linked_orb[(size_t)i * z + l];
+                double q = p->link_strength[(size_t)i * z + l] * fabs(p->init_spin[i]) * fabs(p->init_spin[j]);
+                linkcls[(size_t)i * z + l] = qcls.find_or_add(&q);
+                if (qcls.keys.size() > MCS_MAXC) break;
+            }
+        std::vector<double> qv;
+        for (auto &k : qcls.keys) qv.push_back(k[0]);
+        if (qv.size() > MCS_MAXC) FAIL(MCS_EUNSUPPORTED, "Ising model with more than 4 distinct coupling values");
+        if (qv.empty()) qv.push_back(0.0);
+        m->nclass = (int)qv.size();
+        for (int c = 0; c < m->nclass; ++c) m->Q[c] = qv[c];
+    }
+
+    // ---------------------------------------------------------------- geometry
+    // square lattice: site id = x*Ly + y, four links to (x+-1,y), (x,y+-1),
+    // each direction one coupling class; both sides even
+    m->geom = MCS_GEOM_ELL;
+    if (z >= 4) {
+        for (int Ly = 4; Ly <= N / 4 && m->geom == MCS_GEOM_ELL; Ly += 2) {
+            if (N % Ly) continue;
+            int Lx = N / Ly;
+            if (Lx < 4 || (Lx & 1)) continue;
+            bool okg = true;
+            int code0[4] = {-1, -1, -1, -1};
+            for (int i = 0; i < N && okg; ++i) {
+                if (p->nlink[i] != 4) { okg = false; break; }
+                int x = i / Ly, y = i % Ly;
+                int want[4] = {((x + 1) % Lx) * Ly + y, ((x - 1 + Lx) % Lx) * Ly + y, x * Ly + (y + 1) % Ly,
+                               x * Ly + (y - 1 + Ly) % Ly};
+                int seen = 0;
+                for (int l = 0; l < 4; ++l) {
+                    int j = p->linked_orb[(size_t)i * z + l];
+                    int d = -1;
+                    for (int q = 0; q < 4; ++q)
+                        if (j == want[q] && !(seen & (1 << q))) { d = q; break; }
+                    if (d < 0) { okg = false; break; }
+                    seen |= 1 << d;
+                    int cc = linkcls[(size_t)i * z + l];
+                    if (code0[d] < 0) code0[d] = cc;
+                    else if (code0[d] != cc) { okg = false; break; }
+                }
+            }
+            if (okg) {
+                m->geom = MCS_GEOM_SQUARE;
+                m->Lx = Lx; m->Ly = Ly;
+                for (int d = 0; d < 4; ++d) {
+                    m->sq_cls[d] = code0[d];
+                    if (dim > 1) m->sq_code[d] = code0[d];
+                }
+            }
+        }
+    }
     // ---------------------------------------------------------------- colouring
+    // A square lattice with even sides gets the parity colouring (x + y) & 1,
+    // which is what the greedy colouring in site order produces on it: every
+    // earlier neighbour of a site has the other parity.  Other lattices are
+    // coloured greedily.
+    std::vector<int> colour(N, 0);
+    int ncol = 0;
+    if (m->geom == MCS_GEOM_SQUARE) {
+        for (int i = 0; i < N; ++i) colour[i] = ((i / m->Ly) + (i % m->Ly)) & 1;
+        ncol = 2;
+    } else {
     std::vector<int> off(N + 1, 0), adj;
     {
         std::vector<int> degc(N, 0);
@@ -163,10 +278,7 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
                 adj[off[j] + fill[j]++] = i;
             }
     }
-    std::vector<int> colour(N, 0);
-    int ncol = 0;
     {
-        std::vector<int> mark(2 * MCS_MAXZ + 8, -1);
         std::vector<char> used;
         for (int i = 0; i < N; ++i) {
             used.assign(off[i + 1] - off[i] + 2, 0);
@@ -179,6 +291,7 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
             colour[i] = c;
             ncol = std::max(ncol, c + 1);
         }
+    }
     }
     if (ncol > 64) FAIL(MCS_EUNSUPPORTED, "bond graph needs more than 64 colours");
     m->ncol = ncol;
@@ -194,33 +307,8 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
     }
     const std::vector<int> &pos = m->pos, &sites = m->sites;
 
-    // ---------------------------------------------------------------- coupling classes
-    // O(n): exchange-matrix classes over all links (exact equality).
-    std::vector<int> linkcls((size_t)N * std::max(z, 1), 0);
+    // ---------------------------------------------------------------- site classes
     if (dim > 1) {
-        const bool ign = p->ignore_offdiag > 0;
-        ClassTable<9> cls;
-        bool anyoff = false;
-        for (int i = 0; i < N; ++i)
-            for (int l = 0; l < p->nlink[i]; ++l) {
-                const double *J = p->link_strength + ((size_t)i * z + l) * 9;
-                double v[9];
-                memcpy(v, J, sizeof v);
-                if (ign) v[3] = v[4] = v[5] = v[6] = v[7] = v[8] = 0.0;
-                if (dim == 2) v[2] = v[4] = v[5] = v[7] = v[8] = 0.0;  // XY reads xx,yy,xy,yx (xyLib.c:150-153)
-                for (int k = 3; k < 9; ++k) anyoff |= v[k] != 0.0;
-                linkcls[(size_t)i * z + l] = cls.find_or_add(v);
-            }
-        if (cls.keys.size() > 65535) FAIL(MCS_EUNSUPPORTED, "too many distinct exchange matrices");
-        std::vector<std::vector<double>> tab;
-        for (auto &k : cls.keys) tab.push_back(std::vector<double>(k.begin(), k.end()));
-        if (tab.empty()) tab.push_back(std::vector<double>(9, 0.0));
-        m->njc = (int)tab.size();
-        m->fullJ = anyoff ? 1 : 0;
-        m->jtab.resize(9 * tab.size());
-        m->jtab64.resize(9 * tab.size());
-        for (size_t c = 0; c < tab.size(); ++c)
-            for (int k = 0; k < 9; ++k) { m->jtab[9 * c + k] = (float)tab[c][k]; m->jtab64[9 * c + k] = tab[c][k]; }
         // site classes: anisotropy vector and spin length |S|
         ClassTable<4> dcls;
         m->stype.assign(N, 0);
@@ -243,21 +331,6 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
         for (size_t c = 0; c < dt.size(); ++c)
             for (int k = 0; k < 4; ++k) m->dtab[4 * c + k] = (float)dt[c][k];
     } else {
-        // Ising: classes of Q = K |s_i| |s_j|, site types (|s_i|, class counts)
-        ClassTable<1> qcls;
-        for (int i = 0; i < N; ++i)
-            for (int l = 0; l < p->nlink[i]; ++l) {
-                int j = p->linked_orb[(size_t)i * z + l];
-                double q = p->link_strength[(size_t)i * z + l] * fabs(p->init_spin[i]) * fabs(p->init_spin[j]);
-                linkcls[(size_t)i * z + l] = qcls.find_or_add(&q);
-                if (qcls.keys.size() > MCS_MAXC) break;
-            }
-        std::vector<double> qv;
-        for (auto &k : qcls.keys) qv.push_back(k[0]);
-        if (qv.size() > MCS_MAXC) FAIL(MCS_EUNSUPPORTED, "Ising model with more than 4 distinct coupling values");
-        if (qv.empty()) qv.push_back(0.0);
-        m->nclass = (int)qv.size();
-        for (int c = 0; c < m->nclass; ++c) m->Q[c] = qv[c];
         ClassTable<1 + MCS_MAXC> tcls;
         std::vector<std::vector<int>> tcount;
         std::vector<double> tS;
@@ -340,47 +413,10 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
                 ok = rev;
             }
         m->exact_ok = ok ? 1 : 0;
-    }
-
-    // ---------------------------------------------------------------- geometry
-    // square lattice: site id = x*Ly + y, four links to (x+-1,y), (x,y+-1)
-    m->geom = MCS_GEOM_ELL;
-    if (z >= 4) {
-        for (int Ly = 4; Ly <= N / 4 && m->geom == MCS_GEOM_ELL; Ly += 2) {
-            if (N % Ly) continue;
-            int Lx = N / Ly;
-            if (Lx < 4 || (Lx & 1)) continue;
-            bool okg = true;
-            int code0[4] = {-1, -1, -1, -1};
-            for (int i = 0; i < N && okg; ++i) {
-                if (p->nlink[i] != 4) { okg = false; break; }
-                int x = i / Ly, y = i % Ly;
-                int want[4] = {((x + 1) % Lx) * Ly + y, ((x - 1 + Lx) % Lx) * Ly + y, x * Ly + (y + 1) % Ly,
-                               x * Ly + (y - 1 + Ly) % Ly};
-                int seen = 0;
-                for (int l = 0; l < 4; ++l) {
-                    int j = p->linked_orb[(size_t)i * z + l];
-                    int d = -1;
-                    for (int q = 0; q < 4; ++q)
-                        if (j == want[q] && !(seen & (1 << q))) { d = q; break; }
-                    if (d < 0) { okg = false; break; }
-                    seen |= 1 << d;
-                    int cc = linkcls[(size_t)i * z + l];
-                    if (code0[d] < 0) code0[d] = cc;
-                    else if (code0[d] != cc) { okg = false; break; }
-                }
-                if (okg && colour[i] != ((x + y) & 1)) okg = false;
-            }
-            if (okg && (dim > 1 || m->ntype == 1)) {
-                m->geom = MCS_GEOM_SQUARE;
-                m->Lx = Lx; m->Ly = Ly;
-                for (int d = 0; d < 4; ++d) {
-                    m->sq_cls[d] = code0[d];
-                    if (dim > 1) m->sq_code[d] = code0[d];
-                }
-            }
         }
-    }
+    // the Ising square rule needs one site type (one acceptance table)
+    if (dim == 1 && m->geom == MCS_GEOM_SQUARE && m->ntype != 1) m->geom = MCS_GEOM_ELL;
+
     // per-link codes in sweep-index space
     if (dim == 1) {
         // stride of a class for each type

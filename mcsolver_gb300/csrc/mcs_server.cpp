@@ -145,6 +145,13 @@ extern "C" int mcs_server_step(mcs_server *s, int32_t *completed)
     if (!any) return MCS_OK;
     rc = b.sync_descriptors();
     if (rc != MCS_OK) return rc;
+    {
+        std::vector<Replica *> done_r;
+        for (auto &r : b.replicas)
+            if (r->rep.u >= r->hm.units_total) done_r.push_back(r.get());
+        rc = fetch_result_blocks(done_r, s->device);  // one synchronisation for all of them
+        if (rc != MCS_OK) return rc;
+    }
     std::vector<std::pair<uint64_t, mcs_server::Done>> fin;
     std::vector<std::unique_ptr<Replica>> keep;
     std::vector<uint64_t> keep_t;
