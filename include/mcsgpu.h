@@ -87,7 +87,8 @@ typedef struct mcs_options {
     int32_t random_init;        /* 1: ignore init_spin directions, draw them
                                    from the seed (Ising sign, XY angle,
                                    Heisenberg sphere); lengths stay |S|       */
-    int32_t fp64_update;        /* 1: FP64 spin updates (drift study)         */
+    int32_t fp64_update;        /* must be 0: FP32 spin updates only (1 is    */
+                                /* rejected with MCS_EUNSUPPORTED)            */
     int32_t device;             /* CUDA device ordinal                        */
     int32_t reserved_;
 } mcs_options;

@@ -129,6 +129,9 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
     if (p->n_circuits < 0 || (p->n_circuits > 0 && !p->circuits)) FAIL(MCS_EINVAL, "bad circuit list");
     if (p->spin_frames < 0 || p->spin_frames > p->nsweep)
         FAIL(MCS_EINVAL, "spinFrame must be in [0, nsweep]");
+    if (o && o->fp64_update)
+        FAIL(MCS_EUNSUPPORTED, "fp64_update: the engine updates spins in FP32 only; the FP64 reference of the same "
+                               "stream is the oracle's engine-stream mode");
     const int dim = p->model == 1 ? 1 : (p->model == 2 ? 2 : 3);
     if (dim > 1 && !p->init_d) FAIL(MCS_EINVAL, "initD missing");
     m->model = p->model; m->dim = dim; m->alg = p->algorithm; m->N = N; m->zmax = z;

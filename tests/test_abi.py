@@ -53,3 +53,19 @@ def test_dropin_rejects_wrong_arity(engine):
     mod = engine.load_dropin("isinglib")
     with pytest.raises(TypeError):
         mod.MCMainFunction(1, 2, 3)
+
+
+def test_fp64_update_is_rejected_not_ignored(engine):
+    """The engine updates spins in FP32 only; asking for FP64 updates is an
+    error (compiled on the host, before any device work)."""
+    import ctypes as ct
+    L = engine.lib()
+    P = engine.Problem("xy", C.square_args("xy", 8, 1.0))
+    o = engine.make_options()
+    o.fp64_update = 1
+    srv = ct.c_void_p()
+    assert L.mcs_server_create(0, 1 << 20, 4, ct.byref(srv)) == 0
+    t = ct.c_uint64()
+    rc = L.mcs_server_submit(srv, ct.byref(P.struct), ct.byref(o), ct.byref(t))
+    assert rc != 0 and b"fp64_update" in L.mcs_last_error()
+    L.mcs_server_destroy(srv)
