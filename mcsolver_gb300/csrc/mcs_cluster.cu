@@ -1,18 +1,21 @@
 // mcs_cluster.cu -- cluster schedule of the Metropolis sweep (square lattice, XY / Heisenberg).
 //
-// One replica is split by rows over a thread-block cluster of C CTAs (C = 2, 4
-// or 8).  CTA r owns rows [r*RP, (r+1)*RP) of both colours (RP = Lx/C, even)
-// and keeps one ghost row on each side:
+// One replica is split by rows over a thread-block cluster of C CTAs (C = 1,
+// 2, 4, 8 or 16).  The Lx/2 row pairs are dealt out as evenly as possible:
+// CTA r owns RP_r = 2*(P/C + (r < P%C)) rows starting at x0_r (P = Lx/2; every
+// slab starts on an even row, so the parity colouring of a local row is that
+// of the global row) and keeps one ghost row on each side:
 //
-//   local index (c, xl, yh) = c*(RP+2)*hy + (xl+1)*hy + yh,   xl in [-1, RP]
+//   local index (c, xl, yh) = c*rows*hy + (xl+1)*hy + yh,   xl in [-1, RP_r]
 //
-// A colour phase updates the CTA's own sites of that colour from local data
-// only; a cluster barrier follows, then each CTA pulls the two boundary rows
-// of the colour just updated from its neighbours' shared memory (DSMEM) into
-// its ghost rows.  Measurements reduce per-CTA partial sums through DSMEM into
-// rank 0, which owns the replica's FP64 accumulators for the launch.  The
-// per-site update, the Philox counters and the measurement sums are the ones
-// of the other schedules, so the spin trajectory is the same.
+// (rows = the largest RP_r + 2, the same stride in every CTA).  A colour phase
+// updates the CTA's own sites of that colour from local data; a CTA that
+// accepts a move on its first or last row also stores the new spin into the
+// neighbouring CTA's ghost row (DSMEM), and one cluster barrier per colour
+// publishes those stores.  Measurements reduce per-CTA partial sums through
+// DSMEM into rank 0, which owns the replica's FP64 accumulators for the
+// launch.  The per-site update, the Philox counters and the measurement sums
+// are the ones of the other schedules, so the spin trajectory is the same.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -39,14 +42,29 @@ struct ClusterLayout {
     int rows, hy, nloc, nchosen;
 };
 
+// Row slab of CTA r: first row x0 and row count rp (both even).
+__host__ __device__ inline void cl_split(int Lx, int C, int r, int *x0, int *rp)
+{
+    const int P = Lx >> 1, b = P / C, e = P % C;
+    *x0 = 2 * (r * b + (r < e ? r : e));
+    *rp = 2 * (b + (r < e ? 1 : 0));
+}
+// CTA that owns row pair `pr` (rows 2pr, 2pr+1).
+__host__ __device__ inline int cl_owner(int Lx, int C, int pr)
+{
+    const int P = Lx >> 1, b = P / C, e = P % C, big = e * (b + 1);
+    return pr < big ? pr / (b + 1) : e + (pr - big) / b;
+}
+
 __host__ __device__ inline ClusterLayout cluster_layout(const Rep &R, int C)
 {
     ClusterLayout L;
-    const int RP = R.Lx / C;
+    const int P = R.Lx >> 1;
+    const int RP = 2 * (P / C + (P % C ? 1 : 0));  // the largest slab
     L.rows = RP + 2;
     L.hy = R.hy;
     L.nloc = 2 * L.rows * L.hy;
-    L.nchosen = (RP / 2) * (R.Ly / 2);
+    L.nchosen = (RP / 2) * (R.Ly / 2);  // chosen sites of the largest slab
     size_t off = 0;
     L.spins = off; off += a16((size_t)R.dim * L.nloc * sizeof(float));
     L.tables = off; off += a16((size_t)R.njc * 9 * sizeof(float) + (size_t)R.ndc * 4 * sizeof(float));
@@ -160,7 +178,11 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
     if (R.u >= R.units_total) return;
     const ClusterLayout L = cluster_layout(R, C);
     const int tid = threadIdx.x, bd = blockDim.x;
-    const int hy = L.hy, rows = L.rows, RP = rows - 2, x0 = rank * RP, nloc = L.nloc;
+    const int hy = L.hy, rows = L.rows, nloc = L.nloc;
+    int x0, RP;
+    cl_split(R.Lx, C, rank, &x0, &RP);
+    const int nch = (RP / 2) * (R.Ly / 2);  // chosen sites (even rows x even columns) of this slab
+    const int hb = R.Ly >> 1;
     const int half = R.half;
     float *sp = (float *)(smem + L.spins);
     Spins S;
@@ -176,6 +198,7 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
         const int c = i / (rows * hy);
         const int rem = i - c * rows * hy;
         const int xl = rem / hy - 1, yh = rem - (xl + 1) * hy;
+        if (xl > RP) continue;  // beyond this slab's bottom ghost row
         int x = x0 + xl;
         if (x < 0) x += R.Lx;
         if (x >= R.Lx) x -= R.Lx;
@@ -201,6 +224,18 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
     const int rprev = (rank + C - 1) % C, rnext = (rank + 1) % C;
     float *prev_sp = cl.map_shared_rank(sp, rprev);
     float *next_sp = cl.map_shared_rank(sp, rnext);
+    int x0p, RPp, x0n, RPn;  // the neighbouring slabs (the previous one's bottom ghost row is its local row RPp + 1)
+    cl_split(R.Lx, C, rprev, &x0p, &RPp);
+    cl_split(R.Lx, C, rnext, &x0n, &RPn);
+    (void)RPn;
+    // chosen index t (block row t / hb) -> owning CTA and index in its majc
+    auto chosen_owner = [&](int t, int &lq) {
+        const int o = cl_owner(R.Lx, C, t / hb);
+        int xo, rpo;
+        cl_split(R.Lx, C, o, &xo, &rpo);
+        lq = t - (xo >> 1) * hb;
+        return o;
+    };
 
     // Measurements.  Every CTA reduces its own sites into its partial slot
     // part[m & 1]; rank 0 folds measurement m into the FP64 accumulators while
@@ -232,8 +267,8 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
     float fa[4] = {0.f, 0.f, 0.f, 0.f};
     auto measure = [&](long long m, bool efull, bool fused) {
         // block spins of the own chosen sites
-        const int r0 = rank * L.nchosen;
-        for (int q = tid; q < L.nchosen; q += bd) {
+        const int r0 = (x0 >> 1) * hb;  // first chosen index of this slab
+        for (int q = tid; q < nch; q += bd) {
             const int pr = q / (R.Ly / 2);           // even-row index inside the CTA
             const int yc = q - pr * (R.Ly / 2);
             const int xl = 2 * pr, y = 2 * yc;     // chosen: even x, even y
@@ -335,21 +370,24 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
         // pass B over own chosen sites; regular lattices by arithmetic (block
         // (xr, yb) links to its four neighbour blocks), others from the lists
         if (R.meas_regular) {
-            const int hb = R.Ly >> 1, nbx = R.Lx >> 1;
-            for (int q = tid; q < L.nchosen; q += bd) {
+            const int nbx = R.Lx >> 1;
+            for (int q = tid; q < nch; q += bd) {
                 const int r = r0 + q;
                 const int xr = r / hb, yb = r - xr * hb;
                 const float mx = majc[3 * q], my = majc[3 * q + 1], mz = majc[3 * q + 2];
                 a[10] += mx; a[11] += my; a[12] += mz; a[13] += mx * mx + my * my + mz * mz;
                 const int tg[4] = {(xr + 1 == nbx ? 0 : xr + 1) * hb + yb, (xr == 0 ? nbx - 1 : xr - 1) * hb + yb,
                                    xr * hb + (yb + 1 == hb ? 0 : yb + 1), xr * hb + (yb == 0 ? hb - 1 : yb - 1)};
+                // +-y neighbours are in the same block row; +x leaves the slab
+                // after its last block row, -x before its first
+                const int brl = (x0 >> 1) + (RP >> 1) - 1;
                 float corr = 0.f;
 #pragma unroll
                 for (int d = 0; d < 4; ++d) {
-                    const int tr = tg[d];
-                    const int owner = tr / L.nchosen;
+                    int owner = rank, lq = tg[d] - r0;
+                    if (d == 0 && xr == brl) { owner = rnext; lq = tg[d] - (x0n >> 1) * hb; }
+                    if (d == 1 && xr == (x0 >> 1)) { owner = rprev; lq = tg[d] - (x0p >> 1) * hb; }
                     const float *mc = owner == rank ? majc : cl.map_shared_rank(majc, owner);
-                    const int lq = tr - owner * L.nchosen;
                     corr += on_jdot<DIM>(jt + 9 * R.rdir_cls[d], full, mx, my, mz, mc[3 * lq], mc[3 * lq + 1], mc[3 * lq + 2]);
                 }
                 a[14] += corr;
@@ -364,7 +402,7 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
                 a[15] += e - h * ((DIM == 3) ? sz : sx);
             }
         } else
-        for (int q = tid; q < L.nchosen; q += bd) {
+        for (int q = tid; q < nch; q += bd) {
             const int r = r0 + q;
             const int v = R.rorb[r];
             const float mx = majc[3 * q], my = majc[3 * q + 1], mz = majc[3 * q + 2];
@@ -374,9 +412,9 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
             for (int l = 0; l < d; ++l) {
                 const int tr = __ldg(&R.rtgt[(size_t)r * R.zmax + l]);
                 if (tr < 0) continue;
-                const int owner = tr / L.nchosen;
+                int lq;
+                const int owner = chosen_owner(tr, lq);
                 const float *mc = owner == rank ? majc : cl.map_shared_rank(majc, owner);
-                const int lq = tr - owner * L.nchosen;
                 corr += on_jdot<DIM>(jt + 9 * R.rjc[(size_t)r * R.zmax + l], full, mx, my, mz, mc[3 * lq], mc[3 * lq + 1], mc[3 * lq + 2]);
             }
             a[14] += corr;
@@ -486,10 +524,10 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
                 if (on_trial<DIM>(R, jt, dt, S, li, 0, w, beta, h, [&](auto &&f) { cl_links(R, rows, c, xl, yh, f); }, &dE)) {
                     dEf += dE;
                     ++nacc;
-                    // own row 0 is the previous CTA's bottom ghost (local row RP+1),
-                    // own row RP-1 the next CTA's top ghost (local row 0)
+                    // own row 0 is the previous CTA's bottom ghost (its local row
+                    // RPp+1), own row RP-1 the next CTA's top ghost (local row 0)
                     if (xl == 0) {
-                        const int g = cb + (RP + 1) * hy + yh;
+                        const int g = cb + (RPp + 1) * hy + yh;
                         prev_sp[g] = S.x[li];
                         prev_sp[nloc + g] = S.y[li];
                         if (DIM == 3) prev_sp[2 * nloc + g] = S.z[li];
@@ -561,29 +599,80 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
 
 long long cluster_smem_bytes(const Rep &r, int C) { return (long long)cluster_layout(r, C).total; }
 
+// Shared-memory and cluster-size attributes of one instantiation (set once,
+// raised when a larger request comes).
 template <int DIM, int NT>
-static cudaError_t launch_cluster_t(Rep *reps, const int *ids, int nrep, int C, size_t smem, long long max_units,
-                                    cudaStream_t st)
+static cudaError_t prep_cluster_kernel(size_t smem, int C)
 {
     static size_t done = 0;
+    static bool nonportable = false;
     if (smem > done) {
         cudaError_t e = cudaFuncSetAttribute(k_cluster_metro<DIM, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         done = smem;
     }
-    cudaLaunchConfig_t cfg = {};
+    if (C > 8 && !nonportable) {  // clusters above 8 CTAs are an opt-in
+        cudaError_t e = cudaFuncSetAttribute(k_cluster_metro<DIM, NT>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) return e;
+        nonportable = true;
+    }
+    return cudaSuccess;
+}
+
+template <int DIM, int NT>
+static void cluster_config(cudaLaunchConfig_t &cfg, cudaLaunchAttribute *attr, int nrep, int C, size_t smem,
+                           cudaStream_t st)
+{
+    cfg = {};
     cfg.gridDim = dim3(nrep * C, 1, 1);
     cfg.blockDim = dim3(NT, 1, 1);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
-    cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = C;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+}
+
+template <int DIM, int NT>
+static cudaError_t launch_cluster_t(Rep *reps, const int *ids, int nrep, int C, size_t smem, long long max_units,
+                                    cudaStream_t st)
+{
+    cudaError_t e = prep_cluster_kernel<DIM, NT>(smem, C);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr[1];
+    cluster_config<DIM, NT>(cfg, attr, nrep, C, smem, st);
     return cudaLaunchKernelEx(&cfg, k_cluster_metro<DIM, NT>, reps, ids, max_units, C);
+}
+
+// Clusters of this shape the device can hold at once (0: it cannot launch one).
+template <int DIM, int NT>
+static int cluster_active_t(int C, size_t smem)
+{
+    if (prep_cluster_kernel<DIM, NT>(smem, C) != cudaSuccess) { cudaGetLastError(); return 0; }
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr[1];
+    cluster_config<DIM, NT>(cfg, attr, 1, C, smem, 0);
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, k_cluster_metro<DIM, NT>, &cfg) != cudaSuccess) { cudaGetLastError(); return 0; }
+    return n;
+}
+
+int cluster_active(int dim, int C, int threads, size_t smem)
+{
+    if (dim == 2) {
+        if (threads == 256) return cluster_active_t<2, 256>(C, smem);
+        if (threads == 512) return cluster_active_t<2, 512>(C, smem);
+        if (threads == 1024) return cluster_active_t<2, 1024>(C, smem);
+    } else if (dim == 3) {
+        if (threads == 256) return cluster_active_t<3, 256>(C, smem);
+        if (threads == 512) return cluster_active_t<3, 512>(C, smem);
+        if (threads == 1024) return cluster_active_t<3, 1024>(C, smem);
+    }
+    return 0;
 }
 
 template <int DIM>

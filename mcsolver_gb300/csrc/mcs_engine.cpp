@@ -630,9 +630,8 @@ void Batch::place_replicas(int max_smem)
         }
         if (resident_smem_bytes(r.rep) <= max_smem) q.opts.push_back(1);
         if (clusterable)
-            for (int C : {2, 4, 8}) {
-                const int Lx = r.hm.Lx;
-                if (Lx % C || (Lx / C) % 2 || cluster_smem_bytes(r.rep, C) > max_smem) continue;
+            for (int C : {2, 4, 8, 16}) {
+                if (r.hm.Lx / 2 < C || cluster_smem_bytes(r.rep, C) > max_smem) continue;
                 if (cluster_override > 1 && C != cluster_override) continue;
                 q.opts.push_back(C);
             }
@@ -747,7 +746,7 @@ int Batch::prepare()
                 if (kind == 1) for (int id : ids) sets.push_back({id});
                 else if (kind == 6) {
                     // one launch configuration per group: split by the balancer's cluster size
-                    for (int C : {0, 2, 4, 8}) {
+                    for (int C : {0, 2, 4, 8, 16}) {
                         std::vector<int> sub;
                         for (int id : ids) if (replicas[id]->pref_C == C) sub.push_back(id);
                         if (!sub.empty()) sets.push_back(sub);
@@ -792,19 +791,20 @@ int Batch::prepare()
                         if (kind == 2) G->candidates.push_back({0, G->threads});
                         if (all_cl && cluster_override != 1) {
                             const int pc = kind == 6 ? replicas[set[0]]->pref_C : 0;
-                            for (int C : {1, 2, 4, 8}) {
+                            for (int C : {1, 2, 4, 8, 16}) {
                                 if (C == 1 && kind != 2) continue;
                                 if (cluster_override > 1 && C != cluster_override) continue;
                                 if (pc > 0 && C != pc) continue;
                                 bool ok = true;
                                 size_t sm = 0;
                                 for (int id : set) {
-                                    const int Lx = replicas[id]->hm.Lx;
-                                    ok &= Lx % C == 0 && (Lx / C) % 2 == 0 && Lx / C >= 2;
+                                    // every CTA holds at least one row pair
+                                    ok &= replicas[id]->hm.Lx / 2 >= C;
                                     sm = std::max<size_t>(sm, (size_t)cluster_smem_bytes(replicas[id]->rep, C));
                                 }
                                 if (!ok || (int)sm > max_smem) continue;
-                                for (int th : {512, 256, 1024}) G->candidates.push_back({C, th});
+                                for (int th : {512, 256, 1024})
+                                    if (cluster_active(d, C, th, sm) > 0) G->candidates.push_back({C, th});
                             }
                             G->can_cluster = 1;
                         }

@@ -172,6 +172,7 @@ long long wolff_smem_bytes(const Rep &r, int *gstate);
 cudaError_t launch_wolff(int dim, int geom, Rep *reps, const int *ids, int nrep, int threads, size_t smem,
                          long long max_units, int gstate, cudaStream_t st);
 long long cluster_smem_bytes(const Rep &r, int C);
+int cluster_active(int dim, int C, int threads, size_t smem);  // 0: this cluster shape cannot launch
 cudaError_t launch_pt_exchange(Rep *reps, int nt, int *perm, unsigned long long seed, long long *acc_cnt,
                                long long *att_cnt, cudaStream_t st);
 cudaError_t launch_cluster_metro(int dim, Rep *reps, const int *ids, int nrep, int C, int threads, size_t smem,

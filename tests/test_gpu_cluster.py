@@ -48,6 +48,43 @@ def test_cluster_matches_resident(engine, name, model, mk, csize):
     assert eb["site_updates"] == ea["site_updates"]
 
 
+UNEVEN = [
+    ("xy_L36_C8", "xy", 8, lambda: C.square_args("xy", 36, 0.9, nthermal=6, nsweep=12, frames=12)),
+    ("xy_L40_C16", "xy", 16, lambda: C.square_args("xy", 40, 1.1, nthermal=6, nsweep=12, frames=12)),
+    ("heis_L44_C4_dmi_h", "heisenberg", 4, lambda: C.square_args("heisenberg", 44, 0.6, h=0.2, dmi=0.4,
+                                                                  nthermal=6, nsweep=12, frames=12)),
+    ("heis_L72_C16_dmi", "heisenberg", 16, lambda: C.square_args_fast("heisenberg", 72, 0.7, dmi=0.4,
+                                                                      nthermal=4, nsweep=8, frames=8)),
+]
+
+
+@pytest.mark.parametrize("name,model,csize,mk", UNEVEN, ids=[c[0] for c in UNEVEN])
+def test_uneven_row_split_matches_resident(engine, name, model, csize, mk):
+    """Row pairs dealt out unevenly (slabs of different heights, up to 16 CTAs)
+    give the resident schedule's trajectory and observables."""
+    args = mk()
+    a, ea = _run(engine, model, args, 1)
+    old = os.environ.get("MCSGPU_CLUSTER")
+    os.environ["MCSGPU_CLUSTER"] = str(csize)
+    try:
+        bt = engine.Batch()
+        bt.add(model, args, seed=3, random_init=True)
+        bt.prepare()
+        bt.run()
+        sched = bt.schedules()
+        b, eb = bt.result(0)
+        bt.close()
+    finally:
+        if old is None:
+            os.environ.pop("MCSGPU_CLUSTER", None)
+        else:
+            os.environ["MCSGPU_CLUSTER"] = old
+    assert sched[0][0] == "cluster" and sched[0][1] == csize, sched
+    np.testing.assert_allclose(eb["frames"], ea["frames"], atol=2e-5)
+    np.testing.assert_allclose(np.array(b[:27]), np.array(a[:27]), rtol=1e-5, atol=1e-6)
+    assert eb["site_updates"] == ea["site_updates"]
+
+
 def test_replica_too_large_for_any_cluster_runs_once_on_tiles(engine):
     """XY L=512: 2 MB of spins fit neither one CTA nor a cluster of 8; the
     cluster group falls back to the tiled schedule and the replica must join
