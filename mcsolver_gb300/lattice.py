@@ -67,9 +67,11 @@ def _lattice_links(L, norb, bonds):
 
 
 def lattice_args(model, L, norb, bonds, T, h=0.0, S=None, D=None, nthermal=10, nsweep=10, tau=0, algo=0,
-                 ki=((0, 0), (0, 0, 0)), groups=(), circuits=(), frames=0, flunc=0.0):
+                 ki=((0, 0), (0, 0, 0)), groups=(), circuits=(), frames=0, flunc=0.0, group_in_sc=True):
     """MCMainFunction tuple for a periodic lattice; J, D and h are divided by T
-    as mcMain.py does (mcMain.py:21-31, :121, :244)."""
+    as mcMain.py does (mcMain.py:21-31, :121, :244).  An orbital group holds
+    its orbitals in every cell (group_in_sc) or in cell (0,0,0) only
+    (Lattice.py:208-211)."""
     T = max(T, 0.1)
     S = S or [1.0] * norb
     D = D or [[0.0, 0.0, 0.0]] * norb
@@ -138,7 +140,10 @@ def lattice_args(model, L, norb, bonds, T, h=0.0, S=None, D=None, nthermal=10, n
                         circ.append(sid(x + ov[0], y + ov[1], zz + ov[2], o))
     grp = []
     maxg = 1
-    gl = [[sid(x, y, zz, o) for o in g for x in range(Lx) for y in range(Ly) for zz in range(Lz)] for g in groups]
+    if group_in_sc:
+        gl = [[sid(x, y, zz, o) for o in g for x in range(Lx) for y in range(Ly) for zz in range(Lz)] for g in groups]
+    else:
+        gl = [[sid(0, 0, 0, o) for o in g] for g in groups]
     if gl:
         maxg = max(len(g) for g in gl)
         for g in gl:
