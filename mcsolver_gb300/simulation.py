@@ -213,10 +213,11 @@ def start_simulation(rpath: str, workdir: str = ".", seed: int = 1, device: int 
     built = [point_args(p, T, H) for (_, T, H) in pts]
     b = Batch(device=device)
     with ThreadPoolExecutor(max_workers=max(1, threads)) as pool:
-        list(pool.map(lambda k: b.add(built[k][0], built[k][1], seed=seed + pts[k][0], schedule=schedule),
-                      range(len(pts))))
+        # adds from several threads: the engine's replica index is returned by add
+        idx = list(pool.map(lambda k: b.add(built[k][0], built[k][1], seed=seed + pts[k][0], schedule=schedule),
+                            range(len(pts))))
     b.run()
-    res = [b.result(k) for k in range(len(pts))]
+    res = [b.result(i) for i in idx]
     b.close()
     Lx, Ly, Lz = p["LPack"]
     N = Lx * Ly * Lz * len(p["pos"])
