@@ -483,6 +483,31 @@ def main():
     run_ours(args)
 
 
+def replica_seeds(rank: int, n: int):
+    """Philox keys of the n replicas of rank `rank`: disjoint across ranks."""
+    return [1000 + 100000 * rank + k for k in range(n)]
+
+
+def combine_ranks(t_local: float, work_local: float, dist, device):
+    """Slowest rank's time and the summed work of all ranks (replicas only:
+    nothing else crosses ranks)."""
+    import torch
+    tt = torch.tensor([t_local], dtype=torch.float64, device=device)
+    ww = torch.tensor([work_local], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    dist.all_reduce(ww, op=dist.ReduceOp.SUM)
+    return tt.item(), ww.item()
+
+
+def multi_line(work_total: float, tmax: float, n: int, K: int, W: int, S: int, launches: int):
+    return {"metric": "site_updates_per_s", "value": work_total / tmax, "unit": "site_updates/s",
+            "n_gpus": n, "steps": K, "warmup": W, "ms_per_step": tmax * 1000 / K,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 update / f64 accumulate", "data": "synthetic", "gpu_launches": launches,
+            "config": {"workload": WORKLOAD, "model": "XY", "L": L, "n_temperatures": NTEMP,
+                       "sweeps_per_step": S, "parallelism": "replicas only (%d independent copies)" % n}}
+
+
 def run_multi(args):
     """Replicas only: every rank runs the full workload on its own GPU; value
     sums the ranks' work over the slowest rank's time."""
@@ -498,24 +523,22 @@ def run_multi(args):
     dist.barrier()
     K, W, S = args.steps, args.warmup, args.sweeps
     batch = eng.Batch(device=local)
+    seeds = replica_seeds(dist.get_rank(), NTEMP)
     for k, a in enumerate(workload_args(nsweep=(W + K) * S + 1)):
-        batch.add("xy", a, seed=1000 + 100000 * dist.get_rank() + k, random_init=True)
+        batch.add("xy", a, seed=seeds[k], random_init=True)
     batch.prepare()
     for _ in range(W):
         batch.advance(S)
+    l0 = batch.stats()["launches"]
     dist.barrier()
     torch.cuda.synchronize()
     t = sum(batch.advance(S) for _ in range(K)) / 1000.0
-    tt = torch.tensor([t], device="cuda")
-    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-    n = dist.get_world_size()
+    torch.cuda.synchronize()
+    launches = batch.stats()["launches"] - l0
+    batch.close()
+    tmax, work = combine_ranks(t, float(NTEMP * L * L * S * K), dist, "cuda")
     if dist.get_rank() == 0:
-        per = NTEMP * L * L * S * K
-        print(json.dumps({"metric": "site_updates_per_s", "value": per * n / tt.item(), "unit": "site_updates/s",
-                          "n_gpus": n, "steps": K, "warmup": W, "ms_per_step": tt.item() * 1000 / K,
-                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                          "dtype": "f32 update / f64 accumulate", "data": "synthetic",
-                          "config": {"workload": WORKLOAD, "parallelism": "replicas only"}}))
+        print(json.dumps(multi_line(work, tmax, dist.get_world_size(), K, W, S, launches)))
     dist.destroy_process_group()
 
 

@@ -460,7 +460,9 @@ __device__ void on_frame(const Rep &R, const float *jt, const float *dt, const S
     // is the total spin of pass A
     if (tid < 3 * MCS_MAXG && (R.gall >> (tid / 3)) & 1) Fout[F_G + tid] = Fout[F_TOT + tid % 3];
     for (int g0 = 0; g0 < R.ngroup; g0 += 4) {
-        const int keep = ~(R.gall >> g0) & 15;
+        // groups g0..g0+3 that exist and do not hold every site
+        const int ng = min(4, R.ngroup - g0);
+        const int keep = ~(R.gall >> g0) & ((1 << ng) - 1);
         if (!keep) continue;
         float a[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         const int e = min(ve, R.N);
