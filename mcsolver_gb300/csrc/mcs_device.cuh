@@ -788,13 +788,46 @@ __device__ __forceinline__ int is_majority_sign(const Rep &R, const signed char 
     return ((double)word * (1.0 / 4294967296.0) > 0.5) ? 1 : -1;
 }
 
+// Majority sign from a block's sign sum; a tie takes the Philox word of the
+// evaluating site and slot (the same decision as is_majority_sign).
+__device__ __forceinline__ int is_majority_from_sum(int avg, const uint4 &w, int slot)
+{
+    if (avg > 0) return 1;
+    if (avg < 0) return -1;
+    uint32_t word = (slot & 3) == 0 ? w.x : (slot & 3) == 1 ? w.y : (slot & 3) == 2 ? w.z : w.w;
+    return ((double)word * (1.0 / 4294967296.0) > 0.5) ? 1 : -1;
+}
+
+// Chosen-site lists of the Ising frame staged in shared memory by a resident
+// launch: tgt[r*zmax+l] = chosen index of the l-th renormalised target, -1
+// when that target is not a chosen site, -2 when the link does not exist.
+struct IsLists {
+    const int *rorb;
+    const unsigned char *rdeg;
+    const int *tgt;
+    const unsigned char *kc;
+};
+
 // Ising frame over [vb, ve): pairs, renormalised energy, per-type sign sums,
 // full per-class directed bond sums.  Fd (4 doubles) and Fi (MAXT+MAXC ints).
+// msum: optional shared cache [n_rorb] of the chosen blocks' sign sums, used
+// when the block covers every chosen site (one spin length): each block's sum
+// is then formed once per measurement instead of at each of its evaluations.
+// il: optional staged lists (with msum).
 template <int GEOM>
 __device__ void is_frame(const Rep &R, const IsEntry *itab, const signed char *s, int vb, int ve, long long m,
-                         double *red, double *Fd, long long *redl, long long *Fi)
+                         double *red, double *Fd, long long *redl, long long *Fi, signed char *msum = nullptr,
+                         const IsLists *il = nullptr)
 {
     const int tid = threadIdx.x, bd = blockDim.x;
+    if (R.is_fast && msum) {
+        for (int r = tid; r < R.n_rorb; r += bd) {
+            int a = 0;
+            for (int k = 0; k < R.ncl; ++k) a += s[__ldg(&R.rcl[(size_t)r * R.ncl + k])];
+            msum[r] = (signed char)a;
+        }
+        __syncthreads();
+    }
     if (R.is_fast) {
         // one spin length S0 and <= 4 renormalised coupling values: every sum
         // of the frame is an integer times a constant
@@ -808,17 +841,44 @@ __device__ void is_frame(const Rep &R, const IsEntry *itab, const signed char *s
             c[0] += sp; c[1] += sq; c[2] += sp * sq;
         }
         e = min(ve, R.n_rorb);
+        if (il && msum) {
+            const int z = R.zmax;
+            for (int v = vb + tid; v < e; v += bd) {
+                const int j = il->rorb[v];
+                uint4 w = philox_t((uint32_t)j, m, 0x3000u, R.seed);
+                const int mj = is_majority_from_sum(msum[v], w, 0);
+                const int d = il->rdeg[v];
+                for (int l = 0; l < d; ++l) {
+                    const int slot = 1 + l;
+                    if ((slot & 3) == 0) w = philox_t((uint32_t)j, m, 0x3000u + (uint32_t)(slot >> 2), R.seed);
+                    const int tr = il->tgt[v * z + l];
+                    if (tr == -2) continue;
+                    const int mt = is_majority_from_sum(tr >= 0 ? msum[tr] : 0, w, slot);
+                    const int k = il->kc[v * z + l];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) c[3 + q] += (q == k) ? mj * mt : 0;
+                }
+                c[7] += s[j];
+            }
+            e = 0;  // done
+        }
         for (int v = vb + tid; v < e; v += bd) {
             const int j = __ldg(&R.rorb[v]);
             uint4 w = philox_t((uint32_t)j, m, 0x3000u, R.seed);
-            const int mj = is_majority_sign(R, s, j, w, 0);
+            const int mj = msum ? is_majority_from_sum(msum[v], w, 0) : is_majority_sign(R, s, j, w, 0);
             const int d = R.rdeg[v];
             for (int l = 0; l < d; ++l) {
                 const int slot = 1 + l;
                 if ((slot & 3) == 0) w = philox_t((uint32_t)j, m, 0x3000u + (uint32_t)(slot >> 2), R.seed);
                 const int t = __ldg(&R.rlink[(size_t)v * R.zmax + l]);
                 if (t < 0) continue;
-                const int mt = is_majority_sign(R, s, t, w, slot);
+                int mt;
+                if (msum) {
+                    const int tr = __ldg(&R.rtgt[(size_t)v * R.zmax + l]);  // chosen index of t, -1: not chosen
+                    mt = is_majority_from_sum(tr >= 0 ? msum[tr] : 0, w, slot);
+                } else {
+                    mt = is_majority_sign(R, s, t, w, slot);
+                }
                 const int k = R.rkc[(size_t)v * R.zmax + l];
 #pragma unroll
                 for (int q = 0; q < 4; ++q) c[3 + q] += (q == k) ? mj * mt : 0;

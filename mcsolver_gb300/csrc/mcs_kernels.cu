@@ -27,6 +27,7 @@ static __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~
 
 struct SmemLayout {
     size_t spins, tables, stype, majc, red, F, redl, Fi, acc, total;
+    size_t il_rorb, il_rdeg, il_tgt, il_kc;  // staged Ising chosen-site lists (0: not staged)
 };
 // Shared-memory plan of a resident replica.  The block-spin cache of the
 // renormalised lattice is included only when it fits (flag returned in majc
@@ -49,9 +50,21 @@ __host__ __device__ inline SmemLayout smem_layout(const Rep &R, size_t limit = 2
     L.redl = off; off += (32 * 16 + 16) * sizeof(long long);
     L.Fi = off; off += 16 * sizeof(long long);
     L.acc = off; off += align16((size_t)R.nacc * sizeof(double) + C_NINT * sizeof(long long));
-    L.majc = 0;
-    size_t mbytes = align16((size_t)R.n_rorb * 3 * sizeof(float));
-    if (R.dim > 1 && off + mbytes <= limit) { L.majc = off; off += mbytes; }
+    L.majc = 0;  // O(n): block spins of the chosen sites; Ising: their sign sums
+    size_t mbytes = R.dim > 1 ? align16((size_t)R.n_rorb * 3 * sizeof(float)) : align16((size_t)R.n_rorb);
+    if (off + mbytes <= limit) { L.majc = off; off += mbytes; }
+    // Ising with one spin length: the chosen-site lists of the frame, when they fit
+    L.il_rorb = L.il_rdeg = L.il_tgt = L.il_kc = 0;
+    if (R.dim == 1 && R.is_fast && L.majc) {
+        const size_t nz = (size_t)R.n_rorb * (R.zmax > 0 ? R.zmax : 1);
+        const size_t need = align16((size_t)R.n_rorb * 4) + align16((size_t)R.n_rorb) + align16(nz * 4) + align16(nz);
+        if (off + need <= limit) {
+            L.il_rorb = off; off += align16((size_t)R.n_rorb * 4);
+            L.il_rdeg = off; off += align16((size_t)R.n_rorb);
+            L.il_tgt = off; off += align16(nz * 4);
+            L.il_kc = off; off += align16(nz);
+        }
+    }
     L.total = off;
     return L;
 }
@@ -134,6 +147,21 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
         }
         for (int k = tid; k < R.njc * 9; k += bd) jt[k] = R.jtab[k];
         for (int k = tid; k < R.ndc * 4; k += bd) dt[k] = R.dtab[k];
+    }
+    IsLists il;
+    il.rorb = nullptr;
+    if (DIM == 1 && L.il_rorb) {
+        int *rorb = (int *)(smem + L.il_rorb);
+        unsigned char *rdeg = smem + L.il_rdeg;
+        int *tgt = (int *)(smem + L.il_tgt);
+        unsigned char *kc = smem + L.il_kc;
+        const int z = R.zmax > 0 ? R.zmax : 1;
+        for (int r = tid; r < R.n_rorb; r += bd) { rorb[r] = R.rorb[r]; rdeg[r] = R.rdeg[r]; }
+        for (int i = tid; i < R.n_rorb * z; i += bd) {
+            tgt[i] = R.rlink[i] < 0 ? -2 : R.rtgt[i];
+            kc[i] = R.rkc[i];
+        }
+        il.rorb = rorb; il.rdeg = rdeg; il.tgt = tgt; il.kc = kc;
     }
     __syncthreads();
     acc_to_smem(R, smem + L.acc);
@@ -240,7 +268,8 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
             fold();
             const long long m = R.m;
             if (DIM == 1) {
-                is_frame<GEOM>(R, itab, S.s, 0, max(N, max(R.nlat, R.n_rorb)), m, red, F, redl, Fi);
+                is_frame<GEOM>(R, itab, S.s, 0, max(N, max(R.nlat, R.n_rorb)), m, red, F, redl, Fi,
+                               L.majc ? (signed char *)(smem + L.majc) : nullptr, il.rorb ? &il : nullptr);
                 if (tid == 0) {
                     if (R.alg == 1 && u >= R.units_thermal) R.icnt[C_ACC_MEAS] = 1;
                     is_accumulate(R, F, Fi, S.s[R.last_site], m);
