@@ -148,7 +148,8 @@ int mcs_batch_memory(mcs_batch *b, uint64_t *device_bytes, uint64_t *readback_by
  * 2 resident (one CTA per replica), 3 tiled (global memory, graphs),
  * 4 Wolff in shared memory, 5 Wolff in global memory, 6 thread-block cluster;
  * *cluster = CTAs per replica of the cluster kernel (0 = the one-CTA resident
- * kernel), *threads per CTA, *replicas in the group.
+ * kernel; -k = the resident kernel with k copies of each replica, one per CTA
+ * of a cluster), *threads per CTA, *replicas in the group.
  * Returns MCS_EINVAL when `group` is out of range (no counterpart in the
  * reference, which has one schedule). */
 int mcs_batch_schedule(mcs_batch *b, int32_t group, int32_t *kind, int32_t *cluster, int32_t *threads,

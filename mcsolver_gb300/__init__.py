@@ -340,7 +340,8 @@ class Batch:
             name = self.SCHEDULES.get(k.value, str(k.value))
             if k.value == 2 and c.value >= 1:
                 name = "cluster"  # a resident group the autotuner moved to the cluster kernel
-            out.append((name, max(1, c.value), t.value, n.value))
+            # c < 0: resident kernel with -c copies of each replica (one per CTA of a cluster)
+            out.append((name, -c.value if c.value < 0 else max(1, c.value), t.value, n.value))
             g += 1
 
     def memory(self):

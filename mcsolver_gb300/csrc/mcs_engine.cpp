@@ -563,7 +563,11 @@ int Batch::setup_tiled(Group &G)
 
 cudaError_t Batch::launch_group(Group &G, int C, int threads, long long units, cudaStream_t s)
 {
-    if (C <= 0) return launch_resident_metro(G.dim, G.geom, d_reps, G.d_ids, (int)G.ids.size(), threads, G.smem, units, s);
+    // C = 0: the resident kernel; C < 0: the resident kernel with -C copies of
+    // each replica in a cluster; C >= 1: the row-split cluster kernel
+    if (C <= 0)
+        return launch_resident_metro(G.dim, G.geom, d_reps, G.d_ids, (int)G.ids.size(), threads, G.smem, units, s,
+                                     C < 0 ? -C : 1);
     size_t sm = 0;
     for (int id : G.ids) sm = std::max<size_t>(sm, (size_t)cluster_smem_bytes(replicas[id]->rep, C));
     return launch_cluster_metro(G.dim, d_reps, G.d_ids, (int)G.ids.size(), C, threads, sm, units, s);
@@ -701,6 +705,11 @@ int Batch::prepare()
     const int nrep = (int)replicas.size();
     if (nrep == 0) { prepared = true; return MCS_OK; }
     const int max_smem = resident_max_smem();
+    int nsm_ = 0;
+    if (cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+        cudaGetLastError();
+        nsm_ = 1;
+    }
     if (const char *e = getenv("MCSGPU_CLUSTER")) cluster_override = atoi(e);
     if (const char *e = getenv("MCSGPU_NO_AUTOTUNE")) no_autotune = atoi(e);
     std::vector<Rep> host(nrep);
@@ -788,8 +797,25 @@ int Batch::prepare()
                         // needs no index lists on regular lattices)
                         bool all_cl = g == MCS_GEOM_SQUARE && d > 1;
                         for (int id : set) all_cl &= replicas[id]->hm.cluster_ok != 0;
-                        if (kind == 2) G->candidates.push_back({0, G->threads});
-                        if (all_cl && cluster_override != 1) {
+                        int copies_only = 0;  // MCSGPU_COPIES=k: only the resident kernel with k copies
+                        if (const char *e = getenv("MCSGPU_COPIES")) copies_only = atoi(e);
+                        if (kind == 2 && copies_only > 1) {
+                            if (resident_copies_active(d, g, copies_only, G->threads, G->smem) > 0)
+                                G->candidates.push_back({-copies_only, G->threads});
+                            else
+                                G->candidates.push_back({0, G->threads});
+                        } else if (kind == 2) {
+                            G->candidates.push_back({0, G->threads});
+                            // copies of each replica over a cluster of 2 or 4 CTAs: for groups
+                            // that would leave SMs idle (Metropolis only)
+                            bool metro = true;
+                            for (int id : set) metro &= replicas[id]->hm.alg == 0;
+                            for (int cp : {2, 4})
+                                if (metro && cluster_override != 1 && (int)set.size() * cp <= 2 * nsm_ &&
+                                    resident_copies_active(d, g, cp, G->threads, G->smem) > 0)
+                                    G->candidates.push_back({-cp, G->threads});
+                        }
+                        if (all_cl && cluster_override != 1 && copies_only <= 1) {
                             const int pc = kind == 6 ? replicas[set[0]]->pref_C : 0;
                             for (int C : {1, 2, 4, 8, 16}) {
                                 if (C == 1 && kind != 2) continue;
@@ -1266,9 +1292,31 @@ extern "C" int mcs_pt_run(mcs_pt *pt)
         return launch_pt_exchange(b.d_reps, nt, pt->d_perm, pt->seed ^ 0x5054ULL, pt->d_acc, pt->d_att, s);
     };
     CUDA_TRY(cudaEventRecord(b.ev0, b.stream));
-    const int K = 32;
     long long u = 0;
-    if (total >= 2 * K) {
+    // configuration: time each candidate of the group (one CTA per replica, or
+    // copies of each replica over a cluster) on real sweeps + exchanges
+    if (G.kind == 2 && G.candidates.size() > 1 && total >= 16 * (long long)G.candidates.size()) {
+        float best = 1e30f;
+        for (auto &cand : G.candidates) {
+            const int cC = cand.first, cth = cand.second;
+            CUDA_TRY(cudaEventRecord(b.ev_a, b.stream));
+            cudaError_t e = cudaSuccess;
+            for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
+                e = b.launch_group(G, cC, cth, 1, b.stream);
+                if (e == cudaSuccess)
+                    e = launch_pt_exchange(b.d_reps, nt, pt->d_perm, pt->seed ^ 0x5054ULL, pt->d_acc, pt->d_att, b.stream);
+            }
+            if (e != cudaSuccess) { set_error(std::string("parallel tempering probe: ") + cudaGetErrorString(e)); return MCS_ECUDA; }
+            CUDA_TRY(cudaEventRecord(b.ev_b, b.stream));
+            CUDA_TRY(cudaEventSynchronize(b.ev_b));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, b.ev_a, b.ev_b);
+            if (ms < best) { best = ms; C = cC; threads = cth; }
+            u += 4;
+        }
+    }
+    const int K = 32;
+    if (total - u >= 2 * K) {
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
         CUDA_TRY(cudaStreamBeginCapture(b.stream2, cudaStreamCaptureModeThreadLocal));

@@ -178,7 +178,8 @@ cudaError_t launch_pt_exchange(Rep *reps, int nt, int *perm, unsigned long long 
 cudaError_t launch_cluster_metro(int dim, Rep *reps, const int *ids, int nrep, int C, int threads, size_t smem,
                                  long long max_units, cudaStream_t st);
 cudaError_t launch_resident_metro(int dim, int geom, Rep *reps, const int *ids, int nrep, int threads,
-                                  size_t smem, long long max_units, cudaStream_t st);
+                                  size_t smem, long long max_units, cudaStream_t st, int copies = 1);
+int resident_copies_active(int dim, int geom, int copies, int threads, size_t smem);  // 0: cannot launch
 cudaError_t launch_tiled_sweep(int dim, int geom, Rep *reps, const Item *items, int nitems, int colour,
                                double *dEpart, long long *ipart, int threads, cudaStream_t st);
 cudaError_t launch_tiled_measure(int dim, int geom, Rep *reps, const Item *items, int nitems,

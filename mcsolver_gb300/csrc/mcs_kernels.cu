@@ -10,14 +10,24 @@
 //              replica of the group, tile by tile; a measurement launch writes
 //              per-tile partial sums and a finalize launch (one CTA per replica)
 //              folds them in a fixed order.
+//   resident with copies: a thread-block cluster of C CTAs (C = 2 or 4) per
+//              replica, each holding a full copy of the lattice; a colour phase
+//              is shared out among the CTAs, every accepted move is stored into
+//              every copy (DSMEM), and one cluster barrier ends the phase.
+//              Measurements split the index range among the CTAs; rank 0 sums
+//              the partial frames and owns the accumulators.  For lattices that
+//              fit one CTA but would leave SMs idle (few replicas, any geometry).
 // Both schedules call the same per-site update, so a replica's spin trajectory
 // does not depend on the schedule or on the other replicas of the batch.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "mcs_device.cuh"
 #include "mcs_internal.h"
 #include "mcs_wolff.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace mcs {
 
@@ -109,12 +119,14 @@ __device__ __forceinline__ void load_rep(Rep &dst, const Rep *src)
 
 // ======================================================================= resident Metropolis
 template <int DIM, int GEOM>
-__global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *ids, long long max_units)
+__global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *ids, long long max_units, int C)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ Rep R;
     __shared__ float fsx[MCS_FS_STRIDE];  // FP32 frame for the warp fold
-    Rep *Rg = reps + ids[blockIdx.x];
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = C > 1 ? (int)cl.block_rank() : 0;
+    Rep *Rg = reps + ids[blockIdx.x / C];
     load_rep(R, Rg);
     if (R.u >= R.units_total) return;
     const SmemLayout L = smem_layout(R);
@@ -166,6 +178,34 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
     __syncthreads();
     acc_to_smem(R, smem + L.acc);
 
+    // the other copies of this replica (C > 1): an accepted move is stored
+    // into each of them as well
+    float *rx[3] = {nullptr, nullptr, nullptr}, *ry[3] = {nullptr, nullptr, nullptr}, *rz[3] = {nullptr, nullptr, nullptr};
+    signed char *rs[3] = {nullptr, nullptr, nullptr};
+    int nrem = 0;
+    for (int q = 0; q < C && C > 1; ++q) {
+        if (q == rank) continue;
+        if (DIM == 1) rs[nrem] = cl.map_shared_rank(S.s, q);
+        else {
+            rx[nrem] = cl.map_shared_rank(S.x, q);
+            ry[nrem] = cl.map_shared_rank(S.y, q);
+            if (DIM == 3) rz[nrem] = cl.map_shared_rank(S.z, q);
+        }
+        ++nrem;
+    }
+    // rank 0 adds the other CTAs' values of buf[0..n) to its own (fixed rank order)
+    auto cl_sum = [&](auto *buf, int n) {
+        if (C <= 1) return;
+        cl.sync();
+        if (rank == 0)
+            for (int k = tid; k < n; k += bd) {
+                auto a = buf[k];
+                for (int q = 1; q < C; ++q) a += cl.map_shared_rank(buf, q)[k];
+                buf[k] = a;
+            }
+        cl.sync();
+    };
+
     int dn[MCS_MAXC] = {0, 0, 0, 0}, dm[MCS_MAXT] = {0, 0, 0, 0};
     long long nacc = 0;
     double dEd = 0.0;
@@ -180,7 +220,8 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
             for (int k = 0; k < MCS_MAXT; ++k) c[MCS_MAXC + k] = dm[k];
             c[MCS_MAXC + MCS_MAXT] = nacc;
             block_sum_ll<MCS_MAXC + MCS_MAXT + 1>(c, redl, Fi);
-            if (tid == 0) {
+            cl_sum(Fi, MCS_MAXC + MCS_MAXT + 1);
+            if (rank == 0 && tid == 0) {
                 for (int k = 0; k < MCS_MAXC; ++k) R.icnt[C_DN + k] += -4 * Fi[k];
                 for (int k = 0; k < MCS_MAXT; ++k) R.icnt[C_DM + k] += -2 * Fi[MCS_MAXC + k];
                 R.stats[S_ACCEPT] += Fi[MCS_MAXC + MCS_MAXT];
@@ -192,7 +233,8 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
         } else {
             double c[2] = {dEd, (double)nacc};
             block_sum<2>(c, red, F);
-            if (tid == 0) {
+            cl_sum(F, 2);
+            if (rank == 0 && tid == 0) {
                 R.acc[A_ECUR] += F[0];
                 R.stats[S_ACCEPT] += (long long)F[1];
             }
@@ -207,7 +249,7 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
     for (; u < uend; ++u) {
         if (DIM == 1 && u == R.units_thermal) {
             fold();
-            if (tid == 0) {
+            if (rank == 0 && tid == 0) {
                 double Einc = 0;
                 for (int c = 0; c < R.nclass; ++c) Einc += 0.5 * R.Q[c] * (double)R.icnt[C_DN + c];
                 for (int t = 0; t < R.ntype; ++t) Einc -= R.hd * R.Stype[t] * (double)R.icnt[C_DM + t];
@@ -220,8 +262,10 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
             if (DIM == 1) {
                 const int nq = (nc + 3) >> 2;
                 SqWalk wk;
-                if (GEOM == MCS_GEOM_SQUARE) wk.init(4 * tid, 4 * bd, R.hy);
-                for (int q = tid; q < nq; q += bd) {
+                // with copies the colour is dealt out among the C CTAs
+                const int q0 = rank * bd + tid, qs = C * bd;
+                if (GEOM == MCS_GEOM_SQUARE) wk.init(4 * q0, 4 * qs, R.hy);
+                for (int q = q0; q < nq; q += qs) {
                     uint4 w = philox_t((uint32_t)q, t, (uint32_t)c, R.seed);
                     const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
                     int x = 0, yh = 0;
@@ -238,6 +282,8 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
                             else
                                 a = ising_trial(R, itab, S.s, v, ty, ws[e], [&](auto &&f) { for_links<GEOM>(R, v, f); }, dn, dm);
                             nacc += a;
+                            if (a)
+                                for (int i = 0; i < nrem; ++i) rs[i][v] = S.s[v];
                         }
                         if (GEOM == MCS_GEOM_SQUARE) { if (++yh == R.hy) { yh = 0; ++x; } }
                     }
@@ -246,8 +292,9 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
             } else {
                 float dEf = 0.f;
                 SqWalk wk;
-                if (GEOM == MCS_GEOM_SQUARE) wk.init(tid, bd, R.hy);
-                for (int k = tid; k < nc; k += bd) {
+                const int k0 = rank * bd + tid, ks = C * bd;  // shared out among the copies
+                if (GEOM == MCS_GEOM_SQUARE) wk.init(k0, ks, R.hy);
+                for (int k = k0; k < nc; k += ks) {
                     const int v = c0 + k;
                     uint4 w = philox_t((uint32_t)k, t, (uint32_t)c, R.seed);
                     const int dc = multi ? st[v] : 0;
@@ -257,40 +304,57 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
                         a = on_trial<DIM>(R, jt, dt, S, v, dc, w, beta, h, [&](auto &&f) { sq_links(R, c, wk.x, wk.yh, f); }, &dE);
                     else
                         a = on_trial<DIM>(R, jt, dt, S, v, dc, w, beta, h, [&](auto &&f) { for_links<GEOM>(R, v, f); }, &dE);
-                    if (a) { dEf += dE; ++nacc; }
+                    if (a) {
+                        dEf += dE;
+                        ++nacc;
+                        for (int i = 0; i < nrem; ++i) {
+                            rx[i][v] = S.x[v];
+                            ry[i][v] = S.y[v];
+                            if (DIM == 3) rz[i][v] = S.z[v];
+                        }
+                    }
                     if (GEOM == MCS_GEOM_SQUARE) wk.next();
                 }
                 dEd += (double)dEf;
             }
-            __syncthreads();
+            // every copy holds this colour's new spins before the next phase reads them
+            if (C > 1) cl.sync();
+            else __syncthreads();
         }
         if (measures_after(R, u)) {
             fold();
             const long long m = R.m;
             if (DIM == 1) {
-                is_frame<GEOM>(R, itab, S.s, 0, max(N, max(R.nlat, R.n_rorb)), m, red, F, redl, Fi,
+                const int V = max(N, max(R.nlat, R.n_rorb)), share = (V + C - 1) / C;
+                const int vb = min(V, rank * share), ve = min(V, vb + share);
+                is_frame<GEOM>(R, itab, S.s, vb, ve, m, red, F, redl, Fi,
                                L.majc ? (signed char *)(smem + L.majc) : nullptr, il.rorb ? &il : nullptr);
-                if (tid == 0) {
+                cl_sum(F, 4);
+                cl_sum(Fi, MCS_MAXT + MCS_MAXC);
+                if (rank == 0 && tid == 0) {
                     if (R.alg == 1 && u >= R.units_thermal) R.icnt[C_ACC_MEAS] = 1;
                     is_accumulate(R, F, Fi, S.s[R.last_site], m);
                 }
             } else {
                 const bool efull = (m % R.recheck) == 0;
-                on_frame<DIM, GEOM>(R, jt, dt, S, 0, max(max(N, R.nlat), max(R.n_rorb, R.ncirc)), efull, red, F, majc);
-                if (tid == 0 && efull) {
+                const int V = max(max(N, R.nlat), max(R.n_rorb, R.ncirc)), share = (V + C - 1) / C;
+                const int vb = min(V, rank * share), ve = min(V, vb + share);
+                on_frame<DIM, GEOM>(R, jt, dt, S, vb, ve, efull, red, F, majc);
+                cl_sum(F, F_NON);
+                if (rank == 0 && tid == 0 && efull) {
                     double Ef = F[F_EFB] / 2 + F[F_EFO];
                     double d = fabs(R.acc[A_ECUR] - Ef);
                     if (d > R.acc[A_DRIFT]) R.acc[A_DRIFT] = d;
                     R.acc[A_ECUR] = Ef;
                 }
-                if (tid < 32) {
+                if (rank == 0 && tid < 32) {
                     __syncwarp();
                     for (int f = tid; f < F_NON; f += 32) fsx[f] = (float)F[f];
                     __syncwarp();
                     on_accumulate_frames<DIM>(R, fsx, &R.acc[A_ECUR], m, 1, tid);
                 }
             }
-            if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) {
+            if (rank == 0 && R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) {
                 float *fb = R.frame_buf + (size_t)R.frames_written * N * 3;
                 for (int v = tid; v < N; v += bd) {
                     if (DIM == 1) { fb[3 * v] = (float)(R.Stype[R.stype ? R.stype[v] : 0] * S.s[v]); fb[3 * v + 1] = 0; fb[3 * v + 2] = 0; }
@@ -302,10 +366,14 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
                 if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) R.frames_written++;
                 R.m = m + 1;
             }
-            __syncthreads();
+            // rank 0 has read its copy (frames, the last site): only now may
+            // the next colour phase store into it
+            if (C > 1) cl.sync();
+            else __syncthreads();
         }
     }
     fold();
+    if (rank != 0) return;  // the copies are identical; rank 0 writes the replica back
     acc_to_global(R, Rg);
     for (int v = tid; v < N; v += bd) {
         if (DIM == 1) G.s[v] = S.s[v];
@@ -739,19 +807,69 @@ static cudaError_t set_smem_attr(size_t smem)
         }                                                                                \
     } while (0)
 
+template <int DIM, int GEOM>
+static cudaError_t launch_resident_t(Rep *reps, const int *ids, int nrep, int copies, int threads, size_t smem,
+                                     long long max_units, cudaStream_t st)
+{
+    cudaError_t e = set_smem_attr<DIM, GEOM>(smem);
+    if (e != cudaSuccess) return e;
+    if (copies <= 1) {
+        k_resident_metro<DIM, GEOM><<<nrep, threads, smem, st>>>(reps, ids, max_units, 1);
+        return cudaGetLastError();
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nrep * copies, 1, 1);
+    cfg.blockDim = dim3(threads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = copies;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_resident_metro<DIM, GEOM>, reps, ids, max_units, copies);
+}
+
+// copies: CTAs per replica, each with a full copy of the lattice (1 = one CTA)
 cudaError_t launch_resident_metro(int dim, int geom, Rep *reps, const int *ids, int nrep, int threads, size_t smem,
-                                  long long max_units, cudaStream_t st)
+                                  long long max_units, cudaStream_t st, int copies)
 {
     if (nrep <= 0) return cudaSuccess;
-#define CALL_RES(D, G)                                                                   \
-    {                                                                                    \
-        cudaError_t e = set_smem_attr<D, G>(smem);                                       \
-        if (e != cudaSuccess) return e;                                                  \
-        k_resident_metro<D, G><<<nrep, threads, smem, st>>>(reps, ids, max_units);       \
-    }
+#define CALL_RES(D, G) return launch_resident_t<D, G>(reps, ids, nrep, copies, threads, smem, max_units, st);
     MCS_DISPATCH(dim, geom, CALL_RES);
 #undef CALL_RES
-    return cudaGetLastError();
+    return cudaErrorInvalidValue;
+}
+
+// Resident clusters of `copies` CTAs the device can hold at once (0: cannot launch).
+int resident_copies_active(int dim, int geom, int copies, int threads, size_t smem)
+{
+    int n = 0;
+#define CALL_OCC(D, G)                                                                                   \
+    {                                                                                                    \
+        if (set_smem_attr<D, G>(smem) != cudaSuccess) { cudaGetLastError(); return 0; }                  \
+        cudaLaunchConfig_t cfg = {};                                                                     \
+        cfg.gridDim = dim3(copies, 1, 1);                                                                \
+        cfg.blockDim = dim3(threads, 1, 1);                                                              \
+        cfg.dynamicSmemBytes = smem;                                                                     \
+        cudaLaunchAttribute attr[1];                                                                     \
+        attr[0].id = cudaLaunchAttributeClusterDimension;                                                \
+        attr[0].val.clusterDim.x = copies;                                                               \
+        attr[0].val.clusterDim.y = 1;                                                                    \
+        attr[0].val.clusterDim.z = 1;                                                                    \
+        cfg.attrs = attr;                                                                                \
+        cfg.numAttrs = 1;                                                                                \
+        if (cudaOccupancyMaxActiveClusters(&n, k_resident_metro<D, G>, &cfg) != cudaSuccess) {          \
+            cudaGetLastError();                                                                          \
+            return 0;                                                                                    \
+        }                                                                                                \
+        return n;                                                                                        \
+    }
+    MCS_DISPATCH(dim, geom, CALL_OCC);
+#undef CALL_OCC
+    return 0;
 }
 
 cudaError_t launch_tiled_sweep(int dim, int geom, Rep *reps, const Item *items, int nitems, int colour,

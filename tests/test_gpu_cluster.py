@@ -118,3 +118,46 @@ def test_balanced_batch_equals_alone(engine):
         alone, ex = engine.solve("ising", a, seed=40 + k, schedule="resident", random_init=True)
         np.testing.assert_allclose(np.array(got[k][0][:10]), np.array(alone[:10]), rtol=1e-12, atol=1e-12)
         assert got[k][1]["accepted"] == ex["accepted"] and got[k][1]["site_updates"] == ex["site_updates"]
+
+
+COPIES = [
+    ("ising_L32", "ising", lambda: C.square_args("ising", 32, 2.3, nthermal=8, nsweep=16, frames=4)),
+    ("ising_L24_h", "ising", lambda: C.square_args("ising", 24, 2.6, h=0.1, nthermal=8, nsweep=16)),
+    ("xy_L32", "xy", lambda: C.square_args("xy", 32, 0.9, nthermal=8, nsweep=16, frames=4)),
+    ("heis_honeycomb8", "heisenberg", lambda: C.honeycomb_args("heisenberg", 8, 6.0, nthermal=8, nsweep=16)),
+    ("heis_L24_dmi_h", "heisenberg", lambda: C.square_args("heisenberg", 24, 0.6, h=0.2, dmi=0.4, nthermal=8, nsweep=16)),
+]
+
+
+@pytest.mark.parametrize("copies", [2, 4])
+@pytest.mark.parametrize("name,model,mk", COPIES, ids=[c[0] for c in COPIES])
+def test_resident_copies_match_one_cta(engine, name, model, mk, copies):
+    """A replica held in 2 or 4 CTAs of a cluster (each a full copy, colour
+    phases shared out) runs the one-CTA trajectory: Ising bit-exact, O(n)
+    within FP32 summation order."""
+    args = mk()
+    a, ea = engine.solve(model, args, seed=9, schedule="resident", random_init=True)
+    old = os.environ.get("MCSGPU_COPIES")
+    os.environ["MCSGPU_COPIES"] = str(copies)
+    try:
+        bt = engine.Batch()
+        bt.add(model, args, seed=9, random_init=True, schedule="resident")
+        bt.prepare()
+        bt.run()
+        sched = bt.schedules()
+        b, eb = bt.result(0)
+        bt.close()
+    finally:
+        if old is None:
+            os.environ.pop("MCSGPU_COPIES", None)
+        else:
+            os.environ["MCSGPU_COPIES"] = old
+    assert sched[0][0] == "resident" and sched[0][1] == copies, sched
+    assert eb["site_updates"] == ea["site_updates"] and eb["accepted"] == ea["accepted"]
+    if model == "ising":
+        np.testing.assert_allclose(np.array(b[:10]), np.array(a[:10]), rtol=1e-12, atol=1e-12)
+        assert eb["exact_mismatches"] == 0
+    else:
+        np.testing.assert_allclose(np.array(b[:27]), np.array(a[:27]), rtol=1e-5, atol=1e-6)
+    if "frames" in ea:
+        np.testing.assert_allclose(eb["frames"], ea["frames"], atol=2e-5)
