@@ -145,18 +145,41 @@ __device__ __forceinline__ bool ising_trial(const Rep &R, const IsEntry *__restr
 // Reflection proposal s' = s - 2(s.r)r with r uniform on the circle / sphere.
 // dE = ds . (sum_l J_l s_j) + D.((s+ds)^2 - s^2) - h ds_axis (field along x for
 // XY, z for Heisenberg).  Accept dE <= 0 or exp(-beta dE) > U.
+// The engine stream defines r = (cos phi, sin phi) (XY) or
+// (rho cos phi, rho sin phi, z) (Heisenberg) with phi = 2 pi U.  Every use of r
+// -- the reflection s - 2 (s.r) r and the Wolff bond products (s_i.r)(s_j.r)
+// -- is unchanged under r -> -r, so the device evaluates -r: the angle
+// phi - pi lies in [-pi, pi), where the fast hardware sine and cosine are
+// accurate to about 5e-7, and z is negated with it.
 template <int DIM>
 __device__ __forceinline__ void on_direction(const uint4 &w, float &r0, float &r1, float &r2)
+{
+    const float two_pi = 6.28318530717958647692f, pi = 3.14159265358979323846f;
+    if (DIM == 2) {
+        float sp, cp;
+        __sincosf(fmaf(two_pi, u24(w.x), -pi), &sp, &cp);
+        r0 = cp; r1 = sp; r2 = 0.f;
+    } else {
+        const float zz = 2.0f * u24(w.x) - 1.0f;
+        float sp, cp;
+        __sincosf(fmaf(two_pi, u24(w.y), -pi), &sp, &cp);
+        const float rho = sqrtf(fmaxf(0.f, 1.f - zz * zz));
+        r0 = rho * cp; r1 = rho * sp; r2 = -zz;
+    }
+}
+// The direction itself (random initial spins, where the sign matters).
+template <int DIM>
+__device__ __forceinline__ void on_direction_exact(const uint4 &w, float &r0, float &r1, float &r2)
 {
     if (DIM == 2) {
         float sp, cp;
         sincospif(2.0f * u24(w.x), &sp, &cp);
         r0 = cp; r1 = sp; r2 = 0.f;
     } else {
-        float zz = 2.0f * u24(w.x) - 1.0f;
+        const float zz = 2.0f * u24(w.x) - 1.0f;
         float sp, cp;
         sincospif(2.0f * u24(w.y), &sp, &cp);
-        float rho = sqrtf(fmaxf(0.f, 1.f - zz * zz));
+        const float rho = sqrtf(fmaxf(0.f, 1.f - zz * zz));
         r0 = rho * cp; r1 = rho * sp; r2 = zz;
     }
 }

@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(1024) k_init(Rep *reps, const int *ids)
                 S.s[v] = (w.x & 1) ? 1 : -1;
             } else {
                 float r0, r1, r2;
-                on_direction<DIM>(w, r0, r1, r2);
+                on_direction_exact<DIM>(w, r0, r1, r2);
                 const float a = R.slen[v];
                 S.x[v] = r0 * a; S.y[v] = r1 * a;
                 if (DIM == 3) S.z[v] = r2 * a;
