@@ -445,13 +445,14 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
                     a[j] = keep + __shfl_xor_sync(0xffffffffu, send, w);
                 }
             }
-            double de = dEd, na = (double)nacc;
+            double de = dEd;
+            long long na = nacc;  // the count stays integer (no FP64 work)
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 de += __shfl_xor_sync(0xffffffffu, de, o);
                 na += __shfl_xor_sync(0xffffffffu, na, o);
             }
-            red[wid * CL_SLOT + lane] = lane < CL_NV ? (double)a[0] : (lane == CL_NV ? de : na);
+            red[wid * CL_SLOT + lane] = lane < CL_NV ? (double)a[0] : (lane == CL_NV ? de : (double)na);
             __syncthreads();
             const int slot = (int)(m & 1);
             if (tid < CL_NV + 2) {
@@ -497,8 +498,8 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
         const long long t = R.u0 + u;
         const bool fuse = R.meas_regular && measures_after(R, u) && (mloc % R.recheck) != 0;
         fa[0] = fa[1] = fa[2] = fa[3] = 0.f;
+        float dEf = 0.f;  // this thread's energy change over the sweep (FP32; summed in FP64 per sweep)
         for (int c = 0; c < 2; ++c) {
-            float dEf = 0.f;
             SqWalk wk;
             wk.init(tid, bd, hy);
             const int cb = c * rows * hy;
@@ -546,9 +547,9 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
                 }
               }
             }
-            dEd += (double)dEf;
             cl.sync();
         }
+        dEd += (double)dEf;
         if (measures_after(R, u)) {
             measure(mloc, (mloc % R.recheck) == 0, fuse);
             ++mloc;
