@@ -159,7 +159,7 @@ def run_ours(args):
     prob_args = workload_args(nsweep=total_sweeps)
     batch = eng.Batch(device=0)
     for k, a in enumerate(prob_args):
-        batch.add("xy", a, seed=1000 + k, random_init=True)
+        batch.add("xy", a, seed=1000 + k, random_init=True, schedule=args.schedule)
     batch.prepare()
     for _ in range(W):
         batch.advance(S)
@@ -180,7 +180,8 @@ def run_ours(args):
     ms_per_step = sum(times) / K
     # roofline of the Metropolis kernel the autotuner chose (one launch per step):
     # algorithmic bytes = lattice read + written once per sweep, FP32 (x,y) = 16 B / site update
-    kname = ("k_cluster_metro<2,%d>" % sched[0][2]) if sched[0][0] == "cluster" else "k_resident_metro<2,SQUARE>"
+    kname = {"cluster": "k_cluster_metro<2,%d>" % sched[0][2], "tiled": "k_tiled_sweep<2,SQUARE>"}.get(
+        sched[0][0], "k_resident_metro<2,SQUARE>")
     alg_bytes = 16.0 * per_step_updates
     achieved = alg_bytes / (ms_per_step / 1000.0) / 1e9
     traffic = None
@@ -421,6 +422,62 @@ def run_batched4(args):
                       "batched_over_plain": (st["site_updates"] / (st["device_ms"] / 1000.0)) / (u / s)}))
 
 
+def run_whole_solves(args):
+    """Whole solves of one (model, lattice) over a temperature grid, all
+    temperatures in one batch, against the plain engine on a sample.
+    * ising:    square Ising ferromagnet (Jxx = -1), L = 32, h = 0, 16
+                temperatures 1.5..3.5, Metropolis, tau = N, nthermal 2000,
+                nsweep 10000 (the reference's CPU-runnable case);
+    * xy_wolff: square XY (Jxx = Jyy = -1), L = 128, 32 temperatures 0.5..1.5,
+                Wolff single-cluster updates, one cluster per measurement,
+                nthermal 5000, nsweep 20000.
+    Site updates: one Metropolis trial = 1; Wolff counts the flipped sites
+    (cluster sizes) and also reports clusters/s.  `wall_s` is end to end through
+    the C ABI from host arrays (batch creation, compile, upload, run, results)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import mcsolver_gb300 as eng
+    from mcsolver_gb300 import build as b
+    from mcsolver_gb300.lattice import rescale_args, square_args_fast
+    b.build()
+    if args.workload == "ising":
+        model, Lw, Ts, algo, tau = "ising", 32, [1.5 + k * 2.0 / 15 for k in range(16)], 0, 0
+        nth, nsw = (args.nthermal, args.nsweep) if args.override_sweeps else (2000, 10000)
+    else:
+        model, Lw, Ts, algo, tau = "xy", 128, [0.5 + k * 1.0 / 31 for k in range(32)], 1, 1
+        nth, nsw = (args.nthermal, args.nsweep) if args.override_sweeps else (5000, 20000)
+    base = square_args_fast(model, Lw, 1.0, nthermal=nth, nsweep=nsw, tau=tau, algo=algo, arrays=True)
+    jobs = [rescale_args(model, base, T) for T in Ts]
+    t0 = time.time()
+    bt = eng.Batch()
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as pool:
+        list(pool.map(lambda kj: bt.add(model, kj[1], seed=21 + kj[0], random_init=True), enumerate(jobs)))
+    bt.run()
+    res = [bt.result(i) for i in range(len(jobs))]
+    wall = time.time() - t0
+    st = bt.stats()
+    sched = bt.schedules()
+    bt.close()
+    clusters = sum(r[1]["clusters"] for r in res)
+    mism = sum(r[1]["exact_mismatches"] for r in res)
+    ps, pt = 0, 0.0
+    for k in range(args.plain_sample):
+        u, s = _plain_rate(eng, model, jobs[(k * 7) % len(jobs)], 99 + k)
+        ps += u
+        pt += s
+    rate = st["site_updates"] / (st["device_ms"] / 1000.0)
+    print(json.dumps({"workload": "%s_square_L%d_%dT_%s" % (model, Lw, len(Ts), "wolff" if algo else "metropolis"),
+                      "replicas": len(jobs), "nthermal": nth, "nsweep": nsw, "site_updates": st["site_updates"],
+                      "clusters": clusters if algo else None, "device_ms": st["device_ms"], "wall_s_e2e": wall,
+                      "site_updates_per_s": rate, "e2e_site_updates_per_s": st["site_updates"] / wall,
+                      "clusters_per_s": clusters / (st["device_ms"] / 1000.0) if algo else None,
+                      "exact_mismatches": mism if model == "ising" else None,
+                      "schedule": [{"schedule": g[0], "ctas_per_replica": g[1], "threads": g[2], "replicas": g[3]}
+                                   for g in sched],
+                      "plain_site_updates_per_s": ps / pt if pt > 0 else None,
+                      "batched_over_plain": rate / (ps / pt) if pt > 0 else None}))
+
+
 def run_pt(args):
     """Parallel tempering: honeycomb Heisenberg (2 sites/cell), 1NN Kitaev-type
     J = diag(-1.5,-1.5,-1.8) with Jxy = Jyx = 0.3, 2NN -0.3, Az = -0.5, 64x64
@@ -455,14 +512,18 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--sweeps", type=int, default=STEP_SWEEPS)
+    ap.add_argument("--schedule", default="auto", choices=["auto", "resident", "tiled"],
+                    help="headline workload: schedule of the replicas (auto = autotuner and load balancer)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--workload", default="headline", choices=["headline", "served", "batched4", "pt"])
+    ap.add_argument("--workload", default="headline", choices=["headline", "served", "batched4", "pt", "ising", "xy_wolff"])
     ap.add_argument("--requests", type=int, default=48)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--nthermal", type=int, default=1000)
     ap.add_argument("--nsweep", type=int, default=5000)
+    ap.add_argument("--override-sweeps", action="store_true",
+                    help="ising / xy_wolff: use --nthermal / --nsweep instead of the workload's own counts")
     ap.add_argument("--plain-sample", type=int, default=6)
     ap.add_argument("--pt-sweeps", type=int, default=50000)
     args = ap.parse_args()
@@ -472,6 +533,8 @@ def main():
         return run_batched4(args)
     if args.workload == "pt":
         return run_pt(args)
+    if args.workload in ("ising", "xy_wolff"):
+        return run_whole_solves(args)
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         if rank == 0:

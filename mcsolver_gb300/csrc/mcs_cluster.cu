@@ -294,9 +294,10 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
         // partial layout: 0-2 total spin, 3-5 pair sum, 6 pair s.s, 7/8 full
         // energy bond/onsite, 9 solid angles, 10-12 block-spin pair sum,
         // 13 block s.s, 14/15 renormalised bond/onsite, 16-27 four groups
-        float a[32];  // CL_NV values, padded to the warp width for the halving sum
+        float a[32];  // CL_NV values and the energy change, padded to the warp width for the halving sum
 #pragma unroll
         for (int k = 0; k < 32; ++k) a[k] = 0.f;
+        a[CL_NV] = (float)dEd;  // this thread's energy change since the last measurement
         if (fused) {
             a[0] = fa[0]; a[1] = fa[1]; a[2] = fa[2];
             a[3] = fa[0]; a[4] = fa[1]; a[5] = fa[2]; a[6] = fa[3];
@@ -445,14 +446,12 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
                     a[j] = keep + __shfl_xor_sync(0xffffffffu, send, w);
                 }
             }
-            double de = dEd;
-            long long na = nacc;  // the count stays integer (no FP64 work)
+            // the energy change went through the FP32 halving with the frame
+            // values (lane CL_NV); the count stays integer
+            long long na = nacc;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                de += __shfl_xor_sync(0xffffffffu, de, o);
-                na += __shfl_xor_sync(0xffffffffu, na, o);
-            }
-            red[wid * CL_SLOT + lane] = lane < CL_NV ? (double)a[0] : (lane == CL_NV ? de : (double)na);
+            for (int o = 16; o > 0; o >>= 1) na += __shfl_xor_sync(0xffffffffu, na, o);
+            red[wid * CL_SLOT + lane] = lane <= CL_NV ? (double)a[0] : (double)na;
             __syncthreads();
             const int slot = (int)(m & 1);
             if (tid < CL_NV + 2) {
@@ -504,16 +503,45 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
             wk.init(tid, bd, hy);
             const int cb = c * rows * hy;
             // four sites per thread at a time: their Philox words are drawn
-            // first, as independent instruction streams, then the trials run
-            for (int kb = tid; kb < nown; kb += 4 * bd) {
+            // first, as independent instruction streams, then the trials run.
+            // The loop bound is the warp's first lane's index, the same for
+            // every lane, so the whole warp reaches the pair exchange below;
+            // sites past the end are skipped one by one.
+            const int lane = tid & 31;
+            for (int kb = tid; kb - lane < nown; kb += 4 * bd) {
                 uint4 ws[4];
                 int xs[4], ys[4];
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                     xs[e] = wk.x; ys[e] = wk.yh;
-                    // colour-local index of the whole lattice
-                    if (kb + e * bd < nown) ws[e] = philox_t((uint32_t)((x0 + xs[e]) * hy + ys[e]), t, (uint32_t)c, R.seed);
                     wk.next();
+                }
+                // colour-local index of the whole lattice of site e: x0*hy + kb + e*bd
+                const uint32_t kg = (uint32_t)(x0 * hy + kb);
+                if (DIM == 2) {
+                    // XY: sites k and k^1 share one Philox block (on_words).
+                    // x0 and bd are even, so lanes 2i and 2i+1 hold the two
+                    // sites of one block for every e.  The even lane draws the
+                    // blocks of e = 0, 1 and the odd lane those of e = 2, 3;
+                    // each passes its partner the partner's half.
+                    const bool odd = (lane & 1) != 0;
+                    const uint32_t ka = kg + (uint32_t)((odd ? 2 : 0) * bd);
+                    const uint4 A = philox_t(ka >> 1, t, (uint32_t)c, R.seed);
+                    const uint4 B = philox_t((ka + (uint32_t)bd) >> 1, t, (uint32_t)c, R.seed);
+                    const uint32_t r0 = __shfl_xor_sync(0xffffffffu, odd ? A.x : A.z, 1);
+                    const uint32_t r1 = __shfl_xor_sync(0xffffffffu, odd ? A.y : A.w, 1);
+                    const uint32_t r2 = __shfl_xor_sync(0xffffffffu, odd ? B.x : B.z, 1);
+                    const uint32_t r3 = __shfl_xor_sync(0xffffffffu, odd ? B.y : B.w, 1);
+                    const uint32_t o0 = odd ? A.z : A.x, o1 = odd ? A.w : A.y;
+                    const uint32_t p0 = odd ? B.z : B.x, p1 = odd ? B.w : B.y;
+                    ws[0] = make_uint4(odd ? r0 : o0, odd ? r1 : o1, 0u, 0u);
+                    ws[1] = make_uint4(odd ? r2 : p0, odd ? r3 : p1, 0u, 0u);
+                    ws[2] = make_uint4(odd ? o0 : r0, odd ? o1 : r1, 0u, 0u);
+                    ws[3] = make_uint4(odd ? p0 : r2, odd ? p1 : r3, 0u, 0u);
+                } else {
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                        if (kb + e * bd < nown) ws[e] = on_words<DIM>(kg + (uint32_t)(e * bd), t, (uint32_t)c, R.seed);
                 }
 #pragma unroll
               for (int e = 0; e < 4; ++e) {

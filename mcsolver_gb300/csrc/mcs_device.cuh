@@ -39,6 +39,22 @@ __device__ __forceinline__ uint4 philox_t(uint32_t c0, long long t, uint32_t c3,
 }
 __device__ __forceinline__ float u24(uint32_t w) { return (float)(w >> 8) * (1.0f / 16777216.0f); }
 
+// Words of one O(n) Metropolis trial at colour-local index k of colour c in
+// sweep t.  An XY trial uses two words (direction, acceptance), so sites k and
+// k^1 share one Philox block (counter k >> 1): even k takes words (x, y), odd
+// k words (z, w), returned in .x/.y.  A Heisenberg trial uses three words and
+// has a block of its own (counter k).
+template <int DIM>
+__device__ __forceinline__ uint4 on_words(uint32_t k, long long t, uint32_t c, unsigned long long seed)
+{
+    if (DIM == 2) {
+        uint4 w = philox_t(k >> 1, t, c, seed);
+        if (k & 1u) { w.x = w.z; w.y = w.w; }
+        return w;
+    }
+    return philox_t(k, t, c, seed);
+}
+
 // ------------------------------------------------------------------ geometry
 // SQUARE: N = Lx*Ly, Lx, Ly even; hy = Ly/2, half = N/2.  A site of colour c
 // with colour-local index k = x*hy + yh sits at (x, y = 2*yh + ((x+c)&1)) and

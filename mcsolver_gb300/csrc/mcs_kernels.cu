@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
                 if (GEOM == MCS_GEOM_SQUARE) wk.init(k0, ks, R.hy);
                 for (int k = k0; k < nc; k += ks) {
                     const int v = c0 + k;
-                    uint4 w = philox_t((uint32_t)k, t, (uint32_t)c, R.seed);
+                    uint4 w = on_words<DIM>((uint32_t)k, t, (uint32_t)c, R.seed);
                     const int dc = multi ? st[v] : 0;
                     float dE;
                     bool a;
@@ -435,11 +435,11 @@ __global__ void __launch_bounds__(256) k_tiled_sweep(Rep *reps, const Item *item
         if (tid < 9) ipart[(size_t)it.slot * 9 + tid] = redl[32 * 9 + tid];
     } else {
         float dEf = 0.f;
-        double nacc = 0;
+        unsigned nacc = 0;
         const int k = it.begin + tid;
         if (k < it.end) {
             const int v = c0 + k;
-            uint4 w = philox_t((uint32_t)k, t, (uint32_t)c, R.seed);
+            uint4 w = on_words<DIM>((uint32_t)k, t, (uint32_t)c, R.seed);
             const int dc = multi ? R.stype[v] : 0;
             float dE;
             bool a;
@@ -451,11 +451,17 @@ __global__ void __launch_bounds__(256) k_tiled_sweep(Rep *reps, const Item *item
             }
             if (a) { dEf = dE; nacc = 1; }
         }
-        double v[2] = {(double)dEf, nacc};
-        block_sum<2>(v, red, red + 64);
+        // energy change: FP32 inside each warp, FP64 across the warps; the
+        // accepted count as an integer (one warp reduction instruction)
+        const unsigned cnt = __reduce_add_sync(0xffffffffu, nacc);
+        if ((tid & 31) == 0) redl[tid >> 5] = (long long)cnt;
+        float v[1] = {dEf};
+        block_sum_f<1>(v, red, red + 64);  // its barriers also publish redl
         if (tid == 0) {
+            long long n = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) n += redl[w];
             dEpart[it.slot] = red[64];
-            ipart[(size_t)it.slot * 9 + 8] = (long long)red[65];
+            ipart[(size_t)it.slot * 9 + 8] = n;
         }
     }
 }

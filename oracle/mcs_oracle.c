@@ -32,8 +32,10 @@
  * lattice in that order draws the same words.
  * Philox counter layout of the engine stream (key = seed lo/hi 32 bits):
  *   Metropolis, sweep t, colour c, k-th site of the colour:
- *       Ising   ctr = (k>>2, t_lo, t_hi, c), word k&3
- *       O(n)    ctr = (k,    t_lo, t_hi, c), words 0.. (direction), last = accept
+ *       Ising       ctr = (k>>2, t_lo, t_hi, c), word k&3
+ *       XY          ctr = (k>>1, t_lo, t_hi, c), words 2(k&1) (direction) and
+ *                   2(k&1)+1 (accept)
+ *       Heisenberg  ctr = (k,    t_lo, t_hi, c), words 0, 1 (direction), 2 (accept)
  *   Wolff cluster q: ctr = (0, q_lo, q_hi, 0x1000): seed = sites[(w0*N)>>32],
  *       w1/w2 direction, w3 cluster acceptance
  *   Wolff bond coin, cluster q, directed bond from sweep index a to b:
@@ -769,7 +771,14 @@ static void on_unit(OnState *S, Sweep *sw, int64_t *t)
     for (int c = 0; c < sw->ncol; c++) {
         for (int k = sw->start[c]; k < sw->start[c + 1]; k++) {
             uint32_t w[4];
-            phil(&S->g, (uint32_t)(k - sw->start[c]), (uint64_t)*t, (uint32_t)c, w);
+            const uint32_t kk = (uint32_t)(k - sw->start[c]);
+            if (S->dim == 2) {
+                /* XY: sites kk and kk^1 share one block, even kk words 0-1, odd kk words 2-3 */
+                phil(&S->g, kk >> 1, (uint64_t)*t, (uint32_t)c, w);
+                if (kk & 1u) { w[0] = w[2]; w[1] = w[3]; }
+            } else {
+                phil(&S->g, kk, (uint64_t)*t, (uint32_t)c, w);
+            }
             V3 r = on_eng_dir(S->dim, w[0], w[1]);
             on_metropolis_site(S, sw->sites[k], r, 1, S->dim == 3 ? w[2] : w[1]);
             S->stats[3]++;
