@@ -115,31 +115,35 @@ __device__ __forceinline__ int cl_frame_src(int f, int ngroup, int gall)
 }
 
 // Measurement slots folded per batch by rank 0 (consecutive measurements).
-#define CL_RING 8
+#define CL_RING 16
 
 // Rank 0, warp 0 (lane = slot entry): sum slot `slot` of every CTA of the
-// cluster in fixed rank order into one ring entry.
-__device__ __forceinline__ void cluster_gather(double *part, double *entry, int C, int slot, int lane)
+// cluster in fixed rank order into one ring entry (FP64), and write the
+// measurement's frame in FP32: frame entry f takes slot entry fsrc[f] (a table
+// of cl_frame_src made once per launch), passed between lanes by a shuffle.
+__device__ __forceinline__ void cluster_gather(double *part, double *entry, float *frame, const signed char *fsrc,
+                                               int C, int slot, int lane)
 {
     cg::cluster_group cl = cg::this_cluster();
     double o = 0.0;
     for (int q = 0; q < C; ++q) o += cl.map_shared_rank(part, q)[slot * CL_SLOT + lane];
     entry[lane] = o;
+    const float of = (float)o;
+    for (int f = lane; f - lane < F_NON; f += 32) {  // the bound is the same for every lane
+        const int k = f < F_NON ? (int)fsrc[f] : -1;
+        const float v = __shfl_sync(0xffffffffu, of, k < 0 ? 0 : k);
+        if (f < F_NON) frame[f] = k < 0 ? 0.f : v;
+    }
 }
 
-// Rank 0, warp 0: fold the n ring entries (consecutive measurements) into the
-// FP64 accumulators: running energy in order (lane 0), then the frames
-// together.  Kept out of line so that its registers do not add to the sweep
+// Rank 0, warp 0: fold the n ring entries (consecutive measurements; their
+// FP32 frames in fs) into the FP64 accumulators: running energy in order
+// (lane 0), then the frames together.  Kept out of line so that its registers do not add to the sweep
 // loop's.
 template <int DIM>
 __device__ __noinline__ void cluster_fold_ring(Rep &R, const double *ring, int n, float *fs, double *Eb, int lane)
 {
     __syncwarp();
-    for (int idx = lane; idx < n * F_NON; idx += 32) {
-        const int j = idx / F_NON, f = idx - j * F_NON;
-        const int k = cl_frame_src(f, R.ngroup, R.gall);
-        fs[j * MCS_FS_STRIDE + f] = k < 0 ? 0.f : (float)ring[j * CL_SLOT + k];
-    }
     if (lane == 0) {
         for (int j = 0; j < n; ++j) {
             const double *o = ring + j * CL_SLOT;
@@ -249,11 +253,15 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
     __shared__ double ring[CL_RING * CL_SLOT];
     __shared__ float fsx[CL_RING * MCS_FS_STRIDE];
     __shared__ double Eb[CL_RING];
+    __shared__ signed char fsrc[F_NON];
+    for (int f = tid; f < F_NON; f += bd) fsrc[f] = (signed char)cl_frame_src(f, R.ngroup, R.gall);
+    __syncthreads();
     int nring = 0;  // ring entries gathered and not yet folded (rank 0)
     // rank 0, warp 0: gather the pending slot; fold when the ring is full
     auto gather = [&](bool flush) {
         if (pending >= 0) {
-            if (tid < 32) cluster_gather(part, ring + nring * CL_SLOT, C, pending, tid);
+            if (tid < 32)
+                cluster_gather(part, ring + nring * CL_SLOT, fsx + nring * MCS_FS_STRIDE, fsrc, C, pending, tid);
             ++nring;
         }
         if (nring > 0 && (flush || nring == CL_RING)) {
@@ -451,13 +459,25 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
             long long na = nacc;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) na += __shfl_xor_sync(0xffffffffu, na, o);
-            red[wid * CL_SLOT + lane] = lane <= CL_NV ? (double)a[0] : (double)na;
+            // warp values in FP32 (redf) and the counts as integers (redl),
+            // both inside the red area; across the warps the FP32 values are
+            // summed with Neumaier compensation and enter the FP64 slot as the
+            // sum plus its rounding error (FP64 instructions issue slowly and
+            // this sum is on the measurement's critical path)
+            float *redf = (float *)red;                       // [32 warps][CL_SLOT]
+            long long *redl = (long long *)(red + 16 * CL_SLOT);  // [32 warps]
+            if (lane <= CL_NV) redf[wid * CL_SLOT + lane] = a[0];
+            if (lane == 0) redl[wid] = na;
             __syncthreads();
             const int slot = (int)(m & 1);
-            if (tid < CL_NV + 2) {
-                double s2 = 0.0;
-                for (int w = 0; w < nw; ++w) s2 += red[w * CL_SLOT + tid];
-                part[slot * CL_SLOT + tid] = s2;
+            if (tid <= CL_NV) {
+                float sh = 0.f, sl = 0.f;
+                for (int w = 0; w < nw; ++w) ksum_add(sh, sl, redf[w * CL_SLOT + tid]);
+                part[slot * CL_SLOT + tid] = (double)sh + (double)sl;
+            } else if (tid == CL_NV + 1) {
+                long long n = 0;
+                for (int w = 0; w < nw; ++w) n += redl[w];
+                part[slot * CL_SLOT + tid] = (double)n;
             } else if (tid == CL_NV + 2) {
                 part[slot * CL_SLOT + tid] = efull ? 1.0 : 0.0;
             } else if (tid == CL_NV + 3) {

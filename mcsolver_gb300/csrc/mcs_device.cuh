@@ -707,6 +707,14 @@ __device__ __forceinline__ void on_accumulate(Rep &R, const double *F, double E,
 // (heisenbergLib.c:678-830, xyLib.c:606-757); the per-measurement values carry
 // FP32 rounding (relative 6e-8), the sums over measurements are FP64.
 #define MCS_FS_STRIDE (F_NON + 32)
+// Neumaier's compensated summation step: s + c carries the running sum, c the
+// accumulated rounding errors of the FP32 additions (each recovered exactly).
+__device__ __forceinline__ void ksum_add(float &s, float &c, float v)
+{
+    const float t = s + v;
+    c += (fabsf(s) >= fabsf(v)) ? ((s - t) + v) : ((v - t) + s);
+    s = t;
+}
 template <int DIM>
 __device__ void on_accumulate_frames(Rep &R, float *fs, const double *E, long long m0, int n, int lane)
 {
@@ -714,7 +722,7 @@ __device__ void on_accumulate_frames(Rep &R, float *fs, const double *E, long lo
     if (lane < n) {
         const float *f = fs + lane * MCS_FS_STRIDE;
         float *val = fs + lane * MCS_FS_STRIDE + F_NON;  // [32]: value added to acc[k], k < A_ECUR
-        const float inl = (float)R.inv_nl;
+        const float inl = R.finv_nl;
         const float tx = f[F_TOT], ty = f[F_TOT + 1], tz = DIM == 3 ? f[F_TOT + 2] : 0.f;
         const float six = f[F_SI], siy = f[F_SI + 1], siz = DIM == 3 ? f[F_SI + 2] : 0.f;
         const float sjx = f[F_SJ], sjy = f[F_SJ + 1], sjz = DIM == 3 ? f[F_SJ + 2] : 0.f;
@@ -739,13 +747,13 @@ __device__ void on_accumulate_frames(Rep &R, float *fs, const double *E, long lo
         const float e = (float)(E[lane] * R.inv_N);
         val[A_E] = e;
         val[A_E2] = e * e;
-        const float ici = (float)R.inv_ci, icj = (float)R.inv_cj;
+        const float ici = R.finv_ci, icj = R.finv_cj;
         for (int k = 0; k < 3; ++k) {
             val[A_SIR + k] = fabsf(f[F_SIR + k] * ici);
             val[A_SJR + k] = fabsf(f[F_SJR + k] * icj);
         }
-        val[A_SIJR] = f[F_SIJR] * (float)R.inv_cij;
-        const float er = (f[F_ERB] * 0.5f + f[F_ERO]) * (float)R.inv_nr;
+        val[A_SIJR] = f[F_SIJR] * R.finv_cij;
+        const float er = (f[F_ERB] * 0.5f + f[F_ERO]) * R.finv_nr;
         val[A_ER] = er;
         val[A_ER2] = er * er;
         val[A_Q] = DIM == 3 ? f[F_Q] * (float)(1.0 / (MCS_PI_REF * 4)) : 0.f;
@@ -766,17 +774,23 @@ __device__ void on_accumulate_frames(Rep &R, float *fs, const double *E, long lo
         acc[A_MPREV] = (double)prev;
     }
     __syncwarp();
+    // The n frames' values of one accumulator are summed in FP32 with
+    // Neumaier compensation (the sum and its rounding error, together exact
+    // to about 2^-48 of the values), then added to the FP64 accumulator with
+    // two FP64 adds per fold instead of n: the device issues FP64 at a small
+    // fraction of its FP32 rate, and this fold runs while the other CTAs of
+    // the cluster wait for it.
     if (lane < A_ECUR && lane != A_MPREV) {
-        double a = acc[lane];
-        for (int j = 0; j < n; ++j) a += (double)fs[j * MCS_FS_STRIDE + F_NON + lane];
-        acc[lane] = a;
+        float sh = 0.f, sl = 0.f;
+        for (int j = 0; j < n; ++j) ksum_add(sh, sl, fs[j * MCS_FS_STRIDE + F_NON + lane]);
+        acc[lane] = (acc[lane] + (double)sh) + (double)sl;
     }
     const int G = R.ngroup;
     if (G > 0) {
-        const float inl = (float)R.inv_nl;
+        const float inl = R.finv_nl;
         for (int idx = lane; idx < (G + 1) * (G + 1); idx += 32) {
             const int ga = idx / (G + 1), gb = idx - ga * (G + 1);
-            double a = acc[A_GRP + idx], a4 = ga == gb ? acc[A_GRP + (G + 1) * (G + 1) + ga] : 0.0;
+            float ah = 0.f, al = 0.f, bh = 0.f, bl = 0.f;
             for (int j = 0; j < n; ++j) {
                 const float *f = fs + j * MCS_FS_STRIDE;
                 const float ax = ga < G ? f[F_G + 3 * ga] : f[F_TOT] * inl, ay = ga < G ? f[F_G + 3 * ga + 1] : f[F_TOT + 1] * inl;
@@ -784,11 +798,14 @@ __device__ void on_accumulate_frames(Rep &R, float *fs, const double *E, long lo
                 const float bx = gb < G ? f[F_G + 3 * gb] : f[F_TOT] * inl, by = gb < G ? f[F_G + 3 * gb + 1] : f[F_TOT + 1] * inl;
                 const float bz = DIM == 3 ? (gb < G ? f[F_G + 3 * gb + 2] : f[F_TOT + 2] * inl) : 0.f;
                 const float d = ax * bx + ay * by + az * bz;
-                a += (double)d;
-                a4 += (double)(d * d);
+                ksum_add(ah, al, d);
+                ksum_add(bh, bl, d * d);
             }
-            acc[A_GRP + idx] = a;
-            if (ga == gb) acc[A_GRP + (G + 1) * (G + 1) + ga] = a4;
+            acc[A_GRP + idx] = (acc[A_GRP + idx] + (double)ah) + (double)al;
+            if (ga == gb) {
+                double &a4 = acc[A_GRP + (G + 1) * (G + 1) + ga];
+                a4 = (a4 + (double)bh) + (double)bl;
+            }
         }
     }
     __syncwarp();

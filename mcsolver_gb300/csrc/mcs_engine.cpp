@@ -198,6 +198,8 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool u
     R.ci = m.ci; R.cj = m.cj; R.cij = m.cij;
     R.inv_nl = 1.0 / m.nlat; R.inv_N = 1.0 / m.N;
     R.inv_ci = 1.0 / m.ci; R.inv_cj = 1.0 / m.cj; R.inv_cij = 1.0 / m.cij; R.inv_nr = 1.0 / m.n_rorb;
+    R.finv_nl = (float)R.inv_nl; R.finv_N = (float)R.inv_N; R.finv_ci = (float)R.inv_ci;
+    R.finv_cj = (float)R.inv_cj; R.finv_cij = (float)R.inv_cij; R.finv_nr = (float)R.inv_nr;
     R.nacc = (int)replica_acc_count(m);
     {
         bool uni = true;

@@ -113,6 +113,7 @@ struct Rep {
     int gall;                                    // bitmask of groups that hold every site
     int ci, cj, cij;                             // chosen counts of the pair lists
     double inv_nl, inv_N, inv_ci, inv_cj, inv_cij, inv_nr;  // reciprocals of the divisors above
+    float finv_nl, finv_N, finv_ci, finv_cj, finv_cij, finv_nr;  // the same in FP32 (per-measurement observables)
     int nacc;                                    // FP64 accumulators in acc[]
     int uniform_len;                             // every |S| equal (circuit fast path)
     float inv_len3;                              // 1/|S|^3 when uniform_len

@@ -55,6 +55,11 @@ UNEVEN = [
                                                                   nthermal=6, nsweep=12, frames=12)),
     ("heis_L72_C16_dmi", "heisenberg", 16, lambda: C.square_args_fast("heisenberg", 72, 0.7, dmi=0.4,
                                                                       nthermal=4, nsweep=8, frames=8)),
+    # Ly/2 odd: the first site of row 1 is swept with the boundary rows
+    ("xy_L34_C4_odd_half", "xy", 4, lambda: C.square_args("xy", 34, 0.9, nthermal=6, nsweep=12, frames=12)),
+    ("heis_L30_C2_odd_half", "heisenberg", 2, lambda: C.square_args("heisenberg", 30, 0.6, h=0.2, dmi=0.4,
+                                                                     nthermal=6, nsweep=12, frames=12)),
+    ("xy_L26_C8_odd_half", "xy", 8, lambda: C.square_args("xy", 26, 1.0, nthermal=6, nsweep=12, frames=12)),
 ]
 
 
