@@ -444,15 +444,39 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
         // change and count), then the CTA's slot in FP64 across the warps
         {
             const int lane = tid & 31, wid = tid >> 5, nw = (bd + 31) >> 5;
+            float *redf = (float *)red;                       // [32 warps][CL_SLOT]
+            long long *redl = (long long *)(red + 16 * CL_SLOT);  // [32 warps]
+            if (R.meas_regular) {
+                // regular lattices: entries 3-5 equal 0-2 (every site is a
+                // correlated-pair site) and the group entries 16-27 are 0, so
+                // 14 distinct values are halved over 16 lanes (lane l holds
+                // value l of b, then the xor-16 step adds the two half-warps)
+                float b[16] = {a[0], a[1], a[2], a[6], a[7], a[8], a[9], a[10], a[11], a[12], a[13], a[14], a[15],
+                               a[CL_NV], 0.f, 0.f};
 #pragma unroll
-            for (int w = 16; w >= 1; w >>= 1) {
-                const bool up = (lane & w) != 0;
+                for (int w = 8; w >= 1; w >>= 1) {
+                    const bool up = (lane & w) != 0;
 #pragma unroll
-                for (int j = 0; j < w; ++j) {
-                    const float send = up ? a[j] : a[j + w];
-                    const float keep = up ? a[j + w] : a[j];
-                    a[j] = keep + __shfl_xor_sync(0xffffffffu, send, w);
+                    for (int j = 0; j < w; ++j) {
+                        const float send = up ? b[j] : b[j + w];
+                        const float keep = up ? b[j + w] : b[j];
+                        b[j] = keep + __shfl_xor_sync(0xffffffffu, send, w);
+                    }
                 }
+                const float y = b[0] + __shfl_xor_sync(0xffffffffu, b[0], 16);
+                if (lane < 14) redf[wid * CL_SLOT + lane] = y;
+            } else {
+#pragma unroll
+                for (int w = 16; w >= 1; w >>= 1) {
+                    const bool up = (lane & w) != 0;
+#pragma unroll
+                    for (int j = 0; j < w; ++j) {
+                        const float send = up ? a[j] : a[j + w];
+                        const float keep = up ? a[j + w] : a[j];
+                        a[j] = keep + __shfl_xor_sync(0xffffffffu, send, w);
+                    }
+                }
+                if (lane <= CL_NV) redf[wid * CL_SLOT + lane] = a[0];
             }
             // the energy change went through the FP32 halving with the frame
             // values (lane CL_NV); the count stays integer
@@ -464,15 +488,16 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
             // summed with Neumaier compensation and enter the FP64 slot as the
             // sum plus its rounding error (FP64 instructions issue slowly and
             // this sum is on the measurement's critical path)
-            float *redf = (float *)red;                       // [32 warps][CL_SLOT]
-            long long *redl = (long long *)(red + 16 * CL_SLOT);  // [32 warps]
-            if (lane <= CL_NV) redf[wid * CL_SLOT + lane] = a[0];
             if (lane == 0) redl[wid] = na;
             __syncthreads();
             const int slot = (int)(m & 1);
             if (tid <= CL_NV) {
+                // slot entry tid from warp entry src (regular lattices: the compact order above)
+                const int src = !R.meas_regular ? tid
+                                                : (tid < 3 ? tid : tid < 16 ? tid - 3 : tid == CL_NV ? 13 : -1);
                 float sh = 0.f, sl = 0.f;
-                for (int w = 0; w < nw; ++w) ksum_add(sh, sl, redf[w * CL_SLOT + tid]);
+                if (src >= 0)
+                    for (int w = 0; w < nw; ++w) ksum_add(sh, sl, redf[w * CL_SLOT + src]);
                 part[slot * CL_SLOT + tid] = (double)sh + (double)sl;
             } else if (tid == CL_NV + 1) {
                 long long n = 0;

@@ -352,9 +352,10 @@ __device__ __forceinline__ void block_sum_ll(long long (&v)[K], long long *red, 
 // ------------------------------------------------------------------ measurement helpers
 __device__ __forceinline__ void v_norm_ref(float &x, float &y, float &z)
 {
-    float len = sqrtf(x * x + y * y + z * z);
-    if (len < 1e-5f) return;  // normalize() leaves short vectors unchanged
-    x /= len; y /= len; z /= len;
+    const float l2 = x * x + y * y + z * z;
+    if (l2 < 1e-10f) return;  // normalize() leaves vectors shorter than 1e-5 unchanged
+    const float r = rsqrtf(l2);
+    x *= r; y *= r; z *= r;
 }
 
 // getMajoritySpin (O(n)): normalize(sum of cluster spins) * S (signed)
