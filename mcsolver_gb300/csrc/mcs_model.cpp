@@ -166,22 +166,33 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
         const bool ign = p->ignore_offdiag > 0;
         ClassTable<9> cls;
         bool anyoff = false;
-        const double *prevJ = nullptr;  // a link equal to the previous one has its class
+        // A link whose matrix has the bits of the last matrix seen in the same
+        // link slot (translation-invariant lattices repeat the slot pattern
+        // site after site), or of the previous link, takes that link's class
+        // without a table lookup.
+        const double *slotJ[MCS_MAXZ] = {};
+        int slotc[MCS_MAXZ] = {};
+        const double *prevJ = nullptr;
         int prevc = 0;
         for (int i = 0; i < N; ++i)
             for (int l = 0; l < p->nlink[i]; ++l) {
                 const double *J = p->link_strength + ((size_t)i * z + l) * 9;
-                if (prevJ && same_bits9(J, prevJ)) {
-                    linkcls[(size_t)i * z + l] = prevc;
-                    continue;
+                int c;
+                if (slotJ[l] && same_bits9(J, slotJ[l])) {
+                    c = slotc[l];
+                } else if (prevJ && same_bits9(J, prevJ)) {
+                    c = prevc;
+                } else {
+                    double v[9];
+                    memcpy(v, J, sizeof v);
+                    if (ign) v[3] = v[4] = v[5] = v[6] = v[7] = v[8] = 0.0;
+                    if (dim == 2) v[2] = v[4] = v[5] = v[7] = v[8] = 0.0;  // XY reads xx,yy,xy,yx (xyLib.c:150-153)
+                    for (int k = 3; k < 9; ++k) anyoff |= v[k] != 0.0;
+                    c = cls.find_or_add(v);
                 }
-                double v[9];
-                memcpy(v, J, sizeof v);
-                if (ign) v[3] = v[4] = v[5] = v[6] = v[7] = v[8] = 0.0;
-                if (dim == 2) v[2] = v[4] = v[5] = v[7] = v[8] = 0.0;  // XY reads xx,yy,xy,yx (xyLib.c:150-153)
-                for (int k = 3; k < 9; ++k) anyoff |= v[k] != 0.0;
-                linkcls[(size_t)i * z + l] = prevc = cls.find_or_add(v);
-                prevJ = J;
+                linkcls[(size_t)i * z + l] = c;
+                slotJ[l] = J; slotc[l] = c;
+                prevJ = J; prevc = c;
             }
         if (cls.keys.size() > 65535) FAIL(MCS_EUNSUPPORTED, "too many distinct exchange matrices");
         std::vector<std::vector<double>> tab;
