@@ -92,6 +92,29 @@ __device__ __forceinline__ void cl_links(const Rep &R, int rows, int c, int xl, 
     f(3, base + (xl + 1) * hy + (ym >> 1), R.sq_code[3]);
 }
 
+// The same with the lattice side and the four link codes in registers (the
+// sweep loop's copy; the descriptor lives in shared memory).
+struct SqLinks {
+    int Ly, hy, rows, q0, q1, q2, q3;
+};
+template <class F>
+__device__ __forceinline__ void cl_links_r(const SqLinks &K, int c, int xl, int yh, F &&f)
+{
+    const int hy = K.hy;
+    const int y = 2 * yh + ((xl + c) & 1);
+    const int base = (1 - c) * K.rows * hy;
+    const int yp = (y + 1 == K.Ly) ? 0 : y + 1;
+    const int ym = (y == 0) ? K.Ly - 1 : y - 1;
+    f(0, base + (xl + 2) * hy + yh, K.q0);
+    f(1, base + xl * hy + yh, K.q1);
+    f(2, base + (xl + 1) * hy + (yp >> 1), K.q2);
+    f(3, base + (xl + 1) * hy + (ym >> 1), K.q3);
+}
+// Register copies of the descriptor flags the trial reads.
+struct TrialFlags {
+    bool fullJ, has_d;
+};
+
 // Index of the slot sum that feeds frame entry f (frame layout F_*), -1 for 0.
 __device__ __forceinline__ int cl_frame_src(int f, int ngroup, int gall)
 {
@@ -538,6 +561,8 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
     // orders them before the next phase's reads.
     long long u = R.u;
     const long long uend = min(R.units_total, u + max_units);
+    const SqLinks sql = {R.Ly, hy, rows, R.sq_code[0], R.sq_code[1], R.sq_code[2], R.sq_code[3]};
+    const TrialFlags tflags = {R.fullJ != 0, R.has_d != 0};
     for (; u < uend; ++u) {
         const long long t = R.u0 + u;
         const bool fuse = R.meas_regular && measures_after(R, u) && (mloc % R.recheck) != 0;
@@ -595,7 +620,12 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
                 const int li = cb + (xl + 1) * hy + yh;
                 const uint4 w = ws[e];
                 float dE;
-                if (on_trial<DIM>(R, jt, dt, S, li, 0, w, beta, h, [&](auto &&f) { cl_links(R, rows, c, xl, yh, f); }, &dE)) {
+                bool acc;
+                if (DIM == 2)  // XY: register copies (the Heisenberg loop has no registers to spare)
+                    acc = on_trial<DIM>(tflags, jt, dt, S, li, 0, w, beta, h, [&](auto &&f) { cl_links_r(sql, c, xl, yh, f); }, &dE);
+                else
+                    acc = on_trial<DIM>(R, jt, dt, S, li, 0, w, beta, h, [&](auto &&f) { cl_links(R, rows, c, xl, yh, f); }, &dE);
+                if (acc) {
                     dEf += dE;
                     ++nacc;
                     // own row 0 is the previous CTA's bottom ghost (its local row

@@ -200,8 +200,10 @@ __device__ __forceinline__ void on_direction_exact(const uint4 &w, float &r0, fl
     }
 }
 
-template <int DIM, class LINKS>
-__device__ __forceinline__ void on_field(const Rep &R, const float *__restrict__ jt, const Spins &S, LINKS &&links,
+// RR: the replica descriptor, or any type with its fullJ and has_d fields
+// (a kernel can pass register copies of them)
+template <int DIM, class LINKS, class RR>
+__device__ __forceinline__ void on_field(const RR &R, const float *__restrict__ jt, const Spins &S, LINKS &&links,
                                          float &h0, float &h1, float &h2)
 {
     h0 = h1 = h2 = 0.f;
@@ -228,8 +230,8 @@ __device__ __forceinline__ void on_field(const Rep &R, const float *__restrict__
 
 // returns true when accepted; dE (table units, before beta) in *dEout.
 // dc: site class (anisotropy vector and |S|).
-template <int DIM, class LINKS>
-__device__ __forceinline__ bool on_trial(const Rep &R, const float *__restrict__ jt, const float *__restrict__ dt,
+template <int DIM, class LINKS, class RR>
+__device__ __forceinline__ bool on_trial(const RR &R, const float *__restrict__ jt, const float *__restrict__ dt,
                                          const Spins &S, int v, int dc, const uint4 &w, float beta, float h,
                                          LINKS &&links, float *dEout)
 {
