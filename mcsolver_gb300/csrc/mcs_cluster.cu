@@ -296,8 +296,11 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
     // full-energy pass): each site's value right after its colour phase, in
     // the order pass A would read them
     float fa[4] = {0.f, 0.f, 0.f, 0.f};
-    auto measure = [&](long long m, bool efull, bool fused) {
-        // block spins of the own chosen sites
+    // Block spins of the own chosen sites (own rows only) into majc.  The
+    // sweep computes them after its last colour phase and before that
+    // phase's cluster barrier, which then also publishes them to the other
+    // CTAs' pass B: the measurement needs no barrier of its own.
+    auto block_spins = [&]() {
         const int r0 = (x0 >> 1) * hb;  // first chosen index of this slab
         for (int q = tid; q < nch; q += bd) {
             const int pr = q / (R.Ly / 2);           // even-row index inside the CTA
@@ -318,8 +321,9 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
             const float sv = R.meas_regular ? R.sval0 : R.sval[R.rorb[r0 + q]];
             majc[3 * q] = mx * sv; majc[3 * q + 1] = my * sv; majc[3 * q + 2] = mz * sv;
         }
-        __syncthreads();
-        cl.sync();
+    };
+    auto measure = [&](long long m, bool efull, bool fused) {
+        const int r0 = (x0 >> 1) * hb;  // first chosen index of this slab
         if (rank == 0) gather(false);
         const bool full = R.fullJ;
         // partial layout: 0-2 total spin, 3-5 pair sum, 6 pair s.s, 7/8 full
@@ -649,6 +653,10 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
                     fa[3] += sx * sx + sy * sy + sz * sz;
                 }
               }
+            }
+            if (c == 1 && measures_after(R, u)) {
+                __syncthreads();  // every own site of both colours is final
+                block_spins();
             }
             cl.sync();
         }
