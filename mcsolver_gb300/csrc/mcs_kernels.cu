@@ -687,6 +687,7 @@ __global__ void __launch_bounds__(512) k_wolff(Rep *reps, const int *ids, long l
     long long *Fi = (long long *)(smem + L.Fi);
     int *sh = (int *)(smem + L.sh);
     float *shf = (float *)(sh + 8);
+    __shared__ float wfs[MCS_FS_STRIDE];  // one measurement frame in FP32
     const unsigned char *st = R.stype;
     if (!L.gstate) {
         unsigned char *sts = (unsigned char *)(smem + L.stype);
@@ -744,14 +745,18 @@ __global__ void __launch_bounds__(512) k_wolff(Rep *reps, const int *ids, long l
                 if (tid == 0) { R.acc[A_ECUR] += dEd; dEd = 0.0; }
                 const bool efull = (m % R.recheck) == 0;
                 on_frame<DIM, GEOM>(R, jt, dt, S, 0, max(max(N, R.nlat), max(R.n_rorb, R.ncirc)), efull, red, F, nullptr);
-                if (tid == 0) {
-                    if (efull) {
-                        double Ef = F[F_EFB] / 2 + F[F_EFO];
-                        double d = fabs(R.acc[A_ECUR] - Ef);
-                        if (d > R.acc[A_DRIFT]) R.acc[A_DRIFT] = d;
-                        R.acc[A_ECUR] = Ef;
-                    }
-                    on_accumulate<DIM>(R, F, R.acc[A_ECUR], m);
+                if (tid == 0 && efull) {
+                    double Ef = F[F_EFB] / 2 + F[F_EFO];
+                    double d = fabs(R.acc[A_ECUR] - Ef);
+                    if (d > R.acc[A_DRIFT]) R.acc[A_DRIFT] = d;
+                    R.acc[A_ECUR] = Ef;
+                }
+                // the frame folds into the accumulators with one warp (as in the resident kernel)
+                if (tid < 32) {
+                    __syncwarp();
+                    for (int f = tid; f < F_NON; f += 32) wfs[f] = (float)F[f];
+                    __syncwarp();
+                    on_accumulate_frames<DIM>(R, wfs, &R.acc[A_ECUR], m, 1, tid);
                 }
             }
             if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) {

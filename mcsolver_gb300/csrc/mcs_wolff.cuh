@@ -57,6 +57,7 @@ __device__ void wolff_cluster(Rep &R, const float *jt, const float *dt, const Is
         wq_put(W, 0, seed);
         W.bits[seed >> 5] |= 1u << (seed & 31);
         sh[0] = 0; sh[1] = 1;
+        sh[4] = 0; sh[5] = 0; sh[6] = 0;  // discoveries per level, three in rotation
         float r0 = 0, r1 = 0, r2 = 0;
         if (DIM > 1) on_direction<DIM>(make_uint4(w.y, w.z, 0, 0), r0, r1, r2);
         shf[0] = r0; shf[1] = r1; shf[2] = r2;
@@ -65,9 +66,16 @@ __device__ void wolff_cluster(Rep &R, const float *jt, const float *dt, const Is
     __syncthreads();
     const float r0 = shf[0], r1 = shf[1], r2 = shf[2];
     const bool full = R.fullJ;
-    // ---- growth, one frontier level at a time
-    int lb = 0, le = 1;
+    // ---- growth, one frontier level at a time.  Level k appends the sites
+    // it discovers after the queue's current end, counting them in
+    // sh[4 + k % 3]; after the level's barrier every thread reads that count.
+    // The counter of level k + 3 (= k's) is cleared by thread 0 during level
+    // k + 2: after the barrier that ends level k + 1 (every read of it is done)
+    // and before the barrier that starts level k + 3.  One barrier per level.
+    int lb = 0, le = 1, k = 0;
     while (lb < le) {
+        int *cnt = sh + 4 + k % 3;
+        if (tid == 0) sh[4 + (k + 1) % 3] = 0;
         for (int f = lb + tid; f < le; f += bd) {
             const int i = wq_get(W, f);
             if (DIM == 1) {
@@ -79,9 +87,33 @@ __device__ void wolff_cluster(Rep &R, const float *jt, const float *dt, const Is
                     if (thr == 0) return;
                     if ((unsigned long long)wolff_coin(i, j, q, R.seed) < thr) {
                         unsigned int old = atomicOr(&W.bits[j >> 5], 1u << (j & 31));
-                        if (!((old >> (j & 31)) & 1u)) wq_put(W, atomicAdd(&sh[1], 1), j);
+                        if (!((old >> (j & 31)) & 1u)) wq_put(W, le + atomicAdd(cnt, 1), j);
                     }
                 });
+            } else if (GEOM == MCS_GEOM_SQUARE) {
+                // square lattice: the four bond coins are drawn first, as
+                // independent instruction streams (the growth is a chain of
+                // dependent levels, so latency decides), then the bonds are
+                // tested in link order as below
+                const float sdi = -(S.x[i] * r0 + S.y[i] * r1 + (DIM == 3 ? S.z[i] * r2 : 0.f));
+                int js[4], cs[4];
+                for_links<GEOM>(R, i, [&](int l, int j, int code) { js[l] = j; cs[l] = code; });
+                uint32_t cw[4];
+#pragma unroll
+                for (int l = 0; l < 4; ++l) cw[l] = wolff_coin(i, js[l], q, R.seed);
+#pragma unroll
+                for (int l = 0; l < 4; ++l) {
+                    const int j = js[l];
+                    if ((W.bits[j >> 5] >> (j & 31)) & 1u) continue;
+                    const float sdj = -(S.x[j] * r0 + S.y[j] * r1 + (DIM == 3 ? S.z[j] * r2 : 0.f));
+                    const float rjr = on_jdot<DIM>(jt + 9 * cs[l], full, r0, r1, r2, r0, r1, r2);
+                    const float corr = 2.f * sdi * sdj * rjr;
+                    if (!(corr < 0.f)) continue;
+                    if ((1.f - __expf(corr)) > u24(cw[l])) {
+                        unsigned int old = atomicOr(&W.bits[j >> 5], 1u << (j & 31));
+                        if (!((old >> (j & 31)) & 1u)) wq_put(W, le + atomicAdd(cnt, 1), j);
+                    }
+                }
             } else {
                 const float sdi = -(S.x[i] * r0 + S.y[i] * r1 + (DIM == 3 ? S.z[i] * r2 : 0.f));
                 for_links<GEOM>(R, i, [&](int, int j, int code) {
@@ -92,15 +124,15 @@ __device__ void wolff_cluster(Rep &R, const float *jt, const float *dt, const Is
                     if (!(corr < 0.f)) return;
                     if ((1.f - __expf(corr)) > u24(wolff_coin(i, j, q, R.seed))) {
                         unsigned int old = atomicOr(&W.bits[j >> 5], 1u << (j & 31));
-                        if (!((old >> (j & 31)) & 1u)) wq_put(W, atomicAdd(&sh[1], 1), j);
+                        if (!((old >> (j & 31)) & 1u)) wq_put(W, le + atomicAdd(cnt, 1), j);
                     }
                 });
             }
         }
         __syncthreads();
         lb = le;
-        le = sh[1];
-        __syncthreads();
+        le += *cnt;
+        ++k;
     }
     const int n = le;
     // ---- acceptance step and the energy change of the flip
@@ -184,8 +216,8 @@ __device__ void wolff_cluster(Rep &R, const float *jt, const float *dt, const Is
             a_tot -= R.h * (DIM == 3 ? ti2 : ti0);
             a_dE -= R.h * (DIM == 3 ? di2 : di0);
         }
-        double c2[2] = {(double)a_tot, (double)a_dE};
-        block_sum<2>(c2, red, F);
+        float c2[2] = {a_tot, a_dE};
+        block_sum_f<2>(c2, red, F);  // FP32 inside a warp, FP64 across the warps
         if (tid == 0) {
             const double tot = F[0];
             bool acc = tot <= 0 || exp(-tot) > (double)u24((uint32_t)sh[3]);
