@@ -235,7 +235,8 @@ class _ResultBuf:
         G = P.n_group
         self.ng = (G + 1) ** 2 + (G + 1)
         self.groups = np.zeros(self.ng)
-        self.frames = np.zeros(max(1, P.frames) * P.N * 3, dtype=np.float32)
+        # spin frames only when the problem asks for them (the buffer is N*3 floats per frame)
+        self.frames = np.zeros(P.frames * P.N * 3, dtype=np.float32) if P.frames > 0 else None
         self.series = np.zeros(max(1, P.nsweep) * NSER) if series else None
         r = McsResult()
         r.group_values = self.groups.ctypes.data_as(_f64p)

@@ -45,16 +45,30 @@ const std::string &get_error() { return g_err; }
 
 // ------------------------------------------------------------------ arena builder
 struct ArenaBuilder {
-    std::vector<unsigned char> host = std::vector<unsigned char>(256, 0);  // offset 0 is never used
+    // offsets are handed out as pieces are added; the bytes are gathered into
+    // one allocation by finish() (the pieces' storage must live until then)
+    struct Piece {
+        size_t off;
+        const void *data;
+        size_t bytes;
+    };
+    std::vector<Piece> pieces;
+    size_t size = 256;  // offset 0 is never used
     size_t add(const void *data, size_t bytes)
     {
-        size_t off = (host.size() + 255) & ~(size_t)255;
-        host.resize(off + bytes);
-        if (data && bytes) memcpy(host.data() + off, data, bytes);
-        else if (bytes) memset(host.data() + off, 0, bytes);
+        size_t off = (size + 255) & ~(size_t)255;
+        pieces.push_back({off, data, bytes});
+        size = off + bytes;
         return off;
     }
     template <class T> size_t addv(const std::vector<T> &v) { return add(v.empty() ? nullptr : v.data(), v.size() * sizeof(T)); }
+    std::vector<unsigned char> finish() const
+    {
+        std::vector<unsigned char> host(size, 0);  // pieces without data and the gaps stay zero
+        for (const Piece &q : pieces)
+            if (q.data && q.bytes) memcpy(host.data() + q.off, q.data, q.bytes);
+        return host;
+    }
 };
 
 // Arenas come from the device's default memory pool, kept cached by the
@@ -97,10 +111,11 @@ size_t replica_acc_count(const HostModel &m)
     return A_GRP + (size_t)(G + 1) * (G + 1) + (G + 1);
 }
 
-int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool upload)
+int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool upload, const ModelTemplate *tmpl,
+                  bool *reused)
 {
     std::string err;
-    int rc = compile_model(p, o, &r->hm, &err);
+    int rc = compile_model(p, o, &r->hm, &err, tmpl, reused);
     if (rc != MCS_OK) { set_error(err); return rc; }
     const HostModel &m = r->hm;
     r->record_series = o && o->record_series;
@@ -127,9 +142,10 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool u
     size_t o_sflag = A.addv(m.sflag), o_rtgt = A.addv(m.rtgt);
     int spad = (m.N + 31) & ~31;
     size_t o_spins;
+    std::vector<float> sp;  // O(n) spins padded per component (lives until A.finish())
     if (m.dim == 1) o_spins = A.addv(m.init_sigma);
     else {
-        std::vector<float> sp((size_t)m.dim * spad, 0.f);
+        sp.assign((size_t)m.dim * spad, 0.f);
         for (int c = 0; c < m.dim; ++c)
             memcpy(sp.data() + (size_t)c * spad, m.init_vec.data() + (size_t)c * m.N, sizeof(float) * m.N);
         o_spins = A.addv(sp);
@@ -147,7 +163,7 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool u
         o_wbits = A.add(nullptr, ((size_t)(m.N + 31) / 32) * sizeof(unsigned));
         o_wq = A.add(nullptr, (size_t)m.N * sizeof(int));
     }
-    r->bytes = A.host.size();
+    r->bytes = A.size;
     // the descriptor holds arena offsets until upload_replica() relocates them
     auto P = [](size_t off) { return (void *)(uintptr_t)off; };
     Rep &R = r->rep;
@@ -231,7 +247,7 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool u
     r->acc_off = o_acc; r->icnt_off = o_icnt; r->stats_off = o_stats; r->series_off = o_series;
     r->frames_off = o_frames; r->spins_off = o_spins;
     r->nacc = nacc;
-    r->staging = std::move(A.host);
+    r->staging = A.finish();
     if (upload) return upload_replica(r);
     return MCS_OK;
 }
@@ -474,10 +490,31 @@ int Batch::add(const mcs_problem *p, const mcs_options *o, int *idx)
 {
     std::unique_ptr<Replica> r(new Replica());
     r->device = device;
-    int rc = build_replica(p, o, r.get(), true);
+    // O(n) replicas of a lattice already compiled in this batch (a grid of
+    // temperatures and fields) take its structure from that replica's template
+    std::shared_ptr<const ModelTemplate> t;
+    const bool on = p && p->model != MCS_ISING;
+    if (on) {
+        std::lock_guard<std::mutex> lock(add_mutex);
+        for (auto it = templates.rbegin(); it != templates.rend() && !t; ++it)
+            if ((*it)->in.model == p->model && (*it)->in.N == p->n_sites && (*it)->in.z == p->max_links) t = *it;
+    }
+    bool reused = false;
+    int rc = build_replica(p, o, r.get(), true, t.get(), &reused);
     if (rc != MCS_OK) return rc;
+    std::shared_ptr<const ModelTemplate> nt;
+    if (on && !reused) {
+        bool have = false;
+        {
+            std::lock_guard<std::mutex> lock(add_mutex);
+            for (auto &q : templates) have |= q->in.model == p->model && q->in.N == p->n_sites && q->in.z == p->max_links;
+            have |= templates.size() >= 8;
+        }
+        if (!have) nt = make_template(p, r->hm);
+    }
     std::lock_guard<std::mutex> lock(add_mutex);
     if (prepared) { set_error("batch already prepared: add replicas before the first run or advance"); return MCS_EINVAL; }
+    if (nt) templates.push_back(std::move(nt));
     replicas.push_back(std::move(r));
     if (idx) *idx = (int)replicas.size() - 1;
     return MCS_OK;

@@ -37,7 +37,8 @@ struct Replica {
     ~Replica();
 };
 
-int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool upload);
+int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool upload,
+                  const ModelTemplate *tmpl = nullptr, bool *reused = nullptr);
 int upload_replica(Replica *r);
 int replica_results(Replica *r, const Rep &Rfinal, mcs_result *res);
 // Read the result blocks of many replicas with one synchronisation.
@@ -92,6 +93,7 @@ struct Batch {
     cudaStream_t stream = nullptr, stream2 = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_a = nullptr, ev_b = nullptr, ev_fork = nullptr;
     std::mutex add_mutex;       // mcs_batch_add may be called from several threads
+    std::vector<std::shared_ptr<const ModelTemplate>> templates;  // compiled lattices of this batch (O(n))
     int cluster_override = 0;   // 1: never cluster; 2/4/8: only that size
     int no_autotune = 0;
     int balance = 1;            // place replicas by the load balancer (off for parallel tempering)

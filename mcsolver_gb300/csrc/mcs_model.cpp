@@ -107,8 +107,77 @@ static inline bool same_bits9(const double *a, const double *b)
     return d == 0;
 }
 
-int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std::string *err)
+// The structural inputs of p equal those recorded in the template, bit for bit.
+static bool same_structure(const StructInputs &in, const mcs_problem *p)
 {
+    if (in.model != p->model || in.alg != p->algorithm || in.N != p->n_sites || in.z != p->max_links) return false;
+    if (in.n_circuits != p->n_circuits || in.n_lat != p->n_lat || in.n_group != p->n_group ||
+        in.max_group != p->max_group || in.n_rorb != p->n_rorb || in.n_in_cluster != p->n_in_cluster ||
+        in.ignore_offdiag != p->ignore_offdiag || in.has_rlink != (p->r_link != nullptr))
+        return false;
+    auto eq = [](const auto &v, const void *q) {
+        return v.empty() || (q && memcmp(v.data(), q, v.size() * sizeof(v[0])) == 0);
+    };
+    return eq(in.nlink, p->nlink) && eq(in.linked_orb, p->linked_orb) && eq(in.circuits, p->circuits) &&
+           eq(in.corr_pair, p->corr_pair) && eq(in.group_list, p->group_list) && eq(in.r_orb, p->r_orb) &&
+           eq(in.r_cluster, p->r_cluster) && eq(in.r_link, p->r_link) && eq(in.init_spin, p->init_spin);
+}
+
+std::shared_ptr<const ModelTemplate> make_template(const mcs_problem *p, const HostModel &m)
+{
+    auto t = std::make_shared<ModelTemplate>();
+    t->hm = m;
+    StructInputs &in = t->in;
+    in.model = p->model; in.alg = p->algorithm; in.N = p->n_sites; in.z = p->max_links;
+    in.n_circuits = p->n_circuits; in.n_lat = p->n_lat; in.n_group = p->n_group; in.max_group = p->max_group;
+    in.n_rorb = p->n_rorb; in.n_in_cluster = p->n_in_cluster; in.ignore_offdiag = p->ignore_offdiag;
+    in.has_rlink = p->r_link != nullptr;
+    const size_t N = p->n_sites, z = p->max_links;
+    auto cp = [](auto &v, const auto *q, size_t n) { if (q && n) v.assign(q, q + n); };
+    cp(in.nlink, p->nlink, N);
+    cp(in.linked_orb, p->linked_orb, N * z);
+    cp(in.circuits, p->circuits, 3 * (size_t)p->n_circuits);
+    cp(in.corr_pair, p->corr_pair, 2 * (size_t)p->n_lat);
+    cp(in.group_list, p->group_list, (size_t)p->n_group * p->max_group);
+    cp(in.r_orb, p->r_orb, (size_t)p->n_rorb);
+    cp(in.r_cluster, p->r_cluster, (size_t)p->n_rorb * p->n_in_cluster);
+    cp(in.r_link, p->r_link, (size_t)p->n_rorb * z);
+    cp(in.init_spin, p->init_spin, N);
+    return t;
+}
+
+// O(n) site classes (anisotropy vector and spin length) in the sweep order
+// `sites`: stype per sweep index, the class table dtab [ndc][4], has_d.
+static int onsite_classes(const mcs_problem *p, int dim, int N, const std::vector<int> &sites,
+                          std::vector<uint8_t> *stype, std::vector<float> *dtab, int *ndc, int *has_d, std::string *err)
+{
+    ClassTable<4> dcls;
+    stype->assign(N, 0);
+    bool anyd = false;
+    for (int k = 0; k < N; ++k) {
+        int i = sites[k];
+        double v[4] = {p->init_d[3 * (size_t)i], p->init_d[3 * (size_t)i + 1], p->init_d[3 * (size_t)i + 2],
+                       fabs(p->init_spin[i])};
+        if (dim == 2) v[2] = 0.0;
+        anyd |= v[0] != 0.0 || v[1] != 0.0 || v[2] != 0.0;
+        int c = dcls.find_or_add(v);
+        if (c > 255) FAIL(MCS_EUNSUPPORTED, "more than 256 distinct (anisotropy, spin length) site classes");
+        (*stype)[k] = (uint8_t)c;
+    }
+    *ndc = (int)dcls.keys.size();
+    *has_d = anyd ? 1 : 0;
+    dtab->resize(4 * dcls.keys.size());
+    for (size_t c = 0; c < dcls.keys.size(); ++c)
+        for (int k = 0; k < 4; ++k) (*dtab)[4 * c + k] = (float)dcls.keys[c][k];
+    return MCS_OK;
+}
+
+static int compile_program_state(const mcs_problem *p, const mcs_options *o, HostModel *m, int dim, std::string *err);
+
+int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std::string *err,
+                  const ModelTemplate *tmpl, bool *reused)
+{
+    if (reused) *reused = false;
     if (!p) FAIL(MCS_EINVAL, "null problem");
     if (p->model < 1 || p->model > 3) FAIL(MCS_EINVAL, "model must be 1 (Ising), 2 (XY) or 3 (Heisenberg)");
     if (p->algorithm != 0 && p->algorithm != 1) FAIL(MCS_EINVAL, "algorithm must be 0 (Metropolis) or 1 (Wolff)");
@@ -138,26 +207,31 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
     m->h = p->h; m->flunc = p->flunc;
     m->seed = o ? o->seed : 0;
 
-    for (int i = 0; i < N; ++i) {
-        if (p->nlink[i] < 0 || p->nlink[i] > z) FAIL(MCS_EINVAL, "nlink out of range");
-        for (int l = 0; l < p->nlink[i]; ++l) {
-            int j = p->linked_orb[(size_t)i * z + l];
-            if (j < 0 || j >= N) FAIL(MCS_EINVAL, "linkedOrb index out of range");
+    // a problem whose structural inputs equal a validated template's needs no
+    // second index validation
+    const ModelTemplate *like = (tmpl && dim > 1 && same_structure(tmpl->in, p)) ? tmpl : nullptr;
+    if (!like) {
+        for (int i = 0; i < N; ++i) {
+            if (p->nlink[i] < 0 || p->nlink[i] > z) FAIL(MCS_EINVAL, "nlink out of range");
+            for (int l = 0; l < p->nlink[i]; ++l) {
+                int j = p->linked_orb[(size_t)i * z + l];
+                if (j < 0 || j >= N) FAIL(MCS_EINVAL, "linkedOrb index out of range");
+            }
         }
+        for (int k = 0; k < 2 * p->n_lat; ++k)
+            if (p->corr_pair[k] < 0 || p->corr_pair[k] >= N) FAIL(MCS_EINVAL, "corrOrbPair index out of range");
+        for (int k = 0; k < p->n_rorb; ++k)
+            if (p->r_orb[k] < 0 || p->r_orb[k] >= N) FAIL(MCS_EINVAL, "rOrb index out of range");
+        for (long long k = 0; k < (long long)p->n_rorb * p->n_in_cluster; ++k)
+            if (p->r_cluster[k] < 0 || p->r_cluster[k] >= N) FAIL(MCS_EINVAL, "rOrbCluster index out of range");
+        if (z > 0 && p->r_link)
+            for (long long k = 0; k < (long long)p->n_rorb * z; ++k)
+                if (p->r_link[k] < -1 || p->r_link[k] >= N) FAIL(MCS_EINVAL, "linkedOrb_rnorm index out of range");
+        for (int k = 0; k < 3 * p->n_circuits; ++k)
+            if (p->circuits[k] < 0 || p->circuits[k] >= N) FAIL(MCS_EINVAL, "circuit index out of range");
+        for (long long k = 0; k < (long long)p->n_group * p->max_group; ++k)
+            if (p->group_list[k] >= N) FAIL(MCS_EINVAL, "orbital-group index out of range");
     }
-    for (int k = 0; k < 2 * p->n_lat; ++k)
-        if (p->corr_pair[k] < 0 || p->corr_pair[k] >= N) FAIL(MCS_EINVAL, "corrOrbPair index out of range");
-    for (int k = 0; k < p->n_rorb; ++k)
-        if (p->r_orb[k] < 0 || p->r_orb[k] >= N) FAIL(MCS_EINVAL, "rOrb index out of range");
-    for (long long k = 0; k < (long long)p->n_rorb * p->n_in_cluster; ++k)
-        if (p->r_cluster[k] < 0 || p->r_cluster[k] >= N) FAIL(MCS_EINVAL, "rOrbCluster index out of range");
-    if (z > 0 && p->r_link)
-        for (long long k = 0; k < (long long)p->n_rorb * z; ++k)
-            if (p->r_link[k] < -1 || p->r_link[k] >= N) FAIL(MCS_EINVAL, "linkedOrb_rnorm index out of range");
-    for (int k = 0; k < 3 * p->n_circuits; ++k)
-        if (p->circuits[k] < 0 || p->circuits[k] >= N) FAIL(MCS_EINVAL, "circuit index out of range");
-    for (long long k = 0; k < (long long)p->n_group * p->max_group; ++k)
-        if (p->group_list[k] >= N) FAIL(MCS_EINVAL, "orbital-group index out of range");
 
     // ---------------------------------------------------------------- coupling classes
     // O(n): exchange-matrix classes over all links (exact equality).
@@ -220,6 +294,32 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
         if (qv.empty()) qv.push_back(0.0);
         m->nclass = (int)qv.size();
         for (int c = 0; c < m->nclass; ++c) m->Q[c] = qv[c];
+    }
+
+    // ---------------------------------------------------------------- template
+    // same lattice as the template, with the same partition of the links into
+    // coupling classes and of the sites into anisotropy classes: the geometry,
+    // colouring and measurement lists are the template's; the class values,
+    // the program and the initial state are this problem's
+    if (like && linkcls == like->hm.linkcls) {
+        std::vector<uint8_t> st;
+        std::vector<float> dtab;
+        int ndc = 0, has_d = 0;
+        int rc = onsite_classes(p, dim, N, like->hm.sites, &st, &dtab, &ndc, &has_d, err);
+        if (rc != MCS_OK) return rc;
+        if (st == like->hm.stype) {
+            std::vector<float> jt = std::move(m->jtab);
+            std::vector<double> jt64 = std::move(m->jtab64);
+            const int njc = m->njc, fullJ = m->fullJ;
+            const double h = m->h, flunc = m->flunc;
+            const unsigned long long seed = m->seed;
+            *m = like->hm;
+            m->jtab = std::move(jt); m->jtab64 = std::move(jt64); m->njc = njc; m->fullJ = fullJ;
+            m->dtab = std::move(dtab); m->ndc = ndc; m->has_d = has_d;
+            m->h = h; m->flunc = flunc; m->seed = seed;
+            if (reused) *reused = true;
+            return compile_program_state(p, o, m, dim, err);
+        }
     }
 
     // ---------------------------------------------------------------- geometry
@@ -324,26 +424,8 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
     // ---------------------------------------------------------------- site classes
     if (dim > 1) {
         // site classes: anisotropy vector and spin length |S|
-        ClassTable<4> dcls;
-        m->stype.assign(N, 0);
-        bool anyd = false;
-        for (int k = 0; k < N; ++k) {
-            int i = sites[k];
-            double v[4] = {p->init_d[3 * (size_t)i], p->init_d[3 * (size_t)i + 1], p->init_d[3 * (size_t)i + 2],
-                           fabs(p->init_spin[i])};
-            if (dim == 2) v[2] = 0.0;
-            anyd |= v[0] != 0.0 || v[1] != 0.0 || v[2] != 0.0;
-            int c = dcls.find_or_add(v);
-            if (c > 255) FAIL(MCS_EUNSUPPORTED, "more than 256 distinct (anisotropy, spin length) site classes");
-            m->stype[k] = (uint8_t)c;
-        }
-        std::vector<std::vector<double>> dt;
-        for (auto &k : dcls.keys) dt.push_back(std::vector<double>(k.begin(), k.end()));
-        m->ndc = (int)dt.size();
-        m->has_d = anyd ? 1 : 0;
-        m->dtab.resize(4 * dt.size());
-        for (size_t c = 0; c < dt.size(); ++c)
-            for (int k = 0; k < 4; ++k) m->dtab[4 * c + k] = (float)dt[c][k];
+        int rc = onsite_classes(p, dim, N, sites, &m->stype, &m->dtab, &m->ndc, &m->has_d, err);
+        if (rc != MCS_OK) return rc;
     } else {
         ClassTable<1 + MCS_MAXC> tcls;
         std::vector<std::vector<int>> tcount;
@@ -632,6 +714,16 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
         }
     }
 
+    if (dim > 1) m->linkcls = std::move(linkcls);
+    return compile_program_state(p, o, m, dim, err);
+}
+
+// The sweep program (units, measurement interval, frames) and the initial
+// state of a compiled model (sweep order m->sites / m->pos).
+static int compile_program_state(const mcs_problem *p, const mcs_options *o, HostModel *m, int dim, std::string *err)
+{
+    const int N = p->n_sites;
+    const std::vector<int> &pos = m->pos, &sites = m->sites;
     // ---------------------------------------------------------------- program
     if (p->algorithm == 0) {
         m->upm = (int)std::min<long long>((p->ninterval + N - 1) / N, 1 << 30);

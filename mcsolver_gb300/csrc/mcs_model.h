@@ -3,6 +3,7 @@
 #pragma once
 #include <stdint.h>
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -72,10 +73,37 @@ struct HostModel {
     std::vector<float> init_vec;         // O(n) [dim][N]
     int device_random_init = 0;          // draw the initial state on the device
     unsigned long long seed = 0;
+    // coupling class of every link [N][zmax] (original site order), kept so
+    // that a later replica of the same lattice can be checked against it
+    std::vector<int> linkcls;
 };
 
-// Returns MCS_OK or an error code with a message in *err.
-int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std::string *err);
+// The structural inputs of one O(n) problem (everything but the coupling and
+// anisotropy values, the field, the sweep counts and the options), copied, so
+// that a later problem can be recognised as the same lattice.
+struct StructInputs {
+    int model = 0, alg = 0, N = 0, z = 0;
+    int n_circuits = 0, n_lat = 0, n_group = 0, max_group = 0, n_rorb = 0, n_in_cluster = 0, ignore_offdiag = 0;
+    bool has_rlink = false;
+    std::vector<int32_t> nlink, linked_orb, circuits, corr_pair, group_list, r_orb, r_cluster, r_link;
+    std::vector<double> init_spin;
+};
+// A compiled model together with its structural inputs: the template from
+// which problems of the same lattice are compiled without redoing the
+// geometry, colouring and measurement lists.
+struct ModelTemplate {
+    HostModel hm;
+    StructInputs in;
+};
+std::shared_ptr<const ModelTemplate> make_template(const mcs_problem *p, const HostModel &m);
+
+// Returns MCS_OK or an error code with a message in *err.  With a template of
+// the same lattice (bitwise equal structural inputs, the same partition of the
+// links into coupling classes and of the sites into anisotropy classes) the
+// structure is taken from the template and only the values, the program and
+// the initial state are compiled; *reused tells which path ran.
+int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std::string *err,
+                  const ModelTemplate *tmpl = nullptr, bool *reused = nullptr);
 
 // Philox4x32-10 on the host (the device's generator, for initial states).
 void philox_host(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, unsigned long long seed, uint32_t out[4]);

@@ -187,3 +187,30 @@ def test_dropin_module_matches_c_abi(engine):
     args = C.square_args("heisenberg", 8, 0.5, nthermal=5, nsweep=5)
     out = mod.MCMainFunction(*args, lambda k: None)
     assert len(out) == 29 and isinstance(out[28], tuple)
+
+
+def test_batch_of_one_lattice_equals_individual_solves(engine):
+    """A batch compiles later O(n) replicas of a lattice it already holds from
+    that replica's template (structure reused, values recompiled).  Replicas
+    that differ in couplings, anisotropy, field, initial tilt, seed and
+    initial-state option must give what each gives alone on the same
+    schedule: the same trajectory, so the same results to FP summation order."""
+    cases = []
+    for k, T in enumerate((0.6, 0.9, 1.3)):
+        a = list(C.square_args("xy", 24, T, D=[0.1 * k, -0.05, 0], h=0.1 * k, nthermal=6, nsweep=10))
+        a[15] = 0.2 * k  # flunc
+        cases.append(("xy", tuple(a), 60 + k, k == 2))
+    for k, T in enumerate((0.4, 0.8)):
+        cases.append(("heisenberg", C.square_args("heisenberg", 16, T, h=0.2 * k, dmi=0.4, nthermal=6, nsweep=10),
+                      70 + k, False))
+    cases.append(("heisenberg", C.honeycomb_args("heisenberg", 6, 9.0, nthermal=6, nsweep=10), 80, False))
+    cases.append(("heisenberg", C.honeycomb_args("heisenberg", 6, 5.0, h=0.3, nthermal=6, nsweep=10), 81, True))
+    b = engine.Batch()
+    for m, a, seed, rnd in cases:
+        b.add(m, a, seed=seed, random_init=rnd, schedule="resident")
+    b.run()
+    for i, (m, a, seed, rnd) in enumerate(cases):
+        got, _ = b.result(i)
+        alone, _ = engine.solve(m, a, seed=seed, random_init=rnd, schedule="resident")
+        np.testing.assert_allclose(np.array(got[:27]), np.array(alone[:27]), rtol=1e-6, atol=1e-7)
+    b.close()
