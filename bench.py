@@ -184,14 +184,15 @@ def run_ours(args):
         sched[0][0], "k_resident_metro<2,SQUARE>")
     alg_bytes = 16.0 * per_step_updates
     achieved = alg_bytes / (ms_per_step / 1000.0) / 1e9
-    traffic = None
+    traffic = issue = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.isfile(tpath):
         try:
             tj = json.load(open(tpath))
             traffic = tj.get("dram_bytes_per_step")
+            issue = tj.get("sm_issue_active")
         except Exception:
-            traffic = None
+            traffic = issue = None
     # e2e through the C ABI from host buffers
     # the step's inputs are host arrays in the reference's flattened layout
     e2e_args = workload_args(nsweep=S)
@@ -241,8 +242,10 @@ def run_ours(args):
                         "pinned staging), run, read every result back"},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "kernel": kname,
-                     "note": "lattice is shared-memory resident inside a launch; HBM is touched once per launch"},
+                     "traffic": traffic, "kernel": kname, "sm_issue_active": issue,
+                     "note": "lattice is shared-memory resident inside a launch; HBM is touched once per launch, "
+                             "so the bound is SM issue (sm_issue_active: ncu issue-slot utilisation of the same "
+                             "kernel, profiles/k_cluster_metro_xy_L128x32.md)"},
         "cpu_baseline": cpu,
         "plain_engine": plain,
         "clocks": clocks,
