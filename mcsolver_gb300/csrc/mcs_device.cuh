@@ -269,6 +269,22 @@ __device__ __forceinline__ bool on_trial(const RR &R, const float *__restrict__ 
 }
 
 // ------------------------------------------------------------------ reductions
+// Second stage of the block sums: red[w*K + k] holds warp w's partial of value
+// k (nw <= 32 warps).  Warp k sums value k over the warps by an FP64 shuffle
+// tree (five dependent adds instead of nw: the device issues FP64 slowly, and
+// a block of 1024 threads has 32 partials).  Result in out[0..K-1] for all
+// threads after the call.
+__device__ __forceinline__ void block_sum_warps(const double *red, double *out, int K, int nw)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwb = (blockDim.x + 31) >> 5;
+    for (int k = wid; k < K; k += nwb) {
+        double a = lane < nw ? red[lane * K + k] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) out[k] = a;
+    }
+    __syncthreads();
+}
 // Sum K doubles over the block in a fixed order.  red: shared [32*K] doubles.
 // Result valid in out[0..K-1] (shared) after the call for all threads.
 template <int K>
@@ -283,12 +299,7 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double *red, double *o
         if (lane == 0) red[wid * K + k] = x;
     }
     __syncthreads();
-    if (threadIdx.x < K) {
-        double a = 0.0;
-        for (int w = 0; w < nw; ++w) a += red[w * K + threadIdx.x];
-        out[threadIdx.x] = a;
-    }
-    __syncthreads();
+    block_sum_warps(red, out, K, nw);
 }
 // FP32 inside a warp (32 per-thread partials), FP64 across the warps: the
 // device's FP64 rate is a small fraction of its FP32 rate, so per-lane FP64
@@ -324,12 +335,7 @@ __device__ __forceinline__ void block_sum_f(float (&v)[K], double *red, double *
     const int idx = lane & (P - 1);
     if (lane < P && idx < K) red[wid * K + idx] = (double)y;
     __syncthreads();
-    if (threadIdx.x < K) {
-        double a = 0.0;
-        for (int w = 0; w < nw; ++w) a += red[w * K + threadIdx.x];
-        out[threadIdx.x] = a;
-    }
-    __syncthreads();
+    block_sum_warps(red, out, K, nw);
 }
 template <int K>
 __device__ __forceinline__ void block_sum_ll(long long (&v)[K], long long *red, long long *out)
