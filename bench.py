@@ -41,6 +41,13 @@ STEP_SWEEPS = 50
 WORKLOAD = "xy_square_L128_32T_metropolis"
 
 
+def base_config(sweeps):
+    """The workload both arms of the benchmark report."""
+    return {"workload": WORKLOAD, "model": "XY", "L": L, "n_temperatures": NTEMP, "T_range_K": [0.5, 1.5],
+            "algorithm": "Metropolis", "sweeps_per_step": sweeps, "measurement": "every sweep (tau=N)",
+            "replicas": NTEMP}
+
+
 def workload_args(nsweep, nthermal=0):
     from mcsolver_gb300.lattice import rescale_args, square_args
     base = square_args("xy", L, 1.0, nthermal=nthermal, nsweep=nsweep, tau=0, groups=((0,),))
@@ -232,11 +239,9 @@ def run_ours(args):
         "metric": "site_updates_per_s", "value": value, "unit": "site_updates/s", "n_gpus": 1, "steps": K,
         "warmup": W, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 update / f64 accumulate", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "model": "XY", "L": L, "n_temperatures": NTEMP, "T_range_K": [0.5, 1.5],
-                   "algorithm": "Metropolis", "sweeps_per_step": S, "measurement": "every sweep (tau=N)",
-                   "replicas": NTEMP, "l2": "flushed between steps (256 MB write)",
-                   "schedule": [{"schedule": g[0], "ctas_per_replica": g[1], "threads": g[2], "replicas": g[3]}
-                                for g in sched]},
+        "config": dict(base_config(S), l2="flushed between steps (256 MB write)",
+                       schedule=[{"schedule": g[0], "ctas_per_replica": g[1], "threads": g[2], "replicas": g[3]}
+                                 for g in sched]),
         "e2e": {"value": e2e_value, "unit": "site_updates/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "C ABI mcs_batch_* from host arrays: create, compile+upload 32 replicas (16 host threads, "
                         "pinned staging), run, read every result back"},
@@ -265,8 +270,7 @@ def run_reference(args):
     v = statistics.median(vals)
     line = {"impl": "reference", "metric": "site_updates_per_s", "value": v, "unit": "site_updates/s", "n_gpus": 1,
             "steps": K, "warmup": W, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic", "config": {"workload": WORKLOAD, "model": "XY", "L": L,
-                                                             "n_temperatures": NTEMP, "algorithm": "Metropolis"},
+            "dtype": "f64", "data": "synthetic", "config": base_config(args.sweeps),
             "cpu_baseline": {"value": v, "unit": "site_updates/s", "cores": info["cores"], "kind": info["kind"],
                              "sample": info["sample"]},
             "e2e": {"value": v, "unit": "site_updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -570,8 +574,7 @@ def multi_line(work_total: float, tmax: float, n: int, K: int, W: int, S: int, l
             "n_gpus": n, "steps": K, "warmup": W, "ms_per_step": tmax * 1000 / K,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 update / f64 accumulate", "data": "synthetic", "gpu_launches": launches,
-            "config": {"workload": WORKLOAD, "model": "XY", "L": L, "n_temperatures": NTEMP,
-                       "sweeps_per_step": S, "parallelism": "replicas only (%d independent copies)" % n}}
+            "config": dict(base_config(S), parallelism="replicas only (%d independent copies)" % n)}
 
 
 def run_multi(args):
