@@ -485,6 +485,59 @@ def run_whole_solves(args):
                       "batched_over_plain": rate / (ps / pt) if pt > 0 else None}))
 
 
+def run_noalloc(args):
+    """The allocation-free entry point mcs_ising_square_noalloc on caller-held
+    device buffers: square Ising ferromagnet (K = -1/T, T = 2.3), L x L int8
+    spins from a seeded random start, `--sweeps` sweeps per step (two colour
+    launches and one sums launch per sweep).  Device time with CUDA events on
+    the stream the entry point is given.  Algorithmic bytes: the int8 spin read
+    and written once per site update (2 B); at L = 2048 (4 MB) the lattice
+    lives in L2."""
+    import ctypes
+
+    import torch
+
+    import mcsolver_gb300 as eng
+    from mcsolver_gb300 import build as b
+    b.build()
+    Ln, S, K, W = args.noalloc_L, args.sweeps, args.steps, args.warmup
+    g = torch.Generator(device="cuda").manual_seed(5)
+    sigma = (torch.randint(0, 2, (Ln * Ln,), generator=g, device="cuda", dtype=torch.int8) * 2 - 1).contiguous()
+    sums = torch.zeros(2 * S, dtype=torch.int64, device="cuda")
+    fn = eng.lib().mcs_ising_square_noalloc
+    st = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(st.cuda_stream)
+    T = 2.3
+    sweep = 0
+    for _ in range(W):
+        assert fn(ctypes.c_void_p(sigma.data_ptr()), Ln, Ln, -1.0 / T, 0.0, 7, sweep, S,
+                  ctypes.c_void_p(sums.data_ptr()), sp) == 0, eng.lib().mcs_last_error()
+        sweep += S
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(K):
+        fn(ctypes.c_void_p(sigma.data_ptr()), Ln, Ln, -1.0 / T, 0.0, 7, sweep, S, ctypes.c_void_p(sums.data_ptr()), sp)
+        sweep += S
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / K
+    upd = Ln * Ln * S
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    gbs = 2.0 * upd / (ms / 1000.0) / 1e9
+    m = sums.cpu().numpy().reshape(-1, 2)[-1]
+    print(json.dumps({"workload": "ising_square_noalloc_L%d" % Ln, "sweeps_per_step": S, "steps": K,
+                      "ms_per_step": ms, "site_updates_per_s": upd / (ms / 1000.0),
+                      "launches_per_step": 3 * S, "last_sums": [int(m[0]), int(m[1])],
+                      "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                                   "note": "2 B per site update; the %d MB lattice stays in L2" % (Ln * Ln >> 20)}}))
+
+
 def run_pt(args):
     """Parallel tempering: honeycomb Heisenberg (2 sites/cell), 1NN Kitaev-type
     J = diag(-1.5,-1.5,-1.8) with Jxy = Jyx = 0.3, 2NN -0.3, Az = -0.5, 64x64
@@ -524,7 +577,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--workload", default="headline", choices=["headline", "served", "batched4", "pt", "ising", "xy_wolff"])
+    ap.add_argument("--workload", default="headline", choices=["headline", "served", "batched4", "pt", "ising", "xy_wolff",
+                                                                  "noalloc"])
     ap.add_argument("--requests", type=int, default=48)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--nthermal", type=int, default=1000)
@@ -533,6 +587,7 @@ def main():
                     help="ising / xy_wolff: use --nthermal / --nsweep instead of the workload's own counts")
     ap.add_argument("--plain-sample", type=int, default=6)
     ap.add_argument("--pt-sweeps", type=int, default=50000)
+    ap.add_argument("--noalloc-L", type=int, default=2048, help="noalloc workload: lattice side")
     args = ap.parse_args()
     if args.workload == "served":
         return run_served(args)
@@ -542,6 +597,8 @@ def main():
         return run_pt(args)
     if args.workload in ("ising", "xy_wolff"):
         return run_whole_solves(args)
+    if args.workload == "noalloc":
+        return run_noalloc(args)
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         if rank == 0:

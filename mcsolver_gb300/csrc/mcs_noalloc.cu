@@ -67,7 +67,9 @@ __global__ void __launch_bounds__(NA_THREADS) k_na_colour(signed char *s, int Lx
 }
 
 // sum of sigma and of sigma_i*sigma_j over the bonds (each bond once); the
-// last block to finish adds the partials in block order and writes out[0..1]
+// last block to finish adds the partials (all its threads, then a block sum:
+// the sums are integers, so the order does not change them) and writes
+// out[0..1]
 __global__ void __launch_bounds__(NA_THREADS) k_na_sums(const signed char *s, int Lx, int Ly, long long *scratch,
                                                          long long *out)
 {
@@ -91,16 +93,19 @@ __global__ void __launch_bounds__(NA_THREADS) k_na_sums(const signed char *s, in
         last = atomicAdd(counter, 1u) == gridDim.x - 1;
     }
     __syncthreads();
-    if (last && threadIdx.x == 0) {
+    if (last) {  // the same for every thread of the block
         __threadfence();
-        long long m = 0, b = 0;
-        for (unsigned g = 0; g < gridDim.x; ++g) {
-            m += ((volatile long long *)scratch)[2 * g];
-            b += ((volatile long long *)scratch)[2 * g + 1];
+        long long p[2] = {0, 0};
+        for (unsigned g = threadIdx.x; g < gridDim.x; g += NA_THREADS) {
+            p[0] += ((volatile long long *)scratch)[2 * g];
+            p[1] += ((volatile long long *)scratch)[2 * g + 1];
         }
-        out[0] = m;
-        out[1] = b;
-        *counter = 0u;  // ready for the next sweep
+        block_sum_ll<2>(p, red, red + 64);
+        if (threadIdx.x == 0) {
+            out[0] = red[64];
+            out[1] = red[65];
+            *counter = 0u;  // ready for the next sweep
+        }
     }
 }
 
@@ -166,7 +171,8 @@ extern "C" int mcs_ising_square_noalloc(int8_t *d_sigma, int32_t Lx, int32_t Ly,
     const int N = Lx * Ly;
     const int nq = (N / 2 + 3) / 4;
     const int gsweep = (nq + NA_THREADS - 1) / NA_THREADS;
-    const int gsum = std::min(NA_MAX_BLOCKS, (N + NA_THREADS - 1) / NA_THREADS);
+    // about 16 sites per thread: fewer partials for the last block to add
+    const int gsum = std::min(NA_MAX_BLOCKS, std::max(1, (N + 16 * NA_THREADS - 1) / (16 * NA_THREADS)));
     // the completion counter must start at zero (a previous call may have been interrupted)
     cudaError_t e = cudaMemsetAsync(scratch + 2 * NA_MAX_BLOCKS, 0, sizeof(unsigned int), st);
     for (int k = 0; k < nsweeps && e == cudaSuccess; ++k) {
