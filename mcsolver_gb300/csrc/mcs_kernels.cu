@@ -538,10 +538,18 @@ __global__ void __launch_bounds__(256) k_tiled_finalize(Rep *reps, const int *id
     if (meas) {
         const int m0 = mitem_off[blockIdx.x], m1 = mitem_off[blockIdx.x + 1];
         const int nf = DIM == 1 ? 4 + MCS_MAXT + MCS_MAXC : F_NON;
-        for (int k = tid; k < nf; k += blockDim.x) {
-            double a = 0.0;
-            for (int i = m0; i < m1; ++i) a += fpart[(size_t)i * F_NON + k];
-            F[k] = a;
+        // the measurement tiles' partials: one warp per frame value, lanes
+        // over the tiles, then an FP64 shuffle tree (a replica of a large
+        // lattice has a hundred tiles or more)
+        {
+            const int lane = tid & 31, wid = tid >> 5, nwb = blockDim.x >> 5;
+            for (int k = wid; k < nf; k += nwb) {
+                double a = 0.0;
+                for (int i = m0 + lane; i < m1; i += 32) a += fpart[(size_t)i * F_NON + k];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+                if (lane == 0) F[k] = a;
+            }
         }
         __syncthreads();
         const long long m = R.m;
