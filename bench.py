@@ -29,6 +29,7 @@ import platform
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -63,7 +64,7 @@ class ClockSampler:
     def __init__(self, device=0):
         self.device = device
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+        self.path = os.path.join(tempfile.gettempdir(), "mcsgpu_bench_clocks_%d.csv" % os.getpid())
 
     def __enter__(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)
