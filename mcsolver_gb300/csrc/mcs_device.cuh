@@ -855,6 +855,27 @@ __device__ __forceinline__ int is_majority_sign(const Rep &R, const signed char 
 
 // Majority sign from a block's sign sum; a tie takes the Philox word of the
 // evaluating site and slot (the same decision as is_majority_sign).
+// Majority sign of a block with spin sum avg; a tie (avg = 0) is broken by
+// word slot & 3 of the Philox block (j, m, 0x3000 + slot >> 2), drawn only
+// then: word * 2^-32 > 0.5 exactly when word > 2^31.  The same words and
+// decisions as is_majority_from_sum with w drawn up front.
+__device__ __forceinline__ int is_majority_lazy(int avg, uint32_t j, long long m, int slot, unsigned long long seed)
+{
+    if (avg > 0) return 1;
+    if (avg < 0) return -1;
+    const uint4 w = philox_t(j, m, 0x3000u + (uint32_t)(slot >> 2), seed);
+    const uint32_t word = (slot & 3) == 0 ? w.x : (slot & 3) == 1 ? w.y : (slot & 3) == 2 ? w.z : w.w;
+    return word > 0x80000000u ? 1 : -1;
+}
+// Spin sum of the block of site v (0 when v is not a chosen site).
+__device__ __forceinline__ int is_block_sum(const Rep &R, const signed char *s, int v)
+{
+    int avg = 0;
+    const int r = R.rindex[v];
+    if (r >= 0)
+        for (int k = 0; k < R.ncl; ++k) avg += s[__ldg(&R.rcl[(size_t)r * R.ncl + k])];
+    return avg;
+}
 __device__ __forceinline__ int is_majority_from_sum(int avg, const uint4 &w, int slot)
 {
     if (avg > 0) return 1;
@@ -906,19 +927,17 @@ __device__ void is_frame(const Rep &R, const IsEntry *itab, const signed char *s
             c[0] += sp; c[1] += sq; c[2] += sp * sq;
         }
         e = min(ve, R.n_rorb);
+        // tie-break words are drawn only for tied blocks (is_majority_lazy)
         if (il && msum) {
             const int z = R.zmax;
             for (int v = vb + tid; v < e; v += bd) {
                 const int j = il->rorb[v];
-                uint4 w = philox_t((uint32_t)j, m, 0x3000u, R.seed);
-                const int mj = is_majority_from_sum(msum[v], w, 0);
+                const int mj = is_majority_lazy(msum[v], (uint32_t)j, m, 0, R.seed);
                 const int d = il->rdeg[v];
                 for (int l = 0; l < d; ++l) {
-                    const int slot = 1 + l;
-                    if ((slot & 3) == 0) w = philox_t((uint32_t)j, m, 0x3000u + (uint32_t)(slot >> 2), R.seed);
                     const int tr = il->tgt[v * z + l];
                     if (tr == -2) continue;
-                    const int mt = is_majority_from_sum(tr >= 0 ? msum[tr] : 0, w, slot);
+                    const int mt = is_majority_lazy(tr >= 0 ? msum[tr] : 0, (uint32_t)j, m, 1 + l, R.seed);
                     const int k = il->kc[v * z + l];
 #pragma unroll
                     for (int q = 0; q < 4; ++q) c[3 + q] += (q == k) ? mj * mt : 0;
@@ -929,20 +948,18 @@ __device__ void is_frame(const Rep &R, const IsEntry *itab, const signed char *s
         }
         for (int v = vb + tid; v < e; v += bd) {
             const int j = __ldg(&R.rorb[v]);
-            uint4 w = philox_t((uint32_t)j, m, 0x3000u, R.seed);
-            const int mj = msum ? is_majority_from_sum(msum[v], w, 0) : is_majority_sign(R, s, j, w, 0);
+            const int mj = is_majority_lazy(msum ? (int)msum[v] : is_block_sum(R, s, j), (uint32_t)j, m, 0, R.seed);
             const int d = R.rdeg[v];
             for (int l = 0; l < d; ++l) {
                 const int slot = 1 + l;
-                if ((slot & 3) == 0) w = philox_t((uint32_t)j, m, 0x3000u + (uint32_t)(slot >> 2), R.seed);
                 const int t = __ldg(&R.rlink[(size_t)v * R.zmax + l]);
                 if (t < 0) continue;
                 int mt;
                 if (msum) {
                     const int tr = __ldg(&R.rtgt[(size_t)v * R.zmax + l]);  // chosen index of t, -1: not chosen
-                    mt = is_majority_from_sum(tr >= 0 ? msum[tr] : 0, w, slot);
+                    mt = is_majority_lazy(tr >= 0 ? msum[tr] : 0, (uint32_t)j, m, slot, R.seed);
                 } else {
-                    mt = is_majority_sign(R, s, t, w, slot);
+                    mt = is_majority_lazy(is_block_sum(R, s, t), (uint32_t)j, m, slot, R.seed);
                 }
                 const int k = R.rkc[(size_t)v * R.zmax + l];
 #pragma unroll
