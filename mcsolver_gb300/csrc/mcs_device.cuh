@@ -892,6 +892,8 @@ struct IsLists {
     const unsigned char *rdeg;
     const int *tgt;
     const unsigned char *kc;
+    const int *cp;   // correlated pairs [2*nlat] (nullptr: read R.cpair)
+    const int *rcl;  // block members [n_rorb*ncl] (nullptr: read R.rcl)
 };
 
 // Ising frame over [vb, ve): pairs, renormalised energy, per-type sign sums,
@@ -907,9 +909,10 @@ __device__ void is_frame(const Rep &R, const IsEntry *itab, const signed char *s
 {
     const int tid = threadIdx.x, bd = blockDim.x;
     if (R.is_fast && msum) {
+        const int *rcl = (il && il->rcl) ? il->rcl : R.rcl;  // shared-memory copy when staged
         for (int r = tid; r < R.n_rorb; r += bd) {
             int a = 0;
-            for (int k = 0; k < R.ncl; ++k) a += s[__ldg(&R.rcl[(size_t)r * R.ncl + k])];
+            for (int k = 0; k < R.ncl; ++k) a += s[rcl[(size_t)r * R.ncl + k]];
             msum[r] = (signed char)a;
         }
         __syncthreads();
@@ -921,8 +924,9 @@ __device__ void is_frame(const Rep &R, const IsEntry *itab, const signed char *s
 #pragma unroll
         for (int k = 0; k < 16; ++k) c[k] = 0;
         int e = min(ve, R.nlat);
+        const int *cp = (il && il->cp) ? il->cp : R.cpair;  // shared-memory copy when staged
         for (int v = vb + tid; v < e; v += bd) {
-            int p = __ldg(&R.cpair[2 * v]), q = __ldg(&R.cpair[2 * v + 1]);
+            int p = cp[2 * v], q = cp[2 * v + 1];
             int sp = s[p], sq = s[q];
             c[0] += sp; c[1] += sq; c[2] += sp * sq;
         }

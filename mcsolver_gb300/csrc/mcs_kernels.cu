@@ -38,6 +38,7 @@ static __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~
 struct SmemLayout {
     size_t spins, tables, stype, majc, red, F, redl, Fi, acc, total;
     size_t il_rorb, il_rdeg, il_tgt, il_kc;  // staged Ising chosen-site lists (0: not staged)
+    size_t il_cp, il_rcl;                    // staged Ising pair and block lists (0: not staged)
 };
 // Shared-memory plan of a resident replica.  The block-spin cache of the
 // renormalised lattice is included only when it fits (flag returned in majc
@@ -73,6 +74,15 @@ __host__ __device__ inline SmemLayout smem_layout(const Rep &R, size_t limit = 2
             L.il_rdeg = off; off += align16((size_t)R.n_rorb);
             L.il_tgt = off; off += align16(nz * 4);
             L.il_kc = off; off += align16(nz);
+        }
+    }
+    // and the correlated pairs and the block members, when they fit as well
+    L.il_cp = L.il_rcl = 0;
+    if (L.il_rorb) {
+        const size_t need = align16((size_t)R.nlat * 2 * 4) + align16((size_t)R.n_rorb * R.ncl * 4);
+        if (off + need <= limit) {
+            L.il_cp = off; off += align16((size_t)R.nlat * 2 * 4);
+            L.il_rcl = off; off += align16((size_t)R.n_rorb * R.ncl * 4);
         }
     }
     L.total = off;
@@ -174,6 +184,14 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
             kc[i] = R.rkc[i];
         }
         il.rorb = rorb; il.rdeg = rdeg; il.tgt = tgt; il.kc = kc;
+        il.cp = nullptr; il.rcl = nullptr;
+        if (L.il_cp) {
+            int *cp = (int *)(smem + L.il_cp);
+            int *rcl = (int *)(smem + L.il_rcl);
+            for (int i = tid; i < 2 * R.nlat; i += bd) cp[i] = R.cpair[i];
+            for (int i = tid; i < R.n_rorb * R.ncl; i += bd) rcl[i] = R.rcl[i];
+            il.cp = cp; il.rcl = rcl;
+        }
     }
     __syncthreads();
     acc_to_smem(R, smem + L.acc);
