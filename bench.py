@@ -235,6 +235,9 @@ def run_ours(args):
                  "sequence (one launch per colour, per measurement and per finalize, no graph)",
                  "batched_over_plain": value / plain_v}
     cpu = cpu_baseline(args.cpu_seconds) if not args.no_cpu else None
+    # the served half of the metric (after the timed region): continuous batching
+    # of a Poisson request stream, p50/p99 latency and the gain over the plain engine
+    served = served_stream(args) if not args.no_served else None
     clocks = clk.summary()
     line = {
         "metric": "site_updates_per_s", "value": value, "unit": "site_updates/s", "n_gpus": 1, "steps": K,
@@ -254,6 +257,7 @@ def run_ours(args):
                              "kernel, profiles/k_cluster_metro_xy_L128x32.md)"},
         "cpu_baseline": cpu,
         "plain_engine": plain,
+        "served": served,
         "clocks": clocks,
         "wall_s_timed": wall,
     }
@@ -285,6 +289,10 @@ def _plain_rate(eng, model, args, seed):
 
 
 def run_served(args):
+    print(json.dumps(served_stream(args)))
+
+
+def served_stream(args):
     """Served stream: Poisson arrivals (mean 200 req/s, seeded) of mixed
     Ising / XY / Heisenberg (DMI, field) square-lattice solves, L log-uniform in
     32..512 (even), random (T, H) in each model's range, nthermal / nsweep as
@@ -374,15 +382,15 @@ def run_served(args):
         pt += s
     lat = np.array(lat)
     Ls = np.array([r[2] for r in reqs])
-    print(json.dumps({"workload": "served_stream", "requests": n, "rate_req_s": args.rate,
-                      "nthermal": args.nthermal, "nsweep": args.nsweep,
-                      "L_range": [int(Ls.min()), int(Ls.max())], "site_updates": int(upd),
-                      "makespan_s": makespan, "last_arrival_s": float(arrivals[-1]),
-                      "solves_per_s": n / makespan, "site_updates_per_s": upd / makespan,
-                      "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
-                      "plain_site_updates_per_s": ps / pt if pt > 0 else None,
-                      "served_over_plain": (upd / makespan) / (ps / pt) if pt > 0 else None,
-                      "plain_sample": [int(Ls[k]) for k in pick]}))
+    return {"workload": "served_stream", "requests": n, "rate_req_s": args.rate,
+            "nthermal": args.nthermal, "nsweep": args.nsweep,
+            "L_range": [int(Ls.min()), int(Ls.max())], "site_updates": int(upd),
+            "makespan_s": makespan, "last_arrival_s": float(arrivals[-1]),
+            "solves_per_s": n / makespan, "site_updates_per_s": upd / makespan,
+            "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+            "plain_site_updates_per_s": ps / pt if pt > 0 else None,
+            "served_over_plain": (upd / makespan) / (ps / pt) if pt > 0 else None,
+            "plain_sample": [int(Ls[k]) for k in pick]}
 
 
 def run_batched4(args):
@@ -578,6 +586,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-served", action="store_true", help="headline: skip the served-stream part of the line")
     ap.add_argument("--workload", default="headline", choices=["headline", "served", "batched4", "pt", "ising", "xy_wolff",
                                                                   "noalloc"])
     ap.add_argument("--requests", type=int, default=48)
