@@ -125,3 +125,61 @@ def test_vectorised_builder_equals_reference_order(model, L):
         assert len(a) == len(b)
         for x, y in zip(a, b):
             np.testing.assert_array_equal(np.asarray(x, float), np.asarray(y, float))
+
+
+def _onsager_energy(T, J=1.0):
+    """Exact internal energy per site of the infinite 2D square Ising model
+    (Onsager 1944): u = -J coth(2K) [1 + (2/pi)(2 tanh^2(2K) - 1) K(k)],
+    k = 2 sinh(2K)/cosh^2(2K), K = J/T."""
+    import math
+
+    from scipy.special import ellipk
+    K = J / T
+    k = 2 * math.sinh(2 * K) / math.cosh(2 * K) ** 2
+    return -J / math.tanh(2 * K) * (1 + 2 / math.pi * (2 * math.tanh(2 * K) ** 2 - 1) * ellipk(k * k))
+
+
+def _ising_energy(spins, args):
+    """Energy per site in beta units of an Ising state, summed over the ELL
+    links (each bond seen from both ends, isingLib.c:121-127) and the field."""
+    s = spins[:, 0]
+    N, z = len(s), args[5]
+    nlink = np.asarray(args[6])
+    J = np.asarray(args[7], float).reshape(N, z)
+    nb = np.asarray(args[8]).reshape(N, z)
+    live = np.arange(z)[None, :] < nlink[:, None]
+    bonds = (J * s[:, None] * s[np.where(live, nb, 0)] * live).sum()
+    return 0.5 * bonds / N - args[10] * s.sum() / N
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["reference_stream", "engine_stream"])
+@pytest.mark.parametrize("T", [1.6, 3.2])
+def test_oracle_metropolis_energy_matches_onsager(oracle_lib, mode, T):
+    """Both oracle streams sample the 2D Ising energy Onsager gives, at L=32
+    away from Tc (finite-size shifts below 1e-4 per site).  The reference's
+    Metropolis <e> is offset by the energy at the start of the measurement
+    (isingLib.c:359), so the run starts from a thermalised state whose energy
+    is computed here and added back; the error bar is the binned one of the
+    per-measurement series."""
+    from mcsolver_gb300 import analysis as A
+    L = 32
+    _, th = oracle_lib.solve("ising", C.square_args("ising", L, T, nthermal=1000, nsweep=1), seed=7, mode=mode)
+    args = C.square_args("ising", L, T, nthermal=0, nsweep=4000)
+    e0 = _ising_energy(th["spins"], args)
+    _, ex = oracle_lib.solve("ising", args, seed=8, mode=mode, spins_in=th["spins"], want_series=True)
+    m, err, _ = A.mean_error((ex["series"][:, 0] + e0) * T)
+    exact = _onsager_energy(T)
+    assert abs(m - exact) < 3.5 * err + 1e-4, (m, exact, err)
+
+
+@pytest.mark.parametrize("T", [1.6, 2.0])
+def test_oracle_wolff_energy_matches_onsager(oracle_lib, T):
+    """The reference's Wolff path recomputes the absolute energy after every
+    accepted cluster (isingLib.c:230-233), so its <e> is compared directly."""
+    from mcsolver_gb300 import analysis as A
+    args = C.square_args("ising", 32, T, nthermal=500, nsweep=4000, tau=1, algo=1)
+    res, ex = oracle_lib.solve("ising", args, seed=9, mode=0, want_series=True)
+    m, err, _ = A.mean_error(ex["series"][:, 0] * T)
+    assert m == pytest.approx(res[4] * T, rel=1e-12)
+    exact = _onsager_energy(T)
+    assert abs(m - exact) < 3.5 * err + 1e-4, (m, exact, err)
