@@ -203,6 +203,7 @@ static PyObject *MCMainFunction(PyObject *self, PyObject *args)
         int G = (p.model == MCS_ISING) ? 0 : (int)ngroup;
         int ng = (G + 1) * (G + 1) + (G + 1);
         gbuf = (double *)calloc((size_t)ng, sizeof(double));
+        if (!gbuf) { PyErr_NoMemory(); goto done; }
         r.group_values = gbuf;
         r.group_capacity = ng;
         if (frames > 0) {
@@ -224,33 +225,57 @@ static PyObject *MCMainFunction(PyObject *self, PyObject *args)
         PyObject *frameobj;
         if (frames > 0) {
             frameobj = PyTuple_New(frames);
+            if (!frameobj) goto done;
             for (long long f = 0; f < frames; ++f) {
                 if (f >= r.frames_written) { Py_INCREF(Py_None); PyTuple_SET_ITEM(frameobj, f, Py_None); continue; }
                 PyObject *fr = PyTuple_New(N);
+                if (!fr) { Py_DECREF(frameobj); goto done; }
+                PyTuple_SET_ITEM(frameobj, f, fr);
                 for (Py_ssize_t i = 0; i < N; ++i) {
                     const float *q = fbuf + ((size_t)f * N + i) * 3;
-                    if (p.model == MCS_ISING) PyTuple_SET_ITEM(fr, i, PyFloat_FromDouble(q[0]));
-                    else PyTuple_SET_ITEM(fr, i, Py_BuildValue("(ddd)", (double)q[0], (double)q[1], (double)q[2]));
+                    PyObject *v = (p.model == MCS_ISING)
+                                      ? PyFloat_FromDouble(q[0])
+                                      : Py_BuildValue("(ddd)", (double)q[0], (double)q[1], (double)q[2]);
+                    if (!v) { Py_DECREF(frameobj); goto done; }
+                    PyTuple_SET_ITEM(fr, i, v);
                 }
-                PyTuple_SET_ITEM(frameobj, f, fr);
             }
         } else {
             frameobj = PyFloat_FromDouble(0.0);
+            if (!frameobj) goto done;
         }
 #if MCS_PYMOD == 1
         ret = PyTuple_New(11);
-        for (int k = 0; k < 10; ++k) PyTuple_SET_ITEM(ret, k, PyFloat_FromDouble(r.values[k]));
+        if (!ret) { Py_DECREF(frameobj); goto done; }
         PyTuple_SET_ITEM(ret, 10, frameobj);
+        for (int k = 0; k < 10; ++k) {
+            PyObject *v = PyFloat_FromDouble(r.values[k]);
+            if (!v) { Py_CLEAR(ret); goto done; }
+            PyTuple_SET_ITEM(ret, k, v);
+        }
 #else
         ret = PyTuple_New(29);
-        for (int k = 0; k < 27; ++k) PyTuple_SET_ITEM(ret, k, PyFloat_FromDouble(r.values[k]));
+        if (!ret) { Py_DECREF(frameobj); goto done; }
         PyTuple_SET_ITEM(ret, 27, frameobj);
+        for (int k = 0; k < 27; ++k) {
+            PyObject *v = PyFloat_FromDouble(r.values[k]);
+            if (!v) { Py_CLEAR(ret); goto done; }
+            PyTuple_SET_ITEM(ret, k, v);
+        }
+        PyObject *gt;
         if (G > 0) {
-            PyObject *gt = PyTuple_New(ng);
-            for (int k = 0; k < ng; ++k) PyTuple_SET_ITEM(gt, k, PyFloat_FromDouble(gbuf[k]));
+            gt = PyTuple_New(ng);
+            if (!gt) { Py_CLEAR(ret); goto done; }
             PyTuple_SET_ITEM(ret, 28, gt);
+            for (int k = 0; k < ng; ++k) {
+                PyObject *v = PyFloat_FromDouble(gbuf[k]);
+                if (!v) { Py_CLEAR(ret); goto done; }
+                PyTuple_SET_ITEM(gt, k, v);
+            }
         } else {
-            PyTuple_SET_ITEM(ret, 28, PyFloat_FromDouble(0.0));
+            gt = PyFloat_FromDouble(0.0);
+            if (!gt) { Py_CLEAR(ret); goto done; }
+            PyTuple_SET_ITEM(ret, 28, gt);
         }
 #endif
     }
