@@ -10,7 +10,7 @@
  *   mcs_solve() with model MCS_ISING      <- MCMainFunction, mcsolver/isingLib.c:259-451
  *                                            (arguments isingLib.c:277-284, result :436-447)
  *   mcs_solve() with model MCS_XY         <- MCMainFunction, mcsolver/xyLib.c:413-809
- *                                            (arguments xyLib.c:439-447, result :782-809)
+ *                                            (arguments xyLib.c:439-447, result :778-807)
  *   mcs_solve() with model MCS_HEISENBERG <- MCMainFunction, mcsolver/heisenbergLib.c:478-885
  *                                            (arguments heisenbergLib.c:504-512, result :853-884)
  *   mcs_batch_*()                         <- the process-pool fan-out over the (T,H) grid,

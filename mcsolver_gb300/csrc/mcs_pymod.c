@@ -6,7 +6,7 @@
  * 3 (heisenberglib).  Each module exports one METH_VARARGS function
  * MCMainFunction with the reference's positional arguments:
  *   isinglib       isingLib.c:277-284      16 arguments, returns the 11-tuple of isingLib.c:436-447
- *   xylib          xyLib.c:439-447         23 arguments, returns the 29-tuple of xyLib.c:781-809
+ *   xylib          xyLib.c:439-447         23 arguments, returns the 29-tuple of xyLib.c:778-807
  *   heisenberglib  heisenbergLib.c:504-512 23 arguments, returns the 29-tuple of heisenbergLib.c:853-884
  * and forwards to mcs_solve() of libmcsgpu.so with the GIL released.
  *

@@ -9,7 +9,7 @@
  * It takes the same flattened arrays that MCMainFunction receives
  * (isingLib.c:277-335, heisenbergLib.c:504-583, xyLib.c:439-513) and returns the
  * same result values (isingLib.c:436-447, heisenbergLib.c:853-884,
- * xyLib.c:782-809).  The update and measurement arithmetic is restated in the
+ * xyLib.c:778-807).  The update and measurement arithmetic is restated in the
  * reference's own evaluation order, in double precision.
  *
  * Two random streams:
