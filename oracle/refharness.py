@@ -147,6 +147,43 @@ def _quiet_stdout():
         os.close(saved)
 
 
+def _run_caller(spec: dict, mod) -> object:
+    """Build the model of ``spec`` with the reference's own Python and run its
+    caller (``mainLoopViaCLib`` mcMain.py:51-135 or ``mainLoopViaCLib_On``
+    mcMain.py:137-272) with ``mod`` standing in for the compiled library (the
+    caller imports it by name, mcMain.py:110-113 / :228-237).  Runs in the
+    current directory, where the caller writes its files.  Returns what the
+    caller returns."""
+    mcMain, Lattice = reference_python()
+    model = spec["model"]
+    on = model != "ising"
+    bonds = [Lattice.Bond(b[0], b[1], np.array([int(x) for x in b[2]]), *b[3], on) for b in spec["bonds"]]
+    name = LIBNAME[model]
+    saved = sys.modules.get(name)
+    sys.modules[name] = mod
+    try:
+        ki = spec.get("ki", ((0, 0), (0, 0, 0)))
+        kw = dict(pos=spec["pos"], S=spec["S"], D=spec["D"], bondList=bonds, T=spec["T"],
+                  Lx=spec["L"][0], Ly=spec["L"][1], Lz=spec["L"][2],
+                  ki_s=ki[0][0], ki_t=ki[0][1], ki_overLat=list(ki[1]),
+                  orbGroupList=spec.get("orbGroups", []), groupInSC=spec.get("groupInSC", True),
+                  h=spec.get("h", 0.0), dipoleAlpha=0, spinFrame=spec.get("spinFrame", 0))
+        if on:
+            kw["On"] = 2 if model == "xy" else 3
+            kw["localCircuitList"] = spec.get("circuits", [])
+        mc = mcMain.MC(0, spec["LMatrix"], **kw)
+        if on:
+            return mc.mainLoopViaCLib_On(nsweep=spec["nsweep"], nthermal=spec["nthermal"],
+                                         ninterval=spec["tau"], algo=spec["algo"], On=kw["On"])
+        return mc.mainLoopViaCLib(nsweep=spec["nsweep"], nthermal=spec["nthermal"],
+                                  ninterval=spec["tau"], algo=spec["algo"])
+    finally:
+        if saved is None:
+            sys.modules.pop(name, None)
+        else:
+            sys.modules[name] = saved
+
+
 def capture_args(spec: dict) -> tuple:
     """Run the reference's model build + marshalling for ``spec`` and return
     the positional argument tuple it passes to MCMainFunction.
@@ -156,50 +193,36 @@ def capture_args(spec: dict) -> tuple:
     L (Lx,Ly,Lz), T, h, nthermal, nsweep, tau, algo ('Metropolis'|'Wolff'),
     ki ((s,t),(ox,oy,oz)), orbGroups, groupInSC, circuits, spinFrame.
     """
-    mcMain, Lattice = reference_python()
-    model = spec["model"]
-    on = model != "ising"
-    bonds = [Lattice.Bond(b[0], b[1], np.array([int(x) for x in b[2]]), *b[3], on) for b in spec["bonds"]]
     captured = {}
 
     def fake(*args):
         captured["args"] = args
         raise _Captured()
 
-    name = LIBNAME[model]
-    fake_mod = types.ModuleType(name)
+    fake_mod = types.ModuleType(LIBNAME[spec["model"]])
     fake_mod.MCMainFunction = fake
-    saved = sys.modules.get(name)
-    sys.modules[name] = fake_mod
-    try:
-        with _in_tmpdir(), _quiet_stdout():
-            ki = spec.get("ki", ((0, 0), (0, 0, 0)))
-            kw = dict(pos=spec["pos"], S=spec["S"], D=spec["D"], bondList=bonds, T=spec["T"],
-                      Lx=spec["L"][0], Ly=spec["L"][1], Lz=spec["L"][2],
-                      ki_s=ki[0][0], ki_t=ki[0][1], ki_overLat=list(ki[1]),
-                      orbGroupList=spec.get("orbGroups", []), groupInSC=spec.get("groupInSC", True),
-                      h=spec.get("h", 0.0), dipoleAlpha=0, spinFrame=spec.get("spinFrame", 0))
-            if on:
-                kw["On"] = 2 if model == "xy" else 3
-                kw["localCircuitList"] = spec.get("circuits", [])
-            mc = mcMain.MC(0, spec["LMatrix"], **kw)
-            try:
-                if on:
-                    mc.mainLoopViaCLib_On(nsweep=spec["nsweep"], nthermal=spec["nthermal"],
-                                          ninterval=spec["tau"], algo=spec["algo"], On=kw["On"])
-                else:
-                    mc.mainLoopViaCLib(nsweep=spec["nsweep"], nthermal=spec["nthermal"],
-                                       ninterval=spec["tau"], algo=spec["algo"])
-            except _Captured:
-                pass
-    finally:
-        if saved is None:
-            sys.modules.pop(name, None)
-        else:
-            sys.modules[name] = saved
+    with _in_tmpdir(), _quiet_stdout():
+        try:
+            _run_caller(spec, fake_mod)
+        except _Captured:
+            pass
     args = captured["args"]
     # drop the trailing callback (never called by the libraries)
     return tuple(args[:-1])
+
+
+def run_caller_with(spec: dict, mod, workdir: str) -> object:
+    """Run the reference's caller for ``spec`` in ``workdir`` with ``mod``
+    (a module exposing MCMainFunction, e.g. a drop-in) in place of the
+    compiled library; returns the caller's return value.  The caller's files
+    (``out``, spin frames, ``spinDotSpin.txt``) are left in ``workdir``."""
+    old = os.getcwd()
+    os.chdir(workdir)
+    try:
+        with _quiet_stdout():
+            return _run_caller(spec, mod)
+    finally:
+        os.chdir(old)
 
 
 class _Captured(Exception):

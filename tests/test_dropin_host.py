@@ -161,3 +161,47 @@ def test_ising_validation_before_the_engine(dropin, k, bad, msg):
     args[k] = bad
     with pytest.raises(ValueError, match=msg):
         mods["isinglib"].MCMainFunction(*args, None)
+
+
+def _reference_present():
+    from oracle import refharness as rh
+    return rh.reference_tree_present()
+
+
+@pytest.mark.skipif(not _reference_present(), reason="reference tree absent")
+@pytest.mark.parametrize("model", ["ising", "xy", "heisenberg"])
+def test_reference_caller_runs_unchanged_on_the_dropin(dropin, tmp_path, model):
+    """mcsolver's own caller (mainLoopViaCLib, mcMain.py:51-135;
+    mainLoopViaCLib_On, mcMain.py:137-272), unmodified, calls the drop-in
+    module in place of its compiled library: it marshals its arguments,
+    unpacks the result tuple, rescales the energies by T, writes ``out``,
+    the spin-frame files and ``spinDotSpin.txt``."""
+    from oracle import refharness as rh
+    mods, fake = dropin
+    fake.fake_set(0, -1)
+    J = C.J9(-1.0, -1.0, -1.0) if model != "ising" else C.J9(-1.0)
+    T = 0.8
+    spec = dict(model=model, LMatrix=[[1, 0, 0], [0, 1, 0], [0, 0, 1]], pos=[[0, 0, 0]], S=[1.0], D=[[0, 0, 0]],
+                bonds=[(0, 0, (1, 0, 0), J), (0, 0, (0, 1, 0), J)], L=(4, 4, 1), T=T, h=0.1,
+                nthermal=2, nsweep=3, tau=0, algo="Metropolis", spinFrame=2, orbGroups=[[0]])
+    if model != "ising":
+        spec["circuits"] = [[[0, (0, 0, 0)], [0, (1, 0, 0)], [0, (0, 1, 0)]]]
+    name = {"ising": "isinglib", "xy": "xylib", "heisenberg": "heisenberglib"}[model]
+    ret = rh.run_caller_with(spec, mods[name], str(tmp_path))
+    p = fake.fake_last().contents
+    assert (p.n_sites, p.nthermal, p.nsweep, p.spin_frames) == (16, 2, 3, 2)
+    out = (tmp_path / "out").read_text().split()
+    if model == "ising":
+        # T h <|s_i|> <|s_j|> spin_tot <s_i s_j> E E2 E_r E2_r U4 (mcMain.py:128-130)
+        assert float(out[0]) == pytest.approx(T) and float(out[2]) == pytest.approx(0.5)
+        assert float(out[6]) == pytest.approx(4.5 * T, abs=1e-3)
+        assert ret[4] == pytest.approx(4.5 * T)
+        frames = sorted(tmp_path.glob("IsingSpinDistribution.*.txt"))
+    else:
+        vals = dict(zip(out[0::2], out[1::2]))
+        assert float(vals["<E>="]) == pytest.approx(8.5 * T) and float(vals["<Q>="]) == pytest.approx(26.5)
+        frames = sorted(tmp_path.glob("OnSpinDistribution.*.txt"))
+        assert (tmp_path / "spinDotSpin.txt").is_file()
+    assert len(frames) == 2
+    rows = frames[1].read_text().splitlines()[1:]
+    assert len(rows) == 16 and float(rows[3].split()[3]) == pytest.approx(103.0)

@@ -97,7 +97,12 @@ def test_oracle_engine_stream_agrees_with_reference(oracle_lib, name):
         assert z < 3.5, (k, a.mean(), b.mean(), z)
 
 
-@pytest.mark.skipif(not os.path.isfile("/root/reference/mcsolver/mcMain.py"), reason="reference tree absent")
+def _reference_present():
+    from oracle import refharness as rh
+    return rh.reference_tree_present()
+
+
+@pytest.mark.skipif(not _reference_present(), reason="reference tree absent")
 def test_reference_crashes_are_documented_cases():
     """Odd lattice sides give -1 renormalised links (the reference would read
     lattice[-1]); the oracle skips them."""
