@@ -36,17 +36,19 @@ def test_dropin_modules_import_and_export_mcmainfunction(engine):
 
 
 @pytest.mark.parametrize("mutate,msg", [
-    (lambda a: a[:1] + ((),) + a[2:], "empty"),
-    (lambda a: a[:8] + (tuple([10 ** 6] + list(a[8][1:])),) + a[9:], "out of range"),
-    (lambda a: a[:9] + ((),) + a[10:], "pair"),
+    (lambda a: a[:1] + ((),) + a[2:], "empty lattice"),
+    (lambda a: a[:8] + (tuple([10 ** 6] + list(a[8][1:])),) + a[9:], "linkedOrb index out of range"),
+    (lambda a: a[:9] + ((),) + a[10:], "at least one pair"),
     (lambda a: a[:4] + (0,) + a[5:], "ninterval"),
 ])
 def test_malformed_input_is_rejected_without_gpu(engine, mutate, msg):
+    """mcs_solve validates the whole problem before any device call: the
+    error is MCS_EINVAL with its message, not a CUDA error."""
     args = C.square_args("ising", 8, 2.0)
     bad = mutate(args)
-    with pytest.raises(Exception) as ei:
+    with pytest.raises(engine.EngineError) as ei:
         engine.solve("ising", bad)
-    assert msg.split()[0] in str(ei.value).lower() or "mcsgpu error" in str(ei.value)
+    assert ei.value.code == 1 and msg in str(ei.value), str(ei.value)
 
 
 def test_dropin_rejects_wrong_arity(engine):
