@@ -127,6 +127,10 @@ std::shared_ptr<const ModelTemplate> make_template(const mcs_problem *p, const H
 {
     auto t = std::make_shared<ModelTemplate>();
     t->hm = m;
+    t->linkcls = std::move(t->hm.linkcls);
+    std::vector<int>().swap(t->hm.linkcls);
+    std::vector<float>().swap(t->hm.init_vec);
+    std::vector<int8_t>().swap(t->hm.init_sigma);
     StructInputs &in = t->in;
     in.model = p->model; in.alg = p->algorithm; in.N = p->n_sites; in.z = p->max_links;
     in.n_circuits = p->n_circuits; in.n_lat = p->n_lat; in.n_group = p->n_group; in.max_group = p->max_group;
@@ -301,7 +305,7 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
     // coupling classes and of the sites into anisotropy classes: the geometry,
     // colouring and measurement lists are the template's; the class values,
     // the program and the initial state are this problem's
-    if (like && linkcls == like->hm.linkcls) {
+    if (like && linkcls == like->linkcls) {
         std::vector<uint8_t> st;
         std::vector<float> dtab;
         int ndc = 0, has_d = 0;

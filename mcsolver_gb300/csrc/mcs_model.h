@@ -90,10 +90,14 @@ struct StructInputs {
 };
 // A compiled model together with its structural inputs: the template from
 // which problems of the same lattice are compiled without redoing the
-// geometry, colouring and measurement lists.
+// geometry, colouring and measurement lists.  The model is stored without
+// what every problem recomputes (initial state) and without its link classes,
+// which are kept beside it: a problem compiled from the template copies only
+// the structure.
 struct ModelTemplate {
     HostModel hm;
     StructInputs in;
+    std::vector<int> linkcls;   // coupling class of every link, as HostModel::linkcls
 };
 std::shared_ptr<const ModelTemplate> make_template(const mcs_problem *p, const HostModel &m);
 
