@@ -337,11 +337,12 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
             if (Lx < 4 || (Lx & 1)) continue;
             bool okg = true;
             int code0[4] = {-1, -1, -1, -1};
-            for (int i = 0; i < N && okg; ++i) {
+            // site i = x*Ly + y, with (x, y) stepped along i
+            for (int i = 0, x = 0, y = 0; i < N && okg; ++i, y = (y + 1 == Ly) ? (++x, 0) : y + 1) {
                 if (p->nlink[i] != 4) { okg = false; break; }
-                int x = i / Ly, y = i % Ly;
-                int want[4] = {((x + 1) % Lx) * Ly + y, ((x - 1 + Lx) % Lx) * Ly + y, x * Ly + (y + 1) % Ly,
-                               x * Ly + (y - 1 + Ly) % Ly};
+                const int xp = x + 1 == Lx ? 0 : x + 1, xm = x == 0 ? Lx - 1 : x - 1;
+                const int yp = y + 1 == Ly ? 0 : y + 1, ym = y == 0 ? Ly - 1 : y - 1;
+                int want[4] = {xp * Ly + y, xm * Ly + y, x * Ly + yp, x * Ly + ym};
                 int seen = 0;
                 for (int l = 0; l < 4; ++l) {
                     int j = p->linked_orb[(size_t)i * z + l];
@@ -373,7 +374,8 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
     std::vector<int> colour(N, 0);
     int ncol = 0;
     if (m->geom == MCS_GEOM_SQUARE) {
-        for (int i = 0; i < N; ++i) colour[i] = ((i / m->Ly) + (i % m->Ly)) & 1;
+        for (int x = 0, i = 0; x < m->Lx; ++x)
+            for (int y = 0; y < m->Ly; ++y, ++i) colour[i] = (x + y) & 1;
         ncol = 2;
     } else {
     std::vector<int> off(N + 1, 0), adj;
@@ -674,13 +676,18 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
         }
         if (ok && m->ncirc > 0) {
             ok = (m->ncirc % N) == 0;
-            int per = ok ? m->ncirc / N : 0;
-            for (int ci = 0; ci < m->ncirc && ok; ++ci) {
-                int cell = ci / per, x = cell / Ly;
-                for (int k = 0; k < 3; ++k) {
-                    int xs = p->circuits[3 * ci + k] / Ly;
-                    if (xs != x && xs != (x + 1) % Lx) { ok = false; break; }
-                }
+            const int per = ok ? m->ncirc / N : 0;
+            // circuit ci belongs to cell ci / per, in row x = cell / Ly; each of
+            // its sites must lie in row x or the next one (ids x*Ly .. x*Ly+Ly-1
+            // or the next row's), compared as unsigned offsets from the rows' first ids
+            for (int x = 0, ci = 0; x < Lx && ok; ++x) {
+                const unsigned lo0 = (unsigned)(x * Ly), lo1 = (unsigned)(((x + 1) % Lx) * Ly);
+                const int end = (x + 1) * Ly * per;
+                for (; ci < end && ok; ++ci)
+                    for (int k = 0; k < 3; ++k) {
+                        const unsigned id = (unsigned)p->circuits[3 * ci + k];
+                        if (id - lo0 >= (unsigned)Ly && id - lo1 >= (unsigned)Ly) { ok = false; break; }
+                    }
             }
             for (int k = 0; k < N && ok; ++k) ok = m->slen[k] == m->slen[0] && m->slen[0] > 0;
         }
