@@ -75,3 +75,90 @@ def test_unsupported_inputs_are_rejected(tmp_path):
     bad.write_text(text)
     with pytest.raises(ValueError, match="Ncores"):
         sim.load_param(str(bad))
+
+
+def _reference_ready():
+    from oracle import refharness as rh
+    return rh.reference_tree_present() and rh.reference_libs_present()
+
+
+class _OracleBatch:
+    """Stand-in for mcsolver_gb300.Batch on CPU: each replica is solved by the
+    oracle's reference stream (mode 0, bit-identical to the reference
+    libraries for the same seed)."""
+
+    def __init__(self, device=0):
+        self.items = []
+
+    def add(self, model, args, seed=1, **opt):
+        self.items.append((model, args, seed))
+        return len(self.items) - 1
+
+    def run(self):
+        pass
+
+    def result(self, i):
+        from oracle import oracle as orc
+        model, args, seed = self.items[i]
+        r, ex = orc.solve(model, args, seed=seed, mode=0)
+        N = len(args[1])
+        nf = args[14] if model == "ising" else args[20]
+        ex["frames"] = [np.zeros((N, 3))] * nf
+        return r, ex
+
+    def close(self):
+        pass
+
+
+@pytest.mark.skipif(not _reference_ready(), reason="reference tree or reference libraries absent")
+@pytest.mark.parametrize("name", ["square_xy", "honeycomb_heisenberg", "square_ising_field"])
+def test_grid_files_match_the_reference_caller(monkeypatch, tmp_path, name):
+    """The grid driver writes what the reference writes for the same results.
+    Our side: start_simulation with every point solved by the oracle's
+    reference stream (seed + point ID).  Reference side: for every point,
+    srand(seed + ID), then the reference's own caller (mcMain.MC +
+    mainLoopViaCLib[_On]) on the reference library, which writes ``out`` and
+    ``spinDotSpin.txt`` itself; the result.txt rows are formed as
+    win.startSimulation forms them (win.py:92-102, :131-142, :169-172).
+    The files must agree line for line."""
+    import mcsolver_gb300
+    from oracle import refharness as rh
+    monkeypatch.setattr(mcsolver_gb300, "Batch", _OracleBatch)
+    path = os.path.join(GOLD, "params", name + ".txt")
+    p = sim.load_param(path)
+    seed = 11
+    ours = tmp_path / "ours"
+    ref = tmp_path / "ref"
+    ours.mkdir()
+    ref.mkdir()
+    sim.start_simulation(path, workdir=str(ours), seed=seed, threads=1)
+
+    model = {"Ising": "ising", "XY": "xy", "Heisenberg": "heisenberg"}[p["modelType"]]
+    lib = rh.load_reference_lib(rh.LIBNAME[model])
+    for f in ("out", "spinDotSpin.txt"):
+        (ref / f).write_text("#T #H\n")  # win.py:43-46
+    Lx, Ly, Lz = p["LPack"]
+    N = Lx * Ly * Lz * len(p["pos"])
+    rows = []
+    TList = np.linspace(p["T0"], p["T1"], p["nT"])
+    HList = np.linspace(p["H0"], p["H1"], p["nH"])
+    for iH, H in enumerate(HList):
+        for iT, T in enumerate(TList):
+            spec = dict(model=model, LMatrix=p["LMatrix"], pos=p["pos"], S=p["S"], D=p["DList"],
+                        bonds=[(b[0], b[1], tuple(b[2]), list(b[3])) for b in p["bondList"]], L=p["LPack"],
+                        T=float(T), h=float(H), nthermal=p["nthermal"], nsweep=p["nsweep"], tau=p["ninterval"],
+                        algo=p["algorithm"], ki=p["GcOrb"], orbGroups=p["orbGroupList"], groupInSC=p["groupInSC"],
+                        circuits=p["localCircuitList"], spinFrame=p["spinFrame"])
+            rh.srand(seed + iH * len(TList) + iT)
+            ret = rh.run_caller_with(spec, lib, str(ref))
+            if model == "ising":
+                si, sj, sij, ac, E, E2, U4 = ret
+                rows.append((T, H, si, sj, (sij - si * sj) / T, E, (E2 - E * E) / T ** 2 * N, 0.0, U4, ac))
+            else:
+                si, sj, sij, ac, E, E2, U4, Q = ret
+                rows.append((T, H, np.sqrt(sum(si * si)), np.sqrt(sum(sj * sj)), (sij - np.dot(si, sj)) / T, E,
+                             (E2 - E * E) / T ** 2 * N, Q, U4, ac))
+    for f in ("out", "spinDotSpin.txt"):
+        assert (ours / f).read_text().splitlines() == (ref / f).read_text().splitlines(), f
+    want = ["%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E" % r for r in rows]
+    assert (ours / "result.txt").read_text().splitlines()[1:] == want
