@@ -252,8 +252,24 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
         int slotc[MCS_MAXZ] = {};
         const double *prevJ = nullptr;
         int prevc = 0;
-        for (int i = 0; i < N; ++i)
-            for (int l = 0; l < p->nlink[i]; ++l) {
+        for (int i = 0; i < N; ++i) {
+            const int nl = p->nlink[i];
+            const double *Ji = p->link_strength + (size_t)i * z * 9;
+            // a site with as many links as the previous one and the same bits
+            // in every one of them: each link matches the same slot of the
+            // previous site, so the slot rule below gives it that slot's class
+            // (one block compare instead of one per link)
+            if (i > 0 && nl > 0 && nl == p->nlink[i - 1] &&
+                memcmp(Ji, Ji - (size_t)z * 9, sizeof(double) * 9 * (size_t)nl) == 0) {
+                for (int l = 0; l < nl; ++l) {
+                    linkcls[(size_t)i * z + l] = slotc[l];
+                    slotJ[l] = Ji + 9 * l;
+                }
+                prevJ = Ji + 9 * (nl - 1);
+                prevc = slotc[nl - 1];
+                continue;
+            }
+            for (int l = 0; l < nl; ++l) {
                 const double *J = p->link_strength + ((size_t)i * z + l) * 9;
                 int c;
                 if (slotJ[l] && same_bits9(J, slotJ[l])) {
@@ -272,6 +288,7 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
                 slotJ[l] = J; slotc[l] = c;
                 prevJ = J; prevc = c;
             }
+        }
         if (cls.keys.size() > 65535) FAIL(MCS_EUNSUPPORTED, "too many distinct exchange matrices");
         std::vector<std::vector<double>> tab;
         for (auto &k : cls.keys) tab.push_back(std::vector<double>(k.begin(), k.end()));
