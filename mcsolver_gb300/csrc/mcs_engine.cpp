@@ -1158,6 +1158,47 @@ extern "C" {
 
 const char *mcs_last_error(void) { return get_error().c_str(); }
 int mcs_abi_version(void) { return 1; }
+
+// Host-compile check, exported for the CPU tests and deliberately not declared
+// in include/mcsgpu.h: compiles `problem` on the host (no device call) and
+// returns an FNV-1a digest of its arena image and descriptor, the bytes a
+// batch uploads.  With `template_problem` set, that problem is compiled first
+// and `problem` is compiled from its template (*reused tells whether the
+// template's structure was taken), so a test can check that the template path
+// and a full compile give the same bytes.
+int mcs_test_compile_digest(const mcs_problem *template_problem, const mcs_problem *problem,
+                            const mcs_options *options, uint64_t *digest, int32_t *reused)
+{
+    try {
+        mcs_options def;
+        memset(&def, 0, sizeof def);
+        const mcs_options *o = options ? options : &def;
+        std::shared_ptr<const ModelTemplate> t;
+        if (template_problem) {
+            Replica a;
+            int rc = build_replica(template_problem, o, &a, false);
+            if (rc != MCS_OK) return rc;
+            if (template_problem->model != MCS_ISING) t = make_template(template_problem, a.hm);
+        }
+        Replica r;
+        bool re = false;
+        int rc = build_replica(problem, o, &r, false, t.get(), &re);
+        if (rc != MCS_OK) return rc;
+        uint64_t h = 1469598103934665603ULL;
+        auto mix = [&h](const void *d, size_t n) {
+            const unsigned char *c = (const unsigned char *)d;
+            for (size_t i = 0; i < n; ++i) { h ^= c[i]; h *= 1099511628211ULL; }
+        };
+        mix(r.staging.data(), r.staging.size());
+        mix(&r.rep, sizeof(Rep));
+        if (digest) *digest = h;
+        if (reused) *reused = re ? 1 : 0;
+        return MCS_OK;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return MCS_EINVAL;
+    }
+}
 const char *mcs_build_info(void)
 {
     return "mcsgpu: sm_103a Monte Carlo spin-lattice engine (Ising/XY/Heisenberg; Metropolis colour sweeps, "

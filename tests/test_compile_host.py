@@ -122,3 +122,65 @@ def test_request_larger_than_the_budget_is_refused(engine):
 def test_server_needs_a_budget_and_a_slot(engine, budget, slots):
     e = _code(engine, lambda: engine.Server(hbm_budget_bytes=budget, max_slots=slots))
     assert e.code == EINVAL
+
+
+def _digest(engine, problem, template=None, **opt):
+    import ctypes
+    L = engine.lib()
+    fn = L.mcs_test_compile_digest
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64),
+                   ctypes.POINTER(ctypes.c_int32)]
+    o = engine.make_options(**opt)
+    d, r = ctypes.c_uint64(), ctypes.c_int32()
+    tp = ctypes.addressof(template.struct) if template is not None else None
+    rc = fn(tp, ctypes.addressof(problem.struct), ctypes.addressof(o), ctypes.byref(d), ctypes.byref(r))
+    assert rc == 0, L.mcs_last_error()
+    return d.value, r.value
+
+
+def _xy(T, **kw):
+    return C.square_args("xy", 24, T, nthermal=3, nsweep=5, **kw)
+
+
+TEMPLATE_CASES = [
+    # (model, template problem, problem, the template's structure is taken)
+    ("xy", lambda: _xy(0.6), lambda: _xy(1.3, D=[0.1, -0.05, 0], h=0.2), True),
+    ("xy", lambda: _xy(0.6), lambda: tuple(list(_xy(0.9))[:15] + [0.3] + list(_xy(0.9))[16:]), True),  # flunc
+    ("heisenberg", lambda: C.square_args("heisenberg", 16, 0.4, dmi=0.4, nthermal=3, nsweep=5),
+     lambda: C.square_args("heisenberg", 16, 0.8, h=0.2, dmi=0.4, nthermal=7, nsweep=9, frames=3), True),
+    ("heisenberg", lambda: C.honeycomb_args("heisenberg", 6, 9.0, nthermal=3, nsweep=5),
+     lambda: C.honeycomb_args("heisenberg", 6, 5.0, h=0.3, nthermal=3, nsweep=5), True),
+    # a different partition of the links into coupling classes (DMI on one lattice only): full compile
+    ("heisenberg", lambda: C.square_args("heisenberg", 16, 0.4, nthermal=3, nsweep=5),
+     lambda: C.square_args("heisenberg", 16, 0.4, dmi=0.4, nthermal=3, nsweep=5), False),
+    # another lattice size: full compile
+    ("xy", lambda: _xy(0.6), lambda: C.square_args("xy", 26, 0.6, nthermal=3, nsweep=5), False),
+]
+
+
+@pytest.mark.parametrize("k", range(len(TEMPLATE_CASES)))
+@pytest.mark.parametrize("random_init", [False, True])
+def test_template_compile_gives_the_bytes_of_a_full_compile(engine, k, random_init):
+    """A batch compiles later O(n) replicas of a lattice it already holds from
+    that replica's template.  The arena image and descriptor it uploads must
+    be the bytes a full compile of the same problem gives."""
+    model, mk_t, mk_p, taken = TEMPLATE_CASES[k]
+    tp, pp = engine.Problem(model, mk_t()), engine.Problem(model, mk_p())
+    full, r0 = _digest(engine, pp, seed=5, random_init=random_init)
+    via, r1 = _digest(engine, pp, template=tp, seed=5, random_init=random_init)
+    assert r0 == 0 and r1 == int(taken)
+    assert via == full
+
+
+def test_compile_is_deterministic_and_sees_every_input(engine):
+    """The same problem compiles to the same bytes; the seed, the field and a
+    coupling each change them."""
+    base = engine.Problem("heisenberg", C.square_args("heisenberg", 12, 0.5, dmi=0.4, nthermal=3, nsweep=5))
+    d0, _ = _digest(engine, base, seed=3)
+    assert _digest(engine, base, seed=3)[0] == d0
+    assert _digest(engine, base, seed=4)[0] != d0
+    other = engine.Problem("heisenberg", C.square_args("heisenberg", 12, 0.5, h=0.1, dmi=0.4, nthermal=3, nsweep=5))
+    assert _digest(engine, other, seed=3)[0] != d0
+    other = engine.Problem("heisenberg", C.square_args("heisenberg", 12, 0.5, dmi=0.41, nthermal=3, nsweep=5))
+    assert _digest(engine, other, seed=3)[0] != d0
