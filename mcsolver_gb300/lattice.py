@@ -33,37 +33,44 @@ def _lattice_links(L, norb, bonds):
                     if x % 2 + y % 2 + z % 2 == 0:
                         chosen[sid(x, y, z, o)] = True
 
-    def add(lst, i, j, s, merge):
-        for k, (t, s0) in enumerate(lst[i]):
+    # every link carries a tag (bond index, 0 forward / 1 inverse) of the bond
+    # whose strength it holds; a second bond to the same target (duplicate
+    # targets on supercells of side <= 2) is merged or dropped by comparing
+    # strengths, which depends on their values, and is counted in `merged`
+    merged = [0]
+
+    def add(lst, i, j, s, merge, tag):
+        for k, (t, s0, _) in enumerate(lst[i]):
             if t == j:
                 if merge:
+                    merged[0] += 1
                     if np.sum(np.abs(np.asarray(s0) - np.asarray(s))) < 1e-5:
                         return
-                    lst[i][k] = (t, np.asarray(s0) + np.asarray(s))
+                    lst[i][k] = (t, np.asarray(s0) + np.asarray(s), None)
                 return
-        lst[i].append((j, np.asarray(s)))
+        lst[i].append((j, np.asarray(s), tag))
 
     for x in range(Lx):
         for y in range(Ly):
             for z in range(Lz):
                 for o in range(norb):
                     i = sid(x, y, z, o)
-                    for (src, tgt, ov, J, Jinv) in bonds:
+                    for b, (src, tgt, ov, J, Jinv) in enumerate(bonds):
                         if o != src:
                             continue
                         j = sid(x + ov[0], y + ov[1], z + ov[2], tgt)
-                        add(links, i, j, J, True)
+                        add(links, i, j, J, True, (b, 0))
                         if i != j:
-                            add(links, j, i, Jinv, True)
+                            add(links, j, i, Jinv, True, (b, 1))
                     if chosen[i]:
-                        for (src, tgt, ov, J, Jinv) in bonds:
+                        for b, (src, tgt, ov, J, Jinv) in enumerate(bonds):
                             if o != src:
                                 continue
                             j = sid(x + 2 * ov[0], y + 2 * ov[1], z + 2 * ov[2], tgt)
-                            add(rlinks, i, j, J, False)
+                            add(rlinks, i, j, J, False, (b, 0))
                             if i != j:
-                                add(rlinks, j, i, Jinv, False)
-    return N, links, rlinks, chosen, sid
+                                add(rlinks, j, i, Jinv, False, (b, 1))
+    return N, links, rlinks, chosen, sid, merged[0]
 
 
 def lattice_args(model, L, norb, bonds, T, h=0.0, S=None, D=None, nthermal=10, nsweep=10, tau=0, algo=0,
@@ -72,6 +79,14 @@ def lattice_args(model, L, norb, bonds, T, h=0.0, S=None, D=None, nthermal=10, n
     as mcMain.py does (mcMain.py:21-31, :121, :244).  An orbital group holds
     its orbitals in every cell (group_in_sc) or in cell (0,0,0) only
     (Lattice.py:208-211)."""
+    return _lattice_build(model, L, norb, bonds, T, h, S, D, nthermal, nsweep, tau, algo, ki, groups, circuits,
+                          frames, flunc, group_in_sc)[0]
+
+
+def _lattice_build(model, L, norb, bonds, T, h, S, D, nthermal, nsweep, tau, algo, ki, groups, circuits, frames,
+                   flunc, group_in_sc):
+    """lattice_args, also returning the link lists (with their bond tags) and
+    the number of duplicate-target merges."""
     T = max(T, 0.1)
     S = S or [1.0] * norb
     D = D or [[0.0, 0.0, 0.0]] * norb
@@ -85,7 +100,7 @@ def lattice_args(model, L, norb, bonds, T, h=0.0, S=None, D=None, nthermal=10, n
             bl.append((src, tgt, ov, J9, inv))
         else:
             bl.append((src, tgt, ov, J9[0], J9[0]))
-    N, links, rlinks, chosen, sid = _lattice_links(L, norb, bl)
+    N, links, rlinks, chosen, sid, merged = _lattice_links(L, norb, bl)
     Lx, Ly, Lz = L
     z = max(len(l) for l in links)
     init = [S[i % norb] for i in range(N)]
@@ -127,7 +142,7 @@ def lattice_args(model, L, norb, bonds, T, h=0.0, S=None, D=None, nthermal=10, n
     tau = N if tau <= 0 else tau
     if not on:
         return (algo, tuple(init), nthermal, nsweep, tau, z, tuple(nlink), tuple(ls), tuple(lo), tuple(cp),
-                h / T, tuple(rorb), tuple(rcl), tuple(rlk), frames)
+                h / T, tuple(rorb), tuple(rcl), tuple(rlk), frames), links, merged
     initD = []
     for i in range(N):
         initD += [float(d) / T for d in D[i % norb]]
@@ -155,7 +170,80 @@ def lattice_args(model, L, norb, bonds, T, h=0.0, S=None, D=None, nthermal=10, n
                 ign = 0
     return (algo, tuple(init), tuple(initD), nthermal, nsweep, tau, z, tuple(nlink), tuple(ls), tuple(lo),
             tuple(circ), tuple(cp), len(groups), maxg, tuple(grp), flunc, h / T, tuple(rorb), tuple(rcl),
-            tuple(rlk), frames, ign)
+            tuple(rlk), frames, ign), links, merged
+
+
+# tuple positions of the arrays (for arrays=True) and of the T-dependent entries
+_ISING_ARRAYS = (1, 6, 7, 8, 9, 11, 12, 13)
+_ON_ARRAYS = (1, 2, 7, 8, 9, 10, 11, 14, 17, 18, 19)
+_INV_PERM = [0, 1, 2, 6, 7, 8, 3, 4, 5]   # xx,yy,zz,xy,xz,yz,yx,zx,zy of the transpose (Lattice.py:137)
+
+
+class LatticeTemplate:
+    """The MCMainFunction tuples of one lattice at many (T, H) points.
+
+    The structure (links in the reference's order, renormalised lists,
+    correlated pairs, circuits, groups) is built once.  Each point recomputes
+    only what depends on T and H: every link's coupling J/T (the J of the bond
+    the link comes from, or its transpose for the reverse link), the
+    anisotropy D/T, the field h/T and the off-diagonal flag.  ``at(T, h)``
+    equals ``lattice_args(..., T, h=h, ...)`` value for value.  On supercells
+    where two bonds of a site reach the same target (a side of 1 or 2), the
+    reference merges or drops the second by comparing J/T values
+    (Lattice.py:34-57), a decision that can depend on T; there every point is
+    built by lattice_args.
+    """
+
+    def __init__(self, model, L, norb, bonds, S=None, D=None, nthermal=10, nsweep=10, tau=0, algo=0,
+                 ki=((0, 0), (0, 0, 0)), groups=(), circuits=(), frames=0, flunc=0.0, group_in_sc=True):
+        self.model, self.on = model, model != "ising"
+        self.kw = dict(L=L, norb=norb, bonds=bonds, S=S, D=D, nthermal=nthermal, nsweep=nsweep, tau=tau, algo=algo,
+                       ki=ki, groups=groups, circuits=circuits, frames=frames, flunc=flunc, group_in_sc=group_in_sc)
+        self.base, links, self.merged = _lattice_build(model, L, norb, bonds, 1.0, 0.0, S, D, nthermal, nsweep, tau,
+                                                       algo, ki, groups, circuits, frames, flunc, group_in_sc)
+        N = len(links)
+        z = max(len(l) for l in links)
+        self.tagb = np.full((N, z), -1, dtype=np.int64)
+        self.tagi = np.zeros((N, z), dtype=np.int64)
+        for i, l in enumerate(links):
+            for k, (_, _, tag) in enumerate(l):
+                if tag is not None:
+                    self.tagb[i, k], self.tagi[i, k] = tag
+        self.pad = self.tagb < 0
+        self.J = np.asarray([b[3] for b in bonds], dtype=float).reshape(len(bonds), 9)
+        Dn = np.asarray(D or [[0.0, 0.0, 0.0]] * norb, dtype=float)
+        self.Dsite = Dn[np.arange(N) % norb]
+        self.arrays = {k: np.asarray(self.base[k]) for k in (_ON_ARRAYS if self.on else _ISING_ARRAYS)}
+
+    def at(self, T, h=0.0, arrays=False):
+        """The tuple at (T, h); with arrays=True its arrays are numpy arrays
+        (what mcsolver_gb300.Problem takes without a copy into a tuple)."""
+        if self.merged:
+            return lattice_args(self.model, T=T, h=h, **self.kw)
+        T = max(T, 0.1)
+        J = self.J / T
+        b = np.where(self.pad, 0, self.tagb)
+        a = list(self.base)
+        if self.on:
+            both = np.stack([J, J[:, _INV_PERM]])               # [fwd/inv, bond, 9]
+            ls = np.where(self.pad[..., None], 0.0, both[self.tagi, b])
+            ign = 0 if np.any(np.abs(ls[..., 3:]) > 1e-6) else 1
+            a[2] = (self.Dsite / T).reshape(-1)
+            a[8] = ls.reshape(-1)
+            a[16] = h / T
+            a[21] = ign
+            keys = _ON_ARRAYS
+        else:
+            ls = np.where(self.pad, 0.0, J[:, 0][b])
+            a[7] = ls.reshape(-1)
+            a[10] = h / T
+            keys = _ISING_ARRAYS
+        for k in keys:
+            if k not in ((2, 8) if self.on else (7,)):
+                a[k] = self.arrays[k]
+            if not arrays:
+                a[k] = tuple(np.asarray(a[k]).tolist())
+        return tuple(a)
 
 
 def J9(xx, yy=0, zz=0, xy=0, xz=0, yz=0, yx=0, zx=0, zy=0):

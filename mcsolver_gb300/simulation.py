@@ -10,8 +10,9 @@ per (T, H) point, and mcMain writes ``out``, ``spinDotSpin.txt``, spin frames
 and ``result.txt`` (mcMain.py:126-135, :259-289, :291-323; win.py:170-177).
 
 Here the whole grid is one batch on the GPU: every point becomes one replica of
-``mcsolver_gb300.Batch`` (the tuples are built by ``lattice.lattice_args`` with
-the reference's site order, couplings divided by the clamped temperature), and
+``mcsolver_gb300.Batch`` (the tuples are built with the reference's site order
+and couplings divided by the clamped temperature; the lattice is built once by
+``lattice.LatticeTemplate`` and each point rescales J, D and h), and
 the same files are written with the reference's formats, points in grid order
 (H outer, T inner; the reference writes them in pool completion order).
 
@@ -161,10 +162,10 @@ def save_param(p: dict, path: str) -> None:
 _MODEL = {"Ising": "ising", "XY": "xy", "Heisenberg": "heisenberg"}
 
 
-def point_args(p: dict, T: float, H: float):
-    """(model, MCMainFunction tuple) of one grid point, as win.startMC /
-    startMCForOn with mcMain.MC would build it (mcMain.py:16-105, :137-235)."""
-    from .lattice import lattice_args
+def _lattice_inputs(p: dict):
+    """(model, lattice_args positional inputs, keyword inputs) of a parameter
+    file, after the checks the reference's caller makes (win.py:68-72,
+    :105-113; the dipole path is refused, Lattice.py:298)."""
     model = _MODEL.get(p["modelType"])
     if model is None:
         raise ValueError("for now only Ising, XY and Heisenberg models are supported")
@@ -174,11 +175,27 @@ def point_args(p: dict, T: float, H: float):
         raise ValueError("dipole couplings are not supported (the reference's dipole path fails, Lattice.py:298)")
     Lx, Ly, Lz = p["LPack"]
     bonds = [(src, tgt, tuple(ov), list(J)) for (src, tgt, ov, J) in p["bondList"]]
-    return model, lattice_args(model, (Lx, Ly, Lz), len(p["pos"]), bonds, T, h=H, S=list(p["S"]), D=list(p["DList"]),
-                               nthermal=p["nthermal"], nsweep=p["nsweep"], tau=p["ninterval"],
-                               algo=1 if p["algorithm"] == "Wolff" else 0, ki=p["GcOrb"],
-                               groups=p.get("orbGroupList", []), group_in_sc=p.get("groupInSC", True),
-                               circuits=p.get("localCircuitList", []), frames=p.get("spinFrame", 0))
+    kw = dict(S=list(p["S"]), D=list(p["DList"]), nthermal=p["nthermal"], nsweep=p["nsweep"], tau=p["ninterval"],
+              algo=1 if p["algorithm"] == "Wolff" else 0, ki=p["GcOrb"], groups=p.get("orbGroupList", []),
+              group_in_sc=p.get("groupInSC", True), circuits=p.get("localCircuitList", []),
+              frames=p.get("spinFrame", 0))
+    return model, ((Lx, Ly, Lz), len(p["pos"]), bonds), kw
+
+
+def point_args(p: dict, T: float, H: float):
+    """(model, MCMainFunction tuple) of one grid point, as win.startMC /
+    startMCForOn with mcMain.MC would build it (mcMain.py:16-105, :137-235)."""
+    from .lattice import lattice_args
+    model, (L, norb, bonds), kw = _lattice_inputs(p)
+    return model, lattice_args(model, L, norb, bonds, T, h=H, **kw)
+
+
+def grid_template(p: dict):
+    """(model, LatticeTemplate) of a parameter file: the lattice is built once
+    and ``template.at(T, H)`` gives point_args(p, T, H)[1] at every grid point."""
+    from .lattice import LatticeTemplate
+    model, (L, norb, bonds), kw = _lattice_inputs(p)
+    return model, LatticeTemplate(model, L, norb, bonds, **kw)
 
 
 def _positions(p):
@@ -210,7 +227,9 @@ def start_simulation(rpath: str, workdir: str = ".", seed: int = 1, device: int 
         f.write("#T #H\n")
     with open(os.path.join(workdir, "spinDotSpin.txt"), "w") as f:
         f.write("#T #H\n")
-    built = [point_args(p, T, H) for (_, T, H) in pts]
+    # one lattice build for the whole grid; each point rescales J, D and h
+    model, tmpl = grid_template(p)
+    built = [(model, tmpl.at(T, H, arrays=True)) for (_, T, H) in pts]
     b = Batch(device=device)
     with ThreadPoolExecutor(max_workers=max(1, threads)) as pool:
         # adds from several threads: the engine's replica index is returned by add

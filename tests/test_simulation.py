@@ -162,3 +162,53 @@ def test_grid_files_match_the_reference_caller(monkeypatch, tmp_path, name):
         assert (ours / f).read_text().splitlines() == (ref / f).read_text().splitlines(), f
     want = ["%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E%15.6E" % r for r in rows]
     assert (ours / "result.txt").read_text().splitlines()[1:] == want
+
+
+def _bits(x):
+    a = np.asarray(x)
+    return a.view(np.uint64) if a.dtype == np.float64 else a
+
+
+TEMPLATE_LATTICES = [
+    ("xy", (8, 8, 1), 1, [(0, 0, (1, 0, 0), [-1, -1, -1, 0, 0, 0, 0, 0, 0]), (0, 0, (0, 1, 0), [-1, -1, -1, 0, 0, 0, 0, 0, 0])],
+     dict(D=[[0.1, -0.2, 0.0]], groups=[[0]], frames=2)),
+    ("heisenberg", (6, 6, 1), 1, [(0, 0, (1, 0, 0), [-1, -1, -1, 0, 0.4, 0, 0, -0.4, 0]),
+                                  (0, 0, (0, 1, 0), [-1, -1, -1, 0, 0, 0.4, 0, 0, -0.4])],
+     dict(D=[[0, 0, -0.2]], circuits=[((0, (0, 0, 0)), (0, (1, 0, 0)), (0, (1, 1, 0)))])),     # DMI
+    ("heisenberg", (4, 4, 1), 2, [(0, 1, (0, 0, 0), [-1.5, -1.5, -1.8, 0.3, 0, 0, 0.3, 0, 0]),
+                                  (0, 1, (-1, 0, 0), [-1.5, -1.5, -1.8, 0.3, 0, 0, 0.3, 0, 0]),
+                                  (0, 0, (1, 0, 0), [-0.3, -0.3, -0.3, 0, 0, 0, 0, 0, 0])],
+     dict(S=[1.5, 1.0], D=[[0, 0, -0.5], [0, 0, 0.1]], groups=[[0], [1]], group_in_sc=False, ki=((0, 1), (0, 0, 0)))),
+    ("ising", (6, 6, 1), 2, [(0, 1, o, [-1.0] + [0] * 8) for o in ((0, 0, 0), (-1, 0, 0), (0, 1, 0))],
+     dict(S=[1.5, 1.5], ki=((0, 1), (0, 0, 0)))),
+    ("xy", (2, 2, 1), 1, [(0, 0, (1, 0, 0), [-1, -1, -1, 0, 0, 0, 0, 0, 0]), (0, 0, (0, 1, 0), [-1, -1, -1, 0, 0, 0, 0, 0, 0])],
+     dict()),                                                                                    # merged duplicates
+]
+
+
+@pytest.mark.parametrize("k", range(len(TEMPLATE_LATTICES)))
+def test_lattice_template_equals_lattice_args_bit_for_bit(k):
+    """The grid driver builds a lattice once (LatticeTemplate) and rescales J,
+    D and h per point; every point's tuple must be the one lattice_args (itself
+    checked against the reference's marshalling) builds, bit for bit,
+    including the clamp T -> 0.1 and the off-diagonal flag."""
+    from mcsolver_gb300.lattice import LatticeTemplate, lattice_args
+    model, L, norb, bonds, kw = TEMPLATE_LATTICES[k]
+    t = LatticeTemplate(model, L, norb, bonds, **kw)
+    assert bool(t.merged) == (L[0] <= 2)
+    for T, H in ((0.05, 0.0), (0.7, 0.2), (2.5, -0.1), (1e7, 0.0)):
+        want = lattice_args(model, L, norb, bonds, T, h=H, **kw)
+        for arrays in (False, True):
+            got = t.at(T, H, arrays=arrays)
+            assert len(got) == len(want)
+            for i, (a, b) in enumerate(zip(got, want)):
+                assert np.array_equal(_bits(np.asarray(a, dtype=np.asarray(b).dtype)), _bits(b)), (T, H, arrays, i)
+
+
+def test_grid_template_matches_point_args():
+    for name in ("square_xy", "honeycomb_heisenberg", "square_ising_field"):
+        p = sim.load_param(os.path.join(GOLD, "params", name + ".txt"))
+        model, t = sim.grid_template(p)
+        for T, H in ((p["T0"], p["H0"]), (p["T1"], p["H1"])):
+            m2, want = sim.point_args(p, T, H)
+            assert m2 == model and t.at(T, H) == want
