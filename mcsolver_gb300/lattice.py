@@ -173,6 +173,108 @@ def _lattice_build(model, L, norb, bonds, T, h, S, D, nthermal, nsweep, tau, alg
             tuple(rlk), frames, ign), links, merged
 
 
+_RCL_OFFSETS = ((0, 0, 0), (0, 0, 1), (0, 1, 0), (1, 0, 0), (0, 1, 1), (1, 0, 1), (1, 1, 0), (1, 1, 1))
+
+
+def _structure_np(model, L, norb, bonds, S, D, nthermal, nsweep, tau, algo, ki, groups, circuits, frames, flunc,
+                  group_in_sc):
+    """The T-independent part of _lattice_build with numpy, for supercells in
+    which no site holds two links (or two renormalised links) to one target.
+    Returns (tuple at T = 1 with the T-dependent entries left as None, link
+    bond index [N, z] (-1 = padding), link direction [N, z] (1 = reverse))
+    or None when a duplicate target makes the reference's order depend on
+    values.  The insertion order of Lattice.py:247-271 is a sort: the sites
+    are visited in id order and, per site, the bonds in list order, each
+    adding the forward link to its source and then the reverse link to its
+    target; so a site's links are ordered by (visited site, bond, direction)."""
+    Lx, Ly, Lz = L
+    N = Lx * Ly * Lz * norb
+    on = model != "ising"
+    cell = np.arange(Lx * Ly * Lz, dtype=np.int64)
+    cx, cy, cz = cell // (Ly * Lz), (cell // Lz) % Ly, cell % Lz
+
+    def sid(x, y, z, o):
+        return ((x % Lx) * Ly * Lz + (y % Ly) * Lz + (z % Lz)) * norb + o
+
+    def ordered(owner_sites, step):
+        own, tgt, src_site, bidx, rev = [], [], [], [], []
+        for b, (src, t, ov, _) in enumerate(bonds):
+            sel = owner_sites[src]
+            i = sid(cx[sel], cy[sel], cz[sel], src)
+            j = sid(cx[sel] + step * ov[0], cy[sel] + step * ov[1], cz[sel] + step * ov[2], t)
+            m = i != j
+            own += [i, j[m]]
+            tgt += [j, i[m]]
+            src_site += [i, i[m]]
+            bidx += [np.full(len(i), b), np.full(int(m.sum()), b)]
+            rev += [np.zeros(len(i), np.int64), np.ones(int(m.sum()), np.int64)]
+        if not own:
+            e = np.zeros(0, np.int64)
+            return e, e, e, e, e
+        own, tgt, src_site, bidx, rev = (np.concatenate(v).astype(np.int64) for v in (own, tgt, src_site, bidx, rev))
+        order = np.lexsort((rev, bidx, src_site, own))
+        own, tgt, bidx, rev = own[order], tgt[order], bidx[order], rev[order]
+        counts = np.bincount(own, minlength=N)
+        slot = np.arange(len(own)) - (np.cumsum(counts) - counts)[own]
+        return own, tgt, bidx, rev, slot
+
+    every = {o: np.ones(len(cell), bool) for o in range(norb)}
+    own, tgt, bidx, rev, slot = ordered(every, 1)
+    if len(np.unique(own * N + tgt)) != len(own):
+        return None
+    nlink = np.bincount(own, minlength=N)
+    z = int(nlink.max()) if N else 0
+    lo = np.full((N, z), -1, np.int64)
+    tagb = np.full((N, z), -1, np.int64)
+    tagi = np.zeros((N, z), np.int64)
+    lo[own, slot], tagb[own, slot], tagi[own, slot] = tgt, bidx, rev
+    # renormalised links of the chosen sites (even x, y, z), Lattice.py:185-205, :263-271
+    chosen_cell = (cx % 2 == 0) & (cy % 2 == 0) & (cz % 2 == 0)
+    rown, rtgt, _, _, rslot = ordered({o: chosen_cell for o in range(norb)}, 2)
+    if len(np.unique(rown * N + rtgt)) != len(rown):
+        return None
+    rl = np.full((N, max(z, 1)), -1, np.int64)
+    keep = rslot < z
+    rl[rown[keep], rslot[keep]] = rtgt[keep]
+    ch_cells = np.nonzero(chosen_cell)[0]
+    rorb = (ch_cells[:, None] * norb + np.arange(norb)[None, :]).reshape(-1)
+    rlk = rl[rorb, :z].reshape(-1)
+    x, y, zc = cx[rorb // norb], cy[rorb // norb], cz[rorb // norb]
+    o = rorb % norb
+    cand = np.stack([sid(x + dx, y + dy, zc + dz, o) for (dx, dy, dz) in _RCL_OFFSETS], axis=1)
+    dup = np.zeros(cand.shape, bool)
+    for k in range(1, cand.shape[1]):
+        dup[:, k] = (cand[:, :k] == cand[:, k:k + 1]).any(axis=1)
+    kept = (~dup).sum(axis=1)
+    ncl = int(kept[0]) if len(kept) else 0
+    if len(kept) == 0 or kept.min() < ncl:
+        return None
+    idx = np.argsort(dup, axis=1, kind="stable")[:, :ncl]
+    rcl = np.take_along_axis(cand, idx, axis=1).reshape(-1)
+    (ks, kt), kov = ki
+    cp = np.stack([sid(cx, cy, cz, ks), sid(cx + kov[0], cy + kov[1], cz + kov[2], kt)], axis=1).reshape(-1)
+    S = S or [1.0] * norb
+    init = np.asarray(S)[np.arange(N) % norb]
+    tau = N if tau <= 0 else tau
+    if not on:
+        base = (algo, init, nthermal, nsweep, tau, z, nlink, None, lo.reshape(-1), cp, None, rorb, rcl, rlk, frames)
+        return base, tagb, tagi
+    circ = [sid(cx + ov[0], cy + ov[1], cz + ov[2], oo) for c in circuits for (oo, ov) in c]
+    circ = np.stack(circ, axis=1).reshape(-1) if circ else np.zeros(0, np.int64)
+    if group_in_sc:
+        gl = [np.concatenate([sid(cx, cy, cz, oo) for oo in g]) if len(g) else np.zeros(0, np.int64) for g in groups]
+    else:
+        gl = [np.asarray([sid(0, 0, 0, oo) for oo in g], np.int64) for g in groups]
+    maxg = 1
+    grp = np.zeros(0, np.int64)
+    if gl:
+        maxg = max(len(g) for g in gl)
+        grp = np.concatenate([np.concatenate([g, np.full(maxg - len(g), -1, np.int64)]) for g in gl])
+    base = (algo, init, None, nthermal, nsweep, tau, z, nlink, None, lo.reshape(-1), circ, cp, len(groups), maxg,
+            grp, flunc, None, rorb, rcl, rlk, frames, None)
+    return base, tagb, tagi
+
+
 # tuple positions of the arrays (for arrays=True) and of the T-dependent entries
 _ISING_ARRAYS = (1, 6, 7, 8, 9, 11, 12, 13)
 _ON_ARRAYS = (1, 2, 7, 8, 9, 10, 11, 14, 17, 18, 19)
@@ -199,21 +301,29 @@ class LatticeTemplate:
         self.model, self.on = model, model != "ising"
         self.kw = dict(L=L, norb=norb, bonds=bonds, S=S, D=D, nthermal=nthermal, nsweep=nsweep, tau=tau, algo=algo,
                        ki=ki, groups=groups, circuits=circuits, frames=frames, flunc=flunc, group_in_sc=group_in_sc)
-        self.base, links, self.merged = _lattice_build(model, L, norb, bonds, 1.0, 0.0, S, D, nthermal, nsweep, tau,
-                                                       algo, ki, groups, circuits, frames, flunc, group_in_sc)
-        N = len(links)
-        z = max(len(l) for l in links)
-        self.tagb = np.full((N, z), -1, dtype=np.int64)
-        self.tagi = np.zeros((N, z), dtype=np.int64)
-        for i, l in enumerate(links):
-            for k, (_, _, tag) in enumerate(l):
-                if tag is not None:
-                    self.tagb[i, k], self.tagi[i, k] = tag
+        fast = _structure_np(model, L, norb, bonds, S, D, nthermal, nsweep, tau, algo, ki, groups, circuits, frames,
+                             flunc, group_in_sc)
+        if fast is not None:
+            self.base, self.tagb, self.tagi = fast
+            self.merged = 0
+        else:
+            self.base, links, self.merged = _lattice_build(model, L, norb, bonds, 1.0, 0.0, S, D, nthermal, nsweep,
+                                                           tau, algo, ki, groups, circuits, frames, flunc, group_in_sc)
+            z = max(len(l) for l in links)
+            self.tagb = np.full((len(links), z), -1, dtype=np.int64)
+            self.tagi = np.zeros((len(links), z), dtype=np.int64)
+            for i, l in enumerate(links):
+                for k, (_, _, tag) in enumerate(l):
+                    if tag is not None:
+                        self.tagb[i, k], self.tagi[i, k] = tag
+        self.vectorised = fast is not None
+        N = self.tagb.shape[0]
         self.pad = self.tagb < 0
         self.J = np.asarray([b[3] for b in bonds], dtype=float).reshape(len(bonds), 9)
         Dn = np.asarray(D or [[0.0, 0.0, 0.0]] * norb, dtype=float)
         self.Dsite = Dn[np.arange(N) % norb]
-        self.arrays = {k: np.asarray(self.base[k]) for k in (_ON_ARRAYS if self.on else _ISING_ARRAYS)}
+        self.arrays = {k: np.asarray(self.base[k]) for k in (_ON_ARRAYS if self.on else _ISING_ARRAYS)
+                       if self.base[k] is not None}
 
     def at(self, T, h=0.0, arrays=False):
         """The tuple at (T, h); with arrays=True its arrays are numpy arrays

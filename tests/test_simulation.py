@@ -183,7 +183,25 @@ TEMPLATE_LATTICES = [
      dict(S=[1.5, 1.5], ki=((0, 1), (0, 0, 0)))),
     ("xy", (2, 2, 1), 1, [(0, 0, (1, 0, 0), [-1, -1, -1, 0, 0, 0, 0, 0, 0]), (0, 0, (0, 1, 0), [-1, -1, -1, 0, 0, 0, 0, 0, 0])],
      dict()),                                                                                    # merged duplicates
+    ("xy", (7, 5, 1), 1, [(0, 0, (1, 0, 0), [-1, -1, -1, 0, 0, 0, 0, 0, 0]), (0, 0, (0, 1, 0), [-1, -1, -1, 0, 0, 0, 0, 0, 0])],
+     dict(groups=[[0]])),                                                                        # odd sides
+    ("heisenberg", (5, 5, 3), 1, [(0, 0, ov, [-1, -1, -1, 0, 0, 0, 0, 0, 0]) for ov in ((1, 0, 0), (0, 1, 0), (0, 0, 1))],
+     dict()),                                                                                    # 3D
+    ("heisenberg", (5, 7, 1), 2, [(0, 1, (0, 0, 0), [-1, -1, -1, 0, 0, 0, 0, 0, 0]), (1, 0, (1, 0, 0), [-1, -1, -1, 0, 0, 0, 0, 0, 0]),
+                                  (0, 0, (0, 1, 0), [-1, -1, -1, 0, 0, 0, 0, 0, 0])],
+     dict(S=[1.0, 0.5], groups=[[0], [1], [0, 1]], ki=((1, 0), (1, 1, 0)))),                     # two orbitals, groups
+    ("ising", (4, 4, 1), 1, [(0, 0, (0, 0, 0), [-1.0] + [0] * 8), (0, 0, (1, 0, 0), [-1.0] + [0] * 8)], dict()),  # self link
 ]
+
+
+def test_lattice_template_vectorises_lattices_without_duplicate_links():
+    """The structure is built with numpy unless a site holds two links (or two
+    renormalised links) to one target, where the reference's order depends
+    on values and the per-site builder is kept."""
+    from mcsolver_gb300.lattice import LatticeTemplate
+    want = [True, True, False, True, False, True, True, True, False]
+    for (model, L, norb, bonds, kw), v in zip(TEMPLATE_LATTICES, want):
+        assert LatticeTemplate(model, L, norb, bonds, **kw).vectorised == v, (model, L)
 
 
 @pytest.mark.parametrize("k", range(len(TEMPLATE_LATTICES)))
