@@ -184,15 +184,17 @@ def _lattice_inputs(p: dict):
 
 def point_args(p: dict, T: float, H: float):
     """(model, MCMainFunction tuple) of one grid point, as win.startMC /
-    startMCForOn with mcMain.MC would build it (mcMain.py:16-105, :137-235)."""
-    from .lattice import lattice_args
-    model, (L, norb, bonds), kw = _lattice_inputs(p)
-    return model, lattice_args(model, L, norb, bonds, T, h=H, **kw)
+    startMCForOn with mcMain.MC would build it (mcMain.py:16-105, :137-235).
+    Built through the lattice template (numpy structure, values rescaled to
+    (T, H)), which equals lattice.lattice_args bit for bit."""
+    model, tmpl = grid_template(p)
+    return model, tmpl.at(T, H)
 
 
 def grid_template(p: dict):
     """(model, LatticeTemplate) of a parameter file: the lattice is built once
-    and ``template.at(T, H)`` gives point_args(p, T, H)[1] at every grid point."""
+    and ``template.at(T, H)`` gives the MCMainFunction tuple of every grid
+    point (equal to lattice.lattice_args at that point)."""
     from .lattice import LatticeTemplate
     model, (L, norb, bonds), kw = _lattice_inputs(p)
     return model, LatticeTemplate(model, L, norb, bonds, **kw)

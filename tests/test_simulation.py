@@ -223,10 +223,11 @@ def test_lattice_template_equals_lattice_args_bit_for_bit(k):
                 assert np.array_equal(_bits(np.asarray(a, dtype=np.asarray(b).dtype)), _bits(b)), (T, H, arrays, i)
 
 
-def test_grid_template_matches_point_args():
+def test_grid_template_matches_the_per_site_builder():
+    from mcsolver_gb300.lattice import lattice_args
     for name in ("square_xy", "honeycomb_heisenberg", "square_ising_field"):
         p = sim.load_param(os.path.join(GOLD, "params", name + ".txt"))
-        model, t = sim.grid_template(p)
+        model, (L, norb, bonds), kw = sim._lattice_inputs(p)
         for T, H in ((p["T0"], p["H0"]), (p["T1"], p["H1"])):
-            m2, want = sim.point_args(p, T, H)
-            assert m2 == model and t.at(T, H) == want
+            m2, got = sim.point_args(p, T, H)
+            assert m2 == model and got == lattice_args(model, L, norb, bonds, T, h=H, **kw)
