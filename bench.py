@@ -124,29 +124,78 @@ def _cpu_one(job):
     return time.time() - t
 
 
-def cpu_baseline(target_s=15.0):
-    """The oracle's reference-stream restatement (bit-identical to the
-    reference library) on every host core through a process pool, the way
-    the reference's win.startSimulation fans temperatures out."""
+def _cpu_warm(_):
     from oracle import oracle as orc
-    orc.build()
-    cores = os.cpu_count() or 1
-    cal = workload_args(nsweep=4)[0]
-    t0 = time.time()
-    orc.solve("xy", cal, seed=1, mode=0)
-    per_sweep = max(1e-4, (time.time() - t0) / 4)
-    sweeps = max(4, int(target_s * cores / (NTEMP * per_sweep)))
-    jobs = [("xy", a, 1 + k) for k, a in enumerate(workload_args(nsweep=sweeps))]
-    ctx = mp.get_context("spawn")
+    orc.lib()
+    return os.getpid()
+
+
+class CpuPool:
+    """The reference's fan-out (win.startSimulation: one process per host
+    core, one (T, H) point per task) over the oracle's reference-stream
+    restatement of the compiled library (bit-identical to it).  The pool is
+    started and its workers load the library before any timing."""
+
+    def __init__(self):
+        from oracle import oracle as orc
+        orc.build()
+        self.cores = os.cpu_count() or 1
+        self.pool = mp.get_context("spawn").Pool(processes=self.cores)
+        self.pool.map(_cpu_warm, range(self.cores))
+        cal = workload_args(nsweep=4)[0]
+        orc.lib()
+        t0 = time.time()
+        orc.solve("xy", cal, seed=1, mode=0)
+        self.per_sweep = max(1e-4, (time.time() - t0) / 4)
+
+    def sweeps_for(self, seconds):
+        return max(4, int(seconds * self.cores / (NTEMP * self.per_sweep)))
+
+    def run(self, sweeps, seed0=1):
+        jobs = [("xy", a, seed0 + k) for k, a in enumerate(workload_args(nsweep=sweeps))]
+        t = time.time()
+        self.pool.map(_cpu_one, jobs, chunksize=1)
+        return time.time() - t
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+
+
+def build_marshal_seconds(points=2):
+    """Host time to build and marshal one (T, H) point of the workload the way
+    the reference's caller does (Lattice.establishLattice / establishLinking
+    site by site, then the flattened tuples of mcMain.mainLoopViaCLib_On), by
+    this package's per-site restatement of that code (lattice.square_args)."""
+    from mcsolver_gb300.lattice import square_args
     t = time.time()
-    with ctx.Pool(processes=cores) as pool:
-        pool.map(_cpu_one, jobs)
-    wall = time.time() - t
+    for k in range(points):
+        square_args("xy", L, TEMPS[k], nthermal=0, nsweep=10, tau=0, groups=((0,),))
+    return (time.time() - t) / points
+
+
+def cpu_baseline(target_s=15.0):
+    """Solve-only throughput of the reference's CPU path on every host core,
+    and the same with the reference caller's model build and marshalling of
+    each point added (done per point inside each pool worker)."""
+    cp = CpuPool()
+    try:
+        sweeps = cp.sweeps_for(target_s)
+        wall = cp.run(sweeps)
+    finally:
+        cp.close()
     updates = NTEMP * sweeps * L * L
-    return {"value": updates / wall, "unit": "site_updates/s", "cores": cores, "kind": "port",
-            "sample": "%d temperatures x %d sweeps (tau=N, measurement every sweep) of XY L=%d, %s %s" % (
-                NTEMP, sweeps, L, platform.machine(), platform.processor() or ""),
-            "wall_s": wall}
+    bm = build_marshal_seconds()
+    wall_b = wall + bm * math.ceil(NTEMP / cp.cores)
+    return {"value": updates / wall, "unit": "site_updates/s", "cores": cp.cores, "kind": "port",
+            "sample": "%d temperatures x %d sweeps (tau=N, measurement every sweep) of XY L=%d on %d processes, "
+                      "%s %s" % (NTEMP, sweeps, L, cp.cores, platform.machine(), platform.processor() or ""),
+            "wall_s": wall,
+            "with_build": {"value": updates / wall_b, "unit": "site_updates/s", "wall_s": wall_b,
+                           "build_marshal_s_per_point": bm,
+                           "note": "model build + tuple marshalling per (T, H) point as the reference caller does "
+                                   "it (Lattice.py:155-284, mcMain.py:137-248), timed by this package's per-site "
+                                   "restatement of that code; one point per worker process at a time"}}
 
 
 # ---------------------------------------------------------------- our arm
@@ -186,21 +235,10 @@ def run_ours(args):
     dev_s = sum(times) / 1000.0
     value = per_step_updates * K / dev_s
     ms_per_step = sum(times) / K
-    # roofline of the Metropolis kernel the autotuner chose (one launch per step):
-    # algorithmic bytes = lattice read + written once per sweep, FP32 (x,y) = 16 B / site update
+    # roofline of the Metropolis kernel the autotuner chose (one launch per step)
     kname = {"cluster": "k_cluster_metro<2,%d>" % sched[0][2], "tiled": "k_tiled_sweep<2,SQUARE>"}.get(
         sched[0][0], "k_resident_metro<2,SQUARE>")
-    alg_bytes = 16.0 * per_step_updates
-    achieved = alg_bytes / (ms_per_step / 1000.0) / 1e9
-    traffic = issue = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.isfile(tpath):
-        try:
-            tj = json.load(open(tpath))
-            traffic = tj.get("dram_bytes_per_step")
-            issue = tj.get("sm_issue_active")
-        except Exception:
-            traffic = issue = None
+    prof = kernel_profile(kname)
     # e2e through the C ABI from host buffers
     # the step's inputs are host arrays in the reference's flattened layout
     e2e_args = workload_args(nsweep=S)
@@ -234,11 +272,19 @@ def run_ours(args):
         plain = {"value": plain_v, "unit": "site_updates/s", "sample": "4 of the 32 replicas, one solve per launch "
                  "sequence (one launch per colour, per measurement and per finalize, no graph)",
                  "batched_over_plain": value / plain_v}
+    clocks = clk.summary()
+    roof = roofline(per_step_updates, ms_per_step, hbm, prof, clocks, kname)
     cpu = cpu_baseline(args.cpu_seconds) if not args.no_cpu else None
     # the served half of the metric (after the timed region): continuous batching
     # of a Poisson request stream, p50/p99 latency and the gain over the plain engine
     served = served_stream(args) if not args.no_served else None
-    clocks = clk.summary()
+    # the other configurations, each run whole (after the timed region)
+    configs = None
+    if not args.no_configs:
+        configs = {"ising_square_L32_16T_metropolis": run_whole_solves(args, "ising", plain_sample=4),
+                   "xy_square_L128_32T_wolff": run_whole_solves(args, "xy_wolff", plain_sample=2),
+                   "pt_honeycomb_heisenberg_64x64_64T": run_pt(args),
+                   "batched_heisenberg_dmi_256_uneven": run_batched4(args)}
     line = {
         "metric": "site_updates_per_s", "value": value, "unit": "site_updates/s", "n_gpus": 1, "steps": K,
         "warmup": W, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -250,34 +296,95 @@ def run_ours(args):
                 "path": "C ABI mcs_batch_* from host arrays: create, compile+upload 32 replicas (16 host threads, "
                         "pinned staging), run, read every result back"},
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "kernel": kname, "sm_issue_active": issue,
-                     "note": "lattice is shared-memory resident inside a launch; HBM is touched once per launch, "
-                             "so the bound is SM issue (sm_issue_active: ncu issue-slot utilisation of the same "
-                             "kernel, profiles/k_cluster_metro_xy_L128x32.md)"},
+        "roofline": roof,
         "cpu_baseline": cpu,
         "plain_engine": plain,
         "served": served,
+        "configs": configs,
         "clocks": clocks,
         "wall_s_timed": wall,
     }
     print(json.dumps(line))
 
 
+KERNEL_SOURCES = ("mcs_cluster.cu", "mcs_device.cuh", "mcs_internal.h")
+
+
+def kernel_sources_sha():
+    import hashlib
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, "mcsolver_gb300", "csrc", f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
+def kernel_profile(kname):
+    """The ncu figures of the headline kernel (profiles/traffic.json): warp
+    instructions per site update and DRAM bytes per site update of one
+    captured launch, with the hash of the kernel sources they were taken on."""
+    try:
+        tj = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+    except Exception:
+        return None
+    if tj.get("kernel") != kname:
+        return None
+    tj["stale"] = tj.get("sources_sha") != kernel_sources_sha()
+    return tj
+
+
+def roofline(updates, ms, hbm, prof, clocks, kname):
+    """The bound of the headline kernel is SM instruction issue: its lattice
+    stays in shared memory for a whole launch, so DRAM carries about 1 % of
+    the algorithmic bytes.  frac = issue-slot utilisation of this run: the
+    kernel's warp instructions (ncu count per site update, from the profile
+    of the same sources) over the issue slots of the measured launch time
+    (152 SMs x 4 schedulers x the SM clock sampled during the timed steps).
+    The HBM reading (algorithmic bytes: 16 B per XY site update, the FP32
+    (x, y) pair read and written once per sweep) is given beside it."""
+    alg = 16.0 * updates
+    achieved = alg / (ms / 1000.0) / 1e9
+    hb = {"achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "algorithmic_bytes": alg,
+          "traffic": (prof["dram_bytes_per_site_update"] * updates) if prof else None,
+          "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy)"}
+    out = {"bound": "sm_issue", "kernel": kname, "hbm": hb, "traffic": hb["traffic"]}
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    if prof:
+        slots = (ms / 1000.0) * 152 * 4 * mhz * 1e6
+        used = prof["warp_instructions_per_site_update"] * updates
+        out.update({"achieved": used / slots, "peak": 1.0, "unit": "issue slots (fraction)", "frac": used / slots,
+                    "warp_instructions_per_site_update": prof["warp_instructions_per_site_update"],
+                    "ncu_issue_active": prof.get("sm_issue_active"), "profile_stale": prof["stale"]})
+    else:
+        out.update({"achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                    "note": "no profile of this kernel: HBM reading only"})
+    return out
+
+
 def run_reference(args):
+    """The reference's CPU path (the oracle's restatement of the compiled
+    library, bit-identical to it, fanned out over every host core as
+    win.startSimulation does) on the headline workload.  The process pool is
+    started once, before the timed steps; each step is one bounded sample:
+    every temperature for the same number of sweeps."""
     K, W = args.steps, args.warmup
-    vals = []
-    info = None
-    for i in range(W + K):
-        info = cpu_baseline(args.cpu_seconds / max(1, (W + K) / 3))
-        if i >= W:
-            vals.append(info["value"])
+    cp = CpuPool()
+    try:
+        sweeps = cp.sweeps_for(max(1.0, args.cpu_step_seconds))
+        vals = []
+        for i in range(W + K):
+            wall = cp.run(sweeps, seed0=1 + 100 * i)
+            if i >= W:
+                vals.append(NTEMP * sweeps * L * L / wall)
+    finally:
+        cp.close()
     v = statistics.median(vals)
+    sample = "%d temperatures x %d sweeps per step (tau=N, measurement every sweep) of XY L=%d on %d processes, " \
+             "%s %s" % (NTEMP, sweeps, L, cp.cores, platform.machine(), platform.processor() or "")
     line = {"impl": "reference", "metric": "site_updates_per_s", "value": v, "unit": "site_updates/s", "n_gpus": 1,
-            "steps": K, "warmup": W, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic", "config": base_config(args.sweeps),
-            "cpu_baseline": {"value": v, "unit": "site_updates/s", "cores": info["cores"], "kind": info["kind"],
-                             "sample": info["sample"]},
+            "steps": K, "warmup": W, "ms_per_step": NTEMP * sweeps * L * L / v * 1000.0, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": base_config(args.sweeps),
+            "cpu_baseline": {"value": v, "unit": "site_updates/s", "cores": cp.cores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "site_updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -336,7 +443,7 @@ def served_stream(args):
 
     def submit(k, t_arr):
         model, P, L = reqs[k]
-        submitted.put((srv.submit(model, P, seed=7000 + k, random_init=True), t_arr))
+        submitted.put((srv.submit(model, P, seed=7000 + k, random_init=True), t_arr, k))
 
     def dispatch(t0):
         for k in range(n):
@@ -345,7 +452,7 @@ def served_stream(args):
                 time.sleep(d)
             pool.submit(submit, k, t0 + arrivals[k])
 
-    lat, upd, pending = [], 0, {}
+    lat, upd, pending, lat_of = [], 0, {}, {}
     t0 = time.time()
     th = threading.Thread(target=dispatch, args=(t0,))
     th.start()
@@ -353,10 +460,10 @@ def served_stream(args):
     while finished < n:
         while True:
             try:
-                t, ta = submitted.get_nowait()
+                t, ta, k = submitted.get_nowait()
             except queue.Empty:
                 break
-            pending[t] = ta
+            pending[t] = (ta, k)
         if not pending:
             time.sleep(0.0005)
             continue
@@ -365,7 +472,9 @@ def served_stream(args):
         for t in list(pending):
             r = srv.poll(t)
             if r is not None:
-                lat.append(now - pending.pop(t))
+                ta, k = pending.pop(t)
+                lat.append(now - ta)
+                lat_of[k] = now - ta
                 upd += r[1]["site_updates"]
                 finished += 1
     makespan = time.time() - t0
@@ -380,8 +489,32 @@ def served_stream(args):
         u, s = _plain_rate(eng, model, P, 7000 + int(k))
         ps += u
         pt += s
+    # the same requests alone: each through a server of its own, submit to result
+    alone = {}
+    if not args.no_alone:
+        for k in range(n):
+            model, P, Lk = reqs[k]
+            s1 = eng.Server(hbm_budget_bytes=64 << 30, max_slots=4)
+            t1 = time.time()
+            tk = s1.submit(model, P, seed=7000 + k, random_init=True)
+            while s1.poll(tk) is None:
+                s1.step()
+            alone[k] = time.time() - t1
+            s1.close()
     lat = np.array(lat)
     Ls = np.array([r[2] for r in reqs])
+    sizes = np.array([r[2] ** 2 * (1 if r[0] != "heisenberg" else 1) for r in reqs], float)
+    order = np.argsort(sizes, kind="stable")
+    terciles = []
+    for j, part in enumerate(np.array_split(order, 3)):
+        lm = np.array([lat_of[k] for k in part])
+        row = {"tercile": ["small", "medium", "large"][j], "L_range": [int(Ls[part].min()), int(Ls[part].max())],
+               "requests": int(len(part)), "latency_p50_s": float(np.percentile(lm, 50)),
+               "latency_p99_s": float(np.percentile(lm, 99))}
+        if alone:
+            la = np.array([alone[k] for k in part])
+            row.update({"alone_p50_s": float(np.percentile(la, 50)), "alone_p99_s": float(np.percentile(la, 99))})
+        terciles.append(row)
     return {"workload": "served_stream", "requests": n, "rate_req_s": args.rate,
             "nthermal": args.nthermal, "nsweep": args.nsweep,
             "L_range": [int(Ls.min()), int(Ls.max())], "site_updates": int(upd),
@@ -390,7 +523,11 @@ def served_stream(args):
             "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
             "plain_site_updates_per_s": ps / pt if pt > 0 else None,
             "served_over_plain": (upd / makespan) / (ps / pt) if pt > 0 else None,
-            "plain_sample": [int(Ls[k]) for k in pick]}
+            "plain_sample": [int(Ls[k]) for k in pick],
+            "by_size": terciles,
+            "note": "latency = completion - arrival; by_size: requests split by lattice sites into terciles, with "
+                    "the same requests' latency alone (each through a server of its own: compile, upload, run, "
+                    "result)"}
 
 
 def run_batched4(args):
@@ -430,15 +567,15 @@ def run_batched4(args):
     st = bt.stats()
     bt.close()
     u, s = _plain_rate(eng, "heisenberg", jobs[2][1], 99)
-    print(json.dumps({"workload": "batched_heisenberg_dmi_256_uneven", "replicas": len(jobs), "sizes": sizes,
+    return {"workload": "batched_heisenberg_dmi_256_uneven", "replicas": len(jobs), "sizes": sizes,
                       "nthermal": args.nthermal, "nsweep": args.nsweep, "site_updates": st["site_updates"],
                       "device_ms": st["device_ms"], "wall_s": wall,
                       "site_updates_per_s": st["site_updates"] / (st["device_ms"] / 1000.0),
                       "plain_site_updates_per_s_L128": u / s,
-                      "batched_over_plain": (st["site_updates"] / (st["device_ms"] / 1000.0)) / (u / s)}))
+                      "batched_over_plain": (st["site_updates"] / (st["device_ms"] / 1000.0)) / (u / s)}
 
 
-def run_whole_solves(args):
+def run_whole_solves(args, workload=None, plain_sample=None):
     """Whole solves of one (model, lattice) over a temperature grid, all
     temperatures in one batch, against the plain engine on a sample.
     * ising:    square Ising ferromagnet (Jxx = -1), L = 32, h = 0, 16
@@ -456,7 +593,9 @@ def run_whole_solves(args):
     from mcsolver_gb300 import build as b
     from mcsolver_gb300.lattice import rescale_args, square_args_fast
     b.build()
-    if args.workload == "ising":
+    workload = workload or args.workload
+    nplain = args.plain_sample if plain_sample is None else plain_sample
+    if workload == "ising":
         model, Lw, Ts, algo, tau = "ising", 32, [1.5 + k * 2.0 / 15 for k in range(16)], 0, 0
         nth, nsw = (args.nthermal, args.nsweep) if args.override_sweeps else (2000, 10000)
     else:
@@ -477,12 +616,12 @@ def run_whole_solves(args):
     clusters = sum(r[1]["clusters"] for r in res)
     mism = sum(r[1]["exact_mismatches"] for r in res)
     ps, pt = 0, 0.0
-    for k in range(args.plain_sample):
+    for k in range(nplain):
         u, s = _plain_rate(eng, model, jobs[(k * 7) % len(jobs)], 99 + k)
         ps += u
         pt += s
     rate = st["site_updates"] / (st["device_ms"] / 1000.0)
-    print(json.dumps({"workload": "%s_square_L%d_%dT_%s" % (model, Lw, len(Ts), "wolff" if algo else "metropolis"),
+    return {"workload": "%s_square_L%d_%dT_%s" % (model, Lw, len(Ts), "wolff" if algo else "metropolis"),
                       "replicas": len(jobs), "nthermal": nth, "nsweep": nsw, "site_updates": st["site_updates"],
                       "clusters": clusters if algo else None, "device_ms": st["device_ms"], "wall_s_e2e": wall,
                       "site_updates_per_s": rate, "e2e_site_updates_per_s": st["site_updates"] / wall,
@@ -491,7 +630,7 @@ def run_whole_solves(args):
                       "schedule": [{"schedule": g[0], "ctas_per_replica": g[1], "threads": g[2], "replicas": g[3]}
                                    for g in sched],
                       "plain_site_updates_per_s": ps / pt if pt > 0 else None,
-                      "batched_over_plain": rate / (ps / pt) if pt > 0 else None}))
+                      "batched_over_plain": rate / (ps / pt) if pt > 0 else None}
 
 
 def run_noalloc(args):
@@ -566,12 +705,24 @@ def run_pt(args):
     wall = time.time() - t
     st = pt.stats()
     pt.close()
-    print(json.dumps({"workload": "pt_honeycomb_heisenberg_64x64_64T", "replicas": 64,
+    rate = st["site_updates"] / (st["device_ms"] / 1000.0)
+    # the plain engine: one temperature per solve (the reference runs every
+    # temperature on its own, win.py:440-444), host-driven launches, on a sample
+    plain = None
+    if args.plain_sample > 0:
+        ps, ptime = 0, 0.0
+        for k, T in enumerate((5.0, 15.0)):
+            u, sec = _plain_rate(eng, "heisenberg", honeycomb_args("heisenberg", 64, T, nthermal=100, nsweep=400), 50 + k)
+            ps += u
+            ptime += sec
+        plain = ps / ptime
+    return {"workload": "pt_honeycomb_heisenberg_64x64_64T", "replicas": 64,
                       "sweeps": args.pt_sweeps, "site_updates": st["site_updates"],
                       "device_ms": st["device_ms"], "wall_s": wall,
                       "site_updates_per_s": st["site_updates"] / (st["device_ms"] / 1000.0),
                       "swap_acceptance_min": float(np.min(st["swap_acceptance"])),
-                      "swap_acceptance_max": float(np.max(st["swap_acceptance"]))}))
+                      "swap_acceptance_max": float(np.max(st["swap_acceptance"])),
+                      "plain_site_updates_per_s": plain, "batched_over_plain": rate / plain if plain else None}
 
 
 def main():
@@ -583,7 +734,12 @@ def main():
     ap.add_argument("--sweeps", type=int, default=STEP_SWEEPS)
     ap.add_argument("--schedule", default="auto", choices=["auto", "resident", "tiled"],
                     help="headline workload: schedule of the replicas (auto = autotuner and load balancer)")
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="cpu_baseline sample (seconds of CPU work)")
+    ap.add_argument("--cpu-step-seconds", type=float, default=4.0,
+                    help="--impl reference: seconds of CPU work per timed step")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="headline: skip the other configurations (Ising L=32, XY Wolff, PT, uneven DMI batch)")
+    ap.add_argument("--no-alone", action="store_true", help="served: skip the requests' latency alone")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-served", action="store_true", help="headline: skip the served-stream part of the line")
@@ -602,11 +758,11 @@ def main():
     if args.workload == "served":
         return run_served(args)
     if args.workload == "batched4":
-        return run_batched4(args)
+        return print(json.dumps(run_batched4(args)))
     if args.workload == "pt":
-        return run_pt(args)
+        return print(json.dumps(run_pt(args)))
     if args.workload in ("ising", "xy_wolff"):
-        return run_whole_solves(args)
+        return print(json.dumps(run_whole_solves(args)))
     if args.workload == "noalloc":
         return run_noalloc(args)
     rank = int(os.environ.get("RANK", "0"))
@@ -636,12 +792,15 @@ def combine_ranks(t_local: float, work_local: float, dist, device):
     return tt.item(), ww.item()
 
 
-def multi_line(work_total: float, tmax: float, n: int, K: int, W: int, S: int, launches: int):
+def multi_line(work_total: float, tmax: float, n: int, K: int, W: int, S: int, launches: int, clocks=None,
+               e2e=None):
     return {"metric": "site_updates_per_s", "value": work_total / tmax, "unit": "site_updates/s",
             "n_gpus": n, "steps": K, "warmup": W, "ms_per_step": tmax * 1000 / K,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 update / f64 accumulate", "data": "synthetic", "gpu_launches": launches,
-            "config": dict(base_config(S), parallelism="replicas only (%d independent copies)" % n)}
+            "config": dict(base_config(S), parallelism="replicas only (%d independent copies)" % n,
+                           l2="flushed between steps (256 MB write)"),
+            "clocks": clocks, "e2e": e2e}
 
 
 def run_multi(args):
@@ -668,13 +827,35 @@ def run_multi(args):
     l0 = batch.stats()["launches"]
     dist.barrier()
     torch.cuda.synchronize()
-    t = sum(batch.advance(S) for _ in range(K)) / 1000.0
+    t = 0.0
+    with ClockSampler(local) as clk:
+        for _ in range(K):
+            l2_flush()
+            t += batch.advance(S) / 1000.0
     torch.cuda.synchronize()
     launches = batch.stats()["launches"] - l0
     batch.close()
     tmax, work = combine_ranks(t, float(NTEMP * L * L * S * K), dist, "cuda")
+    # end to end on every rank: create, compile + upload, run, read back, from host arrays
+    problems = [eng.Problem("xy", a) for a in workload_args(nsweep=S)]
+    dist.barrier()
+    te = time.time()
+    bb = eng.Batch(device=local)
+    for k, P in enumerate(problems):
+        bb.add("xy", P, seed=seeds[k] + 50000, random_init=True)
+    bb.run()
+    for i in range(NTEMP):
+        bb.result(i)
+    te = time.time() - te
+    mem = bb.memory()
+    bb.close()
+    temax, _ = combine_ranks(te, 0.0, dist, "cuda")
+    e2e = {"value": NTEMP * L * L * S * dist.get_world_size() / temax, "unit": "site_updates/s",
+           "h2d_bytes_per_step": mem["device_bytes"] * dist.get_world_size(),
+           "d2h_bytes_per_step": mem["readback_bytes"] * dist.get_world_size(),
+           "path": "C ABI mcs_batch_* from host arrays on every rank (slowest rank)"}
     if dist.get_rank() == 0:
-        print(json.dumps(multi_line(work, tmax, dist.get_world_size(), K, W, S, launches)))
+        print(json.dumps(multi_line(work, tmax, dist.get_world_size(), K, W, S, launches, clk.summary(), e2e)))
     dist.destroy_process_group()
 
 

@@ -38,6 +38,8 @@ extern "C" {
 #define MCS_EUNSUPPORTED 5 /* model outside what the engine implements        */
 #define MCS_EBUSY 6        /* server: no free slot (try again)                */
 #define MCS_ENOTFOUND 7    /* server: unknown ticket                          */
+#define MCS_ECANCELLED 8   /* server: the request was cancelled               */
+#define MCS_EFAILED 9      /* server: the request failed while it ran         */
 
 #define MCS_ISING 1
 #define MCS_XY 2
@@ -179,12 +181,25 @@ int mcs_server_create(int32_t device, uint64_t hbm_budget_bytes, int32_t max_slo
  * Admission happens in mcs_server_step when slots and memory allow.
  * submit, poll and stats may run on any threads concurrently with step. */
 int mcs_server_submit(mcs_server *s, const mcs_problem *problem, const mcs_options *options, uint64_t *ticket);
-/* Advance the device by one tick (admit, run a chunk of sweeps on every active
- * slot, stopping at the next completion, retire finished ones).  *completed
- * receives the number of requests completed.  One step at a time. */
+/* Advance the device by one tick: retire cancelled requests, admit queued
+ * ones, advance every active request by its own quota of units (about the
+ * same device time per request and step, MCSGPU_SERVER_STEP_US, default
+ * 4000 us: small lattices run many sweeps per step, large ones few), retire
+ * finished ones.  *completed receives the number of requests completed.  One
+ * step at a time.  A request that fails is retired with its own status (see
+ * mcs_server_poll) and the others go on; the step itself returns an error only
+ * when the device context is lost, and then every active request has failed. */
 int mcs_server_step(mcs_server *s, int32_t *completed);
-/* 0 = done (result filled, ticket released), 1 = pending. */
+/* 0 = done (result filled, ticket released), 1 = pending; a request that
+ * failed or was cancelled returns its own status (MCS_ENOMEM, MCS_ECUDA,
+ * MCS_ECANCELLED, MCS_EFAILED ...; never 1), releases the ticket and leaves its
+ * message in mcs_last_error(); MCS_ENOTFOUND for an unknown ticket. */
 int mcs_server_poll(mcs_server *s, uint64_t ticket, mcs_result *result);
+/* Cancel a queued or active request (no counterpart in the reference, whose
+ * solves cannot be stopped): a queued one is released at once, an active one
+ * at the start of the next step; its poll then returns MCS_ECANCELLED.  A
+ * request that already finished keeps its result (MCS_OK). */
+int mcs_server_cancel(mcs_server *s, uint64_t ticket);
 int mcs_server_stats(mcs_server *s, int32_t *active, int32_t *queued, uint64_t *bytes_in_use, int64_t *site_updates);
 void mcs_server_destroy(mcs_server *s);
 
@@ -205,10 +220,14 @@ void mcs_server_destroy(mcs_server *s);
  * mcs_solve() produces for the same lattice, couplings and seed.
  * Scratch: a fixed 64 KiB array in device memory owned by the library (held by
  * every GPU that loads it until exit), which limits the lattice to 8,388,608
- * sites (larger lattices are rejected with MCS_EINVAL).  The first call on a
- * device looks up that array's address; make it before any stream capture.
- * Calls that overlap on the GPU share the array and race: issue them on one
- * stream, one after the other.  Lx, Ly even and >= 4. */
+ * sites (larger lattices are rejected with MCS_EINVAL).  Every call looks up
+ * that array's address on the current device; the first call on a device
+ * (and the first after a device reset) also loads the library's kernels,
+ * which takes some device memory for the module: make that call before
+ * reserving the device's memory or beginning a stream capture.  `stream`
+ * must belong to the current device (MCS_EINVAL otherwise).  Calls that
+ * overlap on the GPU share the array and race: issue them on one stream, one
+ * after the other.  Lx, Ly even and >= 4. */
 int mcs_ising_square_noalloc(int8_t *d_sigma, int32_t Lx, int32_t Ly, double K, double h, uint64_t seed,
                              int64_t sweep0, int32_t nsweeps, int64_t *d_sums, void *stream);
 

@@ -87,8 +87,11 @@ ABI_FUNCTIONS = [
     "mcs_batch_result", "mcs_batch_stats", "mcs_batch_memory", "mcs_batch_schedule", "mcs_batch_destroy",
     "mcs_pt_create", "mcs_pt_run", "mcs_pt_result", "mcs_pt_stats", "mcs_pt_destroy",
     "mcs_server_create", "mcs_server_submit", "mcs_server_step", "mcs_server_poll", "mcs_server_stats",
-    "mcs_server_destroy", "mcs_ising_square_noalloc",
+    "mcs_server_cancel", "mcs_server_destroy", "mcs_ising_square_noalloc",
 ]
+
+# status codes (include/mcsgpu.h)
+MCS_ENOMEM, MCS_ECUDA, MCS_ENOTFOUND, MCS_ECANCELLED, MCS_EFAILED = 4, 2, 7, 8, 9
 
 
 def lib():
@@ -127,6 +130,7 @@ def lib():
         L.mcs_server_poll.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(McsResult)]
         L.mcs_server_stats.argtypes = [ctypes.c_void_p, _i32p, _i32p, ctypes.POINTER(ctypes.c_uint64),
                                        ctypes.POINTER(ctypes.c_int64)]
+        L.mcs_server_cancel.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
         L.mcs_server_destroy.argtypes = [ctypes.c_void_p]
         L.mcs_server_destroy.restype = None
         L.mcs_ising_square_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
@@ -430,17 +434,27 @@ class Server:
         return n.value
 
     def poll(self, ticket: int):
-        """The result tuple and extras when done, else None."""
-        P = self._problems[ticket]
-        rb = _ResultBuf(P, False)
-        rb.r.frames = None
-        rc = lib().mcs_server_poll(self._h, ticket, ctypes.byref(rb.r))
+        """The result tuple and extras when done, else None.  A request that
+        failed or was cancelled raises EngineError with its own status code
+        (``code``: MCS_ECANCELLED, MCS_ENOMEM, MCS_ECUDA, ...) and is released."""
+        P = self._problems.get(ticket)
+        rb = _ResultBuf(P, False) if P is not None else None
+        if rb is not None:
+            rb.r.frames = None
+        rc = lib().mcs_server_poll(self._h, ticket, ctypes.byref(rb.r) if rb is not None else None)
         if rc == 1:
             return None
-        _check(rc)
+        if rc != 0:
+            self._problems.pop(ticket, None)
+            _check(rc)
         del self._problems[ticket]
         P.frames = 0
         return rb.unpack(P)
+
+    def cancel(self, ticket: int) -> None:
+        """Cancel a queued or active request; its poll then raises with
+        code MCS_ECANCELLED (a finished request keeps its result)."""
+        _check(lib().mcs_server_cancel(self._h, ticket))
 
     def stats(self):
         a = ctypes.c_int32()

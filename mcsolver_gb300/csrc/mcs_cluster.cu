@@ -144,12 +144,16 @@ __device__ __forceinline__ int cl_frame_src(int f, int ngroup, int gall)
 // cluster in fixed rank order into one ring entry (FP64), and write the
 // measurement's frame in FP32: frame entry f takes slot entry fsrc[f] (a table
 // of cl_frame_src made once per launch), passed between lanes by a shuffle.
+// The last two entries (re-check flag, measurement index) are the same in
+// every CTA and are taken from rank 0's slot, not summed.
 __device__ __forceinline__ void cluster_gather(double *part, double *entry, float *frame, const signed char *fsrc,
                                                int C, int slot, int lane)
 {
     cg::cluster_group cl = cg::this_cluster();
     double o = 0.0;
-    for (int q = 0; q < C; ++q) o += cl.map_shared_rank(part, q)[slot * CL_SLOT + lane];
+    if (lane >= CL_NV + 2) o = part[slot * CL_SLOT + lane];
+    else
+        for (int q = 0; q < C; ++q) o += cl.map_shared_rank(part, q)[slot * CL_SLOT + lane];
     entry[lane] = o;
     const float of = (float)o;
     for (int f = lane; f - lane < F_NON; f += 32) {  // the bound is the same for every lane
@@ -202,7 +206,7 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
     }
     __syncthreads();
     // every CTA of the cluster reads the same descriptor: the early exit is uniform over the cluster
-    if (R.u >= R.units_total) return;
+    if (R.u >= R.u_stop) return;
     const ClusterLayout L = cluster_layout(R, C);
     const int tid = threadIdx.x, bd = blockDim.x;
     const int hy = L.hy, rows = L.rows, nloc = L.nloc;
@@ -541,13 +545,12 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
         nacc = 0;
         // spin frame: every CTA writes its own rows
         if (R.frames > 0 && (m % R.frame_every) == 0 && fw < R.frames) {
-            float *fb = R.frame_buf + (size_t)fw * R.N * 3;
             for (int c = 0; c < 2; ++c)
                 for (int kk = tid; kk < nown; kk += bd) {
                     const int xl = kk / hy, yh = kk - xl * hy;
                     const int li = c * rows * hy + (xl + 1) * hy + yh;
                     const int v = c * half + (x0 + xl) * hy + yh;
-                    fb[3 * v] = S.x[li]; fb[3 * v + 1] = S.y[li]; fb[3 * v + 2] = DIM == 3 ? S.z[li] : 0.f;
+                    frame_store<DIM>(R, fw, v, S, li);
                 }
             ++fw;
         }
@@ -564,7 +567,7 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
     // ghosts, so one cluster barrier per colour both publishes the pushes and
     // orders them before the next phase's reads.
     long long u = R.u;
-    const long long uend = min(R.units_total, u + max_units);
+    const long long uend = min(R.u_stop, u + max_units);
     const SqLinks sql = {R.Ly, hy, rows, R.sq_code[0], R.sq_code[1], R.sq_code[2], R.sq_code[3]};
     const TrialFlags tflags = {R.fullJ != 0, R.has_d != 0};
     for (; u < uend; ++u) {

@@ -651,7 +651,7 @@ __device__ void on_accumulate_lanes(Rep &R, const double *F, double E, long long
             acc[A_MTOT] += M;
             acc[A_MDM] += acc[A_MPREV] * M;
             acc[A_MPREV] = M;
-            if (R.series) {
+            if (R.series && m < R.nsweep) {
                 double *sr = R.series + (size_t)m * MCS_NSER;
                 const double e = E * R.inv_N;
                 sr[0] = e; sr[1] = M; sr[2] = (F[F_ERB] * 0.5 + F[F_ERO]) * R.inv_nr; sr[3] = F[F_SIJ] * inl;
@@ -766,7 +766,7 @@ __device__ void on_accumulate_frames(Rep &R, float *fs, const double *E, long lo
         val[A_ER] = er;
         val[A_ER2] = er * er;
         val[A_Q] = DIM == 3 ? f[F_Q] * (float)(1.0 / (MCS_PI_REF * 4)) : 0.f;
-        if (R.series) {
+        if (R.series && m0 + lane < R.nsweep) {
             double *sr = R.series + (size_t)(m0 + lane) * MCS_NSER;
             sr[0] = e; sr[1] = M; sr[2] = er; sr[3] = val[A_SIJ];
         }
@@ -1092,9 +1092,26 @@ __device__ inline void is_accumulate(Rep &R, const double *Fd, const long long *
     acc[B_ER] += er;
     acc[B_E2] += e * e;
     acc[B_ER2] += er * er;
-    if (R.series) {
+    if (R.series && m < R.nsweep) {
         double *s = R.series + (size_t)m * MCS_NSER;
         s[0] = e; s[1] = M; s[2] = er; s[3] = Fd[2] * R.inv_nl;
+    }
+}
+
+// Spin frame `fw`, site v (sweep index) from local index li of S: Ising signs
+// as int8 ([N] per frame), O(n) components as FP32 ([N][dim] per frame), stored
+// straight into the replica's page-locked host buffer (mapped into the device),
+// so a snapshot leaves the device as it is taken and holds no device memory.
+template <int DIM>
+__device__ __forceinline__ void frame_store(const Rep &R, int fw, int v, const Spins &S, int li)
+{
+    if (DIM == 1) {
+        ((signed char *)R.frame_buf)[(size_t)fw * R.N + v] = S.s[li];
+    } else {
+        float *fb = (float *)R.frame_buf + ((size_t)fw * R.N + v) * DIM;
+        fb[0] = S.x[li];
+        fb[1] = S.y[li];
+        if (DIM == 3) fb[2] = S.z[li];
     }
 }
 

@@ -102,6 +102,7 @@ Replica::~Replica()
         cudaSetDevice(device);
         cudaFreeAsync(arena, 0);
     }
+    if (frames_host) cudaFreeHost(frames_host);
 }
 
 size_t replica_acc_count(const HostModel &m)
@@ -156,8 +157,8 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool u
     size_t o_stats = A.add(nullptr, S_NSTAT * sizeof(long long));
     size_t o_series = 0;
     if (r->record_series) o_series = A.add(nullptr, (size_t)m.nsweep * MCS_NSER * sizeof(double));
-    size_t o_frames = 0;
-    if (m.frames > 0) o_frames = A.add(nullptr, (size_t)m.frames * m.N * 3 * sizeof(float));
+    // spin frames live in page-locked host memory (upload_replica), not in the arena
+    r->frames_bytes = m.frames > 0 ? (size_t)m.frames * m.N * (m.dim == 1 ? 1 : m.dim * sizeof(float)) : 0;
     size_t o_wbits = 0, o_wq = 0;
     if (m.alg == 1) {
         o_wbits = A.add(nullptr, ((size_t)(m.N + 31) / 32) * sizeof(unsigned));
@@ -239,13 +240,14 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool u
     R.spins = P(o_spins); R.spad = spad;
     R.acc = (double *)P(o_acc);
     R.series = r->record_series ? (double *)P(o_series) : nullptr;
-    R.frame_buf = m.frames > 0 ? (float *)P(o_frames) : nullptr;
+    R.frame_buf = nullptr;  // set by upload_replica
     R.icnt = (long long *)P(o_icnt);
     R.stats = (long long *)P(o_stats);
     if (m.alg == 1) { R.wbits = (unsigned *)P(o_wbits); R.wqueue = (int *)P(o_wq); }
     R.u0 = 0; R.u = 0; R.m = 0;
+    R.u_stop = m.units_total; R.quota = 0;
     r->acc_off = o_acc; r->icnt_off = o_icnt; r->stats_off = o_stats; r->series_off = o_series;
-    r->frames_off = o_frames; r->spins_off = o_spins;
+    r->spins_off = o_spins;
     r->nacc = nacc;
     r->staging = A.finish();
     if (upload) return upload_replica(r);
@@ -288,8 +290,17 @@ int upload_replica(Replica *r)
     RELOC(nbr); RELOC(lcode); RELOC(lcls); RELOC(deg); RELOC(stype); RELOC(jtab); RELOC(jtab64); RELOC(dtab);
     RELOC(itab); RELOC(cpair); RELOC(rorb); RELOC(rcl); RELOC(rlink); RELOC(rjc); RELOC(rK); RELOC(rkc);
     RELOC(rdeg); RELOC(rindex); RELOC(circ); RELOC(slen); RELOC(sval); RELOC(gmask); RELOC(sflag); RELOC(rtgt);
-    RELOC(spins); RELOC(acc); RELOC(series); RELOC(frame_buf); RELOC(icnt); RELOC(stats); RELOC(wbits); RELOC(wqueue);
+    RELOC(spins); RELOC(acc); RELOC(series); RELOC(icnt); RELOC(stats); RELOC(wbits); RELOC(wqueue);
 #undef RELOC
+    // spin frames: kernels store each snapshot straight into page-locked host
+    // memory mapped into the device, so frames take no device memory and need
+    // no copy at the end
+    if (r->frames_bytes > 0 && !r->frames_host) {
+        CUDA_TRY(cudaHostAlloc(&r->frames_host, r->frames_bytes, cudaHostAllocMapped | cudaHostAllocPortable));
+        void *dp = nullptr;
+        CUDA_TRY(cudaHostGetDevicePointer(&dp, r->frames_host, 0));
+        R.frame_buf = dp;
+    }
     std::vector<unsigned char>().swap(r->staging);
     return MCS_OK;
 }
@@ -387,14 +398,29 @@ int replica_results(Replica *r, const Rep &Rfinal, mcs_result *res)
         res->energy_drift = acc[A_DRIFT];
     }
     res->frames_written = 0;
-    if (fr && m.frames > 0) {
-        int nf = Rfinal.frames_written;
-        std::vector<float> buf((size_t)nf * m.N * 3);
-        if (nf > 0)
-            CUDA_TRY(cudaMemcpy(buf.data(), b + r->frames_off, buf.size() * sizeof(float), cudaMemcpyDeviceToHost));
-        for (int f = 0; f < nf; ++f)
-            for (int i = 0; i < m.N; ++i)
-                for (int c = 0; c < 3; ++c) fr[((size_t)f * m.N + i) * 3 + c] = buf[((size_t)f * m.N + m.pos[i]) * 3 + c];
+    if (fr && m.frames > 0 && r->frames_host) {
+        // the kernels stored the frames in sweep-index order (Ising: signs;
+        // O(n): dim components); the reference's order and layout are site id
+        // order with three components
+        const int nf = std::min(Rfinal.frames_written, m.frames), N = m.N;
+        for (int f = 0; f < nf; ++f) {
+            float *o = fr + (size_t)f * N * 3;
+            if (m.dim == 1) {
+                const signed char *sb = (const signed char *)r->frames_host + (size_t)f * N;
+                for (int i = 0; i < N; ++i) {
+                    const int k = m.pos[i];
+                    o[3 * i] = (float)(fabs(m.sval[k]) * sb[k]);
+                    o[3 * i + 1] = 0.f;
+                    o[3 * i + 2] = 0.f;
+                }
+            } else {
+                const float *fb = (const float *)r->frames_host + (size_t)f * N * m.dim;
+                for (int i = 0; i < N; ++i) {
+                    const int k = m.pos[i];
+                    for (int c = 0; c < 3; ++c) o[3 * i + c] = c < m.dim ? fb[(size_t)k * m.dim + c] : 0.f;
+                }
+            }
+        }
         res->frames_written = nf;
     }
     if (ser && r->record_series)
@@ -453,7 +479,7 @@ Batch::~Batch()
     for (cudaStream_t g : gstreams) cudaStreamSynchronize(g);
     groups.clear();
     if (d_reps) cudaFree(d_reps);
-    if (d_all) cudaFree(d_all);
+    if (d_active) cudaFree(d_active);
     if (d_scratch) cudaFree(d_scratch);
     if (stream) cudaStreamDestroy(stream);
     if (stream2) cudaStreamDestroy(stream2);
@@ -546,6 +572,7 @@ Group::~Group()
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     for (void *p : bufs) cudaFree(p);
+    if (d_ids) cudaFree(d_ids);
 }
 
 int Batch::setup_tiled(Group &G)
@@ -642,7 +669,7 @@ cudaError_t Batch::tiled_unit(Group &G, cudaStream_t s, long long *nl)
 // 4 -> 8 -> tiled; resident -> tiled where the cluster kernel does not apply)
 // while the estimate falls.  With the autotuner on, cluster sizes stay the
 // autotuner's choice and only the move to tiled is decided here.
-void Batch::place_replicas(int max_smem)
+void Batch::place_replicas(int max_smem, const std::vector<int> &ids, double base_crit, double base_smsec)
 {
     int nsm = 0;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || nsm < 1) {
@@ -655,7 +682,7 @@ void Batch::place_replicas(int max_smem)
     const double e = 0.8;
     struct P { int i; int opt; double c; std::vector<int> opts; };
     std::vector<P> ps;
-    for (int i = 0; i < (int)replicas.size(); ++i) {
+    for (int i : ids) {
         Replica &r = *replicas[i];
         r.pref_C = 0;
         if (r.requested_schedule != 0 || r.hm.alg != 0 || !(r.schedule == 2 || r.schedule == 6)) continue;
@@ -702,7 +729,7 @@ void Batch::place_replicas(int max_smem)
         for (int d = 0; d < 4; ++d) tiled_sites[d] = 0;
         for (auto &q : ps)
             if (q.opts[q.opt] == 0) tiled_sites[replicas[q.i]->hm.dim] += replicas[q.i]->hm.N;
-        double m = 0, t = 0;
+        double m = base_crit, t = base_smsec;
         for (auto &q : ps) { m = std::max(m, crit(q)); t += smsec(q); }
         return std::max(m, t / nsm);
     };
@@ -735,77 +762,140 @@ void Batch::place_replicas(int max_smem)
     }
 }
 
-int Batch::prepare()
+// Kernel family of each replica of `ids` (and, with the balancer on, the
+// placement among resident, cluster and tiled schedules).
+void Batch::assign_schedules(const std::vector<int> &ids, int max_smem)
 {
-    if (prepared) return MCS_OK;
-    cudaGetLastError();  // a failed call of an earlier batch must not be reported here
-    int src = ensure_streams();
-    if (src != MCS_OK) return src;
-    const int nrep = (int)replicas.size();
-    if (nrep == 0) { prepared = true; return MCS_OK; }
+    for (int i : ids) {
+        Replica &r = *replicas[i];
+        r.schedule = choose_schedule(r, cluster_override > 1 ? 6 : r.requested_schedule, max_smem);
+    }
+    if (!balance) return;
+    // replicas already running (slot mode) count as load the new ones share the
+    // device with: their longest remaining critical path and SM-seconds on
+    // their schedules (rates as in place_replicas)
+    static const double r_cta[4] = {0, 0.40e9, 0.85e9, 0.65e9};
+    std::vector<char> is_new(replicas.size(), 0);
+    for (int i : ids) is_new[i] = 1;
+    double base_crit = 0, base_smsec = 0;
+    for (size_t i = 0; i < replicas.size(); ++i) {
+        const Replica *r = replicas[i].get();
+        if (!r || is_new[i]) continue;
+        const double c = (double)r->hm.N * (double)std::max<long long>(0, r->hm.units_total - r->rep.u);
+        const double rc = r_cta[r->hm.dim];
+        if (r->schedule == 6) {
+            base_crit = std::max(base_crit, c / (0.8 * std::max(1, r->pref_C) * rc));
+            base_smsec += c / (0.8 * rc);
+        } else if (r->schedule == 3) {
+            base_smsec += c / (0.8 * rc);
+        } else {
+            base_crit = std::max(base_crit, c / rc);
+            base_smsec += c / rc;
+        }
+    }
+    place_replicas(max_smem, ids, base_crit, base_smsec);
+}
+
+// Initial energies / exact sums (and random initial states) of the replicas of
+// `ids` not yet initialised; their descriptors are on the device.
+int Batch::init_states(const std::vector<int> &ids)
+{
+    std::vector<int> all;
+    for (int i : ids)
+        if (!replicas[i]->initialized) all.push_back(i);
+    if (all.empty()) return MCS_OK;
+    int *d = nullptr;
+    CUDA_TRY(cudaMallocAsync((void **)&d, all.size() * sizeof(int), stream));
+    CUDA_TRY(cudaMemcpyAsync(d, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
+    for (int dd = 1; dd <= 3; ++dd)
+        for (int g = 0; g <= 1; ++g) {
+            bool any = false;
+            for (int i : all) any |= (replicas[i]->hm.dim == dd && replicas[i]->hm.geom == g);
+            if (!any) continue;
+            cudaError_t e = launch_init_state_dg(dd, g, d_reps, d, (int)all.size(), stream);
+            if (e != cudaSuccess) {
+                cudaFreeAsync(d, stream);
+                set_error(std::string("initial state: ") + cudaGetErrorString(e));
+                return MCS_ECUDA;
+            }
+            launches++;
+        }
+    CUDA_TRY(cudaFreeAsync(d, stream));
+    for (int i : all) replicas[i]->initialized = true;
+    return MCS_OK;
+}
+
+// Device copy of a group's replica indices (reallocated when it grows).
+int Batch::upload_ids(Group &G)
+{
+    if ((int)G.ids.size() > G.ids_cap) {
+        if (G.d_ids) cudaFree(G.d_ids);
+        G.d_ids = nullptr;
+        G.ids_cap = 0;
+        const int cap = std::max<int>(4, (int)G.ids.size() * 2);
+        CUDA_TRY(cudaMalloc(&G.d_ids, cap * sizeof(int)));
+        G.ids_cap = cap;
+    }
+    if (!G.ids.empty())
+        CUDA_TRY(cudaMemcpy(G.d_ids, G.ids.data(), G.ids.size() * sizeof(int), cudaMemcpyHostToDevice));
+    return MCS_OK;
+}
+
+// A tiled group whose membership changed: new tile lists, partial-sum
+// buffers and graph.
+int Batch::reset_tiled(Group &G)
+{
+    if (G.exec) cudaGraphExecDestroy(G.exec);
+    if (G.graph) cudaGraphDestroy(G.graph);
+    G.exec = nullptr;
+    G.graph = nullptr;
+    for (void *q : G.bufs) cudaFree(q);
+    G.bufs.clear();
+    G.cofs.clear();
+    G.ccount.clear();
+    G.maxcol = 0;
+    G.nmeas = 0;
+    G.K = 0;
+    G.per_graph = 0;
+    return setup_tiled(G);
+}
+
+// Groups for the replicas of `ids` (each joins exactly one; a cluster group
+// that falls back to the tiled schedule keeps its replicas).  With `merge`,
+// a set whose launch configuration equals that of an existing group joins it
+// instead of forming a new one (the server admits a few requests at a time).
+int Batch::build_groups(const std::vector<int> &ids, bool merge)
+{
     const int max_smem = resident_max_smem();
     int nsm_ = 0;
     if (cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
         cudaGetLastError();
         nsm_ = 1;
     }
-    if (const char *e = getenv("MCSGPU_CLUSTER")) cluster_override = atoi(e);
-    if (const char *e = getenv("MCSGPU_NO_AUTOTUNE")) no_autotune = atoi(e);
-    std::vector<Rep> host(nrep);
-    for (int i = 0; i < nrep; ++i) {
-        Replica &r = *replicas[i];
-        r.schedule = choose_schedule(r, cluster_override > 1 ? 6 : r.requested_schedule, max_smem);
-    }
-    if (balance) place_replicas(max_smem);
-    for (int i = 0; i < nrep; ++i) host[i] = replicas[i]->rep;
-    CUDA_TRY(cudaMalloc(&d_reps, nrep * sizeof(Rep)));
-    CUDA_TRY(cudaMemcpy(d_reps, host.data(), nrep * sizeof(Rep), cudaMemcpyHostToDevice));
-    // initial energies / exact sums
-    {
-        std::vector<int> all;
-        for (int i = 0; i < nrep; ++i)
-            if (!replicas[i]->initialized) all.push_back(i);
-        CUDA_TRY(cudaMalloc(&d_all, std::max<size_t>(1, all.size()) * sizeof(int)));
-        if (!all.empty()) CUDA_TRY(cudaMemcpy(d_all, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice));
-        for (int d = 1; d <= 3 && !all.empty(); ++d)
-            for (int g = 0; g <= 1; ++g) {
-                bool any = false;
-                for (int i : all) any |= (replicas[i]->hm.dim == d && replicas[i]->hm.geom == g);
-                if (!any) continue;
-                CUDA_TRY(launch_init_state_dg(d, g, d_reps, d_all, (int)all.size(), stream));
-                launches++;
-            }
-        for (int i : all) replicas[i]->initialized = true;
-    }
-    // groups; every replica joins exactly one (a cluster group that falls
-    // back to the tiled schedule keeps its replicas)
-    std::vector<char> grouped(nrep, 0);
+    std::vector<char> grouped(replicas.size(), 0);
     for (int kind : {2, 6, 3, 1, 4, 5})
         for (int d = 1; d <= 3; ++d)
             for (int g = 0; g <= 1; ++g) {
-                std::vector<int> ids;
-                for (int i = 0; i < nrep; ++i) {
+                std::vector<int> sel;
+                for (int i : ids) {
                     Replica &r = *replicas[i];
-                    if (!grouped[i] && r.schedule == kind && r.hm.dim == d && r.hm.geom == g) ids.push_back(i);
+                    if (!grouped[i] && r.schedule == kind && r.hm.dim == d && r.hm.geom == g) sel.push_back(i);
                 }
-                for (int i : ids) grouped[i] = 1;
-                if (ids.empty()) continue;
+                for (int i : sel) grouped[i] = 1;
+                if (sel.empty()) continue;
                 std::vector<std::vector<int>> sets;
-                if (kind == 1) for (int id : ids) sets.push_back({id});
+                if (kind == 1) for (int id : sel) sets.push_back({id});
                 else if (kind == 6) {
                     // one launch configuration per group: split by the balancer's cluster size
                     for (int C : {0, 2, 4, 8, 16}) {
                         std::vector<int> sub;
-                        for (int id : ids) if (replicas[id]->pref_C == C) sub.push_back(id);
+                        for (int id : sel) if (replicas[id]->pref_C == C) sub.push_back(id);
                         if (!sub.empty()) sets.push_back(sub);
                     }
-                } else sets.push_back(ids);
+                } else sets.push_back(sel);
                 for (auto &set : sets) {
                     std::unique_ptr<Group> G(new Group());
                     G->kind = kind; G->dim = d; G->geom = g; G->ids = set;
-                    CUDA_TRY(cudaMalloc(&G->d_ids, set.size() * sizeof(int)));
-                    G->bufs.push_back(G->d_ids);
-                    CUDA_TRY(cudaMemcpy(G->d_ids, set.data(), set.size() * sizeof(int), cudaMemcpyHostToDevice));
                     long long maxn = 0;
                     int maxcs = 0;
                     for (int id : set) {
@@ -877,33 +967,152 @@ int Batch::prepare()
                             // no cluster size fits: run these replicas on the tiled schedule
                             G->kind = 3;
                             for (int id : set) replicas[id]->schedule = 3;
-                            int rc = setup_tiled(*G);
+                        } else {
+                            if (G->candidates.empty()) G->candidates.push_back({0, G->threads});
+                            // MCSGPU_FORCE=C:threads keeps only that candidate when the group has it
+                            // (tests run every configuration of a group this way)
+                            if (const char *e = getenv("MCSGPU_FORCE")) {
+                                int fc = 0, ft = 0;
+                                if (sscanf(e, "%d:%d", &fc, &ft) == 2)
+                                    for (auto &cand : G->candidates)
+                                        if (cand.first == fc && cand.second == ft) { G->candidates = {cand}; break; }
+                            }
+                            if (G->candidates.size() == 1 || no_autotune) {
+                                // without the autotuner: the first candidate, except that a
+                                // resident group runs the one-CTA cluster kernel when it can
+                                size_t pick = 0;
+                                for (size_t ci = 0; ci < G->candidates.size() && kind == 2; ++ci)
+                                    if (G->candidates[ci].first == 1) { pick = ci; break; }
+                                G->C = G->candidates[pick].first;
+                                G->threads = G->candidates[pick].second;
+                                G->tuned = 1;
+                            }
+                        }
+                    }
+                    if (merge) {
+                        // an existing group of the same launch configuration takes the set
+                        Group *H = nullptr;
+                        for (auto &q : groups) {
+                            if (q->kind != G->kind || q->dim != d || q->geom != g || q->kind == 1) continue;
+                            if (q->kind == 2 || q->kind == 6) {
+                                if (!q->tuned || !G->tuned || q->C != G->C || q->threads != G->threads) continue;
+                            }
+                            H = q.get();
+                            break;
+                        }
+                        if (H) {
+                            H->ids.insert(H->ids.end(), set.begin(), set.end());
+                            H->max_units = std::max(H->max_units, G->max_units);
+                            H->smem = std::max(H->smem, G->smem);
+                            H->chunk = std::min(H->chunk, G->chunk);
+                            int rc = upload_ids(*H);
+                            if (rc == MCS_OK && (H->kind == 3 || H->kind == 1)) rc = reset_tiled(*H);
                             if (rc != MCS_OK) return rc;
-                            groups.push_back(std::move(G));
                             continue;
                         }
-                        if (G->candidates.empty()) G->candidates.push_back({0, G->threads});
-                        if (G->candidates.size() == 1 || no_autotune) {
-                            // without the autotuner: the first candidate, except that a
-                            // resident group runs the one-CTA cluster kernel when it can
-                            size_t pick = 0;
-                            for (size_t ci = 0; ci < G->candidates.size() && kind == 2; ++ci)
-                                if (G->candidates[ci].first == 1) { pick = ci; break; }
-                            G->C = G->candidates[pick].first;
-                            G->threads = G->candidates[pick].second;
-                            G->tuned = 1;
-                        }
-                    } else {
-                        int rc = setup_tiled(*G);
+                    }
+                    int rc = upload_ids(*G);
+                    if (rc != MCS_OK) return rc;
+                    if (G->kind == 3 || G->kind == 1) {
+                        rc = setup_tiled(*G);
                         if (rc != MCS_OK) return rc;
                     }
                     groups.push_back(std::move(G));
                 }
             }
-    for (int i = 0; i < nrep; ++i)
+    for (int i : ids)
         if (!grouped[i]) { set_error("internal: replica without a kernel group"); return MCS_EINVAL; }
+    return MCS_OK;
+}
+
+int Batch::setup_device()
+{
+    cudaGetLastError();  // a failed call of an earlier batch must not be reported here
+    int src = ensure_streams();
+    if (src != MCS_OK) return src;
+    if (const char *e = getenv("MCSGPU_CLUSTER")) cluster_override = atoi(e);
+    if (const char *e = getenv("MCSGPU_NO_AUTOTUNE")) no_autotune = atoi(e);
+    return MCS_OK;
+}
+
+int Batch::prepare()
+{
+    if (prepared) return MCS_OK;
+    int rc = setup_device();
+    if (rc != MCS_OK) return rc;
+    const int nrep = (int)replicas.size();
+    if (nrep == 0) { prepared = true; return MCS_OK; }
+    std::vector<int> ids(nrep);
+    for (int i = 0; i < nrep; ++i) ids[i] = i;
+    assign_schedules(ids, resident_max_smem());
+    std::vector<Rep> host(nrep);
+    for (int i = 0; i < nrep; ++i) host[i] = replicas[i]->rep;
+    CUDA_TRY(cudaMalloc(&d_reps, nrep * sizeof(Rep)));
+    CUDA_TRY(cudaMemcpy(d_reps, host.data(), nrep * sizeof(Rep), cudaMemcpyHostToDevice));
+    rc = init_states(ids);
+    if (rc != MCS_OK) return rc;
+    rc = build_groups(ids, false);
+    if (rc != MCS_OK) return rc;
     prepared = true;
     return MCS_OK;
+}
+
+// ------------------------------------------------------------------ slots (server)
+// The server keeps one batch whose replicas vector is indexed by slot (null =
+// free).  Replicas join and leave between steps; only the groups they join or
+// leave change, and each replica advances by its own quota per step.
+int Batch::admit(const std::vector<int> &ids, double step_us)
+{
+    if (ids.empty()) return MCS_OK;
+    if (!d_reps) {
+        int rc = setup_device();
+        if (rc != MCS_OK) return rc;
+        CUDA_TRY(cudaMalloc(&d_reps, (size_t)slot_capacity * sizeof(Rep)));
+        prepared = true;
+    }
+    const int max_smem = resident_max_smem();
+    assign_schedules(ids, max_smem);
+    // quota: the units a replica advances per step, so that each replica's
+    // share of a step takes about step_us of device time on its schedule
+    // (measured rates per CTA: resident 1, cluster C: about 0.8 C, tiled about 4)
+    static const double r_cta[4] = {0, 0.40e9, 0.85e9, 0.65e9};
+    for (int i : ids) {
+        Replica &r = *replicas[i];
+        double ctas = 1.0;
+        if (r.schedule == 6) ctas = 0.8 * std::max(1, r.pref_C);
+        else if (r.schedule == 3) ctas = 4.0;
+        const double per_unit = (double)r.hm.N / (r_cta[r.hm.dim] * ctas);
+        long long q = (long long)(step_us * 1e-6 / per_unit);
+        r.rep.quota = std::max(1LL, std::min(q, r.hm.units_total));
+        r.rep.u_stop = r.rep.u;  // nothing runs before the step sets its bound
+    }
+    for (int i : ids) CUDA_TRY(cudaMemcpyAsync(d_reps + i, &replicas[i]->rep, sizeof(Rep), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    int rc = init_states(ids);
+    if (rc != MCS_OK) return rc;
+    return build_groups(ids, true);
+}
+
+// Take the replicas of `ids` out of their groups.  A group whose device lists
+// cannot be rebuilt is dissolved and its other replicas are returned in
+// *orphans (the caller fails them).
+void Batch::drop(const std::vector<int> &ids, std::vector<int> *orphans)
+{
+    if (ids.empty()) return;
+    std::vector<char> gone(replicas.size(), 0);
+    for (int i : ids) gone[i] = 1;
+    for (auto &G : groups) {
+        const size_t n0 = G->ids.size();
+        G->ids.erase(std::remove_if(G->ids.begin(), G->ids.end(), [&](int i) { return gone[i] != 0; }), G->ids.end());
+        if (G->ids.size() == n0 || G->ids.empty()) continue;
+        if (upload_ids(*G) != MCS_OK || ((G->kind == 3 || G->kind == 1) && reset_tiled(*G) != MCS_OK)) {
+            cudaGetLastError();
+            if (orphans) orphans->insert(orphans->end(), G->ids.begin(), G->ids.end());
+            G->ids.clear();
+        }
+    }
+    groups.erase(std::remove_if(groups.begin(), groups.end(), [](const std::unique_ptr<Group> &G) { return G->ids.empty(); }),
+                 groups.end());
 }
 
 // Autotuner results kept for the life of the process, keyed by the group's
@@ -940,24 +1149,15 @@ int Batch::advance(long long units)
     if (rc != MCS_OK) return rc;
     if (replicas.empty()) return MCS_OK;
     for (auto &r : replicas) r->rblock_fresh = false;
-    const bool multi = groups.size() > 1;
-    while (multi && gstreams.size() < groups.size()) {
-        cudaStream_t gs = nullptr;
-        CUDA_TRY(cudaStreamCreateWithFlags(&gs, cudaStreamNonBlocking));
-        gstreams.push_back(gs);
-        cudaEvent_t ge = nullptr;
-        CUDA_TRY(cudaEventCreateWithFlags(&ge, cudaEventDisableTiming));
-        gevents.push_back(ge);
-    }
     CUDA_TRY(cudaEventRecord(ev0, stream));
     // 1. autotuner: time each candidate (cluster size, block size) of an
     //    untuned group on a few real units, alone on the batch stream, and keep
     //    the fastest
-    std::vector<long long> pre(groups.size(), 0);
+    std::vector<long long> pre(groups.size(), 0), todo(groups.size(), 0);
     for (size_t gi = 0; gi < groups.size(); ++gi) {
         Group &G = *groups[gi];
-        const long long todo = std::min(units, G.max_units - G.done_units);
-        if (todo <= 0 || !(G.kind == 2 || G.kind == 6) || G.tuned) continue;
+        todo[gi] = std::min(units, G.max_units - G.done_units);
+        if (todo[gi] <= 0 || !(G.kind == 2 || G.kind == 6) || G.tuned) continue;
         if (G.tune_key.empty()) G.tune_key = tune_key(*this, G);
         if (!getenv("MCSGPU_NO_TUNE_CACHE")) {
             std::lock_guard<std::mutex> lock(g_tune_mutex);
@@ -970,9 +1170,9 @@ int Batch::advance(long long units)
             }
         }
         long long u = 0;
-        const long long probe = std::max<long long>(1, std::min<long long>(4, todo / (2 * (long long)G.candidates.size() + 1)));
+        const long long probe = std::max<long long>(1, std::min<long long>(4, todo[gi] / (2 * (long long)G.candidates.size() + 1)));
         G.cand_ms.assign(G.candidates.size(), 1e30);
-        for (size_t ci = 0; ci < G.candidates.size() && u + probe <= todo; ++ci) {
+        for (size_t ci = 0; ci < G.candidates.size() && u + probe <= todo[gi]; ++ci) {
             int C = G.candidates[ci].first, th = G.candidates[ci].second;
             CUDA_TRY(cudaEventRecord(ev_a, stream));
             cudaError_t e = launch_group(G, C, th, probe, stream);
@@ -996,8 +1196,30 @@ int Batch::advance(long long units)
             g_tune_cache[G.tune_key] = {G.C, G.threads};
         }
     }
-    // 2. the rest: each group on its own stream, side by side on the device
-    // (MCSGPU_TRACE=1 prints each group's schedule and device time to stderr)
+    rc = run_groups(todo, pre, nullptr);
+    if (rc != MCS_OK) return rc;
+    for (size_t gi = 0; gi < groups.size(); ++gi)
+        if (todo[gi] > 0) groups[gi]->done_units += todo[gi];
+    return MCS_OK;
+}
+
+// 2. the groups' units: each group on its own stream, side by side on the
+// device (MCSGPU_TRACE=1 prints each group's schedule and device time to
+// stderr).  ev0 is recorded on `stream` before the call.  With `failed`, a
+// group whose launch is refused (a configuration error, which leaves the
+// context usable) adds its replicas there and the others go on; an error at
+// the synchronisation is returned.
+int Batch::run_groups(const std::vector<long long> &todo, const std::vector<long long> &pre, std::vector<int> *failed)
+{
+    const bool multi = groups.size() > 1;
+    while (multi && gstreams.size() < groups.size()) {
+        cudaStream_t gs = nullptr;
+        CUDA_TRY(cudaStreamCreateWithFlags(&gs, cudaStreamNonBlocking));
+        gstreams.push_back(gs);
+        cudaEvent_t ge = nullptr;
+        CUDA_TRY(cudaEventCreateWithFlags(&ge, cudaEventDisableTiming));
+        gevents.push_back(ge);
+    }
     const bool trace = getenv("MCSGPU_TRACE") != nullptr;
     std::vector<cudaEvent_t> tev;
     if (trace) {
@@ -1007,55 +1229,61 @@ int Batch::advance(long long units)
     if (multi) CUDA_TRY(cudaEventRecord(ev_fork, stream));
     for (size_t gi = 0; gi < groups.size(); ++gi) {
         Group &G = *groups[gi];
-        const long long todo = std::min(units, G.max_units - G.done_units);
-        if (todo <= 0) continue;
+        const long long n_todo = todo[gi];
+        if (n_todo <= 0) continue;
         cudaStream_t gs = multi ? gstreams[gi] : stream;
         if (multi) CUDA_TRY(cudaStreamWaitEvent(gs, ev_fork, 0));
         if (trace) CUDA_TRY(cudaEventRecord(tev[2 * gi], gs));
+        cudaError_t e = cudaSuccess;
+        const char *what = "";
         if (G.kind == 4 || G.kind == 5) {
-            for (long long u = 0; u < todo; u += G.chunk) {
-                long long n = std::min(G.chunk, todo - u);
-                cudaError_t e = launch_wolff(G.dim, G.geom, d_reps, G.d_ids, (int)G.ids.size(), G.threads, G.smem, n,
-                                             G.kind == 5, gs);
-                if (e != cudaSuccess) { set_error(std::string("wolff launch: ") + cudaGetErrorString(e)); return MCS_ECUDA; }
-                launches++;
+            what = "wolff launch: ";
+            for (long long u = 0; u < n_todo && e == cudaSuccess; u += G.chunk) {
+                long long n = std::min(G.chunk, n_todo - u);
+                e = launch_wolff(G.dim, G.geom, d_reps, G.d_ids, (int)G.ids.size(), G.threads, G.smem, n, G.kind == 5, gs);
+                if (e == cudaSuccess) launches++;
             }
         } else if (G.kind == 2 || G.kind == 6) {
-            for (long long u = pre[gi]; u < todo; u += G.chunk) {
-                long long n = std::min(G.chunk, todo - u);
-                cudaError_t e = launch_group(G, G.C, G.threads, n, gs);
-                if (e != cudaSuccess) { set_error(std::string("resident/cluster launch: ") + cudaGetErrorString(e)); return MCS_ECUDA; }
-                launches++;
+            what = "resident/cluster launch: ";
+            for (long long u = pre[gi]; u < n_todo && e == cudaSuccess; u += G.chunk) {
+                long long n = std::min(G.chunk, n_todo - u);
+                e = launch_group(G, G.C, G.threads, n, gs);
+                if (e == cudaSuccess) launches++;
             }
-        } else if (G.kind == 3 && todo >= 8) {
+        } else if (G.kind == 3 && n_todo >= 8) {
+            what = "tiled: ";
             if (!G.exec) {
-                G.K = (int)std::min<long long>(32, std::max<long long>(1, std::max(todo, G.max_units - G.done_units)));
+                G.K = (int)std::min<long long>(32, std::max<long long>(1, std::max(n_todo, G.max_units - G.done_units)));
                 long long nl = 0;
                 CUDA_TRY(cudaStreamBeginCapture(stream2, cudaStreamCaptureModeThreadLocal));
-                for (int k = 0; k < G.K; ++k) {
-                    cudaError_t e = tiled_unit(G, stream2, &nl);
-                    if (e != cudaSuccess) {
-                        cudaGraph_t g0 = nullptr;
-                        cudaStreamEndCapture(stream2, &g0);
-                        if (g0) cudaGraphDestroy(g0);
-                        set_error(std::string("capture: ") + cudaGetErrorString(e));
-                        return MCS_ECUDA;
-                    }
+                for (int k = 0; k < G.K && e == cudaSuccess; ++k) e = tiled_unit(G, stream2, &nl);
+                cudaGraph_t g0 = nullptr;
+                cudaError_t e2 = cudaStreamEndCapture(stream2, &g0);
+                if (e == cudaSuccess && e2 == cudaSuccess) {
+                    G.graph = g0;
+                    e = cudaGraphInstantiate(&G.exec, G.graph, 0);
+                    G.per_graph = nl;
+                } else {
+                    if (g0) cudaGraphDestroy(g0);
+                    if (e == cudaSuccess) e = e2;
+                    what = "capture: ";
                 }
-                CUDA_TRY(cudaStreamEndCapture(stream2, &G.graph));
-                CUDA_TRY(cudaGraphInstantiate(&G.exec, G.graph, 0));
-                G.per_graph = nl;
             }
             long long u = 0;
-            for (; u + G.K <= todo; u += G.K) {
-                CUDA_TRY(cudaGraphLaunch(G.exec, gs));
-                launches += G.per_graph;
+            for (; e == cudaSuccess && u + G.K <= n_todo; u += G.K) {
+                e = cudaGraphLaunch(G.exec, gs);
+                if (e == cudaSuccess) launches += G.per_graph;
             }
-            for (; u < todo; ++u) CUDA_TRY(tiled_unit(G, gs, &launches));
+            for (; e == cudaSuccess && u < n_todo; ++u) e = tiled_unit(G, gs, &launches);
         } else {
-            for (long long u = 0; u < todo; ++u) CUDA_TRY(tiled_unit(G, gs, &launches));
+            what = "tiled: ";
+            for (long long u = 0; e == cudaSuccess && u < n_todo; ++u) e = tiled_unit(G, gs, &launches);
         }
-        G.done_units += todo;
+        if (e != cudaSuccess) {
+            if (!failed) { set_error(std::string(what) + cudaGetErrorString(e)); return MCS_ECUDA; }
+            cudaGetLastError();
+            failed->insert(failed->end(), G.ids.begin(), G.ids.end());
+        }
         if (trace) CUDA_TRY(cudaEventRecord(tev[2 * gi + 1], gs));
         if (multi) {
             CUDA_TRY(cudaEventRecord(gevents[gi], gs));
@@ -1079,10 +1307,52 @@ int Batch::advance(long long units)
             fprintf(stderr, "mcsgpu trace: group %zu kind %d dim %d C %d threads %d replicas %zu sites %lld max %lld: %.3f ms\n",
                     gi, G.kind, G.dim, G.C, G.threads, G.ids.size(), sites, maxn, gms);
         }
-        fprintf(stderr, "mcsgpu trace: advance %lld units: %.3f ms\n", units, ms);
+        fprintf(stderr, "mcsgpu trace: step %.3f ms\n", ms);
         cudaGetLastError();
-        for (auto &e : tev) if (e) cudaEventDestroy(e);
+        for (auto &e2 : tev) if (e2) cudaEventDestroy(e2);
     }
+    return MCS_OK;
+}
+
+// One server step: every replica of the groups advances by min(quota,
+// remaining units).  A small kernel first sets each replica's stop unit
+// (u + quota) on the device; the host tracks the same progress.
+int Batch::advance_quota(std::vector<int> *failed)
+{
+    if (groups.empty()) return MCS_OK;
+    std::vector<long long> todo(groups.size(), 0), pre(groups.size(), 0);
+    std::vector<int> active;
+    for (size_t gi = 0; gi < groups.size(); ++gi)
+        for (int id : groups[gi]->ids) {
+            const Rep &R = replicas[id]->rep;
+            const long long n = std::min(R.quota, replicas[id]->hm.units_total - R.u);
+            if (n <= 0) continue;
+            todo[gi] = std::max(todo[gi], n);
+            active.push_back(id);
+        }
+    if (active.empty()) return MCS_OK;
+    if ((int)active.size() > active_cap) {
+        if (d_active) cudaFree(d_active);
+        d_active = nullptr;
+        active_cap = 0;
+        CUDA_TRY(cudaMalloc(&d_active, (size_t)slot_capacity * sizeof(int)));
+        active_cap = slot_capacity;
+    }
+    CUDA_TRY(cudaMemcpyAsync(d_active, active.data(), active.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaEventRecord(ev0, stream));
+    CUDA_TRY(launch_set_stop(d_reps, d_active, (int)active.size(), stream));
+    launches++;
+    std::vector<int> fl;
+    int rc = run_groups(todo, pre, &fl);
+    if (rc != MCS_OK) return rc;
+    std::vector<char> bad(replicas.size(), 0);
+    for (int i : fl) bad[i] = 1;
+    for (int id : active) {
+        if (bad[id]) continue;
+        Rep &R = replicas[id]->rep;
+        R.u = std::min(replicas[id]->hm.units_total, R.u + R.quota);
+    }
+    if (failed) failed->insert(failed->end(), fl.begin(), fl.end());
     return MCS_OK;
 }
 
@@ -1105,9 +1375,7 @@ void Batch::release_groups()
 {
     groups.clear();
     if (d_reps) cudaFree(d_reps);
-    if (d_all) cudaFree(d_all);
     d_reps = nullptr;
-    d_all = nullptr;
     prepared = false;
 }
 

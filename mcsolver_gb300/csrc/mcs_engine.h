@@ -22,7 +22,9 @@ struct Replica {
     Rep rep;                 // descriptor (device pointers into the arena)
     void *arena = nullptr;   // one device allocation per replica
     size_t bytes = 0;
-    size_t acc_off = 0, icnt_off = 0, stats_off = 0, series_off = 0, frames_off = 0, spins_off = 0;
+    size_t acc_off = 0, icnt_off = 0, stats_off = 0, series_off = 0, spins_off = 0;
+    void *frames_host = nullptr;       // spin frames: page-locked host memory mapped into the device
+    size_t frames_bytes = 0;
     size_t nacc = 0;
     int schedule = 0;        // 1 plain, 2 resident, 3 tiled, 4/5 Wolff, 6 cluster
     int requested_schedule = 0;
@@ -52,7 +54,8 @@ struct Group {
     int kind = 0;              // 1 plain, 2 resident, 3 tiled
     int dim = 0, geom = 0;
     std::vector<int> ids;
-    int *d_ids = nullptr;
+    int *d_ids = nullptr;      // device copy of ids (capacity ids_cap)
+    int ids_cap = 0;
     long long max_units = 0, done_units = 0;
     // resident / cluster
     int threads = 0;
@@ -85,7 +88,8 @@ struct Batch {
     int device = 0;
     std::vector<std::unique_ptr<Replica>> replicas;
     Rep *d_reps = nullptr;
-    int *d_all = nullptr;
+    int *d_active = nullptr;   // slot mode: replicas of the current step
+    int active_cap = 0;
     void *d_scratch = nullptr;
     bool prepared = false;
     std::vector<std::unique_ptr<Group>> groups;
@@ -111,13 +115,28 @@ struct Batch {
     int add(const mcs_problem *p, const mcs_options *o, int *idx);
     int prepare();                 // upload descriptors, initial energies, build groups
     int advance(long long units);  // every replica runs up to `units` more units
+    // pieces of prepare(), also used by the server's slot mode
+    int setup_device();
+    void assign_schedules(const std::vector<int> &ids, int max_smem);
+    int init_states(const std::vector<int> &ids);
+    int build_groups(const std::vector<int> &ids, bool merge);
+    int upload_ids(Group &G);
+    int reset_tiled(Group &G);
+    // slot mode (server): replicas[i] may be null; d_reps holds slot_capacity descriptors
+    int slot_capacity = 0;
+    int admit(const std::vector<int> &ids, double step_us);        // new replicas in these slots
+    void drop(const std::vector<int> &ids, std::vector<int> *orphans);  // replicas leaving their groups
+    // every replica of the groups advances by its own quota (Rep::quota); the
+    // replicas of a group whose launch failed are added to *failed
+    int advance_quota(std::vector<int> *failed);
+    int run_groups(const std::vector<long long> &todo, const std::vector<long long> &pre, std::vector<int> *failed);
     int collect();                 // read back descriptors and counters
     int sync_descriptors();        // read back descriptors: progress travels with each replica
     void release_groups();         // drop groups and descriptor arrays; the next advance re-prepares
     int run();                     // prepare + advance to completion + collect
     int result(int i, mcs_result *res);
     int setup_tiled(Group &G);
-    void place_replicas(int max_smem);
+    void place_replicas(int max_smem, const std::vector<int> &ids, double base_crit = 0, double base_smsec = 0);
     cudaError_t tiled_unit(Group &G, cudaStream_t s, long long *nl);
     cudaError_t launch_group(Group &G, int C, int threads, long long units, cudaStream_t s);
 };

@@ -142,13 +142,17 @@ struct Rep {
     int spad;
     double *acc;
     double *series;                              // [nsweep][MCS_NSER]
-    float *frame_buf;                            // [frames][N][3]
+    void *frame_buf;                             // spin frames in page-locked host memory mapped into the
+                                                 // device: Ising [frames][N] int8 signs, O(n) [frames][N][dim] FP32
     long long *icnt;                             // Ising counters
     long long *stats;                            // generic counters
     unsigned int *wbits;                         // Wolff in-cluster bits (global schedule)
     int *wqueue;                                 // Wolff queue (global schedule)
     long long u0;                                // RNG unit offset
     long long u;                                 // next unit
+    long long u_stop;                            // a launch stops the replica here (units_total, or the
+                                                 // server's per-step bound u + quota)
+    long long quota;                             // server: units per step (0 = none)
     long long m;                                 // next measurement
     int frames_written;
     int err;
@@ -189,4 +193,6 @@ cudaError_t launch_tiled_finalize_dim(int dim, Rep *reps, const int *ids, int nr
                                       double *dEpart, long long *ipart, const int *mitem_off, double *fpart,
                                       cudaStream_t st);
 cudaError_t launch_init_state_dg(int dim, int geom, Rep *reps, const int *ids, int nrep, cudaStream_t st);
+// reps[ids[i]].u_stop = min(units_total, u + quota)
+cudaError_t launch_set_stop(Rep *reps, const int *ids, int n, cudaStream_t st);
 }  // namespace mcs

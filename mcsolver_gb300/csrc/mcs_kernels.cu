@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
     const int rank = C > 1 ? (int)cl.block_rank() : 0;
     Rep *Rg = reps + ids[blockIdx.x / C];
     load_rep(R, Rg);
-    if (R.u >= R.units_total) return;
+    if (R.u >= R.u_stop) return;
     const SmemLayout L = smem_layout(R);
     const int tid = threadIdx.x, bd = blockDim.x, N = R.N;
     double *red = (double *)(smem + L.red);
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
     };
 
     long long u = R.u;
-    const long long uend = min(R.units_total, u + max_units);
+    const long long uend = min(R.u_stop, u + max_units);
     for (; u < uend; ++u) {
         if (DIM == 1 && u == R.units_thermal) {
             fold();
@@ -372,13 +372,8 @@ __global__ void __launch_bounds__(1024) k_resident_metro(Rep *reps, const int *i
                     on_accumulate_frames<DIM>(R, fsx, &R.acc[A_ECUR], m, 1, tid);
                 }
             }
-            if (rank == 0 && R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) {
-                float *fb = R.frame_buf + (size_t)R.frames_written * N * 3;
-                for (int v = tid; v < N; v += bd) {
-                    if (DIM == 1) { fb[3 * v] = (float)(R.Stype[R.stype ? R.stype[v] : 0] * S.s[v]); fb[3 * v + 1] = 0; fb[3 * v + 2] = 0; }
-                    else { fb[3 * v] = S.x[v]; fb[3 * v + 1] = S.y[v]; fb[3 * v + 2] = DIM == 3 ? S.z[v] : 0.f; }
-                }
-            }
+            if (rank == 0 && R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames)
+                for (int v = tid; v < N; v += bd) frame_store<DIM>(R, R.frames_written, v, S, v);
             __syncthreads();
             if (tid == 0) {
                 if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) R.frames_written++;
@@ -417,7 +412,7 @@ __global__ void __launch_bounds__(256) k_tiled_sweep(Rep *reps, const Item *item
     __shared__ long long redl[32 * 9 + 9];
     const Item it = items[blockIdx.x];
     const Rep &R = reps[it.rep];
-    if (R.u >= R.units_total) return;
+    if (R.u >= R.u_stop) return;
     const long long t = R.u0 + R.u;
     const int c = colour, c0 = R.col_start[c];
     Spins S = spins_global(R);
@@ -496,7 +491,7 @@ __global__ void __launch_bounds__(256) k_tiled_measure(Rep *reps, const Item *it
     __shared__ long long Fi[16];
     const Item it = items[blockIdx.x];
     const Rep &R = reps[it.rep];
-    if (R.u >= R.units_total || !measures_after(R, R.u)) return;
+    if (R.u >= R.u_stop || !measures_after(R, R.u)) return;
     Spins S = spins_global(R);
     double *out = fpart + (size_t)blockIdx.x * F_NON;
     if (DIM == 1) {
@@ -525,7 +520,7 @@ __global__ void __launch_bounds__(256) k_tiled_finalize(Rep *reps, const int *id
     __shared__ int meas;
     const int r = ids[blockIdx.x];
     Rep &R = reps[r];
-    if (R.u >= R.units_total) return;
+    if (R.u >= R.u_stop) return;
     const int tid = threadIdx.x;
     const int i0 = item_off[blockIdx.x], i1 = item_off[blockIdx.x + 1];
     const long long u = R.u;
@@ -591,12 +586,8 @@ __global__ void __launch_bounds__(256) k_tiled_finalize(Rep *reps, const int *id
             else on_accumulate_frames<3>(R, fsx, &R.acc[A_ECUR], m, 1, tid);
         }
         if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) {
-            float *fb = R.frame_buf + (size_t)R.frames_written * R.N * 3;
             Spins S = spins_global(R);
-            for (int v = tid; v < R.N; v += blockDim.x) {
-                if (DIM == 1) { fb[3 * v] = (float)(R.Stype[R.stype ? R.stype[v] : 0] * S.s[v]); fb[3 * v + 1] = 0; fb[3 * v + 2] = 0; }
-                else { fb[3 * v] = S.x[v]; fb[3 * v + 1] = S.y[v]; fb[3 * v + 2] = DIM == 3 ? S.z[v] : 0.f; }
-            }
+            for (int v = tid; v < R.N; v += blockDim.x) frame_store<DIM>(R, R.frames_written, v, S, v);
         }
         __syncthreads();
         if (tid == 0) {
@@ -701,7 +692,7 @@ __global__ void __launch_bounds__(512) k_wolff(Rep *reps, const int *ids, long l
     __shared__ Rep R;
     Rep *Rg = reps + ids[blockIdx.x];
     load_rep(R, Rg);
-    if (R.u >= R.units_total) return;
+    if (R.u >= R.u_stop) return;
     WolffLayout L = wolff_layout(R);
     if (gstate) {  // the host decided: keep the state in global memory
         L = wolff_layout(R, 0);
@@ -757,7 +748,7 @@ __global__ void __launch_bounds__(512) k_wolff(Rep *reps, const int *ids, long l
     long long dnacc = 0;
     int dn[MCS_MAXC] = {0, 0, 0, 0}, dm[MCS_MAXT] = {0, 0, 0, 0};
     long long u = R.u;
-    const long long uend = min(R.units_total, u + max_units);
+    const long long uend = min(R.u_stop, u + max_units);
     for (; u < uend; ++u) {
         if (tid == 0) R.u = u;
         __syncthreads();
@@ -785,13 +776,8 @@ __global__ void __launch_bounds__(512) k_wolff(Rep *reps, const int *ids, long l
                     on_accumulate_frames<DIM>(R, wfs, &R.acc[A_ECUR], m, 1, tid);
                 }
             }
-            if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) {
-                float *fb = R.frame_buf + (size_t)R.frames_written * N * 3;
-                for (int v = tid; v < N; v += bd) {
-                    if (DIM == 1) { fb[3 * v] = (float)(R.Stype[st[v]] * S.s[v]); fb[3 * v + 1] = 0; fb[3 * v + 2] = 0; }
-                    else { fb[3 * v] = S.x[v]; fb[3 * v + 1] = S.y[v]; fb[3 * v + 2] = DIM == 3 ? S.z[v] : 0.f; }
-                }
-            }
+            if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames)
+                for (int v = tid; v < N; v += bd) frame_store<DIM>(R, R.frames_written, v, S, v);
             __syncthreads();
             if (tid == 0) {
                 if (R.frames > 0 && (m % R.frame_every) == 0 && R.frames_written < R.frames) R.frames_written++;
@@ -937,6 +923,23 @@ cudaError_t launch_tiled_finalize_dim(int dim, Rep *reps, const int *ids, int nr
     if (dim == 1) k_tiled_finalize<1><<<nrep, 256, 0, st>>>(reps, ids, item_off, dEpart, ipart, mitem_off, fpart);
     else if (dim == 2) k_tiled_finalize<2><<<nrep, 256, 0, st>>>(reps, ids, item_off, dEpart, ipart, mitem_off, fpart);
     else k_tiled_finalize<3><<<nrep, 256, 0, st>>>(reps, ids, item_off, dEpart, ipart, mitem_off, fpart);
+    return cudaGetLastError();
+}
+
+// Server step bound: each replica of ids stops after its quota of units.
+__global__ void k_set_stop(Rep *reps, const int *ids, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Rep &R = reps[ids[i]];
+    const long long s = R.u + R.quota;
+    R.u_stop = s < R.units_total ? s : R.units_total;
+}
+
+cudaError_t launch_set_stop(Rep *reps, const int *ids, int n, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    k_set_stop<<<(n + 127) / 128, 128, 0, st>>>(reps, ids, n);
     return cudaGetLastError();
 }
 

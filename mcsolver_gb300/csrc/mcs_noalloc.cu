@@ -109,27 +109,47 @@ __global__ void __launch_bounds__(NA_THREADS) k_na_sums(const signed char *s, in
     }
 }
 
-// device address of the scratch array, looked up once per device
+// Device address of the scratch array on the current device, looked up on
+// every call (cheap once the module is loaded, and never stale after a
+// cudaDeviceReset).  The first call on a device also loads both kernels
+// (under lazy module loading a kernel is otherwise loaded at its first launch,
+// which may allocate device memory for the module, even inside a capture).
 static std::mutex g_na_mutex;
-static long long *g_na_ptr[64];
+static bool g_na_loaded[64];
 
-static int noalloc_scratch(long long **out)
+static int noalloc_scratch(cudaStream_t st, long long **out)
 {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) { set_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e)); return MCS_ECUDA; }
     if (dev < 0 || dev >= 64) { set_error("device ordinal out of range"); return MCS_EINVAL; }
-    std::lock_guard<std::mutex> lock(g_na_mutex);
-    if (!g_na_ptr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            set_error(std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
-            return MCS_ECUDA;
+    if (st) {
+        int sdev = -1;
+        e = cudaStreamGetDevice(st, &sdev);
+        if (e != cudaSuccess) { set_error(std::string("cudaStreamGetDevice: ") + cudaGetErrorString(e)); return MCS_EINVAL; }
+        if (sdev != dev) {
+            set_error("the stream belongs to device " + std::to_string(sdev) + " but device " + std::to_string(dev) +
+                      " is current");
+            return MCS_EINVAL;
         }
-        g_na_ptr[dev] = (long long *)p;
     }
-    *out = g_na_ptr[dev];
+    {
+        std::lock_guard<std::mutex> lock(g_na_mutex);
+        if (!g_na_loaded[dev]) {
+            cudaFuncAttributes fa;
+            e = cudaFuncGetAttributes(&fa, k_na_colour);
+            if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_na_sums);
+            if (e != cudaSuccess) { set_error(std::string("loading the kernels: ") + cudaGetErrorString(e)); return MCS_ECUDA; }
+            g_na_loaded[dev] = true;
+        }
+    }
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        set_error(std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
+        return MCS_ECUDA;
+    }
+    *out = (long long *)p;
     return MCS_OK;
 }
 
@@ -147,10 +167,10 @@ extern "C" int mcs_ising_square_noalloc(int8_t *d_sigma, int32_t Lx, int32_t Ly,
         return MCS_EINVAL;
     }
     if (nsweeps < 0 || sweep0 < 0) { set_error("negative sweep count or index"); return MCS_EINVAL; }
-    long long *scratch = nullptr;
-    int rc = noalloc_scratch(&scratch);
-    if (rc != MCS_OK) return rc;
     cudaStream_t st = (cudaStream_t)stream;
+    long long *scratch = nullptr;
+    int rc = noalloc_scratch(st, &scratch);
+    if (rc != MCS_OK) return rc;
     // acceptance thresholds, evaluated as the Ising table of mcs_solve():
     // corr = 2 (sigma * K * (2 n+ - 4) - h * sigma), threshold ceil(exp(corr) 2^32)
     NaThr thr;

@@ -35,7 +35,23 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_BUILD = os.path.join(HERE, "_ref")
-REF_SRC = os.environ.get("MCS_REFERENCE_SRC", "/root/reference/mcsolver")
+def _reference_source() -> str:
+    """The reference's ``mcsolver`` source directory: ``MCS_REFERENCE_SRC``
+    when set, else the REF variable of the oracle's build recipe
+    (``make -C oracle print-ref``), the one place that names it."""
+    env = os.environ.get("MCS_REFERENCE_SRC")
+    if env:
+        return env
+    import subprocess
+    try:
+        out = subprocess.run(["make", "-s", "--no-print-directory", "-C", HERE, "print-ref"], capture_output=True,
+                             text=True, timeout=30)
+        return out.stdout.strip()
+    except Exception:
+        return ""
+
+
+REF_SRC = _reference_source()
 
 _LIBC = ctypes.CDLL(None)
 

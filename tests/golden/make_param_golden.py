@@ -7,8 +7,8 @@ each with the reference's own ``fileio.loadParam`` (fileio.py:169-313, GUI
 modules stubbed), and for one (T, H) point of each captures the argument tuple
 the reference's own model build passes to MCMainFunction (mcMain.MC +
 mainLoopViaCLib[_On], through oracle/refharness.py).  Both go to
-tests/golden/params_parsed.json.gz.  Run in a container that has the reference
-at /root/reference:
+tests/golden/params_parsed.json.gz.  Run where the reference sources are
+present (their directory is the oracle recipe's REF, or MCS_REFERENCE_SRC):
 
     python tests/golden/make_param_golden.py
 """
@@ -22,8 +22,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 from mcsolver_gb300.simulation import save_param  # noqa: E402
-
-REF = "/root/reference/mcsolver"
+from oracle.refharness import REF_SRC as REF  # noqa: E402
 
 J = lambda xx, yy=0, zz=0, xy=0, xz=0, yz=0, yx=0, zx=0, zy=0: [xx, yy, zz, xy, xz, yz, yx, zx, zy]  # noqa: E731
 

@@ -1,0 +1,44 @@
+"""CPU checks of the large-lattice fixtures (tests/golden/golden_large.json.gz,
+made from the reference itself by tests/golden/make_golden_large.py).
+
+The fixtures hold, per case, the reference caller's input specification, a
+fingerprint of the argument tuple the reference's own Python built from it
+(per argument: length, sum, position-weighted sum, sum of squares), and the
+reference library's result tuples for 32 seeds.  Here the package's
+vectorised builder rebuilds each tuple at full size and must give the same
+fingerprint, so the GPU tests that run the engine on these tuples run it on
+the reference's inputs."""
+import numpy as np
+import pytest
+
+from tests import cases as C
+
+G = C.golden_large()
+CASES = sorted(G["cases"]) if G else []
+
+
+@pytest.mark.skipif(not CASES, reason="large fixtures not generated")
+@pytest.mark.parametrize("name", CASES)
+def test_builder_reproduces_reference_tuple(name):
+    import sys
+    sys.path.insert(0, C.os.path.join(C.HERE, "golden"))
+    from make_golden_large import fingerprint
+    c = G["cases"][name]
+    args = C.spec_args(c["spec"], arrays=True)
+    fp = fingerprint(args)
+    want = c["fingerprint"]
+    assert len(fp) == len(want)
+    for k, (a, b) in enumerate(zip(fp, want)):
+        np.testing.assert_allclose(np.asarray(a, float), np.asarray(b, float), rtol=1e-12, atol=1e-9,
+                                   err_msg="argument %d" % k)
+
+
+@pytest.mark.skipif(not CASES, reason="large fixtures not generated")
+@pytest.mark.parametrize("name", CASES)
+def test_reference_runs_are_finite_and_independent(name):
+    """Every seed gave a finite result, and different seeds differ (the
+    reference's glibc stream was reseeded per run)."""
+    c = G["cases"][name]
+    ref = np.array([c["ref"][str(s)] for s in c["seeds"]], float)
+    assert np.isfinite(ref).all()
+    assert len({round(x, 12) for x in ref[:, 8 if c["model"] != "ising" else 4]}) == len(c["seeds"])

@@ -166,3 +166,57 @@ def test_resident_copies_match_one_cta(engine, name, model, mk, copies):
         np.testing.assert_allclose(np.array(b[:27]), np.array(a[:27]), rtol=1e-5, atol=1e-6)
     if "frames" in ea:
         np.testing.assert_allclose(eb["frames"], ea["frames"], atol=2e-5)
+
+
+SERIES_CASES = [
+    ("xy_L16", "xy", lambda: C.square_args("xy", 16, 0.9, nthermal=20, nsweep=200)),
+    ("heis_L12_dmi_h_circ", "heisenberg", lambda: C.square_args("heisenberg", 12, 0.5, h=0.3, dmi=0.4,
+                                                                nthermal=20, nsweep=200)),
+]
+CANDIDATES = [(-2, 0), (-4, 0)] + [(c, t) for c in (1, 2, 4) for t in (256, 512, 1024)]
+
+
+@pytest.mark.parametrize("cand", CANDIDATES, ids=["%d:%d" % c for c in CANDIDATES])
+@pytest.mark.parametrize("name,model,mk", SERIES_CASES, ids=[c[0] for c in SERIES_CASES])
+def test_every_candidate_records_the_same_series(engine, name, model, mk, cand):
+    """Each configuration the autotuner may pick for a group (resident copies,
+    the cluster kernel with 1, 2 or 4 CTAs at 256/512/1024 threads) records
+    the per-measurement series row by row where the one-CTA resident run
+    does, and gives its observables.  (A measurement index summed over the
+    CTAs of a cluster once put rows at C*m.)"""
+    args = mk()
+    ref = engine.Batch()
+    ref.add(model, args, seed=21, record_series=True, schedule="resident", random_init=True)
+    old = os.environ.get("MCSGPU_FORCE")
+    os.environ["MCSGPU_CLUSTER"] = "1"  # the one-CTA resident kernel only
+    try:
+        ref.prepare()
+        ref.run()
+        assert ref.schedules()[0][:2] == ("resident", 1)
+    finally:
+        os.environ.pop("MCSGPU_CLUSTER", None)
+    a, ea = ref.result(0)
+    ref.close()
+    C_, th = cand
+    if th == 0:
+        os.environ["MCSGPU_COPIES"] = str(-C_)
+    else:
+        os.environ["MCSGPU_FORCE"] = "%d:%d" % cand
+    try:
+        bt = engine.Batch()
+        bt.add(model, args, seed=21, record_series=True, random_init=True)
+        bt.prepare()
+        bt.run()
+        sched = bt.schedules()
+        b, eb = bt.result(0)
+        bt.close()
+    finally:
+        os.environ.pop("MCSGPU_FORCE", None)
+        os.environ.pop("MCSGPU_COPIES", None)
+        if old is not None:
+            os.environ["MCSGPU_FORCE"] = old
+    want_kind = "resident" if th == 0 else "cluster"
+    assert sched[0][0] == want_kind and sched[0][1] == abs(C_), sched
+    assert eb["series"].shape == ea["series"].shape
+    np.testing.assert_allclose(eb["series"], ea["series"], rtol=1e-5, atol=2e-5)
+    np.testing.assert_allclose(np.array(b[:27]), np.array(a[:27]), rtol=1e-5, atol=1e-6)

@@ -1,0 +1,163 @@
+"""GPU parity on the benchmark configurations' own lattices.
+
+* Observables against the reference library (tests/golden/golden_large.json.gz:
+  the reference's own marshalling and C libraries, 32 seeds per case):
+  - square XY, L = 128 (16,384 sites), Metropolis, T = 0.5, 0.9, 1.3, on the
+    schedule the benchmark's autotuner picks for this workload: the cluster
+    kernel with 8 CTAs per replica and 256 threads per CTA;
+  - square Heisenberg with DMI 0.4 |J| and field, two circuits per cell,
+    L = 64, at (T, h) = (0.05 -> 0.1 by mcMain's clamp, 0.6), (0.5, 0.3),
+    (1.0, 0.1), with the topological charge Q;
+  - honeycomb Heisenberg (1NN Kitaev-type + 2NN, Az = -0.5), 64 x 64 cells,
+    at the lowest rung (5 K) and rung 20 (10.4 K) of the 64-rung geometric
+    ladder 5..50 K, run by parallel tempering over the whole ladder.
+  The engine runs 48 independent replicas (seeds) of each case from the
+  reference's own initial state (every spin along +x); per-replica results
+  and the reference's per-seed results give two means with standard errors
+  from their spreads, which must agree within 3.5 combined standard errors
+  plus the resolution of FP32 spin state.  Compared: e, e^2, the
+  renormalised e_r and e_r^2, C = N (<e^2> - <e>^2) for every case; the
+  magnetisation components and U4 where their autocorrelation time (measured:
+  about 400 sweeps for XY below 1.2 K at L = 128) is short against the run
+  (XY at 1.3 K, every DMI case, honeycomb); Q for the DMI cases.
+* A trajectory check of the cluster kernel at L = 128: 100 sweeps of the
+  benchmark schedule recorded as spin frames, and from each of ten of those
+  states one sweep of the oracle's FP64 engine stream with the same Philox
+  counters; the FP32 kernel's next frame must match it site by site (1e-4,
+  except borderline acceptance decisions on at most 1% of the sites).
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from tests import cases as C
+
+pytestmark = pytest.mark.gpu
+
+FP32_FLOOR = 2e-6
+G = C.golden_large()
+CASES = sorted(G["cases"]) if G else []
+R = 48
+
+
+def _compared(name, model):
+    base = [8, 9, 18, 19, "C"]
+    if name.startswith("xy_sq128"):
+        return base + ([0, 1, 10] if "_T1.3_" in name else [])
+    if "dmi" in name:
+        return base + [0, 1, 2, 10, 26]
+    return base + [10]
+
+
+def _with_C(res, N, T):
+    """Per-run specific heat (reference convention, win.py:458-468): the
+    energies are per site in units of J/T, so C = N (<e^2> - <e>^2)."""
+    res = np.asarray(res, float)
+    return N * (res[:, 9] - res[:, 8] ** 2)
+
+
+def _engine_runs(engine, name, c):
+    sp = c["spec"]
+    model = c["model"]
+    if name.startswith("heis_hc64"):
+        # parallel tempering over the 64-rung ladder; the rung of this case
+        ladder = 5.0 * 10 ** (np.arange(64) / 63.0)
+        k = int(np.argmin(np.abs(ladder - sp["T"])))
+        phys = C.spec_args(sp, arrays=True, T=1.0, nthermal=1000, nsweep=3000)
+        out = []
+        for r in range(R // 6):
+            pt = engine.ParallelTempering(model, phys, 1.0 / ladder, seed=700 + r)
+            pt.run()
+            out.append(pt.result(k)[0][:27])
+            pt.close()
+        return np.array(out, float)
+    args = C.spec_args(sp, arrays=True)
+    force = "8:256" if name.startswith("xy_sq128") else None
+    old = os.environ.get("MCSGPU_FORCE")
+    if force:
+        os.environ["MCSGPU_FORCE"] = force
+    try:
+        b = engine.Batch()
+        for r in range(R):
+            b.add(model, args, seed=500 + r)
+        b.prepare()
+        b.run()
+        sched = b.schedules()
+        out = np.array([b.result(r)[0][:27] for r in range(R)], float)
+        b.close()
+    finally:
+        if force:
+            os.environ.pop("MCSGPU_FORCE", None)
+            if old is not None:
+                os.environ["MCSGPU_FORCE"] = old
+    if force:
+        assert sched == [("cluster", 8, 256, R)], sched
+    return out
+
+
+@pytest.mark.skipif(not CASES, reason="large fixtures not generated")
+@pytest.mark.parametrize("name", CASES)
+def test_observables_on_configuration_lattices(engine, name, capsys):
+    c = G["cases"][name]
+    model = c["model"]
+    ref = np.array([c["ref"][str(s)] for s in c["seeds"]], float)
+    mine = _engine_runs(engine, name, c)
+    N = int(np.prod(c["spec"]["L"])) * len(c["spec"]["pos"])
+    lines = []
+    worst = 0.0
+    for k in _compared(name, model):
+        if k == "C":
+            x, y = _with_C(ref, N, c["spec"]["T"]), _with_C(mine, N, c["spec"]["T"])
+        else:
+            x, y = ref[:, k], mine[:, k]
+        se = math.sqrt(x.var(ddof=1) / len(x) + y.var(ddof=1) / len(y))
+        z = abs(x.mean() - y.mean()) / se if se > 0 else 0.0
+        worst = max(worst, z)
+        lines.append("  [%s] reference %.6g +- %.2g  engine %.6g +- %.2g  |z| %.2f" % (
+            k, x.mean(), x.std(ddof=1) / math.sqrt(len(x)), y.mean(), y.std(ddof=1) / math.sqrt(len(y)), z))
+        assert abs(x.mean() - y.mean()) <= 3.5 * se + FP32_FLOOR * max(1.0, abs(x.mean())), (name, lines[-1])
+    with capsys.disabled():
+        print("\n%s (reference %d seeds, engine %d runs)\n%s" % (name, len(ref), len(mine), "\n".join(lines)))
+
+
+TRAJ = [
+    ("xy_L128_cluster8x256", "xy", "8:256", lambda: C.square_args_fast("xy", 128, 0.9, nthermal=0, nsweep=100,
+                                                                        frames=100)),
+    ("heis_L64_dmi_h_cluster4", "heisenberg", "4:256",
+     lambda: C.square_args_fast("heisenberg", 64, 0.5, h=0.3, dmi=0.4, nthermal=0, nsweep=100, frames=100)),
+]
+
+
+@pytest.mark.parametrize("name,model,force,mk", TRAJ, ids=[t[0] for t in TRAJ])
+def test_cluster_trajectory_against_oracle(engine, oracle_lib, name, model, force, mk):
+    args = mk()
+    os.environ["MCSGPU_FORCE"] = force
+    try:
+        b = engine.Batch()
+        b.add(model, args, seed=77, random_init=True)
+        b.prepare()
+        b.run()
+        sched = b.schedules()
+        res, ex = b.result(0)
+        b.close()
+    finally:
+        os.environ.pop("MCSGPU_FORCE", None)
+    Cs, th = (int(v) for v in force.split(":"))
+    assert sched[0][:3] == ("cluster", Cs, th), sched
+    frames = ex["frames"].astype(np.float64)
+    assert frames.shape[0] == 100
+    dim = 2 if model == "xy" else 3
+    one = C.with_program(model, args, nthermal=0, nsweep=1)
+    for k in range(0, 99, 11):
+        # the oracle's engine stream from the kernel's state after sweep k,
+        # for sweep k + 1 (Philox counter t = k + 1)
+        _, rex = oracle_lib.solve(model, one, seed=77, mode=1, spins_in=frames[k], sweep_offset=k + 1,
+                                  meas_offset=k + 1)
+        want = rex["spins"][:, :dim]
+        got = frames[k + 1][:, :dim]
+        d = np.abs(got - want).max(axis=1)
+        bad = d > 1e-3
+        assert bad.mean() <= 0.01, (k, int(bad.sum()))
+        assert d[~bad].max() <= 1e-4, (k, float(d[~bad].max()))

@@ -6,6 +6,11 @@
 * submits from several threads while the main thread steps the server
   (host compile beside device work) lose nothing and change nothing;
 * a small HBM budget queues requests without losing any;
+* each request advances by its own quota per step, so small requests that
+  arrive with a large one finish first;
+* a request that fails (an upload or result failure injected on the host) or
+  is cancelled is retired with its own status while the others complete with
+  the results they give alone, and the budget returns to zero;
 * a batch of replicas of uneven lattice sizes (square Heisenberg with DMI,
   field and circuits, L in {64, 96, 128, 192, 256}) matches solves alone.
 """
@@ -39,7 +44,7 @@ def _close(model, a, b):
 
 
 def test_server_results_equal_alone_with_overlapping_arrivals(engine, monkeypatch):
-    monkeypatch.setenv("MCSGPU_SERVER_CHUNK", "8")   # short steps, so that arrivals overlap
+    monkeypatch.setenv("MCSGPU_SERVER_STEP_US", "300")   # short steps, so that arrivals overlap
     reqs = _reqs()
     srv = engine.Server(hbm_budget_bytes=1 << 30, max_slots=64)
     tickets = {}
@@ -75,7 +80,7 @@ def test_server_threaded_submits_while_stepping(engine, monkeypatch):
     import threading
     from concurrent.futures import ThreadPoolExecutor
 
-    monkeypatch.setenv("MCSGPU_SERVER_CHUNK", "5")
+    monkeypatch.setenv("MCSGPU_SERVER_STEP_US", "200")
     reqs = _reqs()
     srv = engine.Server(hbm_budget_bytes=1 << 30, max_slots=64)
     tickets, lock = {}, threading.Lock()
@@ -114,7 +119,7 @@ def test_server_threaded_submits_while_stepping(engine, monkeypatch):
 
 
 def test_server_budget_queues_requests(engine, monkeypatch):
-    monkeypatch.setenv("MCSGPU_SERVER_CHUNK", "8")
+    monkeypatch.setenv("MCSGPU_SERVER_STEP_US", "300")
     reqs = _reqs()[:4]
     srv = engine.Server(hbm_budget_bytes=600_000, max_slots=2)
     ts = [srv.submit(m, a, seed=s) for m, a, s in reqs]
@@ -155,3 +160,98 @@ def test_batch_uneven_sizes(engine):
         alone, _ = engine.solve("heisenberg", probs[i], seed=300 + i, random_init=True)
         _close("heisenberg", res[i], alone)
     assert all(np.isfinite(r[:27]).all() for r in res)
+
+
+def _drain(srv, tickets, steps=5000):
+    """Step until every ticket is done; returns {ticket: result or EngineError}
+    and the step at which each finished."""
+    import mcsolver_gb300 as eng
+    got, when = {}, {}
+    for k in range(steps):
+        srv.step()
+        for t in tickets:
+            if t in got:
+                continue
+            try:
+                r = srv.poll(t)
+            except eng.EngineError as e:
+                r = e
+            if r is not None:
+                got[t] = r
+                when[t] = k
+        if len(got) == len(tickets):
+            break
+    return got, when
+
+
+def test_small_requests_finish_before_a_large_one(engine, monkeypatch):
+    """Requests submitted together: a large XY lattice and small Ising ones.
+    Each advances by its own quota per step (about the same device time per
+    request), so the small ones finish in a few steps while the large one
+    is still running, and every result equals the solve alone."""
+    monkeypatch.setenv("MCSGPU_SERVER_STEP_US", "1000")
+    big = ("xy", C.square_args_fast("xy", 256, 1.0, nthermal=200, nsweep=800), 31)
+    small = [("ising", C.square_args("ising", 16, 2.0 + 0.2 * k, nthermal=100, nsweep=300), 40 + k) for k in range(4)]
+    srv = engine.Server(hbm_budget_bytes=1 << 30, max_slots=16)
+    tb = srv.submit(big[0], big[1], seed=big[2])
+    ts = [srv.submit(m, a, seed=s) for m, a, s in small]
+    got, when = _drain(srv, [tb] + ts)
+    assert len(got) == 5
+    assert max(when[t] for t in ts) < when[tb], when
+    for t, (m, a, s) in zip([tb] + ts, [big] + small):
+        alone, _ = engine.solve(m, a, seed=s)
+        _close(m, got[t][0], alone)
+    assert srv.stats()["bytes_in_use"] == 0
+    srv.close()
+
+
+@pytest.mark.parametrize("inject", ["upload:2", "results:3"])
+def test_injected_failure_retires_one_request(engine, monkeypatch, inject):
+    """A failure injected on the host (the second upload, or the third
+    result read-back, reports an error without touching the device) retires
+    that request with its own status; the others give their results alone."""
+    monkeypatch.setenv("MCSGPU_SERVER_STEP_US", "300")
+    monkeypatch.setenv("MCSGPU_SERVER_INJECT", inject)
+    reqs = _reqs()[:5]
+    srv = engine.Server(hbm_budget_bytes=1 << 30, max_slots=64)
+    ts = [srv.submit(m, a, seed=s) for m, a, s in reqs]
+    got, _ = _drain(srv, ts)
+    assert len(got) == len(ts)
+    failed = [t for t in ts if isinstance(got[t], engine.EngineError)]
+    assert len(failed) == 1, got
+    err = got[failed[0]]
+    assert "injected" in str(err) and err.code in (engine.MCS_ENOMEM, engine.MCS_ECUDA)
+    for t, (m, a, s) in zip(ts, reqs):
+        if t in failed:
+            continue
+        alone, _ = engine.solve(m, a, seed=s)
+        _close(m, got[t][0], alone)
+    st = srv.stats()
+    assert st["active"] == 0 and st["queued"] == 0 and st["bytes_in_use"] == 0
+    srv.close()
+
+
+def test_cancel_active_and_queued_requests(engine, monkeypatch):
+    """One request is cancelled while on the device, one while queued (slots
+    full); both poll as cancelled, the rest complete as alone, and every byte
+    of the budget comes back."""
+    monkeypatch.setenv("MCSGPU_SERVER_STEP_US", "5")   # a few sweeps per step
+    reqs = [("xy", C.square_args("xy", 64, 0.9 + 0.1 * k, nthermal=50, nsweep=400), 60 + k) for k in range(4)]
+    srv = engine.Server(hbm_budget_bytes=1 << 30, max_slots=3)
+    ts = [srv.submit(m, a, seed=s) for m, a, s in reqs]
+    srv.step()
+    st = srv.stats()
+    assert st["active"] == 3 and st["queued"] == 1, st
+    srv.cancel(ts[1])   # on the device
+    srv.cancel(ts[3])   # still queued
+    got, _ = _drain(srv, ts)
+    for t in (ts[1], ts[3]):
+        assert isinstance(got[t], engine.EngineError) and got[t].code == engine.MCS_ECANCELLED
+    for t, (m, a, s) in zip(ts, reqs):
+        if t in (ts[1], ts[3]):
+            continue
+        alone, _ = engine.solve(m, a, seed=s)
+        _close(m, got[t][0], alone)
+    st = srv.stats()
+    assert st["active"] == 0 and st["queued"] == 0 and st["bytes_in_use"] == 0
+    srv.close()
