@@ -18,6 +18,14 @@
  *          the reference, see oracle/xy_shim.c).  In this mode the output is
  *          bit-identical to the reference library built in oracle/_ref; that is
  *          how the restatement is pinned.
+ *   mode 2 "reference algorithm, SplitMix64": mode 0's algorithm and order of
+ *          draws (random-site order, the reference's direction, acceptance and
+ *          tie-break draws, RAND_MAX = 2^31 - 1) with a SplitMix64 generator
+ *          (Steele, Lea and Flood, OOPSLA 2014; 31-bit outputs, state seeded
+ *          from the seed) in place of glibc rand().  It separates the
+ *          reference's algorithm from its random source: glibc rand() (an
+ *          additive lagged-Fibonacci generator) and the 15-bit rand() of the XY
+ *          library both shift low-temperature XY energies measurably.
  *   mode 1 "engine": the GPU engine's stream.  A Metropolis sweep visits the
  *          sites colour by colour (greedy colouring of the bond graph in site
  *          order; ascending site id within a colour) and draws its random words
@@ -103,10 +111,32 @@ typedef struct Rng {
     int mode;
     int rand15;      /* XY reference contract: 15-bit rand() */
     uint32_t key[2];
+    uint64_t sm;     /* mode 2: SplitMix64 state */
 } Rng;
 
+static int splitmix31(Rng *g)
+{
+    uint64_t z = (g->sm += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z ^= z >> 31;
+    return (int)(z >> 33);
+}
 static double rmax(const Rng *g) { return g->rand15 ? 32767.0 : 2147483647.0; }
-static int rnd(const Rng *g) { return g->rand15 ? (rand() & 0x7fff) : rand(); }
+static int rnd(const Rng *g)
+{
+    if (g->mode == 2) return splitmix31((Rng *)g);
+    return g->rand15 ? (rand() & 0x7fff) : rand();
+}
+static void ref_seed(Rng *g, uint64_t seed)
+{
+    if (g->mode == 2) {
+        g->rand15 = 0;
+        g->sm = 0x6A09E667F3BCC909ULL ^ (seed * 0x9E3779B97F4A7C15ULL);
+    } else if (g->mode == 0) {
+        srand((unsigned)seed);
+    }
+}
 /* rand()/(double)RAND_MAX as written throughout the reference */
 static double ref_u(const Rng *g) { return (double)rnd(g) / rmax(g); }
 
@@ -132,8 +162,8 @@ static long ref_seed_site(const Rng *g, int N)
         int r2 = rnd(g);
         return (r1 * 32767 + r2) % N;
     }
-    unsigned long long r1 = (unsigned long long)rand();
-    unsigned long long r2 = (unsigned long long)rand();
+    unsigned long long r1 = (unsigned long long)rnd(g);
+    unsigned long long r2 = (unsigned long long)rnd(g);
     return (long)((r1 * 2147483647ULL + r2) % (unsigned long long)N);
 }
 
@@ -354,7 +384,7 @@ static int ising_run(const OrProblem *p, OrRun *run)
     S.g.key[0] = (uint32_t)run->seed;
     S.g.key[1] = (uint32_t)(run->seed >> 32);
     S.stats = run->stats;
-    if (run->mode == 0) srand((unsigned)run->seed);
+    ref_seed(&S.g, run->seed);
     S.s = malloc((size_t)N * sizeof(double));
     S.inblock = calloc((size_t)N, 1);
     S.block = malloc((size_t)N * sizeof(int));
@@ -757,7 +787,7 @@ static void on_unit(OnState *S, Sweep *sw, int64_t *t)
 {
     const OrProblem *p = S->p;
     int N = p->N;
-    if (S->g.mode == 0) {
+    if (S->g.mode != 1) {
         if (p->algorithm == 1) on_wolff(S, 0);
         else {
             long i = ref_seed_site(&S->g, N);
@@ -799,7 +829,7 @@ static int on_run(const OrProblem *p, OrRun *run)
     S.g.key[0] = (uint32_t)run->seed;
     S.g.key[1] = (uint32_t)(run->seed >> 32);
     S.stats = run->stats;
-    if (run->mode == 0) srand((unsigned)run->seed);
+    ref_seed(&S.g, run->seed);
     S.s = calloc((size_t)N, sizeof(V3));
     S.trans = calloc((size_t)N, sizeof(V3));
     S.perp = calloc((size_t)N, sizeof(V3));
@@ -821,7 +851,7 @@ static int on_run(const OrProblem *p, OrRun *run)
         V3 v = {S0, 0, 0};
         S.len[i] = fabs(S0);
         V3 fl;
-        if (run->mode == 0) fl = on_ref_randvec(&S);
+        if (run->mode != 1) fl = on_ref_randvec(&S);
         else {
             uint32_t w[4];
             phil(&S.g, (uint32_t)sw.pos[i], 0, 0x4000, w);
@@ -847,7 +877,7 @@ static int on_run(const OrProblem *p, OrRun *run)
 
     int64_t t = run->sweep_offset;
 
-    if (run->mode == 0) {
+    if (run->mode != 1) {
         for (int64_t i = 0; i < p->nthermal * p->ninterval; i++) on_unit(&S, &sw, &t);
     } else {
         int64_t units = p->algorithm == 1 ? p->nthermal * p->ninterval : p->nthermal * sweeps_per(p->ninterval, N);
@@ -866,7 +896,7 @@ static int on_run(const OrProblem *p, OrRun *run)
     V3 *gsum = calloc((size_t)G + 1, sizeof(V3));
     double nlat = (double)p->nlat;
     for (int64_t m = 0; m < p->nsweep; m++) {
-        if (run->mode == 0) {
+        if (run->mode != 1) {
             for (int64_t j = 0; j < p->ninterval; j++) on_unit(&S, &sw, &t);
         } else {
             int64_t units = p->algorithm == 1 ? p->ninterval : sweeps_per(p->ninterval, N);

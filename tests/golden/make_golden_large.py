@@ -17,7 +17,14 @@ For every case below it
      not stored;
   3. runs the reference C library (oracle/_ref) on the tuple after srand(seed)
      for every listed seed, one process per host core, and stores each
-     returned result tuple (the orbital-group tuple dropped).
+     returned result tuple (the orbital-group tuple dropped);
+  4. runs the oracle's mode 2 on the same tuple and seeds: the reference's
+     own algorithm and order of draws with a SplitMix64 generator in place of
+     glibc rand() (stored as "alg").  glibc rand() is an additive
+     lagged-Fibonacci generator and the XY library draws from a 15-bit rand();
+     at low temperatures both shift the reference library's energies by more
+     than the statistical error of these runs, so the engine's exact sampling
+     is compared with "alg" as well as with the library.
 
 The reference starts every run from its own initial state (all spins along
 +x, mcMain passes flunc = 0: heisenbergLib.c:154-172, xyLib.c:120-131), so
@@ -52,7 +59,9 @@ def fingerprint(args):
     import numpy as np
     out = []
     for a in args:
-        if isinstance(a, (tuple, list)) or hasattr(a, "shape"):
+        if np.ndim(a) == 0:  # Python or numpy scalar
+            out.append(float(a))
+        elif isinstance(a, (tuple, list)) or hasattr(a, "shape"):
             x = np.asarray(a, dtype=np.float64).reshape(-1)
             w = 1.0 + (np.arange(x.size) % 1009)
             out.append([int(x.size), float(x.sum()), float((x * w).sum()), float((x * x).sum())])
@@ -102,6 +111,28 @@ def _run_one(job):
     return seed, [float(v) for v in r[:n]]
 
 
+def _run_alg(job):
+    from oracle import oracle as orc
+    model, args, seed = job
+    r, _ = orc.solve(model, args, seed=seed, mode=2)
+    n = 10 if model == "ising" else 27
+    return seed, [float(v) for v in r[:n]]
+
+
+def refresh_fingerprints():
+    """Recompute the stored fingerprints from the reference's marshalling
+    (no library runs)."""
+    from oracle import refharness as rh
+    path = os.path.join(HERE, "golden_large.json.gz")
+    with gzip.open(path, "rt") as f:
+        out = json.load(f)
+    cases = _cases()
+    for name, c in out["cases"].items():
+        c["fingerprint"] = fingerprint(rh.capture_args(cases[name]))
+    with gzip.open(path, "wt") as f:
+        json.dump(out, f)
+
+
 def main(names=None):
     from oracle import refharness as rh
     path = os.path.join(HERE, "golden_large.json.gz")
@@ -118,9 +149,10 @@ def main(names=None):
         fp = fingerprint(args)
         with mp.get_context("fork").Pool(os.cpu_count() or 1) as pool:
             res = dict(pool.map(_run_one, [(sp["model"], args, s) for s in SEEDS]))
+            alg = dict(pool.map(_run_alg, [(sp["model"], args, s) for s in SEEDS]))
         out["cases"][name] = {"model": sp["model"], "spec": mg.to_jsonable(sp), "fingerprint": fp,
-                              "ref": {str(s): res[s] for s in SEEDS}, "seeds": SEEDS,
-                              "seconds": round(time.time() - t, 1)}
+                              "ref": {str(s): res[s] for s in SEEDS}, "alg": {str(s): alg[s] for s in SEEDS},
+                              "seeds": SEEDS, "seconds": round(time.time() - t, 1)}
         print(name, "N=%d" % len(args[1]), "%.0f s" % (time.time() - t), flush=True)
         with gzip.open(path, "wt") as f:
             json.dump(out, f)
@@ -128,4 +160,7 @@ def main(names=None):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or None)
+    if sys.argv[1:] == ["--fingerprints"]:
+        refresh_fingerprints()
+    else:
+        main(sys.argv[1:] or None)
