@@ -146,14 +146,25 @@ __device__ __forceinline__ int cl_frame_src(int f, int ngroup, int gall)
 // of cl_frame_src made once per launch), passed between lanes by a shuffle.
 // The last two entries (re-check flag, measurement index) are the same in
 // every CTA and are taken from rank 0's slot, not summed.
+// The remote loads are issued eight at a time before any is added, so a
+// gather waits about one DSMEM round trip per eight CTAs instead of one per
+// CTA; the sum is still taken in rank order (adding the 0.0 of an absent
+// rank changes nothing).
 __device__ __forceinline__ void cluster_gather(double *part, double *entry, float *frame, const signed char *fsrc,
                                                int C, int slot, int lane)
 {
     cg::cluster_group cl = cg::this_cluster();
     double o = 0.0;
-    if (lane >= CL_NV + 2) o = part[slot * CL_SLOT + lane];
+    const int idx = slot * CL_SLOT + lane;
+    if (lane >= CL_NV + 2) o = part[idx];
     else
-        for (int q = 0; q < C; ++q) o += cl.map_shared_rank(part, q)[slot * CL_SLOT + lane];
+        for (int q0 = 0; q0 < C; q0 += 8) {
+            double v[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) v[j] = (q0 + j < C) ? cl.map_shared_rank(part, q0 + j)[idx] : 0.0;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) o += v[j];
+        }
     entry[lane] = o;
     const float of = (float)o;
     for (int f = lane; f - lane < F_NON; f += 32) {  // the bound is the same for every lane

@@ -479,8 +479,10 @@ Batch::~Batch()
     for (cudaStream_t g : gstreams) cudaStreamSynchronize(g);
     groups.clear();
     if (d_reps) cudaFree(d_reps);
-    if (d_active) cudaFree(d_active);
+    if (d_stop) cudaFree(d_stop);
+    if (h_stop) cudaFreeHost(h_stop);
     if (d_scratch) cudaFree(d_scratch);
+    for (cudaEvent_t e : tev) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
     if (stream2) cudaStreamDestroy(stream2);
     if (ev0) cudaEventDestroy(ev0);
@@ -1074,23 +1076,56 @@ int Batch::admit(const std::vector<int> &ids, double step_us)
     assign_schedules(ids, max_smem);
     // quota: the units a replica advances per step, so that each replica's
     // share of a step takes about step_us of device time on its schedule
-    // (measured rates per CTA: resident 1, cluster C: about 0.8 C, tiled about 4)
+    set_quotas(ids, step_us);
+    for (int i : ids) replicas[i]->rep.u_stop = replicas[i]->rep.u;  // nothing runs before the step sets its bound
+    for (int i : ids) CUDA_TRY(cudaMemcpyAsync(d_reps + i, &replicas[i]->rep, sizeof(Rep), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    int rc = init_states(ids);
+    if (rc != MCS_OK) return rc;
+    return build_groups(ids, true);
+}
+
+// Placement of the replicas that remain after others left: the balancer runs
+// again over every active replica (with no other load), and a replica whose
+// schedule or cluster size changes moves to the group of its new
+// configuration (its state is in its arena between launches, so a move needs
+// no copy).  Its quota restarts from the estimate of the new schedule.
+int Batch::rebalance(double step_us, std::vector<int> *orphans)
+{
+    std::vector<int> ids;
+    for (size_t i = 0; i < replicas.size(); ++i)
+        if (replicas[i]) ids.push_back((int)i);
+    if (ids.empty() || !balance) return MCS_OK;
+    std::vector<std::pair<int, int>> before;
+    for (int i : ids) before.push_back({replicas[i]->schedule, replicas[i]->pref_C});
+    assign_schedules(ids, resident_max_smem());
+    std::vector<int> moved;
+    for (size_t k = 0; k < ids.size(); ++k) {
+        Replica &r = *replicas[ids[k]];
+        if (r.schedule != before[k].first || r.pref_C != before[k].second) moved.push_back(ids[k]);
+    }
+    if (moved.empty()) return MCS_OK;
+    drop(moved, orphans);
+    set_quotas(moved, step_us);
+    return build_groups(moved, true);
+}
+
+// Initial quota of the replicas of `ids` from their schedule: the units that
+// take about step_us on it (measured rates per CTA: resident 1, cluster C:
+// about 0.8 C, tiled about 4); the measured group times then adjust it.
+void Batch::set_quotas(const std::vector<int> &ids, double step_us)
+{
     static const double r_cta[4] = {0, 0.40e9, 0.85e9, 0.65e9};
+    quota_ms = step_us * 1e-3;
     for (int i : ids) {
         Replica &r = *replicas[i];
         double ctas = 1.0;
         if (r.schedule == 6) ctas = 0.8 * std::max(1, r.pref_C);
         else if (r.schedule == 3) ctas = 4.0;
         const double per_unit = (double)r.hm.N / (r_cta[r.hm.dim] * ctas);
-        long long q = (long long)(step_us * 1e-6 / per_unit);
+        const long long q = (long long)(step_us * 1e-6 / per_unit);
         r.rep.quota = std::max(1LL, std::min(q, r.hm.units_total));
-        r.rep.u_stop = r.rep.u;  // nothing runs before the step sets its bound
     }
-    for (int i : ids) CUDA_TRY(cudaMemcpyAsync(d_reps + i, &replicas[i]->rep, sizeof(Rep), cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaStreamSynchronize(stream));
-    int rc = init_states(ids);
-    if (rc != MCS_OK) return rc;
-    return build_groups(ids, true);
 }
 
 // Take the replicas of `ids` out of their groups.  A group whose device lists
@@ -1209,7 +1244,8 @@ int Batch::advance(long long units)
 // group whose launch is refused (a configuration error, which leaves the
 // context usable) adds its replicas there and the others go on; an error at
 // the synchronisation is returned.
-int Batch::run_groups(const std::vector<long long> &todo, const std::vector<long long> &pre, std::vector<int> *failed)
+int Batch::run_groups(const std::vector<long long> &todo, const std::vector<long long> &pre, std::vector<int> *failed,
+                      std::vector<float> *group_ms)
 {
     const bool multi = groups.size() > 1;
     while (multi && gstreams.size() < groups.size()) {
@@ -1221,10 +1257,11 @@ int Batch::run_groups(const std::vector<long long> &todo, const std::vector<long
         gevents.push_back(ge);
     }
     const bool trace = getenv("MCSGPU_TRACE") != nullptr;
-    std::vector<cudaEvent_t> tev;
-    if (trace) {
-        tev.resize(2 * groups.size(), nullptr);
-        for (auto &e : tev) CUDA_TRY(cudaEventCreate(&e));
+    const bool timed = trace || group_ms;
+    while (timed && tev.size() < 2 * groups.size()) {  // per-group timing events, kept by the batch
+        cudaEvent_t te = nullptr;
+        CUDA_TRY(cudaEventCreate(&te));
+        tev.push_back(te);
     }
     if (multi) CUDA_TRY(cudaEventRecord(ev_fork, stream));
     for (size_t gi = 0; gi < groups.size(); ++gi) {
@@ -1233,7 +1270,7 @@ int Batch::run_groups(const std::vector<long long> &todo, const std::vector<long
         if (n_todo <= 0) continue;
         cudaStream_t gs = multi ? gstreams[gi] : stream;
         if (multi) CUDA_TRY(cudaStreamWaitEvent(gs, ev_fork, 0));
-        if (trace) CUDA_TRY(cudaEventRecord(tev[2 * gi], gs));
+        if (timed) CUDA_TRY(cudaEventRecord(tev[2 * gi], gs));
         cudaError_t e = cudaSuccess;
         const char *what = "";
         if (G.kind == 4 || G.kind == 5) {
@@ -1284,7 +1321,7 @@ int Batch::run_groups(const std::vector<long long> &todo, const std::vector<long
             cudaGetLastError();
             failed->insert(failed->end(), G.ids.begin(), G.ids.end());
         }
-        if (trace) CUDA_TRY(cudaEventRecord(tev[2 * gi + 1], gs));
+        if (timed) CUDA_TRY(cudaEventRecord(tev[2 * gi + 1], gs));
         if (multi) {
             CUDA_TRY(cudaEventRecord(gevents[gi], gs));
             CUDA_TRY(cudaStreamWaitEvent(stream, gevents[gi], 0));
@@ -1297,11 +1334,17 @@ int Batch::run_groups(const std::vector<long long> &todo, const std::vector<long
     cudaEventElapsedTime(&ms, ev0, ev1);
     device_ms += ms;
     last_ms = ms;
+    if (group_ms) {
+        group_ms->assign(groups.size(), -1.f);
+        for (size_t gi = 0; gi < groups.size(); ++gi)
+            if (todo[gi] > 0) cudaEventElapsedTime(&(*group_ms)[gi], tev[2 * gi], tev[2 * gi + 1]);
+        cudaGetLastError();
+    }
     if (trace) {
         for (size_t gi = 0; gi < groups.size(); ++gi) {
             const Group &G = *groups[gi];
             float gms = -1.f;
-            if (cudaEventQuery(tev[2 * gi + 1]) == cudaSuccess) cudaEventElapsedTime(&gms, tev[2 * gi], tev[2 * gi + 1]);
+            if (todo[gi] > 0) cudaEventElapsedTime(&gms, tev[2 * gi], tev[2 * gi + 1]);
             long long sites = 0, maxn = 0;
             for (int id : G.ids) { sites += replicas[id]->hm.N; maxn = std::max<long long>(maxn, replicas[id]->hm.N); }
             fprintf(stderr, "mcsgpu trace: group %zu kind %d dim %d C %d threads %d replicas %zu sites %lld max %lld: %.3f ms\n",
@@ -1309,7 +1352,6 @@ int Batch::run_groups(const std::vector<long long> &todo, const std::vector<long
         }
         fprintf(stderr, "mcsgpu trace: step %.3f ms\n", ms);
         cudaGetLastError();
-        for (auto &e2 : tev) if (e2) cudaEventDestroy(e2);
     }
     return MCS_OK;
 }
@@ -1331,19 +1373,25 @@ int Batch::advance_quota(std::vector<int> *failed)
             active.push_back(id);
         }
     if (active.empty()) return MCS_OK;
-    if ((int)active.size() > active_cap) {
-        if (d_active) cudaFree(d_active);
-        d_active = nullptr;
-        active_cap = 0;
-        CUDA_TRY(cudaMalloc(&d_active, (size_t)slot_capacity * sizeof(int)));
-        active_cap = slot_capacity;
+    if (!d_stop) {
+        CUDA_TRY(cudaMalloc(&d_stop, (size_t)slot_capacity * sizeof(StopItem)));
+        CUDA_TRY(cudaMallocHost(&h_stop, (size_t)slot_capacity * sizeof(StopItem)));
     }
-    CUDA_TRY(cudaMemcpyAsync(d_active, active.data(), active.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
+    // one copy of (replica, quota) pairs from page-locked memory and one small
+    // kernel set every replica's quota and stop unit for this step
+    CUDA_TRY(cudaStreamSynchronize(stream));  // the previous step's copy has been consumed
+    for (size_t k = 0; k < active.size(); ++k) {
+        h_stop[k].id = active[k];
+        h_stop[k].pad = 0;
+        h_stop[k].quota = replicas[active[k]]->rep.quota;
+    }
+    CUDA_TRY(cudaMemcpyAsync(d_stop, h_stop, active.size() * sizeof(StopItem), cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaEventRecord(ev0, stream));
-    CUDA_TRY(launch_set_stop(d_reps, d_active, (int)active.size(), stream));
+    CUDA_TRY(launch_set_stop(d_reps, d_stop, (int)active.size(), stream));
     launches++;
     std::vector<int> fl;
-    int rc = run_groups(todo, pre, &fl);
+    std::vector<float> gms;
+    int rc = run_groups(todo, pre, &fl, &gms);
     if (rc != MCS_OK) return rc;
     std::vector<char> bad(replicas.size(), 0);
     for (int i : fl) bad[i] = 1;
@@ -1351,6 +1399,21 @@ int Batch::advance_quota(std::vector<int> *failed)
         if (bad[id]) continue;
         Rep &R = replicas[id]->rep;
         R.u = std::min(replicas[id]->hm.units_total, R.u + R.quota);
+    }
+    // quotas follow the measured device time: a group whose launches took t ms
+    // for its largest quota scales its members' quotas by quota_ms / t (at most
+    // x4 or /4 per step), so that every group's share of a step takes about
+    // quota_ms whatever its schedule and however the device is shared (the
+    // next step's stop kernel carries the new quotas to the device)
+    if (quota_ms > 0) {
+        for (size_t gi = 0; gi < groups.size(); ++gi) {
+            if (todo[gi] <= 0 || gms[gi] <= 0.f) continue;
+            const double f = std::min(4.0, std::max(0.25, quota_ms / (double)gms[gi]));
+            for (int id : groups[gi]->ids) {
+                Rep &R = replicas[id]->rep;
+                R.quota = std::max(1LL, std::min((long long)llround((double)R.quota * f), replicas[id]->hm.units_total));
+            }
+        }
     }
     if (failed) failed->insert(failed->end(), fl.begin(), fl.end());
     return MCS_OK;

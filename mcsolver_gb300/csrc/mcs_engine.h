@@ -88,8 +88,8 @@ struct Batch {
     int device = 0;
     std::vector<std::unique_ptr<Replica>> replicas;
     Rep *d_reps = nullptr;
-    int *d_active = nullptr;   // slot mode: replicas of the current step
-    int active_cap = 0;
+    StopItem *d_stop = nullptr;  // slot mode: (replica, quota) of the current step
+    StopItem *h_stop = nullptr;  // page-locked staging of the same
     void *d_scratch = nullptr;
     bool prepared = false;
     std::vector<std::unique_ptr<Group>> groups;
@@ -126,10 +126,15 @@ struct Batch {
     int slot_capacity = 0;
     int admit(const std::vector<int> &ids, double step_us);        // new replicas in these slots
     void drop(const std::vector<int> &ids, std::vector<int> *orphans);  // replicas leaving their groups
+    int rebalance(double step_us, std::vector<int> *orphans);          // re-place the remaining replicas
+    void set_quotas(const std::vector<int> &ids, double step_us);
     // every replica of the groups advances by its own quota (Rep::quota); the
     // replicas of a group whose launch failed are added to *failed
     int advance_quota(std::vector<int> *failed);
-    int run_groups(const std::vector<long long> &todo, const std::vector<long long> &pre, std::vector<int> *failed);
+    int run_groups(const std::vector<long long> &todo, const std::vector<long long> &pre, std::vector<int> *failed,
+                   std::vector<float> *group_ms = nullptr);
+    double quota_ms = 0;             // slot mode: target device time of a group's share of a step
+    std::vector<cudaEvent_t> tev;    // per-group timing events (start, end)
     int collect();                 // read back descriptors and counters
     int sync_descriptors();        // read back descriptors: progress travels with each replica
     void release_groups();         // drop groups and descriptor arrays; the next advance re-prepares

@@ -193,6 +193,11 @@ cudaError_t launch_tiled_finalize_dim(int dim, Rep *reps, const int *ids, int nr
                                       double *dEpart, long long *ipart, const int *mitem_off, double *fpart,
                                       cudaStream_t st);
 cudaError_t launch_init_state_dg(int dim, int geom, Rep *reps, const int *ids, int nrep, cudaStream_t st);
-// reps[ids[i]].u_stop = min(units_total, u + quota)
-cudaError_t launch_set_stop(Rep *reps, const int *ids, int n, cudaStream_t st);
+// reps[items[i].id]: quota = items[i].quota, u_stop = min(units_total, u + quota)
+struct StopItem {
+    int id;
+    int pad;
+    long long quota;
+};
+cudaError_t launch_set_stop(Rep *reps, const StopItem *items, int n, cudaStream_t st);
 }  // namespace mcs

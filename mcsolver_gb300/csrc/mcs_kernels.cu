@@ -926,20 +926,22 @@ cudaError_t launch_tiled_finalize_dim(int dim, Rep *reps, const int *ids, int nr
     return cudaGetLastError();
 }
 
-// Server step bound: each replica of ids stops after its quota of units.
-__global__ void k_set_stop(Rep *reps, const int *ids, int n)
+// Server step bound: each listed replica takes its quota for this step and
+// stops after that many units.
+__global__ void k_set_stop(Rep *reps, const StopItem *items, int n)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    Rep &R = reps[ids[i]];
+    Rep &R = reps[items[i].id];
+    R.quota = items[i].quota;
     const long long s = R.u + R.quota;
     R.u_stop = s < R.units_total ? s : R.units_total;
 }
 
-cudaError_t launch_set_stop(Rep *reps, const int *ids, int n, cudaStream_t st)
+cudaError_t launch_set_stop(Rep *reps, const StopItem *items, int n, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
-    k_set_stop<<<(n + 127) / 128, 128, 0, st>>>(reps, ids, n);
+    k_set_stop<<<(n + 127) / 128, 128, 0, st>>>(reps, items, n);
     return cudaGetLastError();
 }
 

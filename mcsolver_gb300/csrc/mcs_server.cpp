@@ -337,6 +337,23 @@ extern "C" int mcs_server_step(mcs_server *s, int32_t *completed)
     for (auto &f : fin) ok += f.second.status == MCS_OK;
     retire_slots(s, out, fin);
     if (completed) *completed = ok;
+    // the remaining requests are placed again for the lighter load (a large
+    // lattice left alone moves to a larger cluster)
+    std::vector<int> orphans;
+    if (b.rebalance(s->step_us, &orphans) != MCS_OK) {
+        cudaGetLastError();
+        for (int k = 0; k < s->max_slots; ++k)
+            if (b.replicas[k]) {
+                bool grouped = false;
+                for (auto &G : b.groups) grouped |= std::find(G->ids.begin(), G->ids.end(), k) != G->ids.end();
+                if (!grouped) orphans.push_back(k);
+            }
+    }
+    if (!orphans.empty()) {
+        std::vector<std::pair<int, mcs_server::Done>> ofin;
+        for (int k : orphans) ofin.emplace_back(k, failed_done(MCS_ECUDA, "re-placing this request failed: " + get_error()));
+        retire_slots(s, orphans, ofin);
+    }
     return MCS_OK;
 }
 
