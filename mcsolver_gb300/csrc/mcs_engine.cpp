@@ -112,35 +112,86 @@ size_t replica_acc_count(const HostModel &m)
     return A_GRP + (size_t)(G + 1) * (G + 1) + (G + 1);
 }
 
+SharedLists::~SharedLists()
+{
+    if (d) cudaFree(d);
+}
+
+// One allocation holding the index arrays of a lattice (the pieces a replica
+// compiled from its template takes unchanged), uploaded once.
+int make_shared_lists(const HostModel &m, int device, std::unique_ptr<SharedLists> *out)
+{
+    ArenaBuilder A;
+    std::unique_ptr<SharedLists> sh(new SharedLists());
+    size_t o_nbr = 0, o_lcode = 0, o_deg = 0;
+    if (m.geom == MCS_GEOM_ELL) { o_nbr = A.addv(m.nbr); o_lcode = A.addv(m.lcode); o_deg = A.addv(m.deg); }
+    const size_t o_stype = A.addv(m.stype), o_cp = A.addv(m.cpair), o_rorb = A.addv(m.rorb), o_rcl = A.addv(m.rcl),
+                 o_rlink = A.addv(m.rlink), o_rjc = A.addv(m.rjc), o_rdeg = A.addv(m.rdeg), o_rindex = A.addv(m.rindex),
+                 o_circ = A.addv(m.circ), o_slen = A.addv(m.slen), o_sval = A.addv(m.sval), o_gmask = A.addv(m.gmask),
+                 o_sflag = A.addv(m.sflag), o_rtgt = A.addv(m.rtgt);
+    std::vector<unsigned char> img = A.finish();
+    CUDA_TRY(cudaSetDevice(device));
+    CUDA_TRY(cudaMalloc(&sh->d, img.size()));
+    sh->bytes = img.size();
+    CUDA_TRY(cudaMemcpy(sh->d, img.data(), img.size(), cudaMemcpyHostToDevice));
+    unsigned char *b = (unsigned char *)sh->d;
+    if (m.geom == MCS_GEOM_ELL) {
+        sh->nbr = (const int *)(b + o_nbr);
+        sh->lcode = (const unsigned short *)(b + o_lcode);
+        sh->deg = b + o_deg;
+    }
+    sh->stype = b + o_stype;
+    sh->cpair = (const int *)(b + o_cp); sh->rorb = (const int *)(b + o_rorb); sh->rcl = (const int *)(b + o_rcl);
+    sh->rlink = (const int *)(b + o_rlink); sh->rjc = (const unsigned short *)(b + o_rjc); sh->rdeg = b + o_rdeg;
+    sh->rindex = (const int *)(b + o_rindex); sh->circ = (const int *)(b + o_circ);
+    sh->slen = (const float *)(b + o_slen); sh->sval = (const float *)(b + o_sval);
+    sh->gmask = b + o_gmask; sh->sflag = b + o_sflag; sh->rtgt = (const int *)(b + o_rtgt);
+    *out = std::move(sh);
+    return MCS_OK;
+}
+
 int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool upload, const ModelTemplate *tmpl,
-                  bool *reused)
+                  bool *reused, const SharedLists *shared)
 {
     std::string err;
-    int rc = compile_model(p, o, &r->hm, &err, tmpl, reused);
+    bool re = false;
+    int rc = compile_model(p, o, &r->hm, &err, tmpl, &re);
+    if (reused) *reused = re;
     if (rc != MCS_OK) { set_error(err); return rc; }
     const HostModel &m = r->hm;
+    // a replica compiled from its lattice's template reads the batch's shared
+    // copy of the index arrays; its arena holds only its own values and state
+    const bool share = shared && re && m.dim > 1;
+    r->shared = share ? shared : nullptr;
+    static const std::vector<int> no_i;
+    static const std::vector<uint16_t> no_u16;
+    static const std::vector<uint8_t> no_u8;
+    static const std::vector<float> no_f;
     r->record_series = o && o->record_series;
     r->requested_schedule = o ? o->schedule : 0;
     r->recheck = (o && o->recheck_every > 0) ? o->recheck_every : 32;
     ArenaBuilder A;
     size_t o_nbr = 0, o_lcode = 0, o_lcls = 0, o_deg = 0, o_stype = 0, o_jt = 0, o_jt64 = 0, o_dt = 0, o_it = 0;
     if (m.geom == MCS_GEOM_ELL) {
-        o_nbr = A.addv(m.nbr);
-        o_lcode = A.addv(m.lcode);
-        o_deg = A.addv(m.deg);
+        o_nbr = A.addv(share ? no_i : m.nbr);
+        o_lcode = A.addv(share ? no_u16 : m.lcode);
+        o_deg = A.addv(share ? no_u8 : m.deg);
     }
     if (m.dim == 1) o_lcls = A.addv(m.lcls);
-    o_stype = A.addv(m.stype);
+    o_stype = A.addv(share ? no_u8 : m.stype);
     if (m.dim > 1) { o_jt = A.addv(m.jtab); o_jt64 = A.addv(m.jtab64); o_dt = A.addv(m.dtab); }
     else o_it = A.addv(m.itab);
-    size_t o_cp = A.addv(m.cpair), o_rorb = A.addv(m.rorb), o_rcl = A.addv(m.rcl), o_rlink = A.addv(m.rlink);
+    size_t o_cp = A.addv(share ? no_i : m.cpair), o_rorb = A.addv(share ? no_i : m.rorb),
+           o_rcl = A.addv(share ? no_i : m.rcl), o_rlink = A.addv(share ? no_i : m.rlink);
     size_t o_rjc = 0, o_rK = 0;
-    if (m.dim > 1) o_rjc = A.addv(m.rjc);
+    if (m.dim > 1) o_rjc = A.addv(share ? no_u16 : m.rjc);
     else o_rK = A.addv(m.rK);
     size_t o_rkc = m.dim == 1 ? A.addv(m.rkc) : 0;
-    size_t o_rdeg = A.addv(m.rdeg), o_rindex = A.addv(m.rindex), o_circ = A.addv(m.circ);
-    size_t o_slen = A.addv(m.slen), o_sval = A.addv(m.sval), o_gmask = A.addv(m.gmask);
-    size_t o_sflag = A.addv(m.sflag), o_rtgt = A.addv(m.rtgt);
+    size_t o_rdeg = A.addv(share ? no_u8 : m.rdeg), o_rindex = A.addv(share ? no_i : m.rindex),
+           o_circ = A.addv(share ? no_i : m.circ);
+    size_t o_slen = A.addv(share ? no_f : m.slen), o_sval = A.addv(share ? no_f : m.sval),
+           o_gmask = A.addv(share ? no_u8 : m.gmask);
+    size_t o_sflag = A.addv(share ? no_u8 : m.sflag), o_rtgt = A.addv(share ? no_i : m.rtgt);
     int spad = (m.N + 31) & ~31;
     size_t o_spins;
     std::vector<float> sp;  // O(n) spins padded per component (lives until A.finish())
@@ -292,6 +343,12 @@ int upload_replica(Replica *r)
     RELOC(rdeg); RELOC(rindex); RELOC(circ); RELOC(slen); RELOC(sval); RELOC(gmask); RELOC(sflag); RELOC(rtgt);
     RELOC(spins); RELOC(acc); RELOC(series); RELOC(icnt); RELOC(stats); RELOC(wbits); RELOC(wqueue);
 #undef RELOC
+    if (const SharedLists *sh = r->shared) {
+        R.nbr = sh->nbr; R.lcode = sh->lcode; R.deg = sh->deg; R.stype = sh->stype;
+        R.cpair = sh->cpair; R.rorb = sh->rorb; R.rcl = sh->rcl; R.rlink = sh->rlink; R.rjc = sh->rjc;
+        R.rdeg = sh->rdeg; R.rindex = sh->rindex; R.circ = sh->circ; R.slen = sh->slen; R.sval = sh->sval;
+        R.gmask = sh->gmask; R.sflag = sh->sflag; R.rtgt = sh->rtgt;
+    }
     // spin frames: kernels store each snapshot straight into page-locked host
     // memory mapped into the device, so frames take no device memory and need
     // no copy at the end
@@ -527,8 +584,21 @@ int Batch::add(const mcs_problem *p, const mcs_options *o, int *idx)
         for (auto it = templates.rbegin(); it != templates.rend() && !t; ++it)
             if ((*it)->in.model == p->model && (*it)->in.N == p->n_sites && (*it)->in.z == p->max_links) t = *it;
     }
+    // the index arrays of that lattice, uploaded once for the batch
+    const SharedLists *sh = nullptr;
+    if (t) {
+        std::lock_guard<std::mutex> lock(add_mutex);
+        auto it = shared_lists.find(t.get());
+        if (it == shared_lists.end()) {
+            std::unique_ptr<SharedLists> nsh;
+            int rc = make_shared_lists(t->hm, device, &nsh);
+            if (rc != MCS_OK) return rc;
+            it = shared_lists.emplace(t.get(), std::move(nsh)).first;
+        }
+        sh = it->second.get();
+    }
     bool reused = false;
-    int rc = build_replica(p, o, r.get(), true, t.get(), &reused);
+    int rc = build_replica(p, o, r.get(), true, t.get(), &reused, sh);
     if (rc != MCS_OK) return rc;
     std::shared_ptr<const ModelTemplate> nt;
     if (on && !reused) {
@@ -1615,6 +1685,7 @@ int mcs_batch_memory(mcs_batch *b, uint64_t *device_bytes, uint64_t *readback_by
 {
     if (!b) return MCS_EINVAL;
     uint64_t dev = 0, rb = 0;
+    for (auto &sl : b->b.shared_lists) dev += sl.second->bytes;
     for (auto &r : b->b.replicas) {
         dev += r->bytes + sizeof(Rep);
         rb += sizeof(Rep) + r->nacc * sizeof(double) + (C_NINT + S_NSTAT) * sizeof(long long);

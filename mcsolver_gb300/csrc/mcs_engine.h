@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -15,6 +16,23 @@ namespace mcs {
 
 void set_error(const std::string &s);
 const std::string &get_error();
+
+// Device copy of a lattice's index arrays (geometry, classes, measurement
+// lists), shared by every replica of a batch compiled from that lattice's
+// template: the replicas of a temperature grid or a parallel-tempering ladder
+// then read one copy of them (from L2) instead of one each.
+struct SharedLists {
+    void *d = nullptr;
+    size_t bytes = 0;
+    const int *nbr = nullptr;
+    const unsigned short *lcode = nullptr, *rjc = nullptr;
+    const unsigned char *deg = nullptr, *stype = nullptr, *rdeg = nullptr, *gmask = nullptr, *sflag = nullptr;
+    const int *cpair = nullptr, *rorb = nullptr, *rcl = nullptr, *rlink = nullptr, *rindex = nullptr, *circ = nullptr,
+              *rtgt = nullptr;
+    const float *slen = nullptr, *sval = nullptr;
+    ~SharedLists();
+};
+int make_shared_lists(const HostModel &m, int device, std::unique_ptr<SharedLists> *out);
 
 // One solve on the device.
 struct Replica {
@@ -33,6 +51,7 @@ struct Replica {
     int device = 0;
     bool initialized = false;          // initial-state kernel has run
     int pref_C = 0;                    // cluster size chosen by the load balancer (0: none)
+    const SharedLists *shared = nullptr; // index arrays shared with other replicas of the batch (or null)
     std::vector<unsigned char> staging; // host image of the arena until upload
     std::vector<unsigned char> rblock;  // host copy of the result block (acc, icnt, stats)
     bool rblock_fresh = false;          // rblock matches the device (set by a batched readback)
@@ -40,7 +59,7 @@ struct Replica {
 };
 
 int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool upload,
-                  const ModelTemplate *tmpl = nullptr, bool *reused = nullptr);
+                  const ModelTemplate *tmpl = nullptr, bool *reused = nullptr, const SharedLists *shared = nullptr);
 int upload_replica(Replica *r);
 int replica_results(Replica *r, const Rep &Rfinal, mcs_result *res);
 // Read the result blocks of many replicas with one synchronisation.
@@ -98,6 +117,7 @@ struct Batch {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_a = nullptr, ev_b = nullptr, ev_fork = nullptr;
     std::mutex add_mutex;       // mcs_batch_add may be called from several threads
     std::vector<std::shared_ptr<const ModelTemplate>> templates;  // compiled lattices of this batch (O(n))
+    std::map<const ModelTemplate *, std::unique_ptr<SharedLists>> shared_lists;  // their index arrays on the device
     int cluster_override = 0;   // 1: never cluster; 2/4/8: only that size
     int no_autotune = 0;
     int balance = 1;            // place replicas by the load balancer (off for parallel tempering)

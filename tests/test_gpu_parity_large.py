@@ -15,7 +15,19 @@
   reference's own initial state (every spin along +x); per-replica results
   and the reference's per-seed results give two means with standard errors
   from their spreads, which must agree within 3.5 combined standard errors
-  plus the resolution of FP32 spin state.  Compared: e, e^2, the
+  plus the resolution of FP32 spin state.
+  Two references are stored per case: the reference C library itself, and
+  the reference's algorithm with a sound generator (the oracle's mode 2:
+  the library's random-site order, proposals and acceptance, with SplitMix64
+  in place of glibc rand()).  The library draws from glibc rand(), an
+  additive lagged-Fibonacci generator, and the XY library from a 15-bit
+  rand(); at low temperatures these shift its energies by more than the
+  error of 32 seeds (measured on the CPU: at XY L = 32, T = 0.5, 120,000
+  sweeps, the same algorithm gives <e> = -3.45890(9) with glibc rand() and
+  -3.45938(4) with SplitMix64; the engine gives -3.45952(6)).  The engine
+  must agree with the algorithm with the sound generator on every compared
+  observable, and with the library wherever the library agrees with its own
+  algorithm; where it does not, the library's shift is printed.  Compared: e, e^2, the
   renormalised e_r and e_r^2, C = N (<e^2> - <e>^2) for every case; the
   magnetisation components and U4 where their autocorrelation time (measured:
   about 400 sweeps for XY below 1.2 K at L = 128) is short against the run
@@ -103,23 +115,34 @@ def test_observables_on_configuration_lattices(engine, name, capsys):
     c = G["cases"][name]
     model = c["model"]
     ref = np.array([c["ref"][str(s)] for s in c["seeds"]], float)
+    alg = np.array([c["alg"][str(s)] for s in c["seeds"]], float)
     mine = _engine_runs(engine, name, c)
     N = int(np.prod(c["spec"]["L"])) * len(c["spec"]["pos"])
-    lines = []
-    worst = 0.0
-    for k in _compared(name, model):
-        if k == "C":
-            x, y = _with_C(ref, N, c["spec"]["T"]), _with_C(mine, N, c["spec"]["T"])
-        else:
-            x, y = ref[:, k], mine[:, k]
+    lines, failures = [], []
+
+    def col(a, k):
+        return _with_C(a, N, c["spec"]["T"]) if k == "C" else a[:, k]
+
+    def z(x, y):
         se = math.sqrt(x.var(ddof=1) / len(x) + y.var(ddof=1) / len(y))
-        z = abs(x.mean() - y.mean()) / se if se > 0 else 0.0
-        worst = max(worst, z)
-        lines.append("  [%s] reference %.6g +- %.2g  engine %.6g +- %.2g  |z| %.2f" % (
-            k, x.mean(), x.std(ddof=1) / math.sqrt(len(x)), y.mean(), y.std(ddof=1) / math.sqrt(len(y)), z))
-        assert abs(x.mean() - y.mean()) <= 3.5 * se + FP32_FLOOR * max(1.0, abs(x.mean())), (name, lines[-1])
+        d = abs(x.mean() - y.mean())
+        return (d / se if se > 0 else 0.0), d <= 3.5 * se + FP32_FLOOR * max(1.0, abs(x.mean()))
+
+    for k in _compared(name, model):
+        x, a, y = col(ref, k), col(alg, k), col(mine, k)
+        z_alg, ok_alg = z(a, y)
+        z_ref, ok_ref = z(x, y)
+        z_lib, lib_sound = z(x, a)
+        lines.append("  [%s] library %.6g +- %.2g  algorithm %.6g +- %.2g  engine %.6g +- %.2g  "
+                     "|z| engine-algorithm %.2f  engine-library %.2f  library-algorithm %.2f" % (
+                         k, x.mean(), x.std(ddof=1) / math.sqrt(len(x)), a.mean(), a.std(ddof=1) / math.sqrt(len(a)),
+                         y.mean(), y.std(ddof=1) / math.sqrt(len(y)), z_alg, z_ref, z_lib))
+        if not ok_alg or (lib_sound and not ok_ref):
+            failures.append(lines[-1])
     with capsys.disabled():
-        print("\n%s (reference %d seeds, engine %d runs)\n%s" % (name, len(ref), len(mine), "\n".join(lines)))
+        print("\n%s (library and algorithm %d seeds each, engine %d runs)\n%s" % (name, len(ref), len(mine),
+                                                                                 "\n".join(lines)))
+    assert not failures, (name, failures)
 
 
 TRAJ = [
