@@ -633,6 +633,41 @@ def run_whole_solves(args, workload=None, plain_sample=None):
                       "batched_over_plain": rate / (ps / pt) if pt > 0 else None}
 
 
+def run_many_small(args):
+    """Many small replicas: 1024 square Ising ferromagnets, L = 32, h = 0,
+    temperatures spread over 1.5..3.5 K, Metropolis, tau = N, 200 + 1000
+    sweeps, in one batch.  Timed three ways: with the autotuner's choice among
+    its candidates for the group (one 128-thread CTA per replica, one warp per
+    replica, copies over a cluster), and pinned to one CTA of 128 threads and
+    to one warp per replica.  Device time of the whole run."""
+    import mcsolver_gb300 as eng
+    from mcsolver_gb300 import build as b
+    from mcsolver_gb300.lattice import rescale_args, square_args_fast
+    b.build()
+    n, Lw, nth, nsw = 1024, 32, 200, 1000
+    base = square_args_fast("ising", Lw, 1.0, nthermal=nth, nsweep=nsw, arrays=True)
+    jobs = [rescale_args("ising", base, 1.5 + 2.0 * k / (n - 1)) for k in range(n)]
+    out = {"workload": "ising_square_L32_1024_replicas", "replicas": n, "nthermal": nth, "nsweep": nsw}
+    for label, force in (("autotuned", None), ("cta128_per_replica", "0:128"), ("warp_per_replica", "0:32")):
+        if force:
+            os.environ["MCSGPU_FORCE"] = force
+        else:
+            os.environ.pop("MCSGPU_FORCE", None)
+        bt = eng.Batch()
+        for k, a in enumerate(jobs):
+            bt.add("ising", a, seed=40000 + k, random_init=True)
+        bt.prepare()
+        bt.run()
+        st = bt.stats()
+        sched = bt.schedules()
+        bt.close()
+        out[label] = {"site_updates_per_s": st["site_updates"] / (st["device_ms"] / 1000.0), "device_ms": st["device_ms"],
+                      "schedule": [{"schedule": g[0], "ctas_per_replica": g[1], "threads": g[2], "replicas": g[3]}
+                                   for g in sched]}
+    os.environ.pop("MCSGPU_FORCE", None)
+    return out
+
+
 def run_noalloc(args):
     """The allocation-free entry point mcs_ising_square_noalloc on caller-held
     device buffers: square Ising ferromagnet (K = -1/T, T = 2.3), L x L int8
@@ -744,7 +779,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-served", action="store_true", help="headline: skip the served-stream part of the line")
     ap.add_argument("--workload", default="headline", choices=["headline", "served", "batched4", "pt", "ising", "xy_wolff",
-                                                                  "noalloc"])
+                                                                  "noalloc", "many_small"])
     ap.add_argument("--requests", type=int, default=48)
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--nthermal", type=int, default=1000)
@@ -765,6 +800,8 @@ def main():
         return print(json.dumps(run_whole_solves(args)))
     if args.workload == "noalloc":
         return run_noalloc(args)
+    if args.workload == "many_small":
+        return print(json.dumps(run_many_small(args)))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         if rank == 0:

@@ -31,6 +31,16 @@
 namespace mcs {
 
 static thread_local std::string g_err;
+
+// The batch and the server run every launch group on its own stream, side by
+// side; with the runtime's default of 8 hardware connections, groups beyond
+// the eighth share a connection and wait for one another.  Raised to 32 when
+// the library loads, unless the process has set it (it must be set before the
+// device context is created).
+__attribute__((constructor)) static void mcs_raise_connections()
+{
+    setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
+}
 void set_error(const std::string &s) { g_err = s; }
 const std::string &get_error() { return g_err; }
 
@@ -824,6 +834,27 @@ void Batch::place_replicas(int max_smem, const std::vector<int> &ids, double bas
         for (int k : moved) --ps[k].opt;
         break;
     }
+    // Then, one replica at a time in order of its own critical path, a larger
+    // cluster for any replica whose move does not lengthen the estimate: a
+    // replica that cannot move (an Ising lattice without a cluster kernel) no
+    // longer holds the others at one CTA, and each finishes as early as the
+    // device allows.  Moves to the tiled schedule are left to the first pass.
+    std::vector<char> frozen(ps.size(), 0);
+    for (size_t it = 0; it < 4 * ps.size() + 4; ++it) {
+        int pick = -1;
+        double mc = 0;
+        for (int k = 0; k < (int)ps.size(); ++k) {
+            const P &q = ps[k];
+            if (frozen[k] || q.opt + 1 >= (int)q.opts.size() || q.opts[q.opt + 1] <= 1) continue;
+            const double c = crit(q);
+            if (c > mc) { mc = c; pick = k; }
+        }
+        if (pick < 0) break;
+        ++ps[pick].opt;
+        const double now = estimate();
+        if (now <= best * (1.0 + 1e-9)) best = std::min(best, now);
+        else { --ps[pick].opt; frozen[pick] = 1; }
+    }
     for (auto &q : ps) {
         Replica &r = *replicas[q.i];
         const int o = q.opts[q.opt];
@@ -1007,6 +1038,11 @@ int Batch::build_groups(const std::vector<int> &ids, bool merge)
                                 G->candidates.push_back({0, G->threads});
                         } else if (kind == 2) {
                             G->candidates.push_back({0, G->threads});
+                            // one warp per replica (a CTA of 32 threads): for groups of many
+                            // small replicas that fill the device anyway, where the barriers
+                            // and block reductions of a larger CTA cost more than its threads
+                            // gain; the autotuner keeps it only where it is faster
+                            if ((int)set.size() >= 32 && G->threads > 32) G->candidates.push_back({0, 32});
                             // copies of each replica over a cluster of 2 or 4 CTAs: for groups
                             // that would leave SMs idle (Metropolis only)
                             bool metro = true;
@@ -1173,6 +1209,12 @@ int Batch::rebalance(double step_us, std::vector<int> *orphans)
     for (size_t k = 0; k < ids.size(); ++k) {
         Replica &r = *replicas[ids[k]];
         if (r.schedule != before[k].first || r.pref_C != before[k].second) moved.push_back(ids[k]);
+    }
+    if (getenv("MCSGPU_TRACE")) {
+        fprintf(stderr, "mcsgpu trace: rebalance %zu active, %zu moved:", ids.size(), moved.size());
+        for (int i : ids)
+            fprintf(stderr, " [%d N=%d sched %d C %d]", i, replicas[i]->hm.N, replicas[i]->schedule, replicas[i]->pref_C);
+        fprintf(stderr, "\n");
     }
     if (moved.empty()) return MCS_OK;
     drop(moved, orphans);
@@ -1567,6 +1609,28 @@ int mcs_abi_version(void) { return 1; }
 // and `problem` is compiled from its template (*reused tells whether the
 // template's structure was taken), so a test can check that the template path
 // and a full compile give the same bytes.
+// Host-compile facts, exported for the CPU tests and not declared in
+// include/mcsgpu.h: info[0..7] = geometry (0 general, 1 square), cluster
+// schedule applies, regular square measurement, sites, Lx, Ly, colours,
+// every correlated pair (v, v).
+int mcs_test_compile_info(const mcs_problem *problem, const mcs_options *options, int32_t *info)
+{
+    try {
+        mcs_options def;
+        memset(&def, 0, sizeof def);
+        Replica r;
+        int rc = build_replica(problem, options ? options : &def, &r, false);
+        if (rc != MCS_OK) return rc;
+        const HostModel &m = r.hm;
+        const int32_t v[8] = {m.geom, m.cluster_ok, m.meas_regular, m.N, m.Lx, m.Ly, m.ncol, m.pair_identity};
+        for (int k = 0; k < 8; ++k) info[k] = v[k];
+        return MCS_OK;
+    } catch (const std::exception &e) {
+        set_error(e.what());
+        return MCS_EINVAL;
+    }
+}
+
 int mcs_test_compile_digest(const mcs_problem *template_problem, const mcs_problem *problem,
                             const mcs_options *options, uint64_t *digest, int32_t *reused)
 {

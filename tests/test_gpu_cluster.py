@@ -220,3 +220,38 @@ def test_every_candidate_records_the_same_series(engine, name, model, mk, cand):
     assert eb["series"].shape == ea["series"].shape
     np.testing.assert_allclose(eb["series"], ea["series"], rtol=1e-5, atol=2e-5)
     np.testing.assert_allclose(np.array(b[:27]), np.array(a[:27]), rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("model", ["ising", "xy"])
+def test_warp_per_replica_matches_alone(engine, model):
+    """A group of many small replicas on one warp each (the resident kernel
+    with 32-thread CTAs, the autotuner's candidate for groups of 32 or more
+    replicas) runs each replica's trajectory: Ising bit-exact against the
+    replica solved alone, O(n) within FP32 summation order."""
+    probs = []
+    for k in range(40):
+        L = (16, 24, 32)[k % 3]
+        T = (2.0 + 0.03 * k) if model == "ising" else (0.6 + 0.02 * k)
+        probs.append(C.square_args(model, L, T, h=0.05 * (k % 2), nthermal=5, nsweep=12))
+    os.environ["MCSGPU_FORCE"] = "0:32"
+    try:
+        bt = engine.Batch()
+        for k, a in enumerate(probs):
+            bt.add(model, a, seed=600 + k, random_init=True)
+        bt.prepare()
+        bt.run()
+        sched = bt.schedules()
+        got = [bt.result(k) for k in range(len(probs))]
+        bt.close()
+    finally:
+        os.environ.pop("MCSGPU_FORCE", None)
+    assert sched == [("resident", 1, 32, len(probs))], sched
+    n = 10 if model == "ising" else 27
+    for k in (0, 1, 2, 17, 39):
+        alone, ex = engine.solve(model, probs[k], seed=600 + k, schedule="resident", random_init=True)
+        if model == "ising":
+            np.testing.assert_allclose(np.array(got[k][0][:n]), np.array(alone[:n]), rtol=1e-12, atol=1e-12)
+            assert got[k][1]["exact_mismatches"] == 0
+            assert got[k][1]["accepted"] == ex["accepted"]
+        else:
+            np.testing.assert_allclose(np.array(got[k][0][:n]), np.array(alone[:n]), rtol=1e-6, atol=1e-6)
