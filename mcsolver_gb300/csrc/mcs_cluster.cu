@@ -725,6 +725,19 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
 
 long long cluster_smem_bytes(const Rep &r, int C) { return (long long)cluster_layout(r, C).total; }
 
+// Load the cluster kernels on the current device (see preload_kernels_main).
+cudaError_t preload_kernels_cluster()
+{
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, (const void *)k_cluster_metro<2, 256>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)k_cluster_metro<2, 512>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)k_cluster_metro<2, 1024>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)k_cluster_metro<3, 256>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)k_cluster_metro<3, 512>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)k_cluster_metro<3, 1024>);
+    return e;
+}
+
 // Shared-memory and cluster-size attributes of one instantiation (set once,
 // raised when a larger request comes).
 template <int DIM, int NT>

@@ -200,4 +200,7 @@ struct StopItem {
     long long quota;
 };
 cudaError_t launch_set_stop(Rep *reps, const StopItem *items, int n, cudaStream_t st);
+// load the engine's kernels on the current device ahead of their first launch
+cudaError_t preload_kernels_main();
+cudaError_t preload_kernels_cluster();
 }  // namespace mcs

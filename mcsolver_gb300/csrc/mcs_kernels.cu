@@ -938,6 +938,29 @@ __global__ void k_set_stop(Rep *reps, const StopItem *items, int n)
     R.u_stop = s < R.units_total ? s : R.units_total;
 }
 
+// Load every kernel of this file on the current device (CUDA loads a kernel
+// at its first launch otherwise, which stalls that launch by milliseconds).
+cudaError_t preload_kernels_main()
+{
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaSuccess;
+    auto touch = [&](const void *f) {
+        if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, f);
+    };
+#define MCS_TOUCH(D, G)                                                                  \
+    touch((const void *)k_resident_metro<D, G>); touch((const void *)k_tiled_sweep<D, G>); \
+    touch((const void *)k_tiled_measure<D, G>); touch((const void *)k_init<D, G>);        \
+    touch((const void *)k_wolff<D, G>);
+    MCS_TOUCH(1, MCS_GEOM_SQUARE) MCS_TOUCH(2, MCS_GEOM_SQUARE) MCS_TOUCH(3, MCS_GEOM_SQUARE)
+    MCS_TOUCH(1, MCS_GEOM_ELL) MCS_TOUCH(2, MCS_GEOM_ELL) MCS_TOUCH(3, MCS_GEOM_ELL)
+#undef MCS_TOUCH
+    touch((const void *)k_tiled_finalize<1>);
+    touch((const void *)k_tiled_finalize<2>);
+    touch((const void *)k_tiled_finalize<3>);
+    touch((const void *)k_set_stop);
+    return e;
+}
+
 cudaError_t launch_set_stop(Rep *reps, const StopItem *items, int n, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;

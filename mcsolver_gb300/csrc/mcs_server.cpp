@@ -27,6 +27,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <deque>
 #include <memory>
 #include <mutex>
@@ -105,6 +106,17 @@ extern "C" int mcs_server_create(int32_t device, uint64_t hbm_budget_bytes, int3
     s->batch.replicas.resize(max_slots);
     s->slot_ticket.assign(max_slots, 0);
     if (const char *e = getenv("MCSGPU_SERVER_STEP_US")) s->step_us = std::max(1.0, atof(e));
+    // the engine's kernels are loaded now rather than at the first launch of
+    // each, inside some request's step (where no device is present, nothing
+    // happens: requests are still compiled and queued on the host)
+    {
+        int cur = 0;
+        if (cudaGetDevice(&cur) == cudaSuccess && cudaSetDevice(device) == cudaSuccess) {
+            if (preload_kernels_main() == cudaSuccess) preload_kernels_cluster();
+            cudaSetDevice(cur);
+        }
+        cudaGetLastError();
+    }
     if (const char *e = getenv("MCSGPU_SERVER_INJECT")) {
         long long k = 0;
         if (sscanf(e, "upload:%lld", &k) == 1) s->inject_upload = k;
@@ -188,6 +200,12 @@ extern "C" int mcs_server_step(mcs_server *s, int32_t *completed)
     std::lock_guard<std::mutex> slock(s->smu);
     if (completed) *completed = 0;
     Batch &b = s->batch;
+    // MCSGPU_TRACE=1: host time of the step's phases on stderr
+    const bool trace = getenv("MCSGPU_TRACE") != nullptr;
+    const auto t0 = std::chrono::steady_clock::now();
+    auto ms_since = [&](std::chrono::steady_clock::time_point t) {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count();
+    };
     // 1. cancelled requests that are on the device
     {
         std::vector<int> cs;
@@ -257,6 +275,8 @@ extern "C" int mcs_server_step(mcs_server *s, int32_t *completed)
             s->n_active = n;
         }
     }
+    const double t_admit = ms_since(t0);
+    if (trace && !admit.empty()) fprintf(stderr, "mcsgpu trace: server admitted %zu in %.3f ms\n", admit.size(), t_admit);
     if (b.groups.empty()) return MCS_OK;
     // 3. every active request by its own quota
     std::vector<int> failed;
@@ -337,6 +357,8 @@ extern "C" int mcs_server_step(mcs_server *s, int32_t *completed)
     for (auto &f : fin) ok += f.second.status == MCS_OK;
     retire_slots(s, out, fin);
     if (completed) *completed = ok;
+    if (trace) fprintf(stderr, "mcsgpu trace: server step %.3f ms (admission %.3f), retired %zu\n", ms_since(t0), t_admit,
+                       out.size());
     // the remaining requests are placed again for the lighter load (a large
     // lattice left alone moves to a larger cluster)
     std::vector<int> orphans;
@@ -349,6 +371,7 @@ extern "C" int mcs_server_step(mcs_server *s, int32_t *completed)
                 if (!grouped) orphans.push_back(k);
             }
     }
+    if (trace) fprintf(stderr, "mcsgpu trace: server step with rebalance %.3f ms\n", ms_since(t0));
     if (!orphans.empty()) {
         std::vector<std::pair<int, mcs_server::Done>> ofin;
         for (int k : orphans) ofin.emplace_back(k, failed_done(MCS_ECUDA, "re-placing this request failed: " + get_error()));
