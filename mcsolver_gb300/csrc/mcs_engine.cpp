@@ -751,7 +751,8 @@ cudaError_t Batch::tiled_unit(Group &G, cudaStream_t s, long long *nl)
 // 4 -> 8 -> tiled; resident -> tiled where the cluster kernel does not apply)
 // while the estimate falls.  With the autotuner on, cluster sizes stay the
 // autotuner's choice and only the move to tiled is decided here.
-void Batch::place_replicas(int max_smem, const std::vector<int> &ids, double base_crit, double base_smsec)
+void Batch::place_replicas(int max_smem, const std::vector<int> &ids, double base_crit, double base_smsec,
+                           double base_ctas)
 {
     int nsm = 0;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || nsm < 1) {
@@ -839,21 +840,37 @@ void Batch::place_replicas(int max_smem, const std::vector<int> &ids, double bas
     // replica that cannot move (an Ising lattice without a cluster kernel) no
     // longer holds the others at one CTA, and each finishes as early as the
     // device allows.  Moves to the tiled schedule are left to the first pass.
+    // The CTAs of all replicas (a resident or cluster CTA counted as one SM's
+    // worth) stay within the device's SMs, and a slab keeps at least 8 rows:
+    // beyond either, a larger cluster adds waves or barrier-bound CTAs instead
+    // of speed.
     std::vector<char> frozen(ps.size(), 0);
+    auto ctas = [&](const P &q) { const int o = q.opts[q.opt]; return o == 0 ? 0 : (o < 0 ? 4 : o); };
+    double used = base_ctas;
+    for (auto &q : ps) used += ctas(q);
     for (size_t it = 0; it < 4 * ps.size() + 4; ++it) {
         int pick = -1;
         double mc = 0;
         for (int k = 0; k < (int)ps.size(); ++k) {
             const P &q = ps[k];
             if (frozen[k] || q.opt + 1 >= (int)q.opts.size() || q.opts[q.opt + 1] <= 1) continue;
+            const int nxt = q.opts[q.opt + 1];
+            if (replicas[q.i]->hm.Lx / nxt < 8 || used - ctas(q) + nxt > nsm) continue;
             const double c = crit(q);
             if (c > mc) { mc = c; pick = k; }
         }
         if (pick < 0) break;
+        used -= ctas(ps[pick]);
         ++ps[pick].opt;
+        used += ctas(ps[pick]);
         const double now = estimate();
         if (now <= best * (1.0 + 1e-9)) best = std::min(best, now);
-        else { --ps[pick].opt; frozen[pick] = 1; }
+        else {
+            used -= ctas(ps[pick]);
+            --ps[pick].opt;
+            used += ctas(ps[pick]);
+            frozen[pick] = 1;
+        }
     }
     for (auto &q : ps) {
         Replica &r = *replicas[q.i];
@@ -880,7 +897,7 @@ void Batch::assign_schedules(const std::vector<int> &ids, int max_smem)
     static const double r_cta[4] = {0, 0.40e9, 0.85e9, 0.65e9};
     std::vector<char> is_new(replicas.size(), 0);
     for (int i : ids) is_new[i] = 1;
-    double base_crit = 0, base_smsec = 0;
+    double base_crit = 0, base_smsec = 0, base_ctas = 0;
     for (size_t i = 0; i < replicas.size(); ++i) {
         const Replica *r = replicas[i].get();
         if (!r || is_new[i]) continue;
@@ -889,14 +906,16 @@ void Batch::assign_schedules(const std::vector<int> &ids, int max_smem)
         if (r->schedule == 6) {
             base_crit = std::max(base_crit, c / (0.8 * std::max(1, r->pref_C) * rc));
             base_smsec += c / (0.8 * rc);
+            base_ctas += std::max(1, r->pref_C);
         } else if (r->schedule == 3) {
             base_smsec += c / (0.8 * rc);
         } else {
             base_crit = std::max(base_crit, c / rc);
             base_smsec += c / rc;
+            base_ctas += 1;
         }
     }
-    place_replicas(max_smem, ids, base_crit, base_smsec);
+    place_replicas(max_smem, ids, base_crit, base_smsec, base_ctas);
 }
 
 // Initial energies / exact sums (and random initial states) of the replicas of
@@ -1314,6 +1333,19 @@ int Batch::advance(long long units)
                 G.threads = it->second.second;
                 G.tuned = 1;
                 continue;
+            }
+        }
+        // every candidate's kernel is loaded before any is timed (CUDA loads a
+        // kernel at its first launch, which would count against the first
+        // candidate); once per process and device
+        {
+            static std::mutex m;
+            static bool loaded[64];
+            std::lock_guard<std::mutex> lock(m);
+            if (device >= 0 && device < 64 && !loaded[device]) {
+                if (preload_kernels_main() == cudaSuccess) preload_kernels_cluster();
+                cudaGetLastError();
+                loaded[device] = true;
             }
         }
         long long u = 0;

@@ -161,7 +161,8 @@ struct Batch {
     int run();                     // prepare + advance to completion + collect
     int result(int i, mcs_result *res);
     int setup_tiled(Group &G);
-    void place_replicas(int max_smem, const std::vector<int> &ids, double base_crit = 0, double base_smsec = 0);
+    void place_replicas(int max_smem, const std::vector<int> &ids, double base_crit = 0, double base_smsec = 0,
+                        double base_ctas = 0);
     cudaError_t tiled_unit(Group &G, cudaStream_t s, long long *nl);
     cudaError_t launch_group(Group &G, int C, int threads, long long units, cudaStream_t s);
 };

@@ -26,8 +26,10 @@
   sweeps, the same algorithm gives <e> = -3.45890(9) with glibc rand() and
   -3.45938(4) with SplitMix64; the engine gives -3.45952(6)).  The engine
   must agree with the algorithm with the sound generator on every compared
-  observable, and with the library wherever the library agrees with its own
-  algorithm; where it does not, the library's shift is printed.  Compared: e, e^2, the
+  observable within 3.5 combined standard errors, and with the library
+  within 3.5 combined standard errors plus the library's own measured shift
+  from its algorithm (its random-source bias, taken as a systematic error);
+  every comparison is printed.  Compared: e, e^2, the
   renormalised e_r and e_r^2, C = N (<e^2> - <e>^2) for every case; the
   magnetisation components and U4 where their autocorrelation time (measured:
   about 400 sweeps for XY below 1.2 K at L = 128) is short against the run
@@ -79,10 +81,18 @@ def _engine_runs(engine, name, c):
         k = int(np.argmin(np.abs(ladder - sp["T"])))
         phys = C.spec_args(sp, arrays=True, T=1.0, nthermal=1000, nsweep=3000)
         out = []
+        T = ladder[k]
         for r in range(R // 6):
             pt = engine.ParallelTempering(model, phys, 1.0 / ladder, seed=700 + r)
             pt.run()
-            out.append(pt.result(k)[0][:27])
+            v = list(pt.result(k)[0][:27])
+            # parallel tempering reports physical energies; the reference's
+            # are in units of T (its couplings are divided by T)
+            for j in (8, 18):
+                v[j] /= T
+            for j in (9, 19):
+                v[j] /= T * T
+            out.append(v)
             pt.close()
         return np.array(out, float)
     args = C.spec_args(sp, arrays=True)
@@ -132,12 +142,18 @@ def test_observables_on_configuration_lattices(engine, name, capsys):
         x, a, y = col(ref, k), col(alg, k), col(mine, k)
         z_alg, ok_alg = z(a, y)
         z_ref, ok_ref = z(x, y)
-        z_lib, lib_sound = z(x, a)
+        z_lib, _ = z(x, a)
         lines.append("  [%s] library %.6g +- %.2g  algorithm %.6g +- %.2g  engine %.6g +- %.2g  "
                      "|z| engine-algorithm %.2f  engine-library %.2f  library-algorithm %.2f" % (
                          k, x.mean(), x.std(ddof=1) / math.sqrt(len(x)), a.mean(), a.std(ddof=1) / math.sqrt(len(a)),
                          y.mean(), y.std(ddof=1) / math.sqrt(len(y)), z_alg, z_ref, z_lib))
-        if not ok_alg or (lib_sound and not ok_ref):
+        # against the library, its measured shift from its own algorithm
+        # (the random-source bias, estimated on the same inputs and seeds)
+        # counts as a systematic error
+        d_ref = abs(x.mean() - y.mean())
+        se_ref = math.sqrt(x.var(ddof=1) / len(x) + y.var(ddof=1) / len(y))
+        ok_ref_sys = d_ref <= 3.5 * se_ref + abs(x.mean() - a.mean()) + FP32_FLOOR * max(1.0, abs(x.mean()))
+        if not ok_alg or not ok_ref_sys:
             failures.append(lines[-1])
     with capsys.disabled():
         print("\n%s (library and algorithm %d seeds each, engine %d runs)\n%s" % (name, len(ref), len(mine),
