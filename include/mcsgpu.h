@@ -184,7 +184,7 @@ int mcs_server_submit(mcs_server *s, const mcs_problem *problem, const mcs_optio
 /* Advance the device by one tick: retire cancelled requests, admit queued
  * ones, advance every active request by its own quota of units (about the
  * same device time per request and step, MCSGPU_SERVER_STEP_US, default
- * 4000 us: small lattices run many sweeps per step, large ones few), retire
+ * 2000 us: small lattices run many sweeps per step, large ones few), retire
  * finished ones.  *completed receives the number of requests completed.  One
  * step at a time.  A request that fails is retired with its own status (see
  * mcs_server_poll) and the others go on; the step itself returns an error only

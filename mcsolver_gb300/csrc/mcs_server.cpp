@@ -46,7 +46,7 @@ struct mcs_server {
     uint64_t budget = 0;
     int max_slots = 0;
     uint64_t next_ticket = 1;
-    double step_us = 4000.0;  // target device time of a request's share of one step
+    double step_us = 2000.0;  // target device time of a request's share of one step
     struct Done {
         int status = MCS_OK;
         std::string msg;
