@@ -1,7 +1,8 @@
 // mcs_cluster.cu -- cluster schedule of the Metropolis sweep (square lattice, XY / Heisenberg).
 //
-// One replica is split by rows over a thread-block cluster of C CTAs (C = 1,
-// 2, 4, 8 or 16).  The Lx/2 row pairs are dealt out as evenly as possible:
+// One replica is split by rows over a thread-block cluster of C CTAs (any C
+// from 1 to 16; the autotuner offers the powers of two and one wave-filling
+// size).  The Lx/2 row pairs are dealt out as evenly as possible:
 // CTA r owns RP_r = 2*(P/C + (r < P%C)) rows starting at x0_r (P = Lx/2; every
 // slab starts on an even row, so the parity colouring of a local row is that
 // of the global row) and keeps one ghost row on each side:

@@ -1088,6 +1088,39 @@ int Batch::build_groups(const std::vector<int> &ids, bool merge)
                                 for (int th : {512, 256, 1024})
                                     if (cluster_active(d, C, th, sm) > 0) G->candidates.push_back({C, th});
                             }
+                            // a wave-filling size: the largest cluster size at which every
+                            // replica of the group runs at once, when it lies above the
+                            // largest such power of two (32 replicas at 2 CTAs per SM on 152
+                            // SMs: 9 CTAs each, 288 CTAs, beside 8 CTAs each, 256 CTAs)
+                            auto fits = [&](int C, int th) {
+                                size_t sm = 0;
+                                for (int id : set) {
+                                    if (replicas[id]->hm.Lx / 2 < C) return false;
+                                    sm = std::max<size_t>(sm, (size_t)cluster_smem_bytes(replicas[id]->rep, C));
+                                }
+                                return (int)sm <= max_smem && cluster_active(d, C, th, sm) >= (int)set.size();
+                            };
+                            if (cluster_override <= 1 && pc == 0)
+                                for (int th : {512, 256, 1024}) {
+                                    int top = 0;
+                                    for (const auto &c : G->candidates)
+                                        if (c.second == th && c.first > top && fits(c.first, th)) top = c.first;
+                                    if (getenv("MCSGPU_TRACE")) {
+                                        fprintf(stderr, "mcsgpu trace: %zu replicas, %d threads, clusters at once by size:", set.size(), th);
+                                        for (int C = 2; C <= 16; ++C) {
+                                            size_t sm = 0;
+                                            for (int id : set) sm = std::max<size_t>(sm, (size_t)cluster_smem_bytes(replicas[id]->rep, C));
+                                            fprintf(stderr, " %d:%d", C, (int)sm <= max_smem ? cluster_active(d, C, th, sm) : 0);
+                                        }
+                                        fprintf(stderr, "\n");
+                                    }
+                                    if (top == 0) continue;
+                                    for (int C = 16; C > top; --C)
+                                        if ((C & (C - 1)) != 0 && fits(C, th)) {
+                                            G->candidates.push_back({C, th});
+                                            break;
+                                        }
+                                }
                             G->can_cluster = 1;
                         }
                         if (G->candidates.empty() && kind == 6) {
@@ -1366,6 +1399,12 @@ int Batch::advance(long long units)
         }
         size_t best = 0;
         for (size_t ci = 1; ci < G.candidates.size(); ++ci) if (G.cand_ms[ci] < G.cand_ms[best]) best = ci;
+        if (getenv("MCSGPU_TRACE")) {
+            fprintf(stderr, "mcsgpu trace: autotune group %zu (C:threads ms/unit):", gi);
+            for (size_t ci = 0; ci < G.candidates.size(); ++ci)
+                fprintf(stderr, " %d:%d %.4f", G.candidates[ci].first, G.candidates[ci].second, G.cand_ms[ci]);
+            fprintf(stderr, "\n");
+        }
         G.C = G.candidates[best].first;
         G.threads = G.candidates[best].second;
         G.tuned = 1;

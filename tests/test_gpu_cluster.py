@@ -222,6 +222,21 @@ def test_every_candidate_records_the_same_series(engine, name, model, mk, cand):
     np.testing.assert_allclose(np.array(b[:27]), np.array(a[:27]), rtol=1e-5, atol=1e-6)
 
 
+WAVE_CASES = [
+    ("xy_L26", "xy", lambda: C.square_args("xy", 26, 0.9, nthermal=20, nsweep=200), (13, 256)),
+    ("heis_L12_dmi_h_circ", "heisenberg", SERIES_CASES[1][2], (6, 512)),
+]
+
+
+@pytest.mark.parametrize("name,model,mk,cand", WAVE_CASES, ids=[c[0] for c in WAVE_CASES])
+def test_wave_filling_cluster_size_records_the_same_series(engine, name, model, mk, cand):
+    """The autotuner's wave-filling candidate, a cluster size that is not a
+    power of two (for one replica the largest its row pairs allow: 13 CTAs,
+    whose rank-0 gather reads in two batches of eight, and 6), records the
+    series of the one-CTA resident run."""
+    test_every_candidate_records_the_same_series(engine, name, model, mk, cand)
+
+
 @pytest.mark.parametrize("model", ["ising", "xy"])
 def test_warp_per_replica_matches_alone(engine, model):
     """A group of many small replicas on one warp each (the resident kernel
