@@ -66,6 +66,12 @@ __device__ void wolff_cluster(Rep &R, const float *jt, const float *dt, const Is
     __syncthreads();
     const float r0 = shf[0], r1 = shf[1], r2 = shf[2];
     const bool full = R.fullJ;
+    // square lattice: r.J.r of the four link directions (the same for every site)
+    float rj[4] = {0.f, 0.f, 0.f, 0.f};
+    if (DIM > 1 && GEOM == MCS_GEOM_SQUARE) {
+#pragma unroll
+        for (int l = 0; l < 4; ++l) rj[l] = on_jdot<DIM>(jt + 9 * R.sq_code[l], full, r0, r1, r2, r0, r1, r2);
+    }
     // ---- growth, one frontier level at a time.  Level k appends the sites
     // it discovers after the queue's current end, counting them in
     // sh[4 + k % 3]; after the level's barrier every thread reads that count.
@@ -76,6 +82,58 @@ __device__ void wolff_cluster(Rep &R, const float *jt, const float *dt, const Is
     while (lb < le) {
         int *cnt = sh + 4 + k % 3;
         if (tid == 0) sh[4 + (k + 1) % 3] = 0;
+        if (DIM > 1 && GEOM == MCS_GEOM_SQUARE) {
+            // square lattice, O(n): a level is one chain of dependent
+            // latencies per thread, so its steps are laid side by side: the
+            // four bond coins, then the four bond tests (independent of one
+            // another), then the four claims on the bitmask, then one queue
+            // append per warp.  The loop bound is the warp's first lane's, the
+            // same for every lane, so the whole warp reaches the append.
+            const int lane = tid & 31;
+            for (int f0 = lb + tid - lane; f0 < le; f0 += bd) {
+                const int f = f0 + lane;
+                int js[4] = {0, 0, 0, 0};
+                unsigned int take = 0u;
+                if (f < le) {
+                    const int i = wq_get(W, f);
+                    const float sdi = -(S.x[i] * r0 + S.y[i] * r1 + (DIM == 3 ? S.z[i] * r2 : 0.f));
+                    for_links<GEOM>(R, i, [&](int l, int j, int) { js[l] = j; });
+                    uint32_t cw[4];
+#pragma unroll
+                    for (int l = 0; l < 4; ++l) cw[l] = wolff_coin(i, js[l], q, R.seed);
+#pragma unroll
+                    for (int l = 0; l < 4; ++l) {
+                        const int j = js[l];
+                        const bool in = (W.bits[j >> 5] >> (j & 31)) & 1u;
+                        const float sdj = -(S.x[j] * r0 + S.y[j] * r1 + (DIM == 3 ? S.z[j] * r2 : 0.f));
+                        const float corr = 2.f * sdi * sdj * rj[l];
+                        if (!in && corr < 0.f && (1.f - __expf(corr)) > u24(cw[l])) take |= 1u << l;
+                    }
+                    // a site reached along two bonds (of this thread or of
+                    // another) is claimed once: the first atomicOr wins
+#pragma unroll
+                    for (int l = 0; l < 4; ++l)
+                        if ((take >> l) & 1u) {
+                            const int j = js[l];
+                            const unsigned int old = atomicOr(&W.bits[j >> 5], 1u << (j & 31));
+                            if ((old >> (j & 31)) & 1u) take &= ~(1u << l);
+                        }
+                }
+                const int mine = __popc(take);
+                int incl = mine;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += v;
+                }
+                int base = 0;
+                if (lane == 31 && incl > 0) base = atomicAdd(cnt, incl);
+                int pos = le + __shfl_sync(0xffffffffu, base, 31) + incl - mine;
+#pragma unroll
+                for (int l = 0; l < 4; ++l)
+                    if ((take >> l) & 1u) wq_put(W, pos++, js[l]);
+            }
+        } else
         for (int f = lb + tid; f < le; f += bd) {
             const int i = wq_get(W, f);
             if (DIM == 1) {
@@ -90,30 +148,6 @@ __device__ void wolff_cluster(Rep &R, const float *jt, const float *dt, const Is
                         if (!((old >> (j & 31)) & 1u)) wq_put(W, le + atomicAdd(cnt, 1), j);
                     }
                 });
-            } else if (GEOM == MCS_GEOM_SQUARE) {
-                // square lattice: the four bond coins are drawn first, as
-                // independent instruction streams (the growth is a chain of
-                // dependent levels, so latency decides), then the bonds are
-                // tested in link order as below
-                const float sdi = -(S.x[i] * r0 + S.y[i] * r1 + (DIM == 3 ? S.z[i] * r2 : 0.f));
-                int js[4], cs[4];
-                for_links<GEOM>(R, i, [&](int l, int j, int code) { js[l] = j; cs[l] = code; });
-                uint32_t cw[4];
-#pragma unroll
-                for (int l = 0; l < 4; ++l) cw[l] = wolff_coin(i, js[l], q, R.seed);
-#pragma unroll
-                for (int l = 0; l < 4; ++l) {
-                    const int j = js[l];
-                    if ((W.bits[j >> 5] >> (j & 31)) & 1u) continue;
-                    const float sdj = -(S.x[j] * r0 + S.y[j] * r1 + (DIM == 3 ? S.z[j] * r2 : 0.f));
-                    const float rjr = on_jdot<DIM>(jt + 9 * cs[l], full, r0, r1, r2, r0, r1, r2);
-                    const float corr = 2.f * sdi * sdj * rjr;
-                    if (!(corr < 0.f)) continue;
-                    if ((1.f - __expf(corr)) > u24(cw[l])) {
-                        unsigned int old = atomicOr(&W.bits[j >> 5], 1u << (j & 31));
-                        if (!((old >> (j & 31)) & 1u)) wq_put(W, le + atomicAdd(cnt, 1), j);
-                    }
-                }
             } else {
                 const float sdi = -(S.x[i] * r0 + S.y[i] * r1 + (DIM == 3 ? S.z[i] * r2 : 0.f));
                 for_links<GEOM>(R, i, [&](int, int j, int code) {
