@@ -676,9 +676,12 @@ int Batch::setup_tiled(Group &G)
             }
         }
         ioff.push_back(slot);
-        int V = std::max(std::max(m.N, m.nlat), std::max(m.n_rorb, m.ncirc));
-        for (int b0 = 0; b0 < V; b0 += 512) {
-            Item it; it.rep = id; it.begin = b0; it.end = std::min(V, b0 + 512); it.slot = 0;
+        // measurement tiles: the Ising frame's gathers are latency-bound, so
+        // its tiles are smaller (one index per thread; 26.5 against 30.9 us
+        // per sweep at L = 232)
+        const int V = std::max(std::max(m.N, m.nlat), std::max(m.n_rorb, m.ncirc)), mt = dim == 1 ? 256 : 512;
+        for (int b0 = 0; b0 < V; b0 += mt) {
+            Item it; it.rep = id; it.begin = b0; it.end = std::min(V, b0 + mt); it.slot = 0;
             meas.push_back(it);
         }
         moff.push_back((int)meas.size());
@@ -1891,8 +1894,10 @@ extern "C" int mcs_pt_run(mcs_pt *pt)
     if (rc != MCS_OK) return rc;
     if (b.groups.size() != 1) { set_error("parallel tempering replicas must form one kernel group"); return MCS_EINVAL; }
     Group &G = *b.groups[0];
+    // the group's first configuration (the only one when MCSGPU_COPIES or
+    // MCSGPU_FORCE leave one); with several, the probe below picks
     int C = 0, threads = G.threads;
-    if (G.kind == 6 && !G.candidates.empty()) { C = G.candidates[0].first; threads = G.candidates[0].second; }
+    if (!G.candidates.empty()) { C = G.candidates[0].first; threads = G.candidates[0].second; }
     const int nt = pt->nt;
     CUDA_TRY(cudaMalloc(&pt->d_perm, nt * sizeof(int)));
     CUDA_TRY(cudaMalloc(&pt->d_acc, nt * sizeof(long long)));
@@ -1929,6 +1934,9 @@ extern "C" int mcs_pt_run(mcs_pt *pt)
             float ms = 0;
             cudaEventElapsedTime(&ms, b.ev_a, b.ev_b);
             if (ms < best) { best = ms; C = cC; threads = cth; }
+            if (getenv("MCSGPU_TRACE"))
+                fprintf(stderr, "mcsgpu trace: parallel tempering candidate %d:%d %.4f ms per sweep + exchange\n", cC, cth,
+                        ms / 4);
             u += 4;
         }
     }

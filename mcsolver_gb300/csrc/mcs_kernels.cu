@@ -410,8 +410,12 @@ __global__ void __launch_bounds__(256) k_tiled_sweep(Rep *reps, const Item *item
 {
     __shared__ double red[32 * 2 + 4];
     __shared__ long long redl[32 * 9 + 9];
+    // the descriptor in shared memory: its fields are read in every trial,
+    // and from global memory every spin store (which might alias them)
+    // would make the compiler read them again
+    __shared__ Rep R;
     const Item it = items[blockIdx.x];
-    const Rep &R = reps[it.rep];
+    load_rep(R, reps + it.rep);
     if (R.u >= R.u_stop) return;
     const long long t = R.u0 + R.u;
     const int c = colour, c0 = R.col_start[c];
@@ -489,8 +493,9 @@ __global__ void __launch_bounds__(256) k_tiled_measure(Rep *reps, const Item *it
     __shared__ double F[F_NON];
     __shared__ long long redl[32 * 16 + 16];
     __shared__ long long Fi[16];
+    __shared__ Rep R;
     const Item it = items[blockIdx.x];
-    const Rep &R = reps[it.rep];
+    load_rep(R, reps + it.rep);
     if (R.u >= R.u_stop || !measures_after(R, R.u)) return;
     Spins S = spins_global(R);
     double *out = fpart + (size_t)blockIdx.x * F_NON;
@@ -518,8 +523,10 @@ __global__ void __launch_bounds__(256) k_tiled_finalize(Rep *reps, const int *id
     __shared__ long long redl[32 * 9 + 9];
     __shared__ long long Fi[16];
     __shared__ int meas;
+    __shared__ Rep R;  // written back below: u, m, frames_written
     const int r = ids[blockIdx.x];
-    Rep &R = reps[r];
+    Rep *Rg = reps + r;
+    load_rep(R, Rg);
     if (R.u >= R.u_stop) return;
     const int tid = threadIdx.x;
     const int i0 = item_off[blockIdx.x], i1 = item_off[blockIdx.x + 1];
@@ -557,8 +564,17 @@ __global__ void __launch_bounds__(256) k_tiled_finalize(Rep *reps, const int *id
         {
             const int lane = tid & 31, wid = tid >> 5, nwb = blockDim.x >> 5;
             for (int k = wid; k < nf; k += nwb) {
-                double a = 0.0;
-                for (int i = m0 + lane; i < m1; i += 32) a += fpart[(size_t)i * F_NON + k];
+                // four loads in flight per lane
+                double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+                int i = m0 + lane;
+                for (; i + 96 < m1; i += 128) {
+                    a0 += fpart[(size_t)i * F_NON + k];
+                    a1 += fpart[(size_t)(i + 32) * F_NON + k];
+                    a2 += fpart[(size_t)(i + 64) * F_NON + k];
+                    a3 += fpart[(size_t)(i + 96) * F_NON + k];
+                }
+                for (; i < m1; i += 32) a0 += fpart[(size_t)i * F_NON + k];
+                double a = (a0 + a1) + (a2 + a3);
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
                 if (lane == 0) F[k] = a;
@@ -596,8 +612,10 @@ __global__ void __launch_bounds__(256) k_tiled_finalize(Rep *reps, const int *id
         }
     }
     if (tid == 0) {
-        R.u = u + 1;
         R.stats[S_VISITS] += R.N;
+        Rg->u = u + 1;
+        Rg->m = R.m;
+        Rg->frames_written = R.frames_written;
     }
 }
 
