@@ -116,6 +116,52 @@ struct TrialFlags {
     bool fullJ, has_d;
 };
 
+// The XY trial of on_trial with the couplings of the four link directions in
+// registers (cj[d] = M[0], M[1], M[3], M[6] of direction d's class: a
+// regular lattice has one class per direction), the local field formed in
+// on_field's order so that the result is the same to the bit; the site's spin
+// after the trial in (fx, fy), for the sums the sweep forms on the way.
+template <class LINKS>
+__device__ __forceinline__ bool on_trial_xy_r(const TrialFlags &F, const float (&cj)[4][4], const float *__restrict__ dt,
+                                              const Spins &S, int v, const uint4 &w, float beta, float h,
+                                              LINKS &&links, float *dEout, float &fx, float &fy)
+{
+    float h0 = 0.f, h1 = 0.f;
+    links([&](int d, int j, int) {
+        const float a = S.x[j], b = S.y[j];
+        h0 = fmaf(cj[d][0], a, h0);
+        h1 = fmaf(cj[d][1], b, h1);
+        if (F.fullJ) {
+            h0 = fmaf(cj[d][2], b, h0);
+            h1 = fmaf(cj[d][3], a, h1);
+        }
+    });
+    float r0, r1, r2;
+    on_direction<2>(w, r0, r1, r2);
+    const float s0 = S.x[v], s1 = S.y[v];
+    const float sr = s0 * r0 + s1 * r1;
+    const float f = -2.f * sr;
+    const float d0 = f * r0, d1 = f * r1;
+    float dE = d0 * h0 + d1 * h1;
+    if (F.has_d) dE += dt[0] * (d0 * (2.f * s0 + d0)) + dt[1] * (d1 * (2.f * s1 + d1));
+    dE -= h * d0;
+    const float x = beta * dE;
+    const bool acc = (x <= 0.f) || (__expf(-x) > u24(w.y));
+    fx = s0;
+    fy = s1;
+    if (acc) {
+        const float n0 = s0 + d0, n1 = s1 + d1;
+        const float len2 = n0 * n0 + n1 * n1;
+        const float k = len2 > 0.f ? dt[3] * rsqrtf(len2) : 1.f;
+        fx = n0 * k;
+        fy = n1 * k;
+        S.x[v] = fx;
+        S.y[v] = fy;
+        *dEout = dE;
+    }
+    return acc;
+}
+
 // Index of the slot sum that feeds frame entry f (frame layout F_*), -1 for 0.
 __device__ __forceinline__ int cl_frame_src(int f, int ngroup, int gall)
 {
@@ -582,6 +628,12 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
     const long long uend = min(R.u_stop, u + max_units);
     const SqLinks sql = {R.Ly, hy, rows, R.sq_code[0], R.sq_code[1], R.sq_code[2], R.sq_code[3]};
     const TrialFlags tflags = {R.fullJ != 0, R.has_d != 0};
+    float cj[4][4];  // XY: the four directions' couplings (see on_trial_xy_r)
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+        const float *M = jt + 9 * R.sq_code[d];
+        cj[d][0] = M[0]; cj[d][1] = M[1]; cj[d][2] = M[3]; cj[d][3] = M[6];
+    }
     for (; u < uend; ++u) {
         const long long t = R.u0 + u;
         const bool fuse = R.meas_regular && measures_after(R, u) && (mloc % R.recheck) != 0;
@@ -640,8 +692,10 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
                 const uint4 w = ws[e];
                 float dE;
                 bool acc;
+                float fx = 0.f, fy = 0.f;
                 if (DIM == 2)  // XY: register copies (the Heisenberg loop has no registers to spare)
-                    acc = on_trial<DIM>(tflags, jt, dt, S, li, 0, w, beta, h, [&](auto &&f) { cl_links_r(sql, c, xl, yh, f); }, &dE);
+                    acc = on_trial_xy_r(tflags, cj, dt, S, li, w, beta, h, [&](auto &&f) { cl_links_r(sql, c, xl, yh, f); },
+                                        &dE, fx, fy);
                 else
                     acc = on_trial<DIM>(R, jt, dt, S, li, 0, w, beta, h, [&](auto &&f) { cl_links(R, rows, c, xl, yh, f); }, &dE);
                 if (acc) {
@@ -663,7 +717,7 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
                     }
                 }
                 if (fuse) {
-                    const float sx = S.x[li], sy = S.y[li], sz = DIM == 3 ? S.z[li] : 0.f;
+                    const float sx = DIM == 2 ? fx : S.x[li], sy = DIM == 2 ? fy : S.y[li], sz = DIM == 3 ? S.z[li] : 0.f;
                     fa[0] += sx; fa[1] += sy; fa[2] += sz;
                     fa[3] += sx * sx + sy * sy + sz * sz;
                 }
