@@ -544,6 +544,7 @@ Batch::~Batch()
     // advanced); the arenas are freed stream-ordered on the default stream
     if (stream) cudaStreamSynchronize(stream);
     for (cudaStream_t g : gstreams) cudaStreamSynchronize(g);
+    for (cudaStream_t g : gstreams_hi) cudaStreamSynchronize(g);
     groups.clear();
     if (d_reps) cudaFree(d_reps);
     if (d_stop) cudaFree(d_stop);
@@ -558,6 +559,7 @@ Batch::~Batch()
     if (ev_b) cudaEventDestroy(ev_b);
     if (ev_fork) cudaEventDestroy(ev_fork);
     for (cudaStream_t g : gstreams) cudaStreamDestroy(g);
+    for (cudaStream_t g : gstreams_hi) cudaStreamDestroy(g);
     for (cudaEvent_t e : gevents) cudaEventDestroy(e);
 }
 
@@ -1442,6 +1444,21 @@ int Batch::run_groups(const std::vector<long long> &todo, const std::vector<long
         CUDA_TRY(cudaEventCreateWithFlags(&ge, cudaEventDisableTiming));
         gevents.push_back(ge);
     }
+    // tiled groups (a large lattice in global memory, whose every sweep is a
+    // few short launches over the whole device) run on streams of the
+    // device's highest priority, so that their CTAs are placed first and the
+    // resident and cluster groups fill the SMs around them: without it a
+    // served stream's large lattices crawl behind the other groups' CTAs and
+    // finish last (served makespan 1.10-1.16 s against 0.94-1.06 s)
+    bool any_tiled = false;
+    for (const auto &g : groups) any_tiled |= g->kind == 3;
+    while (multi && any_tiled && gstreams_hi.size() < groups.size()) {
+        int least = 0, greatest = 0;
+        CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        cudaStream_t gs = nullptr;
+        CUDA_TRY(cudaStreamCreateWithPriority(&gs, cudaStreamNonBlocking, greatest));
+        gstreams_hi.push_back(gs);
+    }
     const bool trace = getenv("MCSGPU_TRACE") != nullptr;
     const bool timed = trace || group_ms;
     while (timed && tev.size() < 2 * groups.size()) {  // per-group timing events, kept by the batch
@@ -1454,7 +1471,7 @@ int Batch::run_groups(const std::vector<long long> &todo, const std::vector<long
         Group &G = *groups[gi];
         const long long n_todo = todo[gi];
         if (n_todo <= 0) continue;
-        cudaStream_t gs = multi ? gstreams[gi] : stream;
+        cudaStream_t gs = multi ? (G.kind == 3 ? gstreams_hi[gi] : gstreams[gi]) : stream;
         if (multi) CUDA_TRY(cudaStreamWaitEvent(gs, ev_fork, 0));
         if (timed) CUDA_TRY(cudaEventRecord(tev[2 * gi], gs));
         cudaError_t e = cudaSuccess;

@@ -122,6 +122,7 @@ struct Batch {
     int no_autotune = 0;
     int balance = 1;            // place replicas by the load balancer (off for parallel tempering)
     std::vector<cudaStream_t> gstreams;  // one stream per group: groups run side by side
+    std::vector<cudaStream_t> gstreams_hi;  // the same at the device's highest stream priority (tiled groups)
     std::vector<cudaEvent_t> gevents;
     double device_ms = 0;
     long long site_updates = 0;
