@@ -88,22 +88,46 @@ struct ArenaBuilder {
 static std::mutex g_pool_mutex;
 static bool g_pool_ready[64];
 
+static void pool_ready(int device)
+{
+    if (device < 0 || device >= 64) return;
+    std::lock_guard<std::mutex> lock(g_pool_mutex);
+    if (!g_pool_ready[device]) {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t thr = ~0ULL;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+        cudaGetLastError();
+        g_pool_ready[device] = true;
+    }
+}
+
 static int arena_alloc(int device, size_t bytes, void **out, cudaStream_t st)
 {
-    if (device >= 0 && device < 64) {
-        std::lock_guard<std::mutex> lock(g_pool_mutex);
-        if (!g_pool_ready[device]) {
-            cudaMemPool_t pool;
-            if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
-                uint64_t thr = ~0ULL;
-                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
-            }
-            cudaGetLastError();
-            g_pool_ready[device] = true;
-        }
-    }
+    pool_ready(device);
     CUDA_TRY(cudaMallocAsync(out, bytes, st));
     return MCS_OK;
+}
+
+// The batch's own device buffers (descriptors, a lattice's index lists, group
+// tables) come from the same pool on the legacy stream: cudaMalloc and
+// cudaFree synchronise the device, and creating and destroying a batch would
+// pay that for each buffer.  Every user of such a buffer is ordered after its
+// allocation (the legacy stream is synchronised before the buffer is handed
+// out), and every free comes after the batch's streams were synchronised.
+static cudaError_t buf_alloc(int device, void **out, size_t bytes)
+{
+    pool_ready(device);
+    cudaError_t e = cudaMallocAsync(out, std::max<size_t>(bytes, 16), 0);
+    // the buffer is ready for any stream once the legacy stream is (our
+    // streams are non-blocking: this waits for nothing of theirs)
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+    return e;
+}
+static void buf_free(void *p)
+{
+    if (p) cudaFreeAsync(p, 0);
 }
 
 Replica::~Replica()
@@ -124,7 +148,7 @@ size_t replica_acc_count(const HostModel &m)
 
 SharedLists::~SharedLists()
 {
-    if (d) cudaFree(d);
+    buf_free(d);
 }
 
 // One allocation holding the index arrays of a lattice (the pieces a replica
@@ -141,7 +165,7 @@ int make_shared_lists(const HostModel &m, int device, std::unique_ptr<SharedList
                  o_sflag = A.addv(m.sflag), o_rtgt = A.addv(m.rtgt);
     std::vector<unsigned char> img = A.finish();
     CUDA_TRY(cudaSetDevice(device));
-    CUDA_TRY(cudaMalloc(&sh->d, img.size()));
+    CUDA_TRY(buf_alloc(device, &sh->d, img.size()));
     sh->bytes = img.size();
     CUDA_TRY(cudaMemcpy(sh->d, img.data(), img.size(), cudaMemcpyHostToDevice));
     unsigned char *b = (unsigned char *)sh->d;
@@ -546,10 +570,10 @@ Batch::~Batch()
     for (cudaStream_t g : gstreams) cudaStreamSynchronize(g);
     for (cudaStream_t g : gstreams_hi) cudaStreamSynchronize(g);
     groups.clear();
-    if (d_reps) cudaFree(d_reps);
-    if (d_stop) cudaFree(d_stop);
+    buf_free(d_reps);
+    buf_free(d_stop);
     if (h_stop) cudaFreeHost(h_stop);
-    if (d_scratch) cudaFree(d_scratch);
+    buf_free(d_scratch);
     for (cudaEvent_t e : tev) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
     if (stream2) cudaStreamDestroy(stream2);
@@ -655,8 +679,8 @@ Group::~Group()
 {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
-    for (void *p : bufs) cudaFree(p);
-    if (d_ids) cudaFree(d_ids);
+    for (void *p : bufs) buf_free(p);
+    buf_free(d_ids);
 }
 
 int Batch::setup_tiled(Group &G)
@@ -692,7 +716,7 @@ int Batch::setup_tiled(Group &G)
     for (auto &v : sweep) { G.cofs.push_back(all.size()); G.ccount.push_back((int)v.size()); all.insert(all.end(), v.begin(), v.end()); }
     G.nmeas = (int)meas.size();
     auto dalloc = [&](size_t bytes, void **p) -> int {
-        CUDA_TRY(cudaMalloc(p, std::max<size_t>(bytes, 16)));
+        CUDA_TRY(buf_alloc(device, p, bytes));
         G.bufs.push_back(*p);
         return MCS_OK;
     };
@@ -956,11 +980,11 @@ int Batch::init_states(const std::vector<int> &ids)
 int Batch::upload_ids(Group &G)
 {
     if ((int)G.ids.size() > G.ids_cap) {
-        if (G.d_ids) cudaFree(G.d_ids);
+        buf_free(G.d_ids);
         G.d_ids = nullptr;
         G.ids_cap = 0;
         const int cap = std::max<int>(4, (int)G.ids.size() * 2);
-        CUDA_TRY(cudaMalloc(&G.d_ids, cap * sizeof(int)));
+        CUDA_TRY(buf_alloc(device, (void **)&G.d_ids, cap * sizeof(int)));
         G.ids_cap = cap;
     }
     if (!G.ids.empty())
@@ -976,7 +1000,7 @@ int Batch::reset_tiled(Group &G)
     if (G.graph) cudaGraphDestroy(G.graph);
     G.exec = nullptr;
     G.graph = nullptr;
-    for (void *q : G.bufs) cudaFree(q);
+    for (void *q : G.bufs) buf_free(q);
     G.bufs.clear();
     G.cofs.clear();
     G.ccount.clear();
@@ -1212,7 +1236,7 @@ int Batch::prepare()
     assign_schedules(ids, resident_max_smem());
     std::vector<Rep> host(nrep);
     for (int i = 0; i < nrep; ++i) host[i] = replicas[i]->rep;
-    CUDA_TRY(cudaMalloc(&d_reps, nrep * sizeof(Rep)));
+    CUDA_TRY(buf_alloc(device, (void **)&d_reps, nrep * sizeof(Rep)));
     CUDA_TRY(cudaMemcpy(d_reps, host.data(), nrep * sizeof(Rep), cudaMemcpyHostToDevice));
     rc = init_states(ids);
     if (rc != MCS_OK) return rc;
@@ -1232,7 +1256,7 @@ int Batch::admit(const std::vector<int> &ids, double step_us)
     if (!d_reps) {
         int rc = setup_device();
         if (rc != MCS_OK) return rc;
-        CUDA_TRY(cudaMalloc(&d_reps, (size_t)slot_capacity * sizeof(Rep)));
+        CUDA_TRY(buf_alloc(device, (void **)&d_reps, (size_t)slot_capacity * sizeof(Rep)));
         prepared = true;
     }
     const int max_smem = resident_max_smem();
@@ -1577,7 +1601,7 @@ int Batch::advance_quota(std::vector<int> *failed)
         }
     if (active.empty()) return MCS_OK;
     if (!d_stop) {
-        CUDA_TRY(cudaMalloc(&d_stop, (size_t)slot_capacity * sizeof(StopItem)));
+        CUDA_TRY(buf_alloc(device, (void **)&d_stop, (size_t)slot_capacity * sizeof(StopItem)));
         CUDA_TRY(cudaMallocHost(&h_stop, (size_t)slot_capacity * sizeof(StopItem)));
     }
     // one copy of (replica, quota) pairs from page-locked memory and one small
@@ -1640,7 +1664,7 @@ int Batch::sync_descriptors()
 void Batch::release_groups()
 {
     groups.clear();
-    if (d_reps) cudaFree(d_reps);
+    buf_free(d_reps);
     d_reps = nullptr;
     prepared = false;
 }
