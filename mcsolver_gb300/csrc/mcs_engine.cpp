@@ -244,10 +244,11 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool u
     if (r->record_series) o_series = A.add(nullptr, (size_t)m.nsweep * MCS_NSER * sizeof(double));
     // spin frames live in page-locked host memory (upload_replica), not in the arena
     r->frames_bytes = m.frames > 0 ? (size_t)m.frames * m.N * (m.dim == 1 ? 1 : m.dim * sizeof(float)) : 0;
-    size_t o_wbits = 0, o_wq = 0;
+    size_t o_wbits = 0, o_wq = 0, o_wmaj = 0;
     if (m.alg == 1) {
         o_wbits = A.add(nullptr, ((size_t)(m.N + 31) / 32) * sizeof(unsigned));
         o_wq = A.add(nullptr, (size_t)m.N * sizeof(int));
+        if (m.dim > 1) o_wmaj = A.add(nullptr, (size_t)m.n_rorb * 3 * sizeof(float));
     }
     r->bytes = A.size;
     // the descriptor holds arena offsets until upload_replica() relocates them
@@ -328,7 +329,10 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool u
     R.frame_buf = nullptr;  // set by upload_replica
     R.icnt = (long long *)P(o_icnt);
     R.stats = (long long *)P(o_stats);
-    if (m.alg == 1) { R.wbits = (unsigned *)P(o_wbits); R.wqueue = (int *)P(o_wq); }
+    if (m.alg == 1) {
+        R.wbits = (unsigned *)P(o_wbits); R.wqueue = (int *)P(o_wq);
+        if (m.dim > 1) R.wmaj = (float *)P(o_wmaj);
+    }
     R.u0 = 0; R.u = 0; R.m = 0;
     R.u_stop = m.units_total; R.quota = 0;
     r->acc_off = o_acc; r->icnt_off = o_icnt; r->stats_off = o_stats; r->series_off = o_series;
@@ -375,7 +379,7 @@ int upload_replica(Replica *r)
     RELOC(nbr); RELOC(lcode); RELOC(lcls); RELOC(deg); RELOC(stype); RELOC(jtab); RELOC(jtab64); RELOC(dtab);
     RELOC(itab); RELOC(cpair); RELOC(rorb); RELOC(rcl); RELOC(rlink); RELOC(rjc); RELOC(rK); RELOC(rkc);
     RELOC(rdeg); RELOC(rindex); RELOC(circ); RELOC(slen); RELOC(sval); RELOC(gmask); RELOC(sflag); RELOC(rtgt);
-    RELOC(spins); RELOC(acc); RELOC(series); RELOC(icnt); RELOC(stats); RELOC(wbits); RELOC(wqueue);
+    RELOC(spins); RELOC(acc); RELOC(series); RELOC(icnt); RELOC(stats); RELOC(wbits); RELOC(wqueue); RELOC(wmaj);
 #undef RELOC
     if (const SharedLists *sh = r->shared) {
         R.nbr = sh->nbr; R.lcode = sh->lcode; R.deg = sh->deg; R.stype = sh->stype;

@@ -148,6 +148,7 @@ struct Rep {
     long long *stats;                            // generic counters
     unsigned int *wbits;                         // Wolff in-cluster bits (global schedule)
     int *wqueue;                                 // Wolff queue (global schedule)
+    float *wmaj;                                 // O(n) Wolff: the block spins of a measurement ([n_rorb][3])
     long long u0;                                // RNG unit offset
     long long u;                                 // next unit
     long long u_stop;                            // a launch stops the replica here (units_total, or the

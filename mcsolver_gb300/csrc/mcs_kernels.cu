@@ -779,7 +779,10 @@ __global__ void __launch_bounds__(512) k_wolff(Rep *reps, const int *ids, long l
             } else {
                 if (tid == 0) { R.acc[A_ECUR] += dEd; dEd = 0.0; }
                 const bool efull = (m % R.recheck) == 0;
-                on_frame<DIM, GEOM>(R, jt, dt, S, 0, max(max(N, R.nlat), max(R.n_rorb, R.ncirc)), efull, red, F, nullptr);
+                // the block spins once per measurement, in the replica's global
+                // scratch (L2): each is read by its own chosen site and by the
+                // renormalised links of its neighbours instead of formed again
+                on_frame<DIM, GEOM>(R, jt, dt, S, 0, max(max(N, R.nlat), max(R.n_rorb, R.ncirc)), efull, red, F, R.wmaj);
                 if (tid == 0 && efull) {
                     double Ef = F[F_EFB] / 2 + F[F_EFO];
                     double d = fabs(R.acc[A_ECUR] - Ef);
