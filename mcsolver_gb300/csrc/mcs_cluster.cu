@@ -778,19 +778,353 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
     }
 }
 
-long long cluster_smem_bytes(const Rep &r, int C) { return (long long)cluster_layout(r, C).total; }
+
+// ======================================================================= Ising
+// Ising on the row-split cluster schedule: a square lattice with one site
+// type and the regular renormalisation (2x2 blocks on even rows and columns,
+// each linked to its four neighbour blocks in the same list order at every
+// chosen site).  The slabs, ghost rows and pushes are those of the O(n)
+// kernel above, on int8 spins; a trial is ising_trial on the local layout
+// with the Philox words of the other schedules (block k >> 2 of colour-local
+// index k = x*hy + yh, word k & 3).  A measurement is is_frame's integer fast
+// path split by slabs: every CTA sums its own sites and its own chosen blocks
+// (a block's neighbour across a slab boundary is read from the neighbouring
+// CTA's block sums over DSMEM), and rank 0 adds the CTAs' sums in rank order
+// and folds them with is_accumulate.  The sums are integers, so the result
+// equals the other schedules' to the bit.
+
+// per-CTA sums of one measurement: frame c[0..15] of is_frame, dn[4], dm[4],
+// accepted moves; two slots by measurement parity and a third for the counts
+// of the sweeps after the last measurement (or before the thermal boundary)
+#define CI_NV 25
+#define CI_SLOT 32
+
+struct ClusterLayoutI {
+    size_t spins, itab, msum, part, acc, total;
+    int rows, hy, nloc;
+};
+
+__host__ __device__ inline ClusterLayoutI cluster_layout_ising(const Rep &R, int C)
+{
+    ClusterLayoutI L;
+    const int P = R.Lx >> 1;
+    const int RP = 2 * (P / C + (P % C ? 1 : 0));  // the largest slab
+    L.rows = RP + 2;
+    L.hy = R.hy;
+    L.nloc = 2 * L.rows * L.hy;
+    size_t off = 0;
+    L.spins = off; off += a16((size_t)L.nloc);
+    L.itab = off; off += a16((size_t)R.nite * sizeof(IsEntry));
+    L.msum = off; off += a16((size_t)(RP / 2) * (R.Ly / 2));
+    L.part = off; off += 3 * CI_SLOT * sizeof(long long);
+    L.acc = off; off += a16((size_t)R.nacc * sizeof(double) + C_NINT * sizeof(long long));
+    L.total = off;
+    return L;
+}
+
+// Rank 0, thread 0: add slot `slot` of every CTA in rank order; apply its
+// counts to the replica's integer bookkeeping and, for a measurement slot,
+// fold the frame (is_frame's fast-path arithmetic) with is_accumulate.
+__device__ __noinline__ void cluster_ising_fold(Rep &R, long long *part, int C, int slot, bool frame, long long m)
+{
+    cg::cluster_group cl = cg::this_cluster();
+    long long o[CI_NV];
+    for (int k = 0; k < CI_NV; ++k) o[k] = 0;
+    for (int q = 0; q < C; ++q) {
+        const long long *p = cl.map_shared_rank(part, q) + slot * CI_SLOT;
+        for (int k = 0; k < CI_NV; ++k) o[k] += p[k];
+    }
+    for (int k = 0; k < MCS_MAXC; ++k) R.icnt[C_DN + k] += -4 * o[16 + k];
+    for (int k = 0; k < MCS_MAXT; ++k) R.icnt[C_DM + k] += -2 * o[20 + k];
+    R.stats[S_ACCEPT] += o[24];
+    if (!frame) return;
+    const double S0 = R.Stype[0];
+    double Fd[4];
+    Fd[0] = S0 * (double)o[0];
+    Fd[1] = S0 * (double)o[1];
+    Fd[2] = S0 * S0 * (double)o[2];
+    double er = 0;
+    for (int k = 0; k < 4; ++k) er += R.rKv[k] * (double)o[3 + k];
+    Fd[3] = S0 * S0 * er / 2 - R.hd * S0 * (double)o[7];
+    long long Fi[MCS_MAXT + MCS_MAXC];
+    for (int k = 0; k < MCS_MAXT + MCS_MAXC; ++k) Fi[k] = o[8 + k];
+    is_accumulate(R, Fd, Fi, 0, m);
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) k_cluster_ising(Rep *reps, const int *ids, long long max_units, int C)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ Rep R;
+    __shared__ int wsum[NT / 32][CI_NV];
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    Rep *Rg = reps + ids[blockIdx.x / C];
+    {
+        const int *src = (const int *)Rg;
+        int *d = (int *)&R;
+        for (int i = threadIdx.x; i < (int)(sizeof(Rep) / 4); i += blockDim.x) d[i] = src[i];
+    }
+    __syncthreads();
+    // every CTA of the cluster reads the same descriptor: the early exit is uniform over the cluster
+    if (R.u >= R.u_stop) return;
+    const ClusterLayoutI L = cluster_layout_ising(R, C);
+    const int tid = threadIdx.x, bd = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = bd >> 5;
+    const int hy = L.hy, rows = L.rows, nloc = L.nloc;
+    int x0, RP;
+    cl_split(R.Lx, C, rank, &x0, &RP);
+    const int hb = R.Ly >> 1, half = R.half;
+    const int nch = (RP / 2) * hb;  // own chosen blocks
+    signed char *s = (signed char *)(smem + L.spins);
+    IsEntry *itab = (IsEntry *)(smem + L.itab);
+    signed char *msum = (signed char *)(smem + L.msum);
+    long long *part = (long long *)(smem + L.part);
+    const signed char *G = (const signed char *)R.spins;
+    for (int i = tid; i < nloc; i += bd) {
+        const int c = i / (rows * hy);
+        const int rem = i - c * rows * hy;
+        const int xl = rem / hy - 1, yh = rem - (xl + 1) * hy;
+        if (xl > RP) continue;  // beyond this slab's bottom ghost row
+        int x = x0 + xl;
+        if (x < 0) x += R.Lx;
+        if (x >= R.Lx) x -= R.Lx;
+        s[i] = G[c * half + x * hy + yh];
+    }
+    for (int k = tid; k < R.nite; k += bd) itab[k] = R.itab[k];
+    if (rank == 0) {
+        double *a = (double *)(smem + L.acc);
+        long long *ic = (long long *)(a + R.nacc);
+        for (int k = tid; k < R.nacc; k += bd) a[k] = R.acc[k];
+        for (int k = tid; k < C_NINT; k += bd) ic[k] = R.icnt[k];
+        __syncthreads();
+        if (tid == 0) { R.acc = a; R.icnt = ic; }
+    }
+    __syncthreads();
+    cl.sync();
+
+    const int rprev = (rank + C - 1) % C, rnext = (rank + 1) % C;
+    signed char *prev_s = cl.map_shared_rank(s, rprev);
+    signed char *next_s = cl.map_shared_rank(s, rnext);
+    const signed char *prev_m = cl.map_shared_rank(msum, rprev);
+    const signed char *next_m = cl.map_shared_rank(msum, rnext);
+    int x0p, RPp, x0n, RPn;  // the previous slab's bottom ghost row is its local row RPp + 1
+    cl_split(R.Lx, C, rprev, &x0p, &RPp);
+    cl_split(R.Lx, C, rnext, &x0n, &RPn);
+    (void)x0n; (void)RPn;
+    const SqLinks sql = {R.Ly, hy, rows, R.sq_code[0], R.sq_code[1], R.sq_code[2], R.sq_code[3]};
+    const int k_lo = x0 * hy, k_hi = (x0 + RP) * hy;  // own colour-local indices
+    const int q_lo = k_lo >> 2, q_hi = (k_hi + 3) >> 2;
+
+    int dn[MCS_MAXC] = {0, 0, 0, 0}, dm[MCS_MAXT] = {0, 0, 0, 0}, nacc = 0;
+    int frame[16];
+    // this CTA's per-thread counts and frame sums -> slot (fixed order of warps)
+    auto to_slot = [&](int slot, bool with_frame) {
+        int v[CI_NV];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) v[k] = with_frame ? frame[k] : 0;
+#pragma unroll
+        for (int k = 0; k < MCS_MAXC; ++k) v[16 + k] = dn[k];
+#pragma unroll
+        for (int k = 0; k < MCS_MAXT; ++k) v[20 + k] = dm[k];
+        v[24] = nacc;
+#pragma unroll
+        for (int k = 0; k < CI_NV; ++k) {
+            const int w = __reduce_add_sync(0xffffffffu, v[k]);
+            if (lane == 0) wsum[wid][k] = w;
+        }
+        __syncthreads();
+        if (tid < CI_NV) {
+            long long a = 0;
+            for (int w = 0; w < nw; ++w) a += wsum[w][tid];
+            part[slot * CI_SLOT + tid] = a;
+        }
+#pragma unroll
+        for (int k = 0; k < MCS_MAXC; ++k) dn[k] = 0;
+#pragma unroll
+        for (int k = 0; k < MCS_MAXT; ++k) dm[k] = 0;
+        nacc = 0;
+    };
+
+    long long mloc = R.m;
+    int fw = R.frames_written;
+    int pending = -1;  // measurement slot not yet folded (rank 0 folds it at the next measurement)
+    long long pending_m = 0;
+    long long u = R.u;
+    const long long uend = min(R.u_stop, u + max_units);
+    for (; u < uend; ++u) {
+        if (R.alg == 0 && u == R.units_thermal) {
+            // the thermal boundary: the counts so far give the reference's energy offset
+            to_slot(2, false);
+            cl.sync();
+            if (rank == 0 && tid == 0) {
+                if (pending >= 0) cluster_ising_fold(R, part, C, pending, true, pending_m);
+                pending = -1;
+                cluster_ising_fold(R, part, C, 2, false, 0);
+                double Einc = 0;
+                for (int c = 0; c < R.nclass; ++c) Einc += 0.5 * R.Q[c] * (double)R.icnt[C_DN + c];
+                for (int t = 0; t < R.ntype; ++t) Einc -= R.hd * R.Stype[t] * (double)R.icnt[C_DM + t];
+                R.acc[B_EMEAS0] = Einc;
+            }
+            cl.sync();
+        }
+        const long long t = R.u0 + u;
+        const bool meas = measures_after(R, u);
+        for (int c = 0; c < 2; ++c) {
+            const int cb = c * rows * hy;
+            for (int q = q_lo + tid; q < q_hi; q += bd) {
+                const uint4 w = philox_t((uint32_t)q, t, (uint32_t)c, R.seed);
+                const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+                int x = (4 * q) / hy, yh = 4 * q - x * hy;  // walked along the block's four sites
+#pragma unroll
+                for (int e = 0; e < 4; ++e, ++yh) {
+                    if (yh == hy) { yh = 0; ++x; }
+                    const int k = 4 * q + e;
+                    if (k < k_lo || k >= k_hi) continue;
+                    const int xl = x - x0;
+                    const int li = cb + (xl + 1) * hy + yh;
+                    const bool a = ising_trial(R, itab, s, li, 0, ws[e], [&](auto &&f) { cl_links_r(sql, c, xl, yh, f); },
+                                               dn, dm);
+                    if (a) {
+                        ++nacc;
+                        // own row 0 is the previous CTA's bottom ghost (its local row
+                        // RPp+1), own row RP-1 the next CTA's top ghost (local row 0)
+                        if (xl == 0) prev_s[cb + (RPp + 1) * hy + yh] = s[li];
+                        if (xl == RP - 1) next_s[cb + yh] = s[li];
+                    }
+                }
+            }
+            if (c == 1 && meas) {
+                // own sites are final: the sums of the own chosen blocks
+                // (2x2 blocks on even rows and columns lie inside the slab),
+                // published by the colour's cluster barrier
+                __syncthreads();
+                for (int lq = tid; lq < nch; lq += bd) {
+                    const int br = lq / hb, bc = lq - br * hb, xl = 2 * br;
+                    msum[lq] = (signed char)(s[(xl + 1) * hy + bc] + s[rows * hy + (xl + 1) * hy + bc] +
+                                             s[rows * hy + (xl + 2) * hy + bc] + s[(xl + 2) * hy + bc]);
+                }
+            }
+            cl.sync();
+        }
+        if (!meas) continue;
+        // rank 0 folds the previous measurement (every CTA wrote its slot
+        // before this sweep's barriers)
+        if (rank == 0 && tid == 0 && pending >= 0) cluster_ising_fold(R, part, C, pending, true, pending_m);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) frame[k] = 0;
+        // every own site: the pair sums (every site is its own pair), the sign
+        // sum and the per-class bond sums of the full recompute
+        for (int i = tid; i < 2 * RP * hy; i += bd) {
+            const int c = i / (RP * hy), k = i - c * RP * hy;
+            const int xl = k / hy, yh = k - xl * hy;
+            const int li = c * rows * hy + (xl + 1) * hy + yh;
+            const int si = s[li];
+            int idx = R.ibase[0];
+            cl_links_r(sql, c, xl, yh, [&](int, int j, int code) { if (s[j] > 0) idx += code; });
+            const int nc = itab[idx].nc;
+            frame[0] += si; frame[1] += si; frame[2] += si * si;
+            frame[8] += si;
+            frame[12] += si * (int)(signed char)(nc & 0xff);
+            frame[13] += si * (int)(signed char)((nc >> 8) & 0xff);
+            frame[14] += si * (int)(signed char)((nc >> 16) & 0xff);
+            frame[15] += si * (int)(signed char)((nc >> 24) & 0xff);
+        }
+        // own chosen blocks: majority with the engine's tie-breaks, its
+        // renormalised links to the four neighbour blocks (list slot and
+        // coupling class per direction)
+        for (int lq = tid; lq < nch; lq += bd) {
+            const int br = lq / hb, bc = lq - br * hb, xl = 2 * br;
+            const uint32_t j = (uint32_t)((x0 + xl) * hy + bc);  // sweep index of the chosen site (colour 0)
+            const int mj = is_majority_lazy(msum[lq], j, mloc, 0, R.seed);
+            const int bcp = bc + 1 == hb ? 0 : bc + 1, bcm = bc == 0 ? hb - 1 : bc - 1;
+            int tsum[4];
+            tsum[0] = (br + 1 < RP / 2) ? msum[lq + hb] : next_m[bc];
+            tsum[1] = (br > 0) ? msum[lq - hb] : prev_m[(RPp / 2 - 1) * hb + bc];
+            tsum[2] = msum[br * hb + bcp];
+            tsum[3] = msum[br * hb + bcm];
+            const int kind = (x0 + xl == 0 ? 1 : 0) | (bc == 0 ? 2 : 0);
+#pragma unroll
+            for (int d = 0; d < 4; ++d) {
+                const int mt = is_majority_lazy(tsum[d], j, mloc, 1 + R.rdir_slot[4 * kind + d], R.seed);
+                const int kc = R.rdir_cls[d];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) frame[3 + q] += (q == kc) ? mj * mt : 0;
+            }
+            frame[7] += s[(xl + 1) * hy + bc];
+        }
+        to_slot((int)(mloc & 1), true);
+        if (R.frames > 0 && (mloc % R.frame_every) == 0 && fw < R.frames) {
+            Spins S;
+            S.s = s;
+            for (int i = tid; i < 2 * RP * hy; i += bd) {
+                const int c = i / (RP * hy), k = i - c * RP * hy;
+                const int xl = k / hy, yh = k - xl * hy;
+                frame_store<1>(R, fw, c * half + (x0 + xl) * hy + yh, S, c * rows * hy + (xl + 1) * hy + yh);
+            }
+            ++fw;
+        }
+        pending = (int)(mloc & 1);
+        pending_m = mloc;
+        ++mloc;
+        // the measurement read ghost rows, which the neighbours' next colour
+        // phase overwrites
+        cl.sync();
+    }
+    // the counts after the last measurement -> slot 2
+    to_slot(2, false);
+    cl.sync();
+    if (rank == 0 && tid == 0) {
+        if (pending >= 0) cluster_ising_fold(R, part, C, pending, true, pending_m);
+        cluster_ising_fold(R, part, C, 2, false, 0);
+    }
+    // rank 0 has read every CTA's slots before any CTA exits
+    cl.sync();
+    signed char *Gw = (signed char *)R.spins;
+    for (int i = tid; i < 2 * RP * hy; i += bd) {
+        const int c = i / (RP * hy), k = i - c * RP * hy;
+        const int xl = k / hy, yh = k - xl * hy;
+        Gw[c * half + (x0 + xl) * hy + yh] = s[c * rows * hy + (xl + 1) * hy + yh];
+    }
+    if (rank == 0) {
+        __syncthreads();
+        for (int k = tid; k < R.nacc; k += bd) Rg->acc[k] = R.acc[k];
+        for (int k = tid; k < C_NINT; k += bd) Rg->icnt[k] = R.icnt[k];
+        if (tid == 0) {
+            R.stats[S_VISITS] += (uend - R.u) * (long long)R.N;
+            Rg->u = uend;
+            Rg->m = mloc;
+            Rg->frames_written = fw;
+        }
+    }
+}
+
+long long cluster_smem_bytes(const Rep &r, int C)
+{
+    return r.dim == 1 ? (long long)cluster_layout_ising(r, C).total : (long long)cluster_layout(r, C).total;
+}
 
 // Load the cluster kernels on the current device (see preload_kernels_main).
 cudaError_t preload_kernels_cluster()
 {
     cudaFuncAttributes fa;
     cudaError_t e = cudaFuncGetAttributes(&fa, (const void *)k_cluster_metro<2, 256>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)k_cluster_ising<256>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)k_cluster_ising<512>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)k_cluster_ising<1024>);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)k_cluster_metro<2, 512>);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)k_cluster_metro<2, 1024>);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)k_cluster_metro<3, 256>);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)k_cluster_metro<3, 512>);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void *)k_cluster_metro<3, 1024>);
     return e;
+}
+
+// The cluster kernel of a spin dimension (1: Ising).
+template <int DIM, int NT>
+static auto cluster_kernel()
+{
+    if constexpr (DIM == 1) return &k_cluster_ising<NT>;
+    else return &k_cluster_metro<DIM, NT>;
 }
 
 // Shared-memory and cluster-size attributes of one instantiation (set once,
@@ -801,12 +1135,12 @@ static cudaError_t prep_cluster_kernel(size_t smem, int C)
     static size_t done = 0;
     static bool nonportable = false;
     if (smem > done) {
-        cudaError_t e = cudaFuncSetAttribute(k_cluster_metro<DIM, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(cluster_kernel<DIM, NT>(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         done = smem;
     }
     if (C > 8 && !nonportable) {  // clusters above 8 CTAs are an opt-in
-        cudaError_t e = cudaFuncSetAttribute(k_cluster_metro<DIM, NT>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaError_t e = cudaFuncSetAttribute(cluster_kernel<DIM, NT>(), cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         if (e != cudaSuccess) return e;
         nonportable = true;
     }
@@ -839,7 +1173,7 @@ static cudaError_t launch_cluster_t(Rep *reps, const int *ids, int nrep, int C, 
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[1];
     cluster_config<DIM, NT>(cfg, attr, nrep, C, smem, st);
-    return cudaLaunchKernelEx(&cfg, k_cluster_metro<DIM, NT>, reps, ids, max_units, C);
+    return cudaLaunchKernelEx(&cfg, cluster_kernel<DIM, NT>(), reps, ids, max_units, C);
 }
 
 // Clusters of this shape the device can hold at once (0: it cannot launch one).
@@ -851,13 +1185,17 @@ static int cluster_active_t(int C, size_t smem)
     cudaLaunchAttribute attr[1];
     cluster_config<DIM, NT>(cfg, attr, 1, C, smem, 0);
     int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, k_cluster_metro<DIM, NT>, &cfg) != cudaSuccess) { cudaGetLastError(); return 0; }
+    if (cudaOccupancyMaxActiveClusters(&n, cluster_kernel<DIM, NT>(), &cfg) != cudaSuccess) { cudaGetLastError(); return 0; }
     return n;
 }
 
 int cluster_active(int dim, int C, int threads, size_t smem)
 {
-    if (dim == 2) {
+    if (dim == 1) {
+        if (threads == 256) return cluster_active_t<1, 256>(C, smem);
+        if (threads == 512) return cluster_active_t<1, 512>(C, smem);
+        if (threads == 1024) return cluster_active_t<1, 1024>(C, smem);
+    } else if (dim == 2) {
         if (threads == 256) return cluster_active_t<2, 256>(C, smem);
         if (threads == 512) return cluster_active_t<2, 512>(C, smem);
         if (threads == 1024) return cluster_active_t<2, 1024>(C, smem);
@@ -883,6 +1221,7 @@ cudaError_t launch_cluster_metro(int dim, Rep *reps, const int *ids, int nrep, i
                                  long long max_units, cudaStream_t st)
 {
     if (nrep <= 0) return cudaSuccess;
+    if (dim == 1) return launch_cluster_d<1>(reps, ids, nrep, C, threads, smem, max_units, st);
     if (dim == 2) return launch_cluster_d<2>(reps, ids, nrep, C, threads, smem, max_units, st);
     return launch_cluster_d<3>(reps, ids, nrep, C, threads, smem, max_units, st);
 }

@@ -315,6 +315,7 @@ int build_replica(const mcs_problem *p, const mcs_options *o, Replica *r, bool u
     R.meas_regular = m.meas_regular;
     R.sval0 = m.sval.empty() ? 0.f : m.sval[0];
     for (int d = 0; d < 4; ++d) R.rdir_cls[d] = m.rdir_cls[d];
+    for (int k = 0; k < 16; ++k) R.rdir_slot[k] = (unsigned char)m.rdir_slot[k];
     R.sflag = (const unsigned char *)P(o_sflag);
     R.rtgt = (const int *)P(o_rtgt);
     R.units_thermal = m.units_thermal; R.units_total = m.units_total; R.nsweep = m.nsweep; R.upm = m.upm;
@@ -806,7 +807,7 @@ void Batch::place_replicas(int max_smem, const std::vector<int> &ids, double bas
         q.i = i;
         q.c = (double)r.hm.N * (double)std::max<long long>(1, r.hm.units_total - r.rep.u);
         // options in order: 1 = resident, 2/4/8 = cluster, 0 = tiled
-        const bool clusterable = r.hm.cluster_ok && r.hm.geom == MCS_GEOM_SQUARE && r.hm.dim > 1 && cluster_override != 1;
+        const bool clusterable = r.hm.cluster_ok && r.hm.geom == MCS_GEOM_SQUARE && cluster_override != 1;
         if (clusterable && !no_autotune) {
             // the autotuner picks its cluster size; counted here as a cluster of 4
             q.opts.push_back(-1);
@@ -1079,7 +1080,7 @@ int Batch::build_groups(const std::vector<int> &ids, bool merge)
                         // replica's rows into even slabs that fit in shared memory
                         // (C = 1: the cluster kernel on one CTA, whose measurement
                         // needs no index lists on regular lattices)
-                        bool all_cl = g == MCS_GEOM_SQUARE && d > 1;
+                        bool all_cl = g == MCS_GEOM_SQUARE;
                         for (int id : set) all_cl &= replicas[id]->hm.cluster_ok != 0;
                         int copies_only = 0;  // MCSGPU_COPIES=k: only the resident kernel with k copies
                         if (const char *e = getenv("MCSGPU_COPIES")) copies_only = atoi(e);

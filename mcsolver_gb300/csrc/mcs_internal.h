@@ -127,6 +127,8 @@ struct Rep {
     int meas_regular;
     float sval0;
     int rdir_cls[4];
+    unsigned char rdir_slot[16];                 // Ising cluster frame: list slot of the +x, -x, +y, -y renormalised link,
+                                                 // [4 * kind + direction], kind = (first row) | 2 (first column)
     // ---- program
     long long units_thermal, units_total, nsweep;
     int upm;                                     // units per measurement

@@ -742,6 +742,55 @@ int compile_model(const mcs_problem *p, const mcs_options *o, HostModel *m, std:
         }
     }
 
+    // Ising: the cluster schedule's integer frame needs the same regular
+    // renormalisation (2x2 blocks on even rows and columns, every site its own
+    // correlated pair) with the fast path's classes, and the list slot of
+    // each direction's renormalised link (the tie-break of a link's majority
+    // is keyed by its slot) the same at every chosen site of one of four
+    // kinds: first row or not, first column or not (the reference's builder
+    // lists a boundary site's links in another order)
+    if (dim == 1 && m->geom == MCS_GEOM_SQUARE && m->is_fast && m->ntype == 1 && m->pair_identity &&
+        p->n_lat == N && m->ncl == 4 && m->ngroup == 0) {
+        const int Lx = m->Lx, Ly = m->Ly, hb = Ly / 2, zz = std::max(z, 1);
+        bool ok = p->n_rorb == (Lx / 2) * hb;
+        for (int k = 0; k < N && ok; ++k) ok = (m->sflag[k] & 1) != 0;
+        for (int r = 0; r < p->n_rorb && ok; ++r) {
+            const int x = 2 * (r / hb), y = 2 * (r % hb);
+            if (p->r_orb[r] != x * Ly + y) { ok = false; break; }
+            const int want[4] = {x * Ly + y, x * Ly + (y + 1) % Ly, ((x + 1) % Lx) * Ly + y, ((x + 1) % Lx) * Ly + (y + 1) % Ly};
+            for (int k = 0; k < 4; ++k)
+                if (p->r_cluster[(size_t)r * 4 + k] != want[k]) { ok = false; break; }
+        }
+        int slot[16], kc[4] = {-1, -1, -1, -1};
+        for (int k = 0; k < 16; ++k) slot[k] = -1;
+        for (int r = 0; r < p->n_rorb && ok; ++r) {
+            const int x = 2 * (r / hb), y = 2 * (r % hb), kind = (x == 0 ? 1 : 0) | (y == 0 ? 2 : 0);
+            if (m->rdeg[r] != 4) { ok = false; break; }
+            const int want[4] = {(((x + 2) % Lx) / 2) * hb + y / 2, (((x - 2 + Lx) % Lx) / 2) * hb + y / 2,
+                                 (x / 2) * hb + ((y + 2) % Ly) / 2, (x / 2) * hb + ((y - 2 + Ly) % Ly) / 2};
+            int seen = 0;
+            for (int l = 0; l < 4 && ok; ++l) {
+                const int t = m->rtgt[(size_t)r * zz + l];
+                int d = -1;
+                for (int q = 0; q < 4; ++q)
+                    if (t == want[q] && !(seen & (1 << q))) { d = q; break; }
+                if (d < 0) { ok = false; break; }
+                seen |= 1 << d;
+                const int cls = m->rkc[(size_t)r * zz + l];
+                if (slot[4 * kind + d] < 0) slot[4 * kind + d] = l;
+                else if (slot[4 * kind + d] != l) ok = false;
+                if (kc[d] < 0) kc[d] = cls;
+                else if (kc[d] != cls) ok = false;
+            }
+        }
+        for (int k = 0; k < 16 && ok; ++k) ok = slot[k] >= 0;  // every kind of chosen site occurs
+        if (ok) {
+            m->cluster_ok = 1;
+            for (int k = 0; k < 16; ++k) m->rdir_slot[k] = slot[k];
+            for (int d = 0; d < 4; ++d) m->rdir_cls[d] = kc[d];
+        }
+    }
+
     if (dim > 1) m->linkcls = std::move(linkcls);
     return compile_program_state(p, o, m, dim, err);
 }

@@ -59,6 +59,7 @@ struct HostModel {
     int cluster_ok = 0;     // the row-split cluster schedule can run this replica
     int meas_regular = 0;   // cluster frame from arithmetic (see Rep::meas_regular)
     int rdir_cls[4] = {0, 0, 0, 0};
+    int rdir_slot[16] = {};  // Ising: list slot of the renormalised link of each direction, by kind of chosen site
     int nlat = 0, n_rorb = 0, ncl = 0, ncirc = 0, ngroup = 0;
     int ci = 0, cj = 0, cij = 0;
     // program

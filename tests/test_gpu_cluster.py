@@ -103,11 +103,11 @@ def test_replica_too_large_for_any_cluster_runs_once_on_tiles(engine):
 
 
 def test_balanced_batch_equals_alone(engine):
-    """A large Ising replica among small ones is moved to the tiled schedule
-    by the load balancer (its groups run on their own streams beside the
-    resident group); Ising spin trajectories are bit-exact across schedules,
-    so the integer counts are equal and the FP64 averages agree to their
-    summation order (1e-12)."""
+    """A large Ising replica among small ones, placed by the load balancer and
+    the autotuner (the resident group, the cluster schedule or the tiled one);
+    Ising spin trajectories are bit-exact across schedules, so the integer
+    counts are equal and the FP64 averages agree to their summation order
+    (1e-12)."""
     probs = [C.square_args_fast("ising", 256, 2.3, nthermal=4, nsweep=8)]
     probs += [C.square_args("ising", 16 + 4 * k, 2.0 + 0.1 * k, nthermal=4, nsweep=8) for k in range(6)]
     b = engine.Batch()
@@ -115,7 +115,7 @@ def test_balanced_batch_equals_alone(engine):
         b.add("ising", a, seed=40 + k, random_init=True)
     b.prepare()
     kinds = [g[0] for g in b.schedules()]
-    assert "tiled" in kinds and "resident" in kinds
+    assert set(kinds) <= {"resident", "cluster", "tiled"}, kinds
     b.run()
     got = [b.result(k) for k in range(len(probs))]
     b.close()
@@ -169,6 +169,7 @@ def test_resident_copies_match_one_cta(engine, name, model, mk, copies):
 
 
 SERIES_CASES = [
+    ("ising_L16", "ising", lambda: C.square_args("ising", 16, 2.4, nthermal=20, nsweep=200)),
     ("xy_L16", "xy", lambda: C.square_args("xy", 16, 0.9, nthermal=20, nsweep=200)),
     ("heis_L12_dmi_h_circ", "heisenberg", lambda: C.square_args("heisenberg", 12, 0.5, h=0.3, dmi=0.4,
                                                                 nthermal=20, nsweep=200)),
@@ -224,7 +225,7 @@ def test_every_candidate_records_the_same_series(engine, name, model, mk, cand):
 
 WAVE_CASES = [
     ("xy_L26", "xy", lambda: C.square_args("xy", 26, 0.9, nthermal=20, nsweep=200), (13, 256)),
-    ("heis_L12_dmi_h_circ", "heisenberg", SERIES_CASES[1][2], (6, 512)),
+    ("heis_L12_dmi_h_circ", "heisenberg", dict((c[0], c[2]) for c in SERIES_CASES)["heis_L12_dmi_h_circ"], (6, 512)),
 ]
 
 
@@ -270,3 +271,47 @@ def test_warp_per_replica_matches_alone(engine, model):
             assert got[k][1]["accepted"] == ex["accepted"]
         else:
             np.testing.assert_allclose(np.array(got[k][0][:n]), np.array(alone[:n]), rtol=1e-6, atol=1e-6)
+
+
+ISING_CLUSTER = [
+    ("L96_T2.2", lambda: C.square_args("ising", 96, 2.2, nthermal=30, nsweep=300, frames=10), (16, 256)),
+    ("L64_T3_h", lambda: C.square_args("ising", 64, 3.0, h=0.2, nthermal=30, nsweep=300, frames=10), (8, 512)),
+    ("L40_T2.6_uneven", lambda: C.square_args("ising", 40, 2.6, nthermal=30, nsweep=300, frames=10), (16, 256)),
+]
+
+
+@pytest.mark.parametrize("name,mk,cand", ISING_CLUSTER, ids=[c[0] for c in ISING_CLUSTER])
+def test_ising_cluster_kernel_is_bit_exact(engine, name, mk, cand):
+    """Ising on the row-split cluster schedule (int8 slabs, ghost rows over
+    DSMEM, the integer frame split by slabs and added by rank 0) gives the
+    one-CTA resident run's results, per-measurement series and spin frames
+    bit for bit, with the exact bookkeeping intact (uneven slabs included)."""
+    args = mk()
+    ref = engine.Batch()
+    ref.add("ising", args, seed=33, record_series=True, schedule="resident")
+    os.environ["MCSGPU_CLUSTER"] = "1"
+    try:
+        ref.prepare()
+        ref.run()
+        assert ref.schedules()[0][:2] == ("resident", 1)
+    finally:
+        os.environ.pop("MCSGPU_CLUSTER", None)
+    a, ea = ref.result(0)
+    ref.close()
+    os.environ["MCSGPU_FORCE"] = "%d:%d" % cand
+    try:
+        bt = engine.Batch()
+        bt.add("ising", args, seed=33, record_series=True)
+        bt.prepare()
+        bt.run()
+        sched = bt.schedules()
+        b, eb = bt.result(0)
+        bt.close()
+    finally:
+        os.environ.pop("MCSGPU_FORCE", None)
+    assert sched[0][0] == "cluster" and sched[0][1] == cand[0], sched
+    assert eb["exact_mismatches"] == 0 and ea["exact_mismatches"] == 0
+    assert eb["accepted"] == ea["accepted"] and eb["site_updates"] == ea["site_updates"]
+    np.testing.assert_array_equal(eb["series"], ea["series"])
+    np.testing.assert_array_equal(np.array(b[:10]), np.array(a[:10]))
+    np.testing.assert_array_equal(eb["frames"], ea["frames"])

@@ -44,7 +44,7 @@ def _close(model, a, b):
 
 
 def test_server_results_equal_alone_with_overlapping_arrivals(engine, monkeypatch):
-    monkeypatch.setenv("MCSGPU_SERVER_STEP_US", "300")   # short steps, so that arrivals overlap
+    monkeypatch.setenv("MCSGPU_SERVER_STEP_US", "20")   # short steps, so that arrivals overlap
     reqs = _reqs()
     srv = engine.Server(hbm_budget_bytes=1 << 30, max_slots=64)
     tickets = {}
