@@ -1111,12 +1111,15 @@ int Batch::build_groups(const std::vector<int> &ids, bool merge)
                                 if (C == 1 && kind != 2) continue;
                                 if (cluster_override > 1 && C != cluster_override) continue;
                                 if (pc > 0 && C != pc) continue;
-                                // a group whose replicas already fill the device on one CTA
-                                // each gains nothing from splitting them (more waves): the
-                                // resident group of many small lattices is not probed on
+                                // a group of small lattices that fills the device on one CTA
+                                // each gains nothing from splitting them (more waves, and a
+                                // slab of a few rows is all ghost rows): it is not probed on
                                 // clusters of 2 or more
-                                if (C >= 2 && pc == 0 && cluster_override <= 1 && (long long)set.size() * C > 4LL * nsm_)
-                                    continue;
+                                if (C >= 2 && pc == 0 && cluster_override <= 1 && (int)set.size() >= nsm_) {
+                                    long long maxn = 0;
+                                    for (int id : set) maxn = std::max<long long>(maxn, replicas[id]->hm.N);
+                                    if (maxn <= 4096) continue;
+                                }
                                 bool ok = true;
                                 size_t sm = 0;
                                 for (int id : set) {
