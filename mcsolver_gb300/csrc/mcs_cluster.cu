@@ -1,4 +1,5 @@
-// mcs_cluster.cu -- cluster schedule of the Metropolis sweep (square lattice, XY / Heisenberg).
+// mcs_cluster.cu -- cluster schedule of the Metropolis sweep (square lattice: XY / Heisenberg
+// in k_cluster_metro, Ising in k_cluster_ising further down).
 //
 // One replica is split by rows over a thread-block cluster of C CTAs (any C
 // from 1 to 16; the autotuner offers the powers of two and one wave-filling

@@ -871,7 +871,7 @@ void Batch::place_replicas(int max_smem, const std::vector<int> &ids, double bas
     }
     // Then, one replica at a time in order of its own critical path, a larger
     // cluster for any replica whose move does not lengthen the estimate: a
-    // replica that cannot move (an Ising lattice without a cluster kernel) no
+    // replica that cannot move (a lattice the cluster schedule cannot split) no
     // longer holds the others at one CTA, and each finishes as early as the
     // device allows.  Moves to the tiled schedule are left to the first pass.
     // The CTAs of all replicas (a resident or cluster CTA counted as one SM's
