@@ -972,10 +972,12 @@ __global__ void __launch_bounds__(NT) k_cluster_ising(Rep *reps, const int *ids,
         const bool meas = measures_after(R, u);
         for (int c = 0; c < 2; ++c) {
             const int cb = c * rows * hy;
-            for (int q = q_lo + tid; q < q_hi; q += bd) {
+            SqWalk wq;  // (row, half-column) of each block's first site, without divisions
+            wq.init(4 * (q_lo + tid), 4 * bd, hy);
+            for (int q = q_lo + tid; q < q_hi; q += bd, wq.next()) {
                 const uint4 w = philox_t((uint32_t)q, t, (uint32_t)c, R.seed);
                 const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
-                int x = (4 * q) / hy, yh = 4 * q - x * hy;  // walked along the block's four sites
+                int x = wq.x, yh = wq.yh;  // walked along the block's four sites
 #pragma unroll
                 for (int e = 0; e < 4; ++e, ++yh) {
                     if (yh == hy) { yh = 0; ++x; }
@@ -999,8 +1001,10 @@ __global__ void __launch_bounds__(NT) k_cluster_ising(Rep *reps, const int *ids,
                 // (2x2 blocks on even rows and columns lie inside the slab),
                 // published by the colour's cluster barrier
                 __syncthreads();
-                for (int lq = tid; lq < nch; lq += bd) {
-                    const int br = lq / hb, bc = lq - br * hb, xl = 2 * br;
+                SqWalk wb;
+                wb.init(tid, bd, hb);
+                for (int lq = tid; lq < nch; lq += bd, wb.next()) {
+                    const int br = wb.x, bc = wb.yh, xl = 2 * br;
                     msum[lq] = (signed char)(s[(xl + 1) * hy + bc] + s[rows * hy + (xl + 1) * hy + bc] +
                                              s[rows * hy + (xl + 2) * hy + bc] + s[(xl + 2) * hy + bc]);
                 }
@@ -1015,9 +1019,11 @@ __global__ void __launch_bounds__(NT) k_cluster_ising(Rep *reps, const int *ids,
         for (int k = 0; k < 16; ++k) frame[k] = 0;
         // every own site: the pair sums (every site is its own pair), the sign
         // sum and the per-class bond sums of the full recompute
-        for (int i = tid; i < 2 * RP * hy; i += bd) {
-            const int c = i / (RP * hy), k = i - c * RP * hy;
-            const int xl = k / hy, yh = k - xl * hy;
+        for (int c = 0; c < 2; ++c) {
+          SqWalk wk;
+          wk.init(tid, bd, hy);
+          for (int k = tid; k < RP * hy; k += bd, wk.next()) {
+            const int xl = wk.x, yh = wk.yh;
             const int li = c * rows * hy + (xl + 1) * hy + yh;
             const int si = s[li];
             int idx = R.ibase[0];
@@ -1029,12 +1035,15 @@ __global__ void __launch_bounds__(NT) k_cluster_ising(Rep *reps, const int *ids,
             frame[13] += si * (int)(signed char)((nc >> 8) & 0xff);
             frame[14] += si * (int)(signed char)((nc >> 16) & 0xff);
             frame[15] += si * (int)(signed char)((nc >> 24) & 0xff);
+          }
         }
         // own chosen blocks: majority with the engine's tie-breaks, its
         // renormalised links to the four neighbour blocks (list slot and
         // coupling class per direction)
-        for (int lq = tid; lq < nch; lq += bd) {
-            const int br = lq / hb, bc = lq - br * hb, xl = 2 * br;
+        SqWalk wb;
+        wb.init(tid, bd, hb);
+        for (int lq = tid; lq < nch; lq += bd, wb.next()) {
+            const int br = wb.x, bc = wb.yh, xl = 2 * br;
             const uint32_t j = (uint32_t)((x0 + xl) * hy + bc);  // sweep index of the chosen site (colour 0)
             const int mj = is_majority_lazy(msum[lq], j, mloc, 0, R.seed);
             const int bcp = bc + 1 == hb ? 0 : bc + 1, bcm = bc == 0 ? hb - 1 : bc - 1;
