@@ -823,18 +823,29 @@ __host__ __device__ inline ClusterLayoutI cluster_layout_ising(const Rep &R, int
     return L;
 }
 
-// Rank 0, thread 0: add slot `slot` of every CTA in rank order; apply its
+// Rank 0, warp 0: add slot `slot` of every CTA in rank order (lane k sums
+// value k, its remote loads issued eight at a time); then lane 0 applies the
 // counts to the replica's integer bookkeeping and, for a measurement slot,
-// fold the frame (is_frame's fast-path arithmetic) with is_accumulate.
-__device__ __noinline__ void cluster_ising_fold(Rep &R, long long *part, int C, int slot, bool frame, long long m)
+// folds the frame (is_frame's fast-path arithmetic) with is_accumulate.
+// sum: shared scratch of CI_NV values.
+__device__ __noinline__ void cluster_ising_fold(Rep &R, long long *part, int C, int slot, bool frame, long long m,
+                                                long long *sum, int lane)
 {
     cg::cluster_group cl = cg::this_cluster();
-    long long o[CI_NV];
-    for (int k = 0; k < CI_NV; ++k) o[k] = 0;
-    for (int q = 0; q < C; ++q) {
-        const long long *p = cl.map_shared_rank(part, q) + slot * CI_SLOT;
-        for (int k = 0; k < CI_NV; ++k) o[k] += p[k];
+    if (lane < CI_NV) {
+        long long a = 0;
+        for (int q0 = 0; q0 < C; q0 += 8) {
+            long long v[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) v[j] = (q0 + j < C) ? cl.map_shared_rank(part, q0 + j)[slot * CI_SLOT + lane] : 0;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) a += v[j];
+        }
+        sum[lane] = a;
     }
+    __syncwarp();
+    if (lane != 0) return;
+    const long long *o = sum;
     for (int k = 0; k < MCS_MAXC; ++k) R.icnt[C_DN + k] += -4 * o[16 + k];
     for (int k = 0; k < MCS_MAXT; ++k) R.icnt[C_DM + k] += -2 * o[20 + k];
     R.stats[S_ACCEPT] += o[24];
@@ -858,6 +869,7 @@ __global__ void __launch_bounds__(NT) k_cluster_ising(Rep *reps, const int *ids,
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ Rep R;
     __shared__ int wsum[NT / 32][CI_NV];
+    __shared__ long long fsum[CI_NV];  // rank 0's gathered sums of one slot
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank();
     Rep *Rg = reps + ids[blockIdx.x / C];
@@ -957,10 +969,13 @@ __global__ void __launch_bounds__(NT) k_cluster_ising(Rep *reps, const int *ids,
             // the thermal boundary: the counts so far give the reference's energy offset
             to_slot(2, false);
             cl.sync();
+            if (rank == 0 && tid < 32) {
+                if (pending >= 0) cluster_ising_fold(R, part, C, pending, true, pending_m, fsum, tid);
+                __syncwarp();
+                cluster_ising_fold(R, part, C, 2, false, 0, fsum, tid);
+            }
+            pending = -1;
             if (rank == 0 && tid == 0) {
-                if (pending >= 0) cluster_ising_fold(R, part, C, pending, true, pending_m);
-                pending = -1;
-                cluster_ising_fold(R, part, C, 2, false, 0);
                 double Einc = 0;
                 for (int c = 0; c < R.nclass; ++c) Einc += 0.5 * R.Q[c] * (double)R.icnt[C_DN + c];
                 for (int t = 0; t < R.ntype; ++t) Einc -= R.hd * R.Stype[t] * (double)R.icnt[C_DM + t];
@@ -1014,7 +1029,7 @@ __global__ void __launch_bounds__(NT) k_cluster_ising(Rep *reps, const int *ids,
         if (!meas) continue;
         // rank 0 folds the previous measurement (every CTA wrote its slot
         // before this sweep's barriers)
-        if (rank == 0 && tid == 0 && pending >= 0) cluster_ising_fold(R, part, C, pending, true, pending_m);
+        if (rank == 0 && tid < 32 && pending >= 0) cluster_ising_fold(R, part, C, pending, true, pending_m, fsum, tid);
 #pragma unroll
         for (int k = 0; k < 16; ++k) frame[k] = 0;
         // every own site: the pair sums (every site is its own pair), the sign
@@ -1083,9 +1098,10 @@ __global__ void __launch_bounds__(NT) k_cluster_ising(Rep *reps, const int *ids,
     // the counts after the last measurement -> slot 2
     to_slot(2, false);
     cl.sync();
-    if (rank == 0 && tid == 0) {
-        if (pending >= 0) cluster_ising_fold(R, part, C, pending, true, pending_m);
-        cluster_ising_fold(R, part, C, 2, false, 0);
+    if (rank == 0 && tid < 32) {
+        if (pending >= 0) cluster_ising_fold(R, part, C, pending, true, pending_m, fsum, tid);
+        __syncwarp();
+        cluster_ising_fold(R, part, C, 2, false, 0, fsum, tid);
     }
     // rank 0 has read every CTA's slots before any CTA exits
     cl.sync();
