@@ -456,10 +456,26 @@ __device__ void on_frame(const Rep &R, const float *jt, const float *dt, const S
 {
     const int tid = threadIdx.x, bd = blockDim.x;
     const bool full = R.fullJ;
+    // a regular lattice (2x2 blocks on even rows and columns, one spin length,
+    // neighbour blocks two sites away) forms its blocks by arithmetic instead
+    // of from the lists: block r = (xr, yb) holds sites (x, y), (x, y+1),
+    // (x+1, y), (x+1, y+1) with x = 2 xr, y = 2 yb, summed in the lists' order
+    const bool reg = R.meas_regular && majc;
+    const int hb = R.Ly >> 1, hyr = R.hy;
     if (majc) {
         for (int v = tid; v < R.n_rorb; v += bd) {
             float mx, my, mz;
-            on_majority<DIM>(R, S, __ldg(&R.rorb[v]), mx, my, mz);
+            if (reg) {
+                const int xr = v / hb, yb = v - xr * hb;
+                const int a0 = 2 * xr * hyr + yb, a3 = a0 + hyr, a1 = R.half + a0, a2 = R.half + a3;
+                mx = S.x[a0] + S.x[a1] + S.x[a2] + S.x[a3];
+                my = S.y[a0] + S.y[a1] + S.y[a2] + S.y[a3];
+                mz = DIM == 3 ? S.z[a0] + S.z[a1] + S.z[a2] + S.z[a3] : 0.f;
+                v_norm_ref(mx, my, mz);
+                mx *= R.sval0; my *= R.sval0; mz *= R.sval0;
+            } else {
+                on_majority<DIM>(R, S, __ldg(&R.rorb[v]), mx, my, mz);
+            }
             majc[3 * v] = mx; majc[3 * v + 1] = my; majc[3 * v + 2] = mz;
         }
         __syncthreads();
@@ -533,7 +549,24 @@ __device__ void on_frame(const Rep &R, const float *jt, const float *dt, const S
 #pragma unroll
         for (int k = 0; k < 8; ++k) a[k] = 0.f;
         const int e = min(ve, R.n_rorb);
-        for (int r = vb + tid; r < e; r += bd) {
+        for (int r = vb + tid; r < e && reg; r += bd) {
+            // regular lattice: every site is a correlated pair, the four
+            // neighbour blocks and their coupling classes by direction
+            const int xr = r / hb, yb = r - xr * hb, nbx = R.Lx >> 1;
+            const float mx = majc[3 * r], my = majc[3 * r + 1], mz = majc[3 * r + 2];
+            a[0] += mx; a[1] += my; a[2] += mz; a[3] += mx * mx + my * my + mz * mz;
+            const int tg[4] = {(xr + 1 == nbx ? 0 : xr + 1) * hb + yb, (xr == 0 ? nbx - 1 : xr - 1) * hb + yb,
+                               xr * hb + (yb + 1 == hb ? 0 : yb + 1), xr * hb + (yb == 0 ? hb - 1 : yb - 1)};
+            float corr = 0.f;
+#pragma unroll
+            for (int d = 0; d < 4; ++d) {
+                const int t = tg[d];
+                corr += on_jdot<DIM>(jt + 9 * R.rdir_cls[d], full, mx, my, mz, majc[3 * t], majc[3 * t + 1], majc[3 * t + 2]);
+            }
+            a[4] += corr;
+            a[5] += on_onsite<DIM>(R, dt, S, 2 * xr * hyr + yb);
+        }
+        for (int r = vb + tid; r < e && !reg; r += bd) {
             const int v = __ldg(&R.rorb[r]);
             float mx, my, mz;
             if (majc) { mx = majc[3 * r]; my = majc[3 * r + 1]; mz = majc[3 * r + 2]; }
