@@ -494,10 +494,11 @@ __device__ void on_frame(const Rep &R, const float *jt, const float *dt, const S
         float a[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         const int e = min(ve, R.N);
         const bool pid = R.pair_identity;
+        const bool allp = R.meas_regular != 0;  // a regular lattice: every site is a correlated pair
         for (int v = vb + tid; v < e; v += bd) {
             float sx = S.x[v], sy = S.y[v], sz = DIM == 3 ? S.z[v] : 0.f;
             a[0] += sx; a[1] += sy; a[2] += sz;
-            if (pid && (R.sflag[v] & 1)) { a[6] += sx; a[7] += sy; a[8] += sz; a[9] += sx * sx + sy * sy + sz * sz; }
+            if (pid && (allp || (R.sflag[v] & 1))) { a[6] += sx; a[7] += sy; a[8] += sz; a[9] += sx * sx + sy * sy + sz * sz; }
             if (efull) {
                 float h0, h1, h2;
                 on_field<DIM>(R, jt, S, [&](auto &&f) { for_links<GEOM>(R, v, f); }, h0, h1, h2);
