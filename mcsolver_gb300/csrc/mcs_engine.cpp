@@ -1048,6 +1048,18 @@ int Batch::build_groups(const std::vector<int> &ids, bool merge)
                         for (int id : sel) if (replicas[id]->pref_C == C) sub.push_back(id);
                         if (!sub.empty()) sets.push_back(sub);
                     }
+                } else if (kind == 2 && slot_capacity > 0) {
+                    // a server's resident replicas by size (factors of 4 in sites): a
+                    // group's quotas follow its slowest member's measured pace, so a
+                    // small lattice grouped with a large one would advance at the
+                    // large one's speed
+                    std::map<int, std::vector<int>> by;
+                    for (int id : sel) {
+                        int b = 0;
+                        for (long long n = replicas[id]->hm.N; n > 4; n >>= 2) ++b;
+                        by[b].push_back(id);
+                    }
+                    for (auto &kv : by) sets.push_back(kv.second);
                 } else sets.push_back(sel);
                 for (auto &set : sets) {
                     std::unique_ptr<Group> G(new Group());
@@ -1195,11 +1207,19 @@ int Batch::build_groups(const std::vector<int> &ids, bool merge)
                     if (merge) {
                         // an existing group of the same launch configuration takes the set
                         Group *H = nullptr;
+                        auto size_bucket = [&](const std::vector<int> &ids_) {
+                            long long mx = 0;
+                            for (int id : ids_) mx = std::max<long long>(mx, replicas[id]->hm.N);
+                            int b = 0;
+                            for (long long n = mx; n > 4; n >>= 2) ++b;
+                            return b;
+                        };
                         for (auto &q : groups) {
                             if (q->kind != G->kind || q->dim != d || q->geom != g || q->kind == 1) continue;
                             if (q->kind == 2 || q->kind == 6) {
                                 if (!q->tuned || !G->tuned || q->C != G->C || q->threads != G->threads) continue;
                             }
+                            if (q->kind == 2 && slot_capacity > 0 && size_bucket(q->ids) != size_bucket(G->ids)) continue;
                             H = q.get();
                             break;
                         }
