@@ -277,6 +277,10 @@ ISING_CLUSTER = [
     ("L96_T2.2", lambda: C.square_args("ising", 96, 2.2, nthermal=30, nsweep=300, frames=10), (16, 256)),
     ("L64_T3_h", lambda: C.square_args("ising", 64, 3.0, h=0.2, nthermal=30, nsweep=300, frames=10), (8, 512)),
     ("L40_T2.6_uneven", lambda: C.square_args("ising", 40, 2.6, nthermal=30, nsweep=300, frames=10), (16, 256)),
+    # Ly/2 odd: a Philox block of four sites spans two rows, and at a slab
+    # boundary two CTAs
+    ("L34_T2.3_odd_half", lambda: C.square_args("ising", 34, 2.3, nthermal=30, nsweep=300, frames=10), (4, 256)),
+    ("L26_T2.5_odd_half_C8", lambda: C.square_args("ising", 26, 2.5, h=0.1, nthermal=30, nsweep=300, frames=10), (8, 512)),
 ]
 
 
