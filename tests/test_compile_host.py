@@ -184,3 +184,42 @@ def test_compile_is_deterministic_and_sees_every_input(engine):
     assert _digest(engine, other, seed=3)[0] != d0
     other = engine.Problem("heisenberg", C.square_args("heisenberg", 12, 0.5, dmi=0.41, nthermal=3, nsweep=5))
     assert _digest(engine, other, seed=3)[0] != d0
+
+
+def _compile_info(engine, model, args):
+    import ctypes
+    L = engine.lib()
+    fn = L.mcs_test_compile_info
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    P = engine.Problem(model, args)
+    o = engine.make_options()
+    info = (ctypes.c_int32 * 8)()
+    rc = fn(ctypes.addressof(P.struct), ctypes.addressof(o), info)
+    assert rc == 0, L.mcs_last_error()
+    return dict(zip(("geom", "cluster_ok", "meas_regular", "N", "Lx", "Ly", "ncol", "pair_identity"), list(info)))
+
+
+ISING_CLUSTER_ELIGIBLE = [
+    # square, one site type, every site its own pair, 2x2 blocks: the cluster schedule's integer frame
+    ("L16", lambda: C.square_args("ising", 16, 2.4), 1),
+    ("L34_odd_half", lambda: C.square_args("ising", 34, 2.3), 1),
+    ("L26_field", lambda: C.square_args("ising", 26, 2.5, h=0.1), 1),
+    ("L24_antiferro", lambda: C.square_args("ising", 24, 1.5, J=1.0, h=0.5), 1),
+    # odd side: three colours, no square geometry
+    ("L7_odd", lambda: C.square_args("ising", 7, 2.5), 0),
+    # honeycomb: general neighbour lists
+    ("honeycomb", lambda: C.lattice_args("ising", (6, 6, 1), 2, [(0, 1, o, C.J9(-1)) for o in ((0, 0, 0), (-1, 0, 0),
+                                                                                             (0, 1, 0))],
+                                         3.0, S=[1.5, 1.5], ki=((0, 1), (0, 0, 0))), 0),
+]
+
+
+@pytest.mark.parametrize("name,mk,ok", ISING_CLUSTER_ELIGIBLE, ids=[c[0] for c in ISING_CLUSTER_ELIGIBLE])
+def test_ising_cluster_eligibility(engine, name, mk, ok):
+    """The compiler offers the Ising cluster schedule only to square lattices
+    with the regular renormalisation (the reference's builder lists a boundary
+    chosen site's renormalised links in another order; the compiler records
+    the slot of each direction for each of the four kinds of chosen site)."""
+    info = _compile_info(engine, "ising", mk())
+    assert info["cluster_ok"] == ok, info
