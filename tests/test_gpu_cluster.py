@@ -281,6 +281,8 @@ ISING_CLUSTER = [
     # boundary two CTAs
     ("L34_T2.3_odd_half", lambda: C.square_args("ising", 34, 2.3, nthermal=30, nsweep=300, frames=10), (4, 256)),
     ("L26_T2.5_odd_half_C8", lambda: C.square_args("ising", 26, 2.5, h=0.1, nthermal=30, nsweep=300, frames=10), (8, 512)),
+    ("L48_antiferro_h", lambda: C.square_args("ising", 48, 1.5, J=1.0, h=0.5, nthermal=30, nsweep=300, frames=10),
+     (4, 256)),
 ]
 
 
