@@ -320,17 +320,20 @@ def kernel_sources_sha():
 
 
 def kernel_profile(kname):
-    """The ncu figures of the headline kernel (profiles/traffic.json): warp
-    instructions per site update and DRAM bytes per site update of one
-    captured launch, with the hash of the kernel sources they were taken on."""
+    """The ncu figures of the headline kernel configuration the autotuner
+    chose (profiles/traffic.json holds each configuration it picks for this
+    workload): warp instructions per site update and DRAM bytes per site
+    update of one captured launch, with the hash of the kernel sources they
+    were taken on."""
     try:
         tj = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
     except Exception:
         return None
-    if tj.get("kernel") != kname:
+    prof = dict(tj.get("kernels", {}).get(kname) or {})
+    if not prof:
         return None
-    tj["stale"] = tj.get("sources_sha") != kernel_sources_sha()
-    return tj
+    prof["stale"] = tj.get("sources_sha") != kernel_sources_sha()
+    return prof
 
 
 def roofline(updates, ms, hbm, prof, clocks, kname):
