@@ -82,56 +82,49 @@ __device__ void wolff_cluster(Rep &R, const float *jt, const float *dt, const Is
     while (lb < le) {
         int *cnt = sh + 4 + k % 3;
         if (tid == 0) sh[4 + (k + 1) % 3] = 0;
-        if (DIM > 1 && GEOM == MCS_GEOM_SQUARE) {
-            // square lattice, O(n): a level is one chain of dependent
-            // latencies per thread, so its steps are laid side by side: the
-            // four bond coins, then the four bond tests (independent of one
-            // another), then the four claims on the bitmask, then one queue
-            // append per warp.  The loop bound is the warp's first lane's, the
-            // same for every lane, so the whole warp reaches the append.
+        if (GEOM == MCS_GEOM_SQUARE) {
+            // square lattice: one lane per bond.  A level is a chain of
+            // dependent latencies, so it is spread as wide as it goes: bond b
+            // of the level is link b & 3 of frontier entry b >> 2, and its lane
+            // draws that bond's coin, tests it and claims the site on the
+            // bitmask (a site reached along two bonds is claimed once: the
+            // first atomicOr wins).  One ballot places the warp's discoveries
+            // in lane order, i.e. by (frontier entry, link).  The loop bound is
+            // the warp's first lane's, the same for every lane, so the whole
+            // warp reaches the ballot.
             const int lane = tid & 31;
-            for (int f0 = lb + tid - lane; f0 < le; f0 += bd) {
-                const int f = f0 + lane;
-                int js[4] = {0, 0, 0, 0};
-                unsigned int take = 0u;
-                if (f < le) {
-                    const int i = wq_get(W, f);
-                    const float sdi = -(S.x[i] * r0 + S.y[i] * r1 + (DIM == 3 ? S.z[i] * r2 : 0.f));
-                    for_links<GEOM>(R, i, [&](int l, int j, int) { js[l] = j; });
-                    uint32_t cw[4];
-#pragma unroll
-                    for (int l = 0; l < 4; ++l) cw[l] = wolff_coin(i, js[l], q, R.seed);
-#pragma unroll
-                    for (int l = 0; l < 4; ++l) {
-                        const int j = js[l];
-                        const bool in = (W.bits[j >> 5] >> (j & 31)) & 1u;
+            const int nb = 4 * le;
+            for (int b0 = 4 * lb + tid - lane; b0 < nb; b0 += bd) {
+                const int b = b0 + lane;
+                bool take = false;
+                int j = 0;
+                if (b < nb) {
+                    const int i = wq_get(W, b >> 2);
+                    const int l = b & 3;
+                    for_links<GEOM>(R, i, [&](int ll, int jj, int) { if (ll == l) j = jj; });
+                    const uint32_t cw = wolff_coin(i, j, q, R.seed);
+                    const bool in = (W.bits[j >> 5] >> (j & 31)) & 1u;
+                    bool bond;
+                    if (DIM == 1) {
+                        const unsigned long long thr = R.wthr[R.sq_cls[l]][S.s[i] * S.s[j] > 0];
+                        bond = (unsigned long long)cw < thr;
+                    } else {
+                        const float sdi = -(S.x[i] * r0 + S.y[i] * r1 + (DIM == 3 ? S.z[i] * r2 : 0.f));
                         const float sdj = -(S.x[j] * r0 + S.y[j] * r1 + (DIM == 3 ? S.z[j] * r2 : 0.f));
-                        const float corr = 2.f * sdi * sdj * rj[l];
-                        if (!in && corr < 0.f && (1.f - __expf(corr)) > u24(cw[l])) take |= 1u << l;
+                        const float rjl = l == 0 ? rj[0] : l == 1 ? rj[1] : l == 2 ? rj[2] : rj[3];
+                        const float corr = 2.f * sdi * sdj * rjl;
+                        bond = corr < 0.f && (1.f - __expf(corr)) > u24(cw);
                     }
-                    // a site reached along two bonds (of this thread or of
-                    // another) is claimed once: the first atomicOr wins
-#pragma unroll
-                    for (int l = 0; l < 4; ++l)
-                        if ((take >> l) & 1u) {
-                            const int j = js[l];
-                            const unsigned int old = atomicOr(&W.bits[j >> 5], 1u << (j & 31));
-                            if ((old >> (j & 31)) & 1u) take &= ~(1u << l);
-                        }
+                    if (!in && bond) {
+                        const unsigned int old = atomicOr(&W.bits[j >> 5], 1u << (j & 31));
+                        take = !((old >> (j & 31)) & 1u);
+                    }
                 }
-                const int mine = __popc(take);
-                int incl = mine;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int v = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += v;
-                }
+                const unsigned int bal = __ballot_sync(0xffffffffu, take);
                 int base = 0;
-                if (lane == 31 && incl > 0) base = atomicAdd(cnt, incl);
-                int pos = le + __shfl_sync(0xffffffffu, base, 31) + incl - mine;
-#pragma unroll
-                for (int l = 0; l < 4; ++l)
-                    if ((take >> l) & 1u) wq_put(W, pos++, js[l]);
+                if (lane == 0 && bal) base = atomicAdd(cnt, __popc(bal));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (take) wq_put(W, le + base + __popc(bal & ((1u << lane) - 1u)), j);
             }
         } else
         for (int f = lb + tid; f < le; f += bd) {
