@@ -449,10 +449,12 @@ __device__ __forceinline__ double on_signed_area(const Rep &R, const Spins &S, i
 // the full energy (bond and onsite parts).  majc: optional shared cache of the
 // block spins of the chosen sites ([n_rorb][3]); filled here when given, and
 // only usable when the block covers the whole lattice.
+// on_frame_inline is the same code inlined into the caller, so that the
+// compiler sees which memory the spin arrays live in (the Wolff kernel).
 #define MCS_RED (32 * 16 + 32)
 template <int DIM, int GEOM>
-__device__ void on_frame(const Rep &R, const float *jt, const float *dt, const Spins &S, int vb, int ve,
-                         bool efull, double *red, double *Fout, float *majc)
+__device__ __forceinline__ void on_frame_inline(const Rep &R, const float *jt, const float *dt, const Spins &S, int vb,
+                                                int ve, bool efull, double *red, double *Fout, float *majc)
 {
     const int tid = threadIdx.x, bd = blockDim.x;
     const bool full = R.fullJ;
@@ -643,6 +645,12 @@ __device__ void on_frame(const Rep &R, const float *jt, const float *dt, const S
         else if (tid == 15) Fout[F_ERO] = red[32 * 16 + 15];
         __syncthreads();
     }
+}
+template <int DIM, int GEOM>
+__device__ void on_frame(const Rep &R, const float *jt, const float *dt, const Spins &S, int vb, int ve,
+                         bool efull, double *red, double *Fout, float *majc)
+{
+    on_frame_inline<DIM, GEOM>(R, jt, dt, S, vb, ve, efull, red, Fout, majc);
 }
 
 // Fold one measurement frame into the FP64 accumulators.  Follows

@@ -703,18 +703,17 @@ __host__ __device__ inline WolffLayout wolff_layout(const Rep &R, size_t limit =
 }
 long long resident_wolff_smem_bytes(const Rep &r) { return (long long)wolff_layout(r).total; }
 
-template <int DIM, int GEOM>
-__global__ void __launch_bounds__(512) k_wolff(Rep *reps, const int *ids, long long max_units, int gstate)
+// GS: the host keeps this group's state (spins, bitmask, queue) in global
+// memory; otherwise it lives in shared memory, which the compiler then knows.
+template <int DIM, int GEOM, bool GS>
+__global__ void __launch_bounds__(512) k_wolff(Rep *reps, const int *ids, long long max_units)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ Rep R;
     Rep *Rg = reps + ids[blockIdx.x];
     load_rep(R, Rg);
     if (R.u >= R.u_stop) return;
-    WolffLayout L = wolff_layout(R);
-    if (gstate) {  // the host decided: keep the state in global memory
-        L = wolff_layout(R, 0);
-    }
+    const WolffLayout L = GS ? wolff_layout(R, 0) : wolff_layout(R);
     const int tid = threadIdx.x, bd = blockDim.x, N = R.N;
     double *red = (double *)(smem + L.red);
     double *F = (double *)(smem + L.F);
@@ -724,7 +723,7 @@ __global__ void __launch_bounds__(512) k_wolff(Rep *reps, const int *ids, long l
     float *shf = (float *)(sh + 8);
     __shared__ float wfs[MCS_FS_STRIDE];  // one measurement frame in FP32
     const unsigned char *st = R.stype;
-    if (!L.gstate) {
+    if (!GS) {
         unsigned char *sts = (unsigned char *)(smem + L.stype);
         for (int v = tid; v < N; v += bd) sts[v] = R.stype[v];
         st = sts;
@@ -735,7 +734,7 @@ __global__ void __launch_bounds__(512) k_wolff(Rep *reps, const int *ids, long l
     Spins G = spins_global(R);
     Spins S = G;
     WolffMem W;
-    if (L.gstate) {
+    if (GS) {
         W.bits = R.wbits; W.queue = R.wqueue; W.q16 = nullptr;
     } else {
         W.bits = (unsigned int *)(smem + L.bits);
@@ -782,7 +781,7 @@ __global__ void __launch_bounds__(512) k_wolff(Rep *reps, const int *ids, long l
                 // the block spins once per measurement, in the replica's global
                 // scratch (L2): each is read by its own chosen site and by the
                 // renormalised links of its neighbours instead of formed again
-                on_frame<DIM, GEOM>(R, jt, dt, S, 0, max(max(N, R.nlat), max(R.n_rorb, R.ncirc)), efull, red, F, R.wmaj);
+                on_frame_inline<DIM, GEOM>(R, jt, dt, S, 0, max(max(N, R.nlat), max(R.n_rorb, R.ncirc)), efull, red, F, R.wmaj);
                 if (tid == 0 && efull) {
                     double Ef = F[F_EFB] / 2 + F[F_EFO];
                     double d = fabs(R.acc[A_ECUR] - Ef);
@@ -810,7 +809,7 @@ __global__ void __launch_bounds__(512) k_wolff(Rep *reps, const int *ids, long l
     if (DIM > 1 && tid == 0) R.acc[A_ECUR] += dEd;
     __syncthreads();
     acc_to_global(R, Rg);
-    if (!L.gstate)
+    if (!GS)
         for (int v = tid; v < N; v += bd) {
             if (DIM == 1) G.s[v] = S.s[v];
             else {
@@ -971,7 +970,7 @@ cudaError_t preload_kernels_main()
 #define MCS_TOUCH(D, G)                                                                  \
     touch((const void *)k_resident_metro<D, G>); touch((const void *)k_tiled_sweep<D, G>); \
     touch((const void *)k_tiled_measure<D, G>); touch((const void *)k_init<D, G>);        \
-    touch((const void *)k_wolff<D, G>);
+    touch((const void *)k_wolff<D, G, false>); touch((const void *)k_wolff<D, G, true>);
     MCS_TOUCH(1, MCS_GEOM_SQUARE) MCS_TOUCH(2, MCS_GEOM_SQUARE) MCS_TOUCH(3, MCS_GEOM_SQUARE)
     MCS_TOUCH(1, MCS_GEOM_ELL) MCS_TOUCH(2, MCS_GEOM_ELL) MCS_TOUCH(3, MCS_GEOM_ELL)
 #undef MCS_TOUCH
@@ -999,28 +998,38 @@ cudaError_t launch_init_state_dg(int dim, int geom, Rep *reps, const int *ids, i
 }
 
 
-template <int DIM, int GEOM>
+template <int DIM, int GEOM, bool GS>
 static cudaError_t set_wolff_attr(size_t smem)
 {
     static size_t done = 0;
     if (smem > 48 * 1024 && smem > done) {
-        cudaError_t e = cudaFuncSetAttribute(k_wolff<DIM, GEOM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(k_wolff<DIM, GEOM, GS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         done = smem;
     }
     return cudaSuccess;
 }
 
+template <int DIM, int GEOM>
+static cudaError_t launch_wolff_t(Rep *reps, const int *ids, int nrep, int threads, size_t smem, long long max_units,
+                                  int gstate, cudaStream_t st)
+{
+    cudaError_t e;
+    if (gstate) {
+        if ((e = set_wolff_attr<DIM, GEOM, true>(smem)) != cudaSuccess) return e;
+        k_wolff<DIM, GEOM, true><<<nrep, threads, smem, st>>>(reps, ids, max_units);
+    } else {
+        if ((e = set_wolff_attr<DIM, GEOM, false>(smem)) != cudaSuccess) return e;
+        k_wolff<DIM, GEOM, false><<<nrep, threads, smem, st>>>(reps, ids, max_units);
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t launch_wolff(int dim, int geom, Rep *reps, const int *ids, int nrep, int threads, size_t smem,
                          long long max_units, int gstate, cudaStream_t st)
 {
     if (nrep <= 0) return cudaSuccess;
-#define CALL_W(D, G)                                                                     \
-    {                                                                                    \
-        cudaError_t e = set_wolff_attr<D, G>(smem);                                      \
-        if (e != cudaSuccess) return e;                                                  \
-        k_wolff<D, G><<<nrep, threads, smem, st>>>(reps, ids, max_units, gstate);        \
-    }
+#define CALL_W(D, G) return launch_wolff_t<D, G>(reps, ids, nrep, threads, smem, max_units, gstate, st);
     MCS_DISPATCH(dim, geom, CALL_W);
 #undef CALL_W
     return cudaGetLastError();

@@ -41,11 +41,24 @@ __device__ __forceinline__ uint32_t wolff_coin(int a, int b, long long q, unsign
     return w.x;
 }
 
+// O(n) models whose exchange classes are all isotropic (J s_i.s_j), with no
+// single-ion term and no field.
+template <int DIM>
+__device__ __forceinline__ bool wolff_isotropic(const Rep &R, const float *jt)
+{
+    if (R.fullJ || R.has_d || R.h != 0.f) return false;
+    for (int c = 0; c < R.njc; ++c) {
+        const float *M = jt + 9 * c;
+        if (M[0] != M[1] || (DIM == 3 && M[1] != M[2])) return false;
+    }
+    return true;
+}
+
 // One cluster (index q) on a replica.  All threads of the block call it.
 // sh: shared scratch {int head, tail, accept; float r[3]} ; red/F/redl/Fi as in the frame code.
 // Returns nothing; updates spins, bookkeeping and statistics.
 template <int DIM, int GEOM>
-__device__ void wolff_cluster(Rep &R, const float *jt, const float *dt, const IsEntry *itab, const unsigned char *st,
+__device__ __forceinline__ void wolff_cluster(Rep &R, const float *jt, const float *dt, const IsEntry *itab, const unsigned char *st,
                               const Spins &S, const WolffMem &W, long long q, int *sh, float *shf, double *red,
                               double *F, long long *redl, long long *Fi, double &dEd, long long &dnacc,
                               int (&dn)[MCS_MAXC], int (&dm)[MCS_MAXT])
@@ -202,6 +215,40 @@ __device__ void wolff_cluster(Rep &R, const float *jt, const float *dt, const Is
             const int i = wq_get(W, f);
             if (acc) S.s[i] = (signed char)(-S.s[i]);
         }
+    } else if (wolff_isotropic<DIM>(R, jt)) {
+        // Isotropic exchange, no single-ion term, no field: the embedding is
+        // exact.  The exchange terms the acceptance holds are r.J.p_j with p_j
+        // perpendicular to r, which vanish, so the reflection is always
+        // accepted; a bond inside the cluster keeps its energy (both ends are
+        // reflected), and a boundary bond changes by J d_i.s_j with d_i =
+        // 2 sdi r, i.e. -2 J sdi sdj.  A boundary site is never reflected, so
+        // each cluster site is reflected in the same pass that reads its
+        // boundary neighbours.
+        float a_dE = 0.f;
+        for (int f = tid; f < n; f += bd) {
+            const int i = wq_get(W, f);
+            const float si0 = S.x[i], si1 = S.y[i], si2 = DIM == 3 ? S.z[i] : 0.f;
+            const float sdi = -(si0 * r0 + si1 * r1 + si2 * r2);
+            for_links<GEOM>(R, i, [&](int, int j, int code) {
+                if ((W.bits[j >> 5] >> (j & 31)) & 1u) return;
+                const float sdj = -(S.x[j] * r0 + S.y[j] * r1 + (DIM == 3 ? S.z[j] * r2 : 0.f));
+                a_dE += -2.f * jt[9 * code] * sdi * sdj;
+            });
+            float n0 = si0 + 2.f * sdi * r0, n1 = si1 + 2.f * sdi * r1, n2 = si2 + 2.f * sdi * r2;
+            const int dc = st ? st[i] : 0;
+            const float len2 = n0 * n0 + n1 * n1 + n2 * n2;
+            const float k = len2 > 0.f ? dt[4 * dc + 3] * rsqrtf(len2) : 1.f;
+            S.x[i] = n0 * k; S.y[i] = n1 * k;
+            if (DIM == 3) S.z[i] = n2 * k;
+        }
+        float c2[2] = {0.f, a_dE};
+        block_sum_f<2>(c2, red, F);  // its barriers also end every read of the bitmask above
+        if (tid == 0) {
+            R.stats[S_CLUSTERS] += 1;
+            dEd += F[1];
+            R.stats[S_ACCEPT] += 1;
+            R.stats[S_FLIPPED] += n;
+        }
     } else {
         float a_tot = 0.f, a_dE = 0.f;
         for (int f = tid; f < n; f += bd) {
@@ -271,11 +318,16 @@ __device__ void wolff_cluster(Rep &R, const float *jt, const float *dt, const Is
             }
         }
     }
-    // ---- clear the cluster's bits
-    for (int f = tid; f < n; f += bd) {
-        const int i = wq_get(W, f);
-        atomicAnd(&W.bits[i >> 5], ~(1u << (i & 31)));
-    }
+    // ---- clear the cluster's bits: the whole bitmask word by word when that
+    // is fewer stores than the cluster has sites, else site by site
+    const int nw = (N + 31) >> 5;
+    if (n >= nw)
+        for (int k = tid; k < nw; k += bd) W.bits[k] = 0u;
+    else
+        for (int f = tid; f < n; f += bd) {
+            const int i = wq_get(W, f);
+            atomicAnd(&W.bits[i >> 5], ~(1u << (i & 31)));
+        }
     __syncthreads();
     (void)itab; (void)dnacc; (void)dn; (void)dm;
 }

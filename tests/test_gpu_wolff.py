@@ -76,3 +76,16 @@ def test_wolff_counts_and_energy_consistency(engine):
     res, ex = engine.solve("heisenberg", args, seed=5, recheck_every=8)
     assert ex["clusters"] == 250
     assert ex["energy_drift"] < 1e-3 * 24 * 24
+
+
+@pytest.mark.parametrize("model,L,T", [("xy", 32, 0.7), ("heisenberg", 24, 0.5)])
+def test_wolff_isotropic_energy_and_acceptance(engine, model, L, T):
+    """Isotropic exchange without single-ion term or field: every cluster is
+    accepted, and the energy from the boundary bonds alone stays within FP32
+    drift of the full recompute (re-checked every 8 measurements)."""
+    args = C.square_args(model, L, T, nthermal=50, nsweep=300, tau=1, algo=1)
+    res, ex = engine.solve(model, args, seed=9, recheck_every=8)
+    assert ex["clusters"] == 350
+    assert ex["accepted"] == 350
+    assert ex["flipped"] > 350
+    assert ex["energy_drift"] < 1e-3 * L * L
