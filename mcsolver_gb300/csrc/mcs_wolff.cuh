@@ -41,6 +41,27 @@ __device__ __forceinline__ uint32_t wolff_coin(int a, int b, long long q, unsign
     return w.x;
 }
 
+// The links of site v as for_links, with the square lattice's row taken by a
+// multiply-high instead of an integer division when mdiv != 0: mdiv =
+// ceil(2^32 / hy) gives floor(k / hy) exactly for k < 2^16 and 1 < hy < 2^16
+// (the error term k (mdiv hy - 2^32) / (hy 2^32) stays below 1/hy).
+__device__ __forceinline__ uint32_t wolff_mdiv(const Rep &R, int geom)
+{
+    return (geom == MCS_GEOM_SQUARE && R.N <= 65536 && R.hy > 1) ? (uint32_t)((0x100000000ull + R.hy - 1) / R.hy) : 0u;
+}
+template <int GEOM, class F>
+__device__ __forceinline__ void wolff_links(const Rep &R, int v, uint32_t mdiv, F &&f)
+{
+    if (GEOM == MCS_GEOM_SQUARE && mdiv != 0u) {
+        const int c = v >= R.half;
+        const int k = v - c * R.half;
+        const int x = (int)__umulhi((uint32_t)k, mdiv);
+        sq_links(R, c, x, k - x * R.hy, f);
+    } else {
+        for_links<GEOM>(R, v, f);
+    }
+}
+
 // O(n) models whose exchange classes are all isotropic (J s_i.s_j), with no
 // single-ion term and no field.
 template <int DIM>
@@ -79,6 +100,7 @@ __device__ __forceinline__ void wolff_cluster(Rep &R, const float *jt, const flo
     __syncthreads();
     const float r0 = shf[0], r1 = shf[1], r2 = shf[2];
     const bool full = R.fullJ;
+    const uint32_t mdiv = wolff_mdiv(R, GEOM);
     // square lattice: r.J.r of the four link directions (the same for every site)
     float rj[4] = {0.f, 0.f, 0.f, 0.f};
     if (DIM > 1 && GEOM == MCS_GEOM_SQUARE) {
@@ -114,7 +136,7 @@ __device__ __forceinline__ void wolff_cluster(Rep &R, const float *jt, const flo
                 if (b < nb) {
                     const int i = wq_get(W, b >> 2);
                     const int l = b & 3;
-                    for_links<GEOM>(R, i, [&](int ll, int jj, int) { if (ll == l) j = jj; });
+                    wolff_links<GEOM>(R, i, mdiv, [&](int ll, int jj, int) { if (ll == l) j = jj; });
                     const uint32_t cw = wolff_coin(i, j, q, R.seed);
                     const bool in = (W.bits[j >> 5] >> (j & 31)) & 1u;
                     bool bond;
@@ -229,7 +251,7 @@ __device__ __forceinline__ void wolff_cluster(Rep &R, const float *jt, const flo
             const int i = wq_get(W, f);
             const float si0 = S.x[i], si1 = S.y[i], si2 = DIM == 3 ? S.z[i] : 0.f;
             const float sdi = -(si0 * r0 + si1 * r1 + si2 * r2);
-            for_links<GEOM>(R, i, [&](int, int j, int code) {
+            wolff_links<GEOM>(R, i, mdiv, [&](int, int j, int code) {
                 if ((W.bits[j >> 5] >> (j & 31)) & 1u) return;
                 const float sdj = -(S.x[j] * r0 + S.y[j] * r1 + (DIM == 3 ? S.z[j] * r2 : 0.f));
                 a_dE += -2.f * jt[9 * code] * sdi * sdj;

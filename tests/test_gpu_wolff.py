@@ -89,3 +89,30 @@ def test_wolff_isotropic_energy_and_acceptance(engine, model, L, T):
     assert ex["accepted"] == 350
     assert ex["flipped"] > 350
     assert ex["energy_drift"] < 1e-3 * L * L
+
+
+@pytest.mark.parametrize("model,L,T", [("ising", 256, 2.3), ("xy", 160, 0.9)])
+def test_wolff_global_state_schedule(engine, oracle_lib, model, L, T):
+    """Lattices whose Wolff state does not fit in shared memory run the
+    global-state instantiation; Ising stays bit-exact with the oracle there,
+    and the O(n) model's first clusters agree site for site."""
+    args = C.square_args(model, L, T, nthermal=0, nsweep=4, tau=1, algo=1, frames=4)
+    if model == "xy":
+        a = list(args)
+        a[15] = 0.6  # random initial tilt from the engine stream
+        args = tuple(a)
+    b = engine.Batch()
+    b.add(model, args, seed=77)
+    b.prepare()
+    assert b.schedules()[0][0] == "wolff_global"
+    b.run()
+    res, ex = b.result(0)
+    b.close()
+    ref, rex = oracle_lib.solve(model, args, seed=77, mode=1)
+    if model == "ising":
+        assert ex["exact_mismatches"] == 0
+        np.testing.assert_array_equal(ex["frames"][-1][:, 0], rex["spins"][:, 0].astype(np.float32))
+        assert ex["flipped"] == rex["stats"][1]
+    else:
+        d = np.abs(ex["frames"][-1][:, :2].astype(np.float64) - rex["spins"][:, :2]).max()
+        assert d < 1e-4, d
