@@ -307,6 +307,21 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
     __syncthreads();
     cl.sync();
 
+    // Regular lattices whose -x and -y block links carry the transposes of the
+    // +x and +y couplings: summed over the blocks, the -x term of block b is the
+    // +x term of block b - x, so the renormalised bond sum is twice the sum of
+    // the +x and +y terms (pass B then reads no -x neighbour across a slab)
+    bool bpair = false;
+    if (R.meas_regular) {
+        auto transposed = [&](int ca, int cb) {
+            const float *A = jt + 9 * ca, *B = jt + 9 * cb;
+            bool t = A[0] == B[0] && A[1] == B[1] && (!R.fullJ || (A[3] == B[6] && A[6] == B[3]));
+            if (DIM == 3) t = t && A[2] == B[2] && (!R.fullJ || (A[4] == B[7] && A[7] == B[4] && A[5] == B[8] && A[8] == B[5]));
+            return t;
+        };
+        bpair = transposed(R.rdir_cls[0], R.rdir_cls[1]) && transposed(R.rdir_cls[2], R.rdir_cls[3]);
+    }
+
     const float beta = R.beta, h = R.h;
     double dEd = 0.0;
     long long nacc = 0;
@@ -483,13 +498,14 @@ __global__ void __launch_bounds__(NT) k_cluster_metro(Rep *reps, const int *ids,
                 float corr = 0.f;
 #pragma unroll
                 for (int d = 0; d < 4; ++d) {
+                    if (bpair && (d & 1)) continue;
                     int owner = rank, lq = tg[d] - r0;
                     if (d == 0 && xr == brl) { owner = rnext; lq = tg[d] - (x0n >> 1) * hb; }
                     if (d == 1 && xr == (x0 >> 1)) { owner = rprev; lq = tg[d] - (x0p >> 1) * hb; }
                     const float *mc = owner == rank ? majc : cl.map_shared_rank(majc, owner);
                     corr += on_jdot<DIM>(jt + 9 * R.rdir_cls[d], full, mx, my, mz, mc[3 * lq], mc[3 * lq + 1], mc[3 * lq + 2]);
                 }
-                a[14] += corr;
+                a[14] += bpair ? 2.f * corr : corr;
                 // onsite energy of the actual spin at (2 xr, 2 yb): colour 0
                 const int li = (2 * xr - x0 + 1) * hy + yb;
                 const float sx = S.x[li], sy = S.y[li], sz = DIM == 3 ? S.z[li] : 0.f;
