@@ -946,8 +946,33 @@ __global__ void __launch_bounds__(NT) k_cluster_ising(Rep *reps, const int *ids,
 
     int dn[MCS_MAXC] = {0, 0, 0, 0}, dm[MCS_MAXT] = {0, 0, 0, 0}, nacc = 0;
     int frame[16];
-    // this CTA's per-thread counts and frame sums -> slot (fixed order of warps)
+    // this CTA's per-thread counts and frame sums -> slot (fixed order of warps).
+    // The leading barrier keeps warp 0's reads of wsum in the previous call
+    // (a launch's last measurement is followed at once by the closing call)
+    // ahead of this call's writes.
+    // the frame sums over the own sites of colour c: the pair sums (every site
+    // is its own pair), the sign sum and the per-class bond sums of the full
+    // recompute; a colour-c site's neighbours have colour 1 - c
+    auto site_sums = [&](int c) {
+        SqWalk wk;
+        wk.init(tid, bd, hy);
+        for (int k = tid; k < RP * hy; k += bd, wk.next()) {
+            const int xl = wk.x, yh = wk.yh;
+            const int li = c * rows * hy + (xl + 1) * hy + yh;
+            const int si = s[li];
+            int idx = R.ibase[0];
+            cl_links_r(sql, c, xl, yh, [&](int, int j, int code) { if (s[j] > 0) idx += code; });
+            const int nc = itab[idx].nc;
+            frame[0] += si; frame[1] += si; frame[2] += si * si;
+            frame[8] += si;
+            frame[12] += si * (int)(signed char)(nc & 0xff);
+            frame[13] += si * (int)(signed char)((nc >> 8) & 0xff);
+            frame[14] += si * (int)(signed char)((nc >> 16) & 0xff);
+            frame[15] += si * (int)(signed char)((nc >> 24) & 0xff);
+        }
+    };
     auto to_slot = [&](int slot, bool with_frame) {
+        __syncthreads();
         int v[CI_NV];
 #pragma unroll
         for (int k = 0; k < 16; ++k) v[k] = with_frame ? frame[k] : 0;
@@ -1030,7 +1055,9 @@ __global__ void __launch_bounds__(NT) k_cluster_ising(Rep *reps, const int *ids,
             if (c == 1 && meas) {
                 // own sites are final: the sums of the own chosen blocks
                 // (2x2 blocks on even rows and columns lie inside the slab),
-                // published by the colour's cluster barrier
+                // published by the colour's cluster barrier, and the colour-1
+                // site sums, whose colour-0 neighbours (ghost rows included)
+                // no CTA changes before this barrier
                 __syncthreads();
                 SqWalk wb;
                 wb.init(tid, bd, hb);
@@ -1039,6 +1066,9 @@ __global__ void __launch_bounds__(NT) k_cluster_ising(Rep *reps, const int *ids,
                     msum[lq] = (signed char)(s[(xl + 1) * hy + bc] + s[rows * hy + (xl + 1) * hy + bc] +
                                              s[rows * hy + (xl + 2) * hy + bc] + s[(xl + 2) * hy + bc]);
                 }
+#pragma unroll
+                for (int k = 0; k < 16; ++k) frame[k] = 0;
+                site_sums(1);
             }
             cl.sync();
         }
@@ -1046,28 +1076,10 @@ __global__ void __launch_bounds__(NT) k_cluster_ising(Rep *reps, const int *ids,
         // rank 0 folds the previous measurement (every CTA wrote its slot
         // before this sweep's barriers)
         if (rank == 0 && tid < 32 && pending >= 0) cluster_ising_fold(R, part, C, pending, true, pending_m, fsum, tid);
-#pragma unroll
-        for (int k = 0; k < 16; ++k) frame[k] = 0;
-        // every own site: the pair sums (every site is its own pair), the sign
-        // sum and the per-class bond sums of the full recompute
-        for (int c = 0; c < 2; ++c) {
-          SqWalk wk;
-          wk.init(tid, bd, hy);
-          for (int k = tid; k < RP * hy; k += bd, wk.next()) {
-            const int xl = wk.x, yh = wk.yh;
-            const int li = c * rows * hy + (xl + 1) * hy + yh;
-            const int si = s[li];
-            int idx = R.ibase[0];
-            cl_links_r(sql, c, xl, yh, [&](int, int j, int code) { if (s[j] > 0) idx += code; });
-            const int nc = itab[idx].nc;
-            frame[0] += si; frame[1] += si; frame[2] += si * si;
-            frame[8] += si;
-            frame[12] += si * (int)(signed char)(nc & 0xff);
-            frame[13] += si * (int)(signed char)((nc >> 8) & 0xff);
-            frame[14] += si * (int)(signed char)((nc >> 16) & 0xff);
-            frame[15] += si * (int)(signed char)((nc >> 24) & 0xff);
-          }
-        }
+        // the colour-0 site sums read own colour-0 sites and colour-1
+        // neighbours, which the next sweep's colour-0 phase leaves alone in
+        // every CTA (its pushes go to colour-0 ghost rows)
+        site_sums(0);
         // own chosen blocks: majority with the engine's tie-breaks, its
         // renormalised links to the four neighbour blocks (list slot and
         // coupling class per direction)
@@ -1103,13 +1115,14 @@ __global__ void __launch_bounds__(NT) k_cluster_ising(Rep *reps, const int *ids,
                 frame_store<1>(R, fw, c * half + (x0 + xl) * hy + yh, S, c * rows * hy + (xl + 1) * hy + yh);
             }
             ++fw;
+            __syncthreads();  // every own site stored before the next colour-0 phase changes them
         }
         pending = (int)(mloc & 1);
         pending_m = mloc;
         ++mloc;
-        // the measurement read ghost rows, which the neighbours' next colour
-        // phase overwrites
-        cl.sync();
+        // no cluster barrier here: the measurement read colour-0 ghost rows only
+        // before the colour-1 barrier, and the neighbour block sums it reads are
+        // rewritten only after the next sweep's colour-0 barrier
     }
     // the counts after the last measurement -> slot 2
     to_slot(2, false);
